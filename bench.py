@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""SPG iterations/s of the FEM-H1 gamma-step QP on the T = 1e7, K = 3 benchmark signal.
+
+One step = one SPG-QP iteration (SPGQPSolver main loop, src/petscvector/solver/spgqpsolver.cpp:
+140-297) over the whole signal: the fused mixed-precision sweep on the GPU.  The workload is
+the synthetic 1-D signal of the benchmark configuration (T = 1e7 timesteps, K = 3 levels
+{0, 1, 2} in random order per segment, segment lengths U[1e3, 1e5], noise sigma 0.5;
+seeded, see pasc_inference_gb300/datagen.py), epssqr = 10, theta fixed at the true levels
+as in the reference's own SPG benchmark runs (tssolver_maxit = 1 with theta given), GLL
+memory 10.  Every timed step runs the full iteration; stopping tests are off inside the
+timed region so that no step is skipped.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Besides the headline line it measures, on rank 0:
+  e2e        the same metric through the public API with host buffers: set_data, set_gamma,
+             set_theta, spgqp_solve (reference stopping rule, eps 1e-6, m 10), get_gamma, get_fx;
+             host<->device copies inside the timed region.
+  tts        time to an objective within 1e-6 relative of the converged FP64 objective, for the
+             mixed path and for the plain FP64 GPU path on the same problem.
+  roofline   the sweep kernel's algorithmic bytes (16*K*T + 4*T per iteration) over its
+             CUDA-event time, against the measured HBM copy bandwidth.
+  cpu_baseline  the FP64 CPU oracle (a port of the reference's CPU path) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SPG iters/s & time to 1e-6 rel obj, T=1e7 K=3 (1 GB300); HBM GB/s vs peak"
+UNIT = "SPG iterations/s"
+WORKLOAD = "signal1d T=1e7 K=3 levels {0,1,2} sigma=0.5, epssqr=10, theta fixed, GLL m=10"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--T", type=int, default=10_000_000)
+    ap.add_argument("--eps2", type=float, default=10.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tts", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per sweep launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "spg_sweep_k3_t1e7.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.gpu), "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def oracle_iter_rate(sig, theta, eps2, T, iters, nthreads):
+    """FP64 oracle SPG iterations/s on the first T timesteps (all its iterations run)."""
+    from oracle import pasc_oracle as O
+    O.build()
+    K = sig.K
+    data = sig.data[:T]
+    gam = O.permute_blocked_to_interleaved(sig.gamma0[: K * T] if T == sig.T else
+                                           sig.gamma0.reshape(K, sig.T)[:, :T].ravel(), T, K)
+    b = O.residual_b(data, theta, T, K, nthreads=nthreads)
+    coeff = O.A_coeff(eps2, T)
+    o0 = O.spg_opts(maxit=0, m=10)
+    t0 = time.perf_counter()
+    O.spgqp_solve(b, gam, T, K, coeff, o0, nthreads=nthreads)
+    t_init = time.perf_counter() - t0
+    o = O.spg_opts(maxit=iters, m=10, stop_difff=0)
+    t0 = time.perf_counter()
+    _, r, _ = O.spgqp_solve(b, gam, T, K, coeff, o, nthreads=nthreads)
+    t_all = time.perf_counter() - t0
+    dt = max(t_all - t_init, 1e-9)
+    return r.it / dt, dt
+
+
+def run_reference(args, info):
+    """The reference path's CPU implementation (the FP64 oracle port), rank 0 only."""
+    from pasc_inference_gb300 import datagen
+    if info.rank != 0:
+        return None
+    sig = datagen.signal1d_cfg1(T=args.T)
+    theta = np.array([0.0, 1.0, 2.0])
+    cores = cpu_cores()
+    # size the per-step sample so that warmup + steps stay within ~2 minutes
+    rate_full, _ = oracle_iter_rate(sig, theta, args.eps2, args.T, 1, 0)
+    t_full = 1.0 / rate_full
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    Ts = int(min(args.T, max(100_000, args.T * budget / t_full)))
+    steps = args.steps
+    if Ts < args.T:
+        rate, dt = oracle_iter_rate(sig, theta, args.eps2, Ts, steps, 0)
+        value = rate * Ts / args.T
+        sample = f"{steps} SPG iterations on the first {Ts} timesteps, scaled by {Ts}/{args.T}"
+    else:
+        rate, dt = oracle_iter_rate(sig, theta, args.eps2, args.T, steps, 0)
+        value = rate
+        sample = f"{steps} SPG iterations on the full signal"
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "T": args.T, "K": 3, "epssqr": args.eps2,
+                   "parallelism": "replicas", "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return line
+
+
+def main():
+    args = parse()
+    from pasc_inference_gb300 import dist
+    info = dist.init()
+    if args.impl == "reference":
+        line = run_reference(args, info)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        dist.finalize(info)
+        return
+
+    from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Problem, capi, datagen
+    dev = info.local_rank
+    sig = datagen.signal1d_cfg1(T=args.T)
+    T, K = sig.T, sig.K
+    theta = np.array([0.0, 1.0, 2.0])
+    B_it = 16.0 * K * T + 4.0 * T
+
+    p = Problem(T, K, args.eps2, precision=PASC_PREC_MIXED, device=dev)
+    p.set_data(sig.data)
+    p.set_gamma(sig.gamma0)
+    p.permute_gamma()
+    p.set_theta(theta)
+    p.update_b()
+    total_steps = args.warmup + args.steps
+    opts = capi.spgqp_opts(maxit=10 * total_steps + 100, m=10, stop_difff=0)
+    p.spgqp_start(opts)
+    if args.warmup:
+        p.spgqp_iterate(args.warmup, poll=False)
+
+    dist.barrier(info)
+    sampler = ClockSampler(dev) if info.rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    chunk = 500
+    done, ms_total, launches, restarts = 0, 0.0, 0, 0
+    t_wall0 = time.perf_counter()
+    while done < args.steps:
+        n = min(chunk, args.steps - done)
+        st = p.spgqp_iterate(n, poll=False)
+        ms, nl = p.spgqp_last_iterate()
+        if st.status != capi.PASC_SPG_RUNNING:
+            # the solve ended inside the chunk (exact stationarity): the chunk is re-run from a
+            # fresh start so that every timed step is a full iteration
+            restarts += 1
+            p.spgqp_start(opts)
+            continue
+        ms_total += ms
+        launches += nl
+        done += n
+    t_wall = time.perf_counter() - t_wall0
+    clocks = sampler.stop() if sampler else None
+    dist.barrier(info)
+    ms_max = dist.max_over_ranks(info, ms_total)
+    value = info.world_size * args.steps / (ms_max / 1000.0)
+    ms_per_step = ms_max / args.steps
+
+    peak, peak_kind = measured_peaks()
+    achieved = B_it / (ms_per_step / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": profile_traffic(),
+                "peak_source": peak_kind,
+                "bytes_per_launch": B_it, "kernel": "spg_sweep_kernel<3,false>"}
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": info.world_size,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "T": T, "K": K, "epssqr": args.eps2,
+                   "parallelism": f"replicas x{info.world_size}",
+                   "l2": "inputs larger than L2 (x,g,data = 280 MB read per step)",
+                   "wall_s_timed": t_wall, "restarts": restarts},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "clocks": clocks,
+    }
+    p.close()
+
+    if info.rank == 0 and not args.no_e2e:
+        result["e2e"] = measure_e2e(sig, theta, args.eps2, dev)
+    if info.rank == 0 and not args.no_tts:
+        result["time_to_1e-6_rel_obj"] = measure_tts(sig, theta, args.eps2, dev)
+    if info.rank == 0 and not args.no_cpu:
+        rate, dt = oracle_iter_rate(sig, theta, args.eps2, T, 5, 0)
+        result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+                                  "sample": f"5 SPG iterations of the FP64 oracle on the full T={T} "
+                                            f"signal ({dt:.1f} s, OpenMP)"}
+    if info.rank == 0:
+        print(json.dumps(result), flush=True)
+    dist.finalize(info)
+
+
+def measure_e2e(sig, theta, eps2, dev, steps=2):
+    """Public API with host buffers; copies inside the timed region."""
+    from pasc_inference_gb300 import PASC_PREC_MIXED, Problem, capi
+    T, K = sig.T, sig.K
+    gamma_h = np.ascontiguousarray(sig.gamma0)
+    data_h = np.ascontiguousarray(sig.data)
+    out = np.empty(T * K)
+    opts = capi.spgqp_opts(m=10, eps=1e-6)
+    with Problem(T, K, eps2, precision=PASC_PREC_MIXED, device=dev) as p:
+        its, secs, launches = 0, 0.0, 0
+        for rep in range(steps + 1):
+            t0 = time.perf_counter()
+            p.set_data(data_h)
+            p.set_gamma(gamma_h)
+            p.permute_gamma()
+            p.set_theta(theta)
+            p.update_b()
+            st = p.spgqp_solve(opts)
+            out[:] = p.get_gamma()
+            fx = p.get_fx()
+            dt = time.perf_counter() - t0
+            if rep > 0:
+                its += st.it
+                secs += dt
+                launches += st.kernel_launches
+    return {"value": its / secs, "unit": UNIT, "h2d_bytes_per_step": 8 * T + 8 * T * K + 8 * K,
+            "d2h_bytes_per_step": 8 * T * K + 8, "spg_it_per_step": its / steps,
+            "s_per_step": secs / steps, "fx": fx, "gpu_launches_per_step": launches / steps}
+
+
+def measure_tts(sig, theta, eps2, dev):
+    """Time to an objective within 1e-6 (relative) of the converged FP64 objective."""
+    from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Problem, capi
+    T, K = sig.T, sig.K
+    traces = {}
+    for name, prec, maxit, chunk in (("fp64_plain", PASC_PREC_FP64, 4000, 50),
+                                     ("mixed_fused", PASC_PREC_MIXED, 4000, 25)):
+        with Problem(T, K, eps2, precision=prec, device=dev) as p:
+            p.set_data(sig.data)
+            p.set_gamma(sig.gamma0)
+            p.permute_gamma()
+            p.set_theta(theta)
+            p.update_b()
+            o = capi.spgqp_opts(m=10, eps=1e-13 if prec == PASC_PREC_FP64 else 1e-12, maxit=maxit)
+            t0 = time.perf_counter()
+            p.spgqp_start(o)
+            tr = []
+            st = None
+            while True:
+                st = p.spgqp_iterate(chunk, poll=True)
+                tr.append((time.perf_counter() - t0, st.it, st.fx))
+                if st.status != capi.PASC_SPG_RUNNING:
+                    break
+            traces[name] = (tr, st)
+    fstar = traces["fp64_plain"][1].fx
+    res = {"f_star_fp64": fstar}
+    for name, (tr, st) in traces.items():
+        hit = next(((t, it) for t, it, f in tr if abs(f - fstar) <= 1e-6 * abs(fstar)), None)
+        res[name] = {"seconds": hit[0] if hit else None, "spg_it": hit[1] if hit else None,
+                     "final_rel_err": abs(st.fx - fstar) / abs(fstar), "final_it": st.it,
+                     "status": capi.STATUS_NAMES.get(st.status, st.status)}
+    a, b = res["fp64_plain"]["seconds"], res["mixed_fused"]["seconds"]
+    res["speedup_vs_fp64_plain"] = (a / b) if (a and b) else None
+    return res
+
+
+if __name__ == "__main__":
+    main()

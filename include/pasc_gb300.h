@@ -1,0 +1,239 @@
+/*
+ * pasc_gb300.h -- C ABI of the GB300 (sm_103a) FEM-H1 clustering library.
+ *
+ * This is the drop-in boundary for PASC_inference's FEM-H1 time-series clustering hot
+ * path: the gamma-step QP solved by SPGQPSolver inside the alternating TSSolver loop.  Each
+ * entry point names the reference interface it replaces (paths relative to the
+ * PASC_inference tree).  The C++ class surface in include/pasc/ and the ctypes binding in
+ * pasc_inference_gb300/ are thin layers over these functions.
+ *
+ * Conventions
+ *   - Every function returns an int status: PASC_OK (0) or a pasc_gb300_error code.  No C++
+ *     exception crosses the ABI; pasc_gb300_last_error() gives the message of the last
+ *     failure on the calling thread.  (The reference prints through TRYCXX/PetscError and
+ *     continues, include/external/petscvector/algebra/vector/petscvector.h:51, or exits
+ *     through gpuErrchk, include/external/petscvector/petscvector.cuh:12-20.)
+ *   - Host buffers are caller-owned; device buffers behind a handle are library-owned.
+ *     Entry points whose pointers are device pointers say so.  `stream` arguments are
+ *     cudaStream_t values passed as void* (NULL = the legacy default stream).
+ *   - Layouts follow the reference decomposition with R = 1 on one device:
+ *       gamma  N = K*T values, interleaved, index t*K + k
+ *              (src/petscvector/algebra/matrix/blockgraphsparse.cpp:54)
+ *       data   T*xdim values, index t*xdim + j
+ *       theta  K*xdim values, index k*xdim + j (src/petscvector/model/graphh1fem.cpp:94)
+ *   - One handle = one problem on one device with its own CUDA stream.  Calls on one handle
+ *     must not overlap; different handles may be used from different threads.
+ */
+#ifndef PASC_GB300_H
+#define PASC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PASC_GB300_ABI_VERSION 1
+
+/* ---------------------------------------------------------------------------------------
+ * status codes
+ * ------------------------------------------------------------------------------------- */
+enum pasc_gb300_error {
+    PASC_OK = 0,
+    PASC_ERR_ARG = 1,       /* invalid argument (sizes, null pointers, K out of range) */
+    PASC_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+    PASC_ERR_ALLOC = 3,     /* device or host allocation failed */
+    PASC_ERR_STATE = 4,     /* call not valid in the handle's current state */
+    PASC_ERR_NOTSUPP = 5,   /* configuration not supported by this build */
+    PASC_ERR_TIMEOUT = 6    /* a bounded device wait gave up */
+};
+
+/* Solve outcome reported in pasc_gb300_spgqp_stats.status. */
+enum pasc_gb300_solve_status {
+    PASC_SPG_RUNNING = 0,
+    PASC_SPG_CONVERGED = 1, /* a stopping test of spgqpsolver.cpp:260-274 was met */
+    PASC_SPG_MAXIT = 2,     /* maxit iterations done */
+    PASC_SPG_DAD_ZERO = 3,  /* d'Ad <= 0: the projected step vanished (the reference divides
+                               by it unguarded, spgqpsolver.cpp:182-183); x is kept */
+    PASC_SPG_NONFINITE = 4  /* a reduction came out NaN/Inf; x is kept at the last finite iterate */
+};
+
+/* Arithmetic of a handle. */
+enum pasc_gb300_precision {
+    PASC_PREC_FP64 = 0,     /* plain path: FP64 state, one kernel per reference operation,
+                               host-side step-length scalars (the reference's structure) */
+    PASC_PREC_MIXED = 1     /* fused path: FP32 gamma/gradient state, one HBM sweep per SPG
+                               iteration, FP64 reductions and step lengths on the device */
+};
+
+/* ---------------------------------------------------------------------------------------
+ * settings -- field names follow the reference's console options
+ * ------------------------------------------------------------------------------------- */
+
+/* SPGQPSolver settings: include/general/solver/spgqpsolver.h:19-36,162-202. */
+typedef struct {
+    int maxit;              /* spgqpsolver_maxit (1000) */
+    double eps;             /* spgqpsolver_eps (1e-9) */
+    int m;                  /* spgqpsolver_m: GLL memory (20), 1..64 */
+    double gamma;           /* spgqpsolver_gamma (0.9) */
+    double sigma1;          /* spgqpsolver_sigma1 (0) */
+    double sigma2;          /* spgqpsolver_sigma2 (1) */
+    double alphainit;       /* spgqpsolver_alphainit (2) */
+    int stop_difff;         /* |f - f_old| < eps (on) */
+    int stop_normgp;        /* ||d||^2 < eps */
+    int stop_normgp_normb;  /* ||d||^2 < eps*||b|| */
+    int stop_Anormgp;       /* d'Ad < eps */
+    int stop_Anormgp_normb; /* d'Ad < eps*||b|| */
+} pasc_gb300_spgqp_opts;
+
+/* SPGQPSolver results (it_last, hessmult_last, fx, gP of the reference). */
+typedef struct {
+    int it;                 /* iterations of this solve */
+    int hessmult;           /* Hessian products of this solve (1 + it, as the reference counts) */
+    int status;             /* pasc_gb300_solve_status */
+    int kernel_launches;    /* kernels launched by this solve */
+    double fx;              /* final objective 1/2 x'Ax - b'x */
+    double gP;              /* last ||d||^2 */
+    double dAd;             /* last d'Ad */
+    double time_s;          /* device time of the solve (CUDA events) */
+} pasc_gb300_spgqp_stats;
+
+/* TSSolver settings: include/general/solver/tssolver.h:13-15,117-162. */
+typedef struct {
+    int maxit;              /* tssolver_maxit (300) */
+    double eps;             /* tssolver_eps (1e-6) */
+    int init_permute;       /* tssolver_init_permute (1): blocked -> interleaved permutation of
+                               gamma at the start of every annealing run, tssolver.h:528-530 */
+    int annealing;          /* restarts (1) */
+    int relative;           /* 0: stop on |L - L_old| < eps (reference, tssolver.h:642);
+                               1: stop on |L - L_old| < eps*|L| */
+    int thetasolved;        /* 1: theta was given (TSSolver::set_solution_theta), skip theta */
+} pasc_gb300_ts_opts;
+
+typedef struct {
+    int it_last;            /* outer iterations of the kept run */
+    int it_sum;             /* outer iterations over all runs */
+    int spg_it_sum;         /* SPG iterations over the whole solve */
+    int spg_hessmult_sum;
+    int kernel_launches;
+    int L_increased;        /* outer steps where L grew (the reference prints "ERROR") */
+    double L;               /* final objective (gamma solver fx) */
+    double deltaL;          /* last |L - L_old| */
+    double aic;             /* 2 log L + K (include/general/model/graphh1fem.h:444-447) */
+    double time_s;          /* wall time of the solve */
+} pasc_gb300_ts_stats;
+
+void pasc_gb300_spgqp_default_opts(pasc_gb300_spgqp_opts *o);
+void pasc_gb300_ts_default_opts(pasc_gb300_ts_opts *o);
+
+/* ---------------------------------------------------------------------------------------
+ * library
+ * ------------------------------------------------------------------------------------- */
+int pasc_gb300_abi_version(void);
+/* Message of the last failed call on this thread ("" if none). */
+const char *pasc_gb300_last_error(void);
+/* Number of CUDA devices visible (0 on a machine without a GPU; never fails). */
+int pasc_gb300_device_count(void);
+
+/* ---------------------------------------------------------------------------------------
+ * problem handle: TSData + GraphH1FEMModel + SPGQPSolver + TSSolver state on one device.
+ * Replaces the objects the driver builds in examples/test_signal1D/test_signal1D.cpp:188-249
+ * (Decomposition(T,1,K,xdim,1), TSData::set_model, GraphH1FEMModel(tsdata, epssqr),
+ * TSSolver(tsdata)).
+ * ------------------------------------------------------------------------------------- */
+typedef struct pasc_gb300_problem pasc_gb300_problem;
+
+/* T >= 1, 1 <= K <= 32 (mixed) or <= 128 (fp64), xdim == 1.  epssqr as in
+ * GraphH1FEMModel(tsdata, epssqr) (src/petscvector/model/graphh1fem.cpp:8-65). */
+int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int precision,
+                      double epssqr, int device);
+int pasc_gb300_destroy(pasc_gb300_problem *p);
+
+/* GraphH1FEMModel::set_epssqr (include/general/model/graphh1fem.h:287-306).  scalef as the
+ * graphh1femmodel_scalef option (default 1: A = epssqr/T * A_hat, b = -residual/T). */
+int pasc_gb300_set_epssqr(pasc_gb300_problem *p, double epssqr, int scalef);
+
+/* TSData vectors (host buffers, FP64).  set_data replaces Signal1DData loading + permute
+ * (src/petscvector/data/signal1Ddata.cpp:8-52); set_gamma replaces set_random/load_gammavector
+ * (src/petscvector/data/tsdata.cpp:549-627); set_theta replaces TSSolver::set_solution_theta
+ * values (include/general/solver/tssolver.h:778-790). */
+int pasc_gb300_set_data(pasc_gb300_problem *p, const double *data);
+int pasc_gb300_set_gamma(pasc_gb300_problem *p, const double *gamma);
+int pasc_gb300_get_gamma(pasc_gb300_problem *p, double *gamma);
+int pasc_gb300_set_theta(pasc_gb300_problem *p, const double *theta);
+int pasc_gb300_get_theta(pasc_gb300_problem *p, double *theta);
+
+/* TSSolver::gammavector_permute (include/general/solver/tssolver.h:760-775 ->
+ * src/petscvector/common/decomposition.cpp:266-356): blocked k*T+t -> interleaved t*K+k. */
+int pasc_gb300_permute_gamma(pasc_gb300_problem *p);
+
+/* GraphH1FEMModel::updatebeforesolve_thetasolver (src/petscvector/model/graphh1fem.cpp:306-396,
+ * usethetainpenalty = false): theta_k = sum_t gamma_tk x_t / sum_t gamma_tk. */
+int pasc_gb300_update_theta(pasc_gb300_problem *p);
+
+/* GraphH1FEMModel::updatebeforesolve_gammasolver (graphh1fem.cpp:237-289):
+ * b_tk = -(x_t - theta_k)^2 / T.  The mixed path forms b inside its sweep from data and
+ * theta; this call only refreshes the theta it reads.  The fp64 path materialises b. */
+int pasc_gb300_update_b(pasc_gb300_problem *p);
+
+/* SPGQPSolver<PetscVector>::solve (src/petscvector/solver/spgqpsolver.cpp:55-312) on the
+ * current gamma (warm start, spgqpsolver.cpp:110-113) and the current b. */
+int pasc_gb300_spgqp_solve(pasc_gb300_problem *p, const pasc_gb300_spgqp_opts *o,
+                           pasc_gb300_spgqp_stats *st);
+
+/* The two halves of SPGQPSolver::solve, for callers that drive the iteration themselves
+ * (and for timing a fixed number of iterations).  spgqp_start runs the set-up of
+ * spgqpsolver.cpp:104-137 (||b||, projection of the start point, gradient, objective, GLL
+ * memory); spgqp_iterate runs up to n iterations of the main loop :140-297, stopping early on
+ * a stopping test or at maxit.  poll = 1 reads the device status between chunks of
+ * iterations and stops launching once the solve has ended; poll = 0 (mixed path) launches n
+ * iterations back to back with no host synchronisation.  st receives totals since the start.
+ * spgqp_solve == spgqp_start + spgqp_iterate(maxit, poll = 1). */
+int pasc_gb300_spgqp_start(pasc_gb300_problem *p, const pasc_gb300_spgqp_opts *o);
+int pasc_gb300_spgqp_iterate(pasc_gb300_problem *p, long n, int poll, pasc_gb300_spgqp_stats *st);
+/* Device time (CUDA events on the problem's stream) and kernel launches of the last
+ * spgqp_iterate call. */
+int pasc_gb300_spgqp_last_iterate(pasc_gb300_problem *p, double *ms, int *launches);
+
+/* SPGQPSolver<PetscVector>::get_fx (spgqpsolver.cpp:316-345): 1/2 (g - b)'x of the last solve. */
+int pasc_gb300_get_fx(pasc_gb300_problem *p, double *fx);
+
+/* TSSolver<VectorBase>::solve (include/general/solver/tssolver.h:492-715) with the
+ * GraphH1FEMModel hooks.  gamma_restart (nullable, N values) is what set_random() gives
+ * annealing restarts (tssolver.h:700-702). */
+int pasc_gb300_ts_solve(pasc_gb300_problem *p, const pasc_gb300_ts_opts *ts,
+                        const pasc_gb300_spgqp_opts *spg, const double *gamma_restart,
+                        pasc_gb300_ts_stats *st);
+
+/* Signal1DData::compute_abserr_reconstructed (src/petscvector/data/signal1Ddata.cpp:134-191):
+ * || sum_k theta_k gamma_k - solution ||_1, solution a host buffer of T values. */
+int pasc_gb300_abserr_reconstructed(pasc_gb300_problem *p, const double *solution, double *abserr);
+
+/* Hard labels, true argmax per t (lowest k wins ties); host buffer of T ints.  The
+ * reference's TSData::cutgamma (src/petscvector/data/tsdata.cpp:196-235) seeds its running
+ * maximum with gamma[t] instead of gamma[t*K]; this returns the intended argmax. */
+int pasc_gb300_argmax_labels(pasc_gb300_problem *p, int *labels);
+
+/* ---------------------------------------------------------------------------------------
+ * device-pointer kernels: the reference's GPU-side operations, usable on caller buffers
+ * ------------------------------------------------------------------------------------- */
+
+/* SimplexFeasibleSet_Local<PetscVector>::project -> ExternalContent::cuda_project
+ * (src/petscvector/algebra/feasibleset/simplex_local.cpp:38-65, simplex_local.cu:39-139):
+ * in-place projection of T blocks of K on the device.  The fp64 form keeps the reference's
+ * operation order (bit-identical to the host algorithm); K <= 128.  No scratch memory
+ * (the reference allocates K*T doubles for its sort). */
+int pasc_gb300_project_f64(double *x_dev, long T, int K, void *stream);
+/* FP32 form: one thread per t for K <= 8, a lane group per t with shuffles for K <= 32. */
+int pasc_gb300_project_f32(float *x_dev, long T, int K, void *stream);
+
+/* BlockGraphSparseMatrix<PetscVector>::matmult (src/petscvector/algebra/matrix/
+ * blockgraphsparse.cpp:152-194) for R = 1 without theta coefficients: y = coeff * A_hat x,
+ * matrix-free (nothing assembled).  fp64 form sums each row like the assembled CSR MatMult. */
+int pasc_gb300_fem_h1_matmult_f64(const double *x_dev, double *y_dev, long T, int K,
+                                  double coeff, void *stream);
+int pasc_gb300_fem_h1_matmult_f32(const float *x_dev, float *y_dev, long T, int K,
+                                  float coeff, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

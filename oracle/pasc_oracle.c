@@ -1,0 +1,572 @@
+/*
+ * pasc_oracle.c -- FP64 CPU restatement of PASC_inference's FEM-H1 / SPG-QP / TSSolver path.
+ *
+ * TEST INFRASTRUCTURE, NOT PRODUCT CODE: the checker for the GPU library and the timed CPU
+ * baseline.  Compiled with -ffp-contract=off so that no multiply-add is fused, which keeps
+ * the arithmetic identical on x86-64 and aarch64 hosts.
+ *
+ * With nthreads == 1 every reduction runs sequentially in index order, the order of a
+ * single-rank PETSc VecDot/VecSum on the host.  With nthreads > 1 the element-wise operations
+ * are split over OpenMP threads and reductions are summed per static chunk, then in thread
+ * order (deterministic for a fixed thread count); that mode exists for CPU-baseline timing.
+ */
+#include "pasc_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORACLE_KMAX_STACK 64
+
+static int eff_threads(int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads <= 0) return omp_get_max_threads();
+    return nthreads;
+#else
+    (void)nthreads;
+    return 1;
+#endif
+}
+
+void pasc_oracle_spg_default_opts(pasc_oracle_spg_opts *o)
+{
+    /* include/general/solver/spgqpsolver.h:19-36 */
+    o->maxit = 1000;
+    o->eps = 1e-9;
+    o->m = 20;
+    o->gamma = 0.9;
+    o->sigma1 = 0.0;
+    o->sigma2 = 1.0;
+    o->alphainit = 2.0;
+    o->stop_difff = 1;
+    o->stop_normgp = 0;
+    o->stop_normgp_normb = 0;
+    o->stop_Anormgp = 0;
+    o->stop_Anormgp_normb = 0;
+}
+
+void pasc_oracle_ts_default_opts(pasc_oracle_ts_opts *o)
+{
+    /* include/general/solver/tssolver.h:13-15 */
+    o->maxit = 300;
+    o->eps = 1e-6;
+    o->init_permute = 1;
+    o->annealing = 1;
+    o->relative = 0;
+    o->thetasolved = 0;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* vector primitives in PETSc's host semantics                                            */
+/* ------------------------------------------------------------------------------------- */
+
+/* VecDot(x, y) for real vectors: sum_i x_i*y_i, sequential. */
+static double vdot(const double *x, const double *y, long n, int nth)
+{
+    if (nth <= 1) {
+        double s = 0.0;
+        for (long i = 0; i < n; i++) s += x[i] * y[i];
+        return s;
+    }
+    double part[256];
+    int nt = nth > 256 ? 256 : nth;
+    int used = 1;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+    {
+        int id = 0, cnt = 1;
+#ifdef _OPENMP
+        id = omp_get_thread_num();
+        cnt = omp_get_num_threads();
+#endif
+        long lo = n * id / cnt, hi = n * (id + 1) / cnt;
+        double s = 0.0;
+        for (long i = lo; i < hi; i++) s += x[i] * y[i];
+        part[id] = s;
+        if (id == 0) used = cnt;
+    }
+    double tot = 0.0;
+    for (int j = 0; j < used; j++) tot += part[j];
+    return tot;
+}
+
+/* VecAXPY(y, a, x): y_i = y_i + a*x_i */
+static void vaxpy(double *y, double a, const double *x, long n, int nth)
+{
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
+#endif
+    for (long i = 0; i < n; i++) y[i] = y[i] + a * x[i];
+}
+
+/* VecScale(y, a): y_i = a*y_i */
+static void vscale(double *y, double a, long n, int nth)
+{
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
+#endif
+    for (long i = 0; i < n; i++) y[i] = a * y[i];
+}
+
+static void vcopy(double *dst, const double *src, long n, int nth)
+{
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
+#endif
+    for (long i = 0; i < n; i++) dst[i] = src[i];
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* simplex projection                                                                     */
+/* include/general/algebra/feasibleset/simplex_local.h:153-249 (host project_sub) and     */
+/* src/petscvector/algebra/feasibleset/simplex_local.cu:48-139 (same algorithm on device) */
+/* ------------------------------------------------------------------------------------- */
+
+/* Bubble sort with last-swap bound, ascending, stable: simplex_local.h:153-173 */
+static void sort_bubble(double *y, int n)
+{
+    int m = n;
+    while (m > 0) {
+        int mnew = 0;
+        for (int i = 1; i < m; i++) {
+            if (y[i] < y[i - 1]) {
+                double sw = y[i];
+                y[i] = y[i - 1];
+                y[i - 1] = sw;
+                mnew = i;
+            }
+        }
+        m = mnew;
+    }
+}
+
+/* One t-block of K values: simplex_local.h:176-246 */
+static void project_block(double *x, int K, double *y)
+{
+    int inside = 1;
+    double sum = 0.0;
+    for (int k = 0; k < K; k++) {
+        if (x[k] < 0.0) inside = 0;
+        sum += x[k];
+    }
+    if (sum != 1) inside = 0; /* exact equality test, simplex_local.h:195 */
+    if (inside) return;
+
+    for (int k = 0; k < K; k++) y[k] = x[k];
+    sort_bubble(y, K);
+
+    double t_hat = 0.0;
+    int i = K - 1;
+    while (i >= 1) {
+        double sum_y = 0.0;
+        for (int j = i; j < K; j++) sum_y += y[j]; /* recomputed from y[i] upwards */
+        double ti = (sum_y - 1.0) / (double)(K - i);
+        if (ti >= y[i - 1]) {
+            t_hat = ti;
+            i = -1;
+        } else {
+            i = i - 1;
+        }
+    }
+    if (i == 0) t_hat = (sum - 1.0) / (double)K; /* sum over the unsorted block */
+
+    for (int k = 0; k < K; k++) {
+        double ti = x[k] - t_hat;
+        x[k] = ti > 0.0 ? ti : 0.0;
+    }
+}
+
+void pasc_oracle_project(double *x, long T, int K, int nthreads)
+{
+    int nth = eff_threads(nthreads);
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nth) if (nth > 1)
+#endif
+    {
+        double ystack[ORACLE_KMAX_STACK];
+        double *y = K <= ORACLE_KMAX_STACK ? ystack : (double *)malloc(sizeof(double) * (size_t)K);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (long t = 0; t < T; t++) project_block(x + t * (long)K, K, y);
+        if (y != ystack) free(y);
+    }
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* FEM-H1 operator                                                                        */
+/* Assembly: src/petscvector/algebra/matrix/blockgraphsparse.cpp:51-109 with R = 1 and a  */
+/* graph without edges (graphh1fem.cpp:35-46): diagonal Wsum = 2 at t in {0,T-1}, 4       */
+/* inside, 0 when T == 1; off-diagonals -2 at column t-1 and t+1 (stride K).              */
+/* Product: MatMult row by row over columns in ascending order starting from 0.0, then    */
+/* VecScale by the coefficient (spgqpsolver.cpp:122-123,164-165).                          */
+/* ------------------------------------------------------------------------------------- */
+void pasc_oracle_fem_h1_matmult(const double *x, double *y, long T, int K, double coeff, int nthreads)
+{
+    int nth = eff_threads(nthreads);
+    long N = T * (long)K;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
+#endif
+    for (long i = 0; i < N; i++) {
+        long t = i / K;
+        double sum = 0.0;
+        if (T == 1) {
+            sum += 0.0 * x[i];
+        } else {
+            double wsum = (t == 0 || t == T - 1) ? 2.0 : 4.0;
+            if (t > 0) sum += -2.0 * x[i - K];
+            sum += wsum * x[i];
+            if (t < T - 1) sum += -2.0 * x[i + K];
+        }
+        y[i] = sum;
+    }
+    vscale(y, coeff, N, nth);
+}
+
+double pasc_oracle_A_coeff(double epssqr, long T, int scalef)
+{
+    /* graphh1fem.cpp:146-151 and graphh1fem.h:293-298 (T_reduced == T) */
+    double coeff = epssqr;
+    if (scalef) coeff *= (1.0 / ((double)T));
+    else coeff *= ((double)T / ((double)T));
+    return coeff;
+}
+
+double pasc_oracle_b_coeff(long T, int scalef)
+{
+    /* graphh1fem.cpp:280-283 */
+    double coeff = -1.0;
+    if (scalef) coeff *= (1.0 / ((double)T));
+    return coeff;
+}
+
+/* graphh1fem.cpp:258-264 (xdim = 1) followed by VecScale(b, bscale) at :286.
+ * For xdim > 1 the residual is the squared Euclidean distance summed over j in order. */
+void pasc_oracle_residual_b(const double *data, const double *theta, double *b, long T, int K,
+                            int xdim, double bscale, int nthreads)
+{
+    int nth = eff_threads(nthreads);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
+#endif
+    for (long t = 0; t < T; t++) {
+        for (int k = 0; k < K; k++) {
+            double r;
+            if (xdim == 1) {
+                double dv = data[t] - theta[k];
+                r = dv * dv;
+            } else {
+                r = 0.0;
+                for (int j = 0; j < xdim; j++) {
+                    double dv = data[t * (long)xdim + j] - theta[k * (long)xdim + j];
+                    r += dv * dv;
+                }
+            }
+            b[t * (long)K + k] = r;
+        }
+    }
+    vscale(b, bscale, T * (long)K, nth);
+}
+
+/* graphh1fem.cpp:347-380, usethetainpenalty = false: per k, VecDot(data, gamma_k) and
+ * VecSum(gamma_k) over the stride-K sub-vector, theta_k = ratio or 0. */
+void pasc_oracle_theta_update(const double *gamma, const double *data, double *theta, long T,
+                              int K, int xdim, int nthreads)
+{
+    (void)nthreads;
+    for (int k = 0; k < K; k++) {
+        double gsum = 0.0;
+        for (long t = 0; t < T; t++) gsum += gamma[t * (long)K + k];
+        for (int j = 0; j < xdim; j++) {
+            double gx = 0.0;
+            for (long t = 0; t < T; t++) gx += data[t * (long)xdim + j] * gamma[t * (long)K + k];
+            theta[k * (long)xdim + j] = (gsum != 0) ? gx / gsum : 0.0;
+        }
+    }
+}
+
+/* src/petscvector/common/decomposition.cpp:280-356 with R = 1, one rank:
+ * new[t*K + k] = orig[k*T + t]. */
+void pasc_oracle_permute_blocked_to_interleaved(const double *orig, double *out, long T, int K)
+{
+    for (int k = 0; k < K; k++)
+        for (long t = 0; t < T; t++) out[t * (long)K + k] = orig[k * T + t];
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* GLL memory: src/general/solver/spg_fs.cpp:7-63                                         */
+/* ------------------------------------------------------------------------------------- */
+typedef struct {
+    int m;
+    int last_idx;
+    double *fs;
+} spg_fs;
+
+static void fs_init(spg_fs *s, double fx)
+{
+    for (int i = 0; i < s->m; i++) s->fs[i] = fx;
+    s->last_idx = 0;
+}
+
+static double fs_get_max(const spg_fs *s)
+{
+    double mx = s->fs[0];
+    for (int i = 0; i < s->m; i++)
+        if (s->fs[i] > mx) mx = s->fs[i];
+    return mx;
+}
+
+static void fs_update(spg_fs *s, double fx)
+{
+    s->last_idx++;
+    if (s->last_idx >= s->m) s->last_idx = 0;
+    s->fs[s->last_idx] = fx;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* SPG-QP: src/petscvector/solver/spgqpsolver.cpp:55-312, get_fx :316-345,                */
+/* compute_dots :348-367 (three separate VecDot calls).                                   */
+/* ------------------------------------------------------------------------------------- */
+static double get_fx(const double *g, const double *b, const double *x, double *temp, long n, int nth)
+{
+    vcopy(temp, g, n, nth);      /* VecCopy(g, temp)        :336 */
+    vaxpy(temp, -1.0, b, n, nth); /* VecAXPY(temp, -1, b)   :337 */
+    double tempt = vdot(x, temp, n, nth); /* VecDot(x, temp) :338 */
+    return 0.5 * tempt;
+}
+
+int pasc_oracle_spgqp_solve(const double *b, double *x, long T, int K, double coeff,
+                            const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r,
+                            double *trace, int nthreads)
+{
+    int nth = eff_threads(nthreads);
+    long n = T * (long)K;
+    double *g = (double *)malloc(sizeof(double) * (size_t)n);
+    double *d = (double *)malloc(sizeof(double) * (size_t)n);
+    double *Ad = (double *)malloc(sizeof(double) * (size_t)n);
+    double *temp = (double *)malloc(sizeof(double) * (size_t)n);
+    spg_fs fs;
+    fs.m = o->m;
+    fs.last_idx = 0;
+    fs.fs = (double *)malloc(sizeof(double) * (size_t)(o->m > 0 ? o->m : 1));
+    if (!g || !d || !Ad || !temp || !fs.fs) {
+        free(g); free(d); free(Ad); free(temp); free(fs.fs);
+        return -1;
+    }
+
+    int it = 0, hessmult = 0;
+    double fx, fx_old, fx_max, xi, beta_bar, beta_hat, beta = 0.0, dd = 0.0, gd = 0.0, dAd = 0.0, alpha_bb;
+
+    double normb = sqrt(vdot(b, b, n, nth)); /* VecNorm(b, NORM_2)  :104 */
+    alpha_bb = o->alphainit;                 /* :108 */
+
+    pasc_oracle_project(x, T, K, nth); /* :116 */
+
+    pasc_oracle_fem_h1_matmult(x, g, T, K, coeff, nth); /* MatMult + VecScale :122-123 */
+    hessmult += 1;
+    vaxpy(g, -1.0, b, n, nth); /* :128 */
+
+    fx = get_fx(g, b, x, temp, n, nth); /* :133 */
+    fx_old = DBL_MAX;
+    fs_init(&fs, fx);
+    if (trace) {
+        trace[0] = fx;
+        for (int q = 1; q < 8; q++) trace[q] = 0.0;
+    }
+
+    while (it < o->maxit) {
+        it += 1;
+
+        vcopy(d, x, n, nth);              /* :146 */
+        vaxpy(d, -alpha_bb, g, n, nth);   /* :147 */
+        pasc_oracle_project(d, T, K, nth); /* :153 */
+        vaxpy(d, -1.0, x, n, nth);        /* :158 */
+
+        pasc_oracle_fem_h1_matmult(d, Ad, T, K, coeff, nth); /* :164-165 */
+        hessmult += 1;
+
+        dd = vdot(d, d, n, nth);  /* :357 */
+        dAd = vdot(d, Ad, n, nth); /* :360 */
+        gd = vdot(d, g, n, nth);  /* :363 */
+
+        fx_max = fs_get_max(&fs); /* :176 */
+
+        /* :182-195 */
+        xi = (fx_max - fx) / dAd;
+        beta_bar = -gd / dAd;
+        beta_hat = o->gamma * beta_bar + sqrt(o->gamma * o->gamma * beta_bar * beta_bar + 2 * xi);
+        if (beta_hat < o->sigma1) beta_hat = o->sigma1;
+        if (beta_hat < o->sigma2) beta = beta_hat;
+        else beta = o->sigma2;
+
+        vaxpy(x, beta, d, n, nth);  /* :200 */
+        vaxpy(g, beta, Ad, n, nth); /* :201 */
+
+        fx_old = fx;                          /* :207 */
+        fx = get_fx(g, b, x, temp, n, nth);   /* :209 */
+        fs_update(&fs, fx);                   /* :210 */
+
+        alpha_bb = dd / dAd; /* :216 */
+
+        if (trace) {
+            double *row = trace + 8 * (long)it;
+            row[0] = fx;
+            row[1] = dd;
+            row[2] = dAd;
+            row[3] = gd;
+            row[4] = fx_max;
+            row[5] = beta;
+            row[6] = alpha_bb;
+            row[7] = 0.0;
+        }
+
+        /* :260-274 */
+        if (o->stop_difff && fabs(fx - fx_old) < o->eps) break;
+        if (o->stop_normgp && dd < o->eps) break;
+        if (o->stop_normgp_normb && dd < o->eps * normb) break;
+        if (o->stop_Anormgp && dAd < o->eps) break;
+        if (o->stop_Anormgp_normb && dAd < o->eps * normb) break;
+    }
+
+    if (r) {
+        r->it = it;
+        r->hessmult = hessmult;
+        r->fx = fx;
+        r->gP = dd;
+        r->dAd = dAd;
+        r->normb = normb;
+    }
+    free(g); free(d); free(Ad); free(temp); free(fs.fs);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* TSSolver::solve: include/general/solver/tssolver.h:492-715 with the GraphH1FEMModel    */
+/* hooks of src/petscvector/model/graphh1fem.cpp (fem not reduced, R = 1).                */
+/* ------------------------------------------------------------------------------------- */
+int pasc_oracle_tssolver_solve(const double *data, double *gamma, double *theta, long T, int K,
+                               int xdim, double epssqr, int scalef,
+                               const pasc_oracle_ts_opts *ts, const pasc_oracle_spg_opts *spg,
+                               const double *gamma_restart, pasc_oracle_ts_result *r,
+                               double *trace_L, int nthreads)
+{
+    int nth = eff_threads(nthreads);
+    long n = T * (long)K;
+    double *b = (double *)malloc(sizeof(double) * (size_t)n);
+    double *perm = (double *)malloc(sizeof(double) * (size_t)n);
+    double *gbest = NULL, *tbest = NULL;
+    int annealing = ts->annealing > 0 ? ts->annealing : 1;
+    if (annealing > 1) {
+        gbest = (double *)malloc(sizeof(double) * (size_t)n);
+        tbest = (double *)malloc(sizeof(double) * (size_t)K * (size_t)xdim);
+    }
+    if (!b || !perm || (annealing > 1 && (!gbest || !tbest))) {
+        free(b); free(perm); free(gbest); free(tbest);
+        return -1;
+    }
+
+    double coeffA = pasc_oracle_A_coeff(epssqr, T, scalef);
+    double coeffB = pasc_oracle_b_coeff(T, scalef);
+    double best_aic = DBL_MAX; /* TSData aic starts at max */
+    int it_sum = 0, spg_it_sum = 0, spg_hm_sum = 0, increased = 0;
+    double keepL = DBL_MAX, keepdL = DBL_MAX, keepaic = DBL_MAX;
+    int keepit = 0;
+    long trace_pos = 0;
+
+    for (int a = 0; a < annealing; a++) {
+        if (ts->init_permute) { /* :528-530 */
+            pasc_oracle_permute_blocked_to_interleaved(gamma, perm, T, K);
+            memcpy(gamma, perm, sizeof(double) * (size_t)n);
+        }
+        double L = DBL_MAX, L_old, deltaL = DBL_MAX;
+        int it;
+        for (it = 0; it < ts->maxit; it++) {
+            if (!ts->thetasolved) /* :550 */
+                pasc_oracle_theta_update(gamma, data, theta, T, K, xdim, nth);
+
+            pasc_oracle_residual_b(data, theta, b, T, K, xdim, coeffB, nth); /* :586 */
+            pasc_oracle_spg_result sr;
+            pasc_oracle_spgqp_solve(b, gamma, T, K, coeffA, spg, &sr, NULL, nth); /* :590 */
+            spg_it_sum += sr.it;
+            spg_hm_sum += sr.hessmult;
+
+            L_old = L; /* :618-620 */
+            L = sr.fx;
+            deltaL = fabs(L - L_old);
+            if (trace_L) trace_L[trace_pos++] = L;
+            if (L - L_old > 0) increased++; /* :637-639 prints ERROR and continues */
+            if (ts->relative ? (deltaL < ts->eps * fabs(L)) : (deltaL < ts->eps)) break;
+        }
+        it_sum += it;
+        double aic = 2 * log(L) + K; /* graphh1fem.h:444-447 */
+        if ((annealing <= 1) || (aic < best_aic && annealing > 1)) {
+            if (aic < best_aic && annealing > 1) {
+                memcpy(gbest, gamma, sizeof(double) * (size_t)n);
+                memcpy(tbest, theta, sizeof(double) * (size_t)K * (size_t)xdim);
+            }
+            best_aic = aic;
+            keepL = L;
+            keepdL = deltaL;
+            keepaic = aic;
+            keepit = it;
+        }
+        if (a < annealing - 1 && gamma_restart) /* :700-702 set_random */
+            memcpy(gamma, gamma_restart, sizeof(double) * (size_t)n);
+    }
+    if (annealing > 1) {
+        memcpy(gamma, gbest, sizeof(double) * (size_t)n);
+        memcpy(theta, tbest, sizeof(double) * (size_t)K * (size_t)xdim);
+    }
+    if (r) {
+        r->it_last = keepit;
+        r->it_sum = it_sum;
+        r->spg_it_sum = spg_it_sum;
+        r->spg_hessmult_sum = spg_hm_sum;
+        r->L = keepL;
+        r->deltaL = keepdL;
+        r->aic = keepaic;
+        r->L_increased = increased;
+    }
+    free(b); free(perm); free(gbest); free(tbest);
+    return 0;
+}
+
+/* src/petscvector/data/signal1Ddata.cpp:134-191: NORM_1 of -solution + sum_k theta_k gamma_k,
+ * accumulated k by k with VecAXPY. */
+double pasc_oracle_abserr_reconstructed(const double *gamma, const double *theta,
+                                        const double *solution, long T, int K)
+{
+    double s = 0.0;
+    for (long t = 0; t < T; t++) {
+        double v = -solution[t];
+        for (int k = 0; k < K; k++) v = v + theta[k] * gamma[t * (long)K + k];
+        s += fabs(v);
+    }
+    return s;
+}
+
+/* True argmax (lowest k wins ties).  The reference's TSData::cutgamma
+ * (src/petscvector/data/tsdata.cpp:208-221) seeds the running maximum with gamma_arr[t]
+ * instead of gamma_arr[t*K]; this helper follows the intended argmax. */
+void pasc_oracle_argmax_labels(const double *gamma, int *labels, long T, int K)
+{
+    for (long t = 0; t < T; t++) {
+        int best = 0;
+        double bv = gamma[t * (long)K];
+        for (int k = 1; k < K; k++) {
+            double v = gamma[t * (long)K + k];
+            if (v > bv) {
+                bv = v;
+                best = k;
+            }
+        }
+        labels[t] = best;
+    }
+}

@@ -1,0 +1,375 @@
+"""GB300-native FEM-H1 time-series clustering: the host-side mirror of the reference's
+class surface over the C ABI of include/pasc_gb300.h.
+
+Class names, constructor arguments and option names follow PASC_inference:
+  Decomposition(T, R, K, xdim, DDT_size)        include/general/common/decomposition.h:55
+  Signal1DData(filename | array)                 include/general/data/signal1Ddata.h
+  GraphH1FEMModel(tsdata, epssqr, fem=None, usethetainpenalty=False)
+                                                 include/general/model/graphh1fem.h:75
+  TSSolver(tsdata, annealing=1)                  include/general/solver/tssolver.h:80-104
+  SPGQPSolver (reached as TSSolver.get_gammasolver())   include/general/solver/spgqpsolver.h:118-151
+Options use the reference's console keys (spgqpsolver_maxit, tssolver_eps, ...), passed as a
+dict.  All computation runs on the GPU through libpasc_gb300.so; nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import (PASC_PREC_FP64, PASC_PREC_MIXED, PascError, SpgqpOpts, SpgqpStats, TsOpts,
+                   TsStats, check, load)
+
+__all__ = ["Problem", "Decomposition", "Signal1DData", "TSData", "GraphH1FEMModel", "TSSolver",
+           "SPGQPSolver", "PascError", "PASC_PREC_FP64", "PASC_PREC_MIXED", "capi"]
+
+_SPG_KEYS = {"spgqpsolver_maxit": "maxit", "spgqpsolver_eps": "eps", "spgqpsolver_m": "m",
+             "spgqpsolver_gamma": "gamma", "spgqpsolver_sigma1": "sigma1",
+             "spgqpsolver_sigma2": "sigma2", "spgqpsolver_alphainit": "alphainit",
+             "spgqpsolver_stop_difff": "stop_difff", "spgqpsolver_stop_normgp": "stop_normgp",
+             "spgqpsolver_stop_normgp_normb": "stop_normgp_normb",
+             "spgqpsolver_stop_Anormgp": "stop_Anormgp",
+             "spgqpsolver_stop_Anormgp_normb": "stop_Anormgp_normb"}
+_TS_KEYS = {"tssolver_maxit": "maxit", "tssolver_eps": "eps",
+            "tssolver_init_permute": "init_permute"}
+
+
+def spg_opts_from(options: dict | None) -> SpgqpOpts:
+    o = capi.spgqp_opts()
+    for k, v in (options or {}).items():
+        if k in _SPG_KEYS:
+            setattr(o, _SPG_KEYS[k], type(getattr(o, _SPG_KEYS[k]))(v))
+    return o
+
+
+def ts_opts_from(options: dict | None) -> TsOpts:
+    o = capi.ts_opts()
+    for k, v in (options or {}).items():
+        if k in _TS_KEYS:
+            setattr(o, _TS_KEYS[k], type(getattr(o, _TS_KEYS[k]))(v))
+    return o
+
+
+class Problem:
+    """One FEM-H1 problem on one GPU (a pasc_gb300_problem handle)."""
+
+    def __init__(self, T: int, K: int, epssqr: float = 1.0, precision: int = PASC_PREC_MIXED,
+                 xdim: int = 1, device: int = 0):
+        L = load()
+        h = C.c_void_p()
+        check(L.pasc_gb300_create(C.byref(h), int(T), int(K), int(xdim), int(precision),
+                                  float(epssqr), int(device)))
+        self._h = h
+        self.T, self.K, self.xdim, self.precision = int(T), int(K), int(xdim), int(precision)
+        self.epssqr = float(epssqr)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().pasc_gb300_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # TSData vectors
+    def set_epssqr(self, epssqr: float, scalef: bool = True):
+        self.epssqr = float(epssqr)
+        check(load().pasc_gb300_set_epssqr(self._h, float(epssqr), 1 if scalef else 0))
+
+    def set_data(self, data):
+        check(load().pasc_gb300_set_data(self._h, np.ascontiguousarray(data, dtype=np.float64)))
+
+    def set_gamma(self, gamma):
+        check(load().pasc_gb300_set_gamma(self._h, np.ascontiguousarray(gamma, dtype=np.float64)))
+
+    def get_gamma(self) -> np.ndarray:
+        out = np.empty(self.T * self.K)
+        check(load().pasc_gb300_get_gamma(self._h, out))
+        return out
+
+    def set_theta(self, theta):
+        check(load().pasc_gb300_set_theta(self._h, np.ascontiguousarray(theta, dtype=np.float64)))
+
+    def get_theta(self) -> np.ndarray:
+        out = np.empty(self.K * self.xdim)
+        check(load().pasc_gb300_get_theta(self._h, out))
+        return out
+
+    # model hooks
+    def permute_gamma(self):
+        check(load().pasc_gb300_permute_gamma(self._h))
+
+    def update_theta(self):
+        check(load().pasc_gb300_update_theta(self._h))
+
+    def update_b(self):
+        check(load().pasc_gb300_update_b(self._h))
+
+    # solvers
+    def spgqp_solve(self, opts: SpgqpOpts | None = None) -> SpgqpStats:
+        st = SpgqpStats()
+        check(load().pasc_gb300_spgqp_solve(self._h, C.byref(opts or capi.spgqp_opts()), C.byref(st)))
+        return st
+
+    def spgqp_start(self, opts: SpgqpOpts | None = None):
+        check(load().pasc_gb300_spgqp_start(self._h, C.byref(opts or capi.spgqp_opts())))
+
+    def spgqp_iterate(self, n: int, poll: bool = True) -> SpgqpStats:
+        st = SpgqpStats()
+        check(load().pasc_gb300_spgqp_iterate(self._h, int(n), 1 if poll else 0, C.byref(st)))
+        return st
+
+    def spgqp_last_iterate(self):
+        ms = C.c_double()
+        n = C.c_int()
+        check(load().pasc_gb300_spgqp_last_iterate(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def get_fx(self) -> float:
+        v = C.c_double()
+        check(load().pasc_gb300_get_fx(self._h, C.byref(v)))
+        return v.value
+
+    def ts_solve(self, ts: TsOpts | None = None, spg: SpgqpOpts | None = None,
+                 gamma_restart=None) -> TsStats:
+        st = TsStats()
+        gr = None
+        if gamma_restart is not None:
+            gr = np.ascontiguousarray(gamma_restart, dtype=np.float64)
+        check(load().pasc_gb300_ts_solve(self._h, C.byref(ts or capi.ts_opts()),
+                                         C.byref(spg or capi.spgqp_opts()),
+                                         gr.ctypes.data if gr is not None else None, C.byref(st)))
+        return st
+
+    def abserr_reconstructed(self, solution) -> float:
+        v = C.c_double()
+        check(load().pasc_gb300_abserr_reconstructed(
+            self._h, np.ascontiguousarray(solution, dtype=np.float64), C.byref(v)))
+        return v.value
+
+    def argmax_labels(self) -> np.ndarray:
+        out = np.empty(self.T, dtype=np.int32)
+        check(load().pasc_gb300_argmax_labels(self._h, out))
+        return out
+
+
+# ------------------------------------------------------------------------------------------
+# mirror of the reference classes on the path
+# ------------------------------------------------------------------------------------------
+class Decomposition:
+    """Decomposition<VectorBase>(T, R, K, xdim, DDT_size): layouts of one GPU (R = 1)."""
+
+    def __init__(self, T: int, R: int, K: int, xdim: int = 1, DDT_size: int = 1):
+        if R != 1:
+            raise PascError(capi.PASC_ERR_NOTSUPP, "spatial graphs (R > 1) are not supported")
+        if DDT_size != 1:
+            raise PascError(capi.PASC_ERR_NOTSUPP, "one GPU per problem: DDT_size must be 1")
+        self.T, self.R, self.K, self.xdim = int(T), 1, int(K), int(xdim)
+
+    def get_T(self):
+        return self.T
+
+    def get_K(self):
+        return self.K
+
+    def get_R(self):
+        return self.R
+
+    def get_xdim(self):
+        return self.xdim
+
+
+class TSData:
+    """TSData<VectorBase>: data, gamma and theta vectors of one time series."""
+
+    def __init__(self, decomposition: Decomposition | None = None, data=None):
+        self.decomposition = decomposition
+        self.datavector = None if data is None else np.ascontiguousarray(data, dtype=np.float64)
+        self.gammavector = None
+        self.thetavector = None
+        self.model = None
+        self.aic = np.finfo(np.float64).max
+
+    def set_decomposition(self, decomposition: Decomposition):
+        self.decomposition = decomposition
+
+    def set_model(self, model):
+        self.model = model
+
+    def get_T(self):
+        return self.decomposition.get_T()
+
+    def get_K(self):
+        return self.decomposition.get_K()
+
+    def get_xdim(self):
+        return self.decomposition.get_xdim()
+
+    def get_datavector(self):
+        return self.datavector
+
+    def get_gammavector(self):
+        if self.model is not None:
+            self.gammavector = self.model.problem.get_gamma()
+        return self.gammavector
+
+    def get_thetavector(self):
+        if self.model is not None:
+            self.thetavector = self.model.problem.get_theta()
+        return self.thetavector
+
+    def get_aic(self):
+        return self.aic
+
+    def set_aic(self, aic):
+        self.aic = aic
+
+    def load_gammavector(self, gamma0):
+        """TSData::load_gammavector: gamma0 as an array or a PETSc binary file (blocked layout
+        as the reference writes it, permuted to the interleaved layout)."""
+        if isinstance(gamma0, str):
+            from .petscio import load_vec
+            gamma0 = load_vec(gamma0)
+        self.model.problem.set_gamma(gamma0)
+        self.model.problem.permute_gamma()
+
+    def cutgamma(self):
+        """Hard assignment: gamma_tk = 1 for the argmax k (true argmax, see the C ABI note)."""
+        lab = self.model.problem.argmax_labels()
+        g = np.zeros((self.get_T(), self.get_K()))
+        g[np.arange(self.get_T()), lab] = 1.0
+        self.model.problem.set_gamma(g.ravel())
+
+
+class Signal1DData(TSData):
+    """Signal1DData<VectorBase>(filename): a 1-D signal (PETSc binary file or array)."""
+
+    def __init__(self, filename_or_data):
+        if isinstance(filename_or_data, str):
+            from .petscio import load_vec
+            data = load_vec(filename_or_data)
+        else:
+            data = np.ascontiguousarray(filename_or_data, dtype=np.float64)
+        super().__init__(None, data)
+        self.Tpreliminary = data.size
+
+    def get_Tpreliminary(self):
+        return self.Tpreliminary
+
+    def compute_abserr_reconstructed(self, solution) -> float:
+        return self.model.problem.abserr_reconstructed(solution)
+
+    def save_signal1d(self, prefix: str):
+        """saveSignal1D: <prefix>_gamma.bin (blocked layout) and <prefix>_recovered.bin."""
+        from .petscio import save_vec
+        T, K = self.get_T(), self.get_K()
+        g = self.get_gammavector().reshape(T, K)
+        th = self.get_thetavector()
+        save_vec(prefix + "_gamma.bin", g.T.ravel())
+        save_vec(prefix + "_recovered.bin", g @ th)
+
+
+class GraphH1FEMModel:
+    """GraphH1FEMModel<VectorBase>(tsdata, epssqr, fem=None, usethetainpenalty=False).
+    Creates the GPU problem; the initial gamma is tsdata's gamma0 (or uniform [0,1) values of
+    the given seed, the reference's set_random) in the blocked layout."""
+
+    def __init__(self, tsdata: TSData, epssqr: float, fem=None, usethetainpenalty: bool = False,
+                 precision: int = PASC_PREC_MIXED, gamma0=None, seed: int = 13, device: int = 0):
+        if fem is not None and getattr(fem, "fem_reduce", 1.0) != 1.0:
+            raise PascError(capi.PASC_ERR_NOTSUPP, "FEM reduction (fem_reduce < 1) is not supported")
+        if usethetainpenalty:
+            raise PascError(capi.PASC_ERR_NOTSUPP, "usethetainpenalty is not supported")
+        self.tsdata = tsdata
+        self.epssqr = float(epssqr)
+        T, K = tsdata.get_T(), tsdata.get_K()
+        self.problem = Problem(T, K, epssqr, precision=precision, xdim=tsdata.get_xdim(), device=device)
+        self.problem.set_data(tsdata.get_datavector())
+        if gamma0 is None:
+            from .datagen import uniform
+            gamma0 = uniform(seed, 0, T * K)
+        self.problem.set_gamma(gamma0)
+        self.problem.set_theta(np.zeros(K * tsdata.get_xdim()))
+        tsdata.set_model(self)
+
+    def set_epssqr(self, epssqr: float):
+        self.epssqr = float(epssqr)
+        self.problem.set_epssqr(epssqr)
+
+    def get_aic(self, L: float) -> float:
+        return 2 * np.log(L) + self.tsdata.get_K()
+
+    def get_name(self):
+        return "Graph-H1-FEM Time-Series Model"
+
+
+class SPGQPSolver:
+    """SPGQPSolver<VectorBase> on the model's QP (gamma step)."""
+
+    def __init__(self, model: GraphH1FEMModel, options: dict | None = None):
+        self.model = model
+        self.opts = spg_opts_from(options)
+        self.it_sum = 0
+        self.hessmult_sum = 0
+        self.last: SpgqpStats | None = None
+
+    def solve(self):
+        self.last = self.model.problem.spgqp_solve(self.opts)
+        self.it_sum += self.last.it
+        self.hessmult_sum += self.last.hessmult
+
+    def get_fx(self) -> float:
+        return self.model.problem.get_fx()
+
+    def get_it(self) -> int:
+        return self.it_sum
+
+    def get_hessmult(self) -> int:
+        return self.hessmult_sum
+
+
+class TSSolver:
+    """TSSolver<VectorBase>(tsdata, annealing): the alternating theta/gamma loop."""
+
+    def __init__(self, tsdata: TSData, annealing: int = 1, options: dict | None = None):
+        self.tsdata = tsdata
+        self.model = tsdata.model
+        self.annealing = int(annealing)
+        self.options = dict(options or {})
+        self.gammasolver = SPGQPSolver(self.model, self.options)
+        self.thetasolved = False
+        self.L = np.finfo(np.float64).max
+        self.stats: TsStats | None = None
+
+    def set_solution_theta(self, theta):
+        self.model.problem.set_theta(theta)
+        self.thetasolved = True
+
+    def set_annealing(self, annealing: int):
+        self.annealing = int(annealing)
+
+    def solve(self, gamma_restart=None):
+        ts = ts_opts_from(self.options)
+        ts.annealing = self.annealing
+        ts.thetasolved = 1 if self.thetasolved else 0
+        self.stats = self.model.problem.ts_solve(ts, self.gammasolver.opts, gamma_restart)
+        self.L = self.stats.L
+        self.gammasolver.it_sum += self.stats.spg_it_sum
+        self.tsdata.set_aic(self.stats.aic)
+        return self.stats
+
+    def get_L(self) -> float:
+        return self.L
+
+    def get_gammasolver(self) -> SPGQPSolver:
+        return self.gammasolver

@@ -1,0 +1,145 @@
+"""ctypes binding of the C ABI in include/pasc_gb300.h.
+
+This is the binding a Python caller of the reference's path would add: every function of
+the header with its argument types.  Loading fails loudly when libpasc_gb300.so has not
+been built (there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libpasc_gb300.so")
+
+PASC_OK = 0
+PASC_ERR_ARG, PASC_ERR_CUDA, PASC_ERR_ALLOC, PASC_ERR_STATE, PASC_ERR_NOTSUPP, PASC_ERR_TIMEOUT = 1, 2, 3, 4, 5, 6
+PASC_SPG_RUNNING, PASC_SPG_CONVERGED, PASC_SPG_MAXIT, PASC_SPG_DAD_ZERO, PASC_SPG_NONFINITE = 0, 1, 2, 3, 4
+PASC_PREC_FP64, PASC_PREC_MIXED = 0, 1
+
+STATUS_NAMES = {0: "running", 1: "converged", 2: "maxit", 3: "dAd_zero", 4: "nonfinite"}
+
+
+class SpgqpOpts(C.Structure):
+    _fields_ = [
+        ("maxit", C.c_int), ("eps", C.c_double), ("m", C.c_int), ("gamma", C.c_double),
+        ("sigma1", C.c_double), ("sigma2", C.c_double), ("alphainit", C.c_double),
+        ("stop_difff", C.c_int), ("stop_normgp", C.c_int), ("stop_normgp_normb", C.c_int),
+        ("stop_Anormgp", C.c_int), ("stop_Anormgp_normb", C.c_int),
+    ]
+
+
+class SpgqpStats(C.Structure):
+    _fields_ = [("it", C.c_int), ("hessmult", C.c_int), ("status", C.c_int),
+                ("kernel_launches", C.c_int), ("fx", C.c_double), ("gP", C.c_double),
+                ("dAd", C.c_double), ("time_s", C.c_double)]
+
+
+class TsOpts(C.Structure):
+    _fields_ = [("maxit", C.c_int), ("eps", C.c_double), ("init_permute", C.c_int),
+                ("annealing", C.c_int), ("relative", C.c_int), ("thetasolved", C.c_int)]
+
+
+class TsStats(C.Structure):
+    _fields_ = [("it_last", C.c_int), ("it_sum", C.c_int), ("spg_it_sum", C.c_int),
+                ("spg_hessmult_sum", C.c_int), ("kernel_launches", C.c_int),
+                ("L_increased", C.c_int), ("L", C.c_double), ("deltaL", C.c_double),
+                ("aic", C.c_double), ("time_s", C.c_double)]
+
+
+class PascError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"pasc_gb300 error {code}: {msg}")
+        self.code = code
+
+
+_dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_h = C.c_void_p
+
+# name -> (restype, argtypes); the complete list of exported symbols of include/pasc_gb300.h
+PROTOTYPES = {
+    "pasc_gb300_spgqp_default_opts": (None, [C.POINTER(SpgqpOpts)]),
+    "pasc_gb300_ts_default_opts": (None, [C.POINTER(TsOpts)]),
+    "pasc_gb300_abi_version": (C.c_int, []),
+    "pasc_gb300_last_error": (C.c_char_p, []),
+    "pasc_gb300_device_count": (C.c_int, []),
+    "pasc_gb300_create": (C.c_int, [C.POINTER(_h), C.c_long, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]),
+    "pasc_gb300_destroy": (C.c_int, [_h]),
+    "pasc_gb300_set_epssqr": (C.c_int, [_h, C.c_double, C.c_int]),
+    "pasc_gb300_set_data": (C.c_int, [_h, _dp]),
+    "pasc_gb300_set_gamma": (C.c_int, [_h, _dp]),
+    "pasc_gb300_get_gamma": (C.c_int, [_h, _dp]),
+    "pasc_gb300_set_theta": (C.c_int, [_h, _dp]),
+    "pasc_gb300_get_theta": (C.c_int, [_h, _dp]),
+    "pasc_gb300_permute_gamma": (C.c_int, [_h]),
+    "pasc_gb300_update_theta": (C.c_int, [_h]),
+    "pasc_gb300_update_b": (C.c_int, [_h]),
+    "pasc_gb300_spgqp_solve": (C.c_int, [_h, C.POINTER(SpgqpOpts), C.POINTER(SpgqpStats)]),
+    "pasc_gb300_spgqp_start": (C.c_int, [_h, C.POINTER(SpgqpOpts)]),
+    "pasc_gb300_spgqp_iterate": (C.c_int, [_h, C.c_long, C.c_int, C.POINTER(SpgqpStats)]),
+    "pasc_gb300_spgqp_last_iterate": (C.c_int, [_h, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "pasc_gb300_get_fx": (C.c_int, [_h, C.POINTER(C.c_double)]),
+    "pasc_gb300_ts_solve": (C.c_int, [_h, C.POINTER(TsOpts), C.POINTER(SpgqpOpts), C.c_void_p,
+                                      C.POINTER(TsStats)]),
+    "pasc_gb300_abserr_reconstructed": (C.c_int, [_h, _dp, C.POINTER(C.c_double)]),
+    "pasc_gb300_argmax_labels": (C.c_int, [_h, _ip]),
+    "pasc_gb300_project_f64": (C.c_int, [C.c_void_p, C.c_long, C.c_int, C.c_void_p]),
+    "pasc_gb300_project_f32": (C.c_int, [C.c_void_p, C.c_long, C.c_int, C.c_void_p]),
+    "pasc_gb300_fem_h1_matmult_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_double,
+                                                C.c_void_p]),
+    "pasc_gb300_fem_h1_matmult_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_float,
+                                                C.c_void_p]),
+}
+
+_lib = None
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load(path: str | None = None):
+    """Loads libpasc_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} not found: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+                           " (the library has no CPU fallback)")
+    L = C.CDLL(path)
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != PASC_OK:
+        msg = load().pasc_gb300_last_error().decode(errors="replace")
+        raise PascError(rc, msg)
+
+
+def spgqp_opts(**kw) -> SpgqpOpts:
+    o = SpgqpOpts()
+    load().pasc_gb300_spgqp_default_opts(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
+
+
+def ts_opts(**kw) -> TsOpts:
+    o = TsOpts()
+    load().pasc_gb300_ts_default_opts(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o

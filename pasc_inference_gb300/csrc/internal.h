@@ -1,0 +1,99 @@
+// internal.h -- types shared by the library's translation units (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pasc_gb300.h"
+
+namespace pasc {
+
+constexpr int MMAX_STATE = 64;
+
+// Device-resident state of one mixed-precision SPG solve.  The last block of every sweep
+// reads the block partial sums, applies the reference's step-length rules
+// (src/petscvector/solver/spgqpsolver.cpp:176-216) and writes the scalars the next sweep uses.
+// All scalar arithmetic is FP64.
+struct SpgDevState {
+    // step lengths of the pending iterations
+    double alpha_prev;  // alpha used by the direction being applied (recomputed in the sweep)
+    double beta;        // beta of the direction being applied
+    double alpha_cur;   // alpha of the next direction
+    // objective and the dots of the last direction
+    double fx, fx_old;
+    double dd, dAd, gd;
+    double normb;       // ||b|| (stopping variants scaled by ||b||)
+    // problem and settings (copied in by the host before every solve)
+    double coeff;       // A = coeff * A_hat
+    double bscale;      // b = bscale * residual
+    double eps, gamma, sigma1, sigma2;
+    int maxit, m;
+    int stop_difff, stop_normgp, stop_normgp_normb, stop_Anormgp, stop_Anormgp_normb;
+    // GLL ring (src/general/solver/spg_fs.cpp)
+    double fs[MMAX_STATE];
+    int fs_last;
+    // progress
+    int it;             // completed iterations
+    int hessmult;
+    int status;         // pasc_gb300_solve_status
+    int cur;            // buffer (0/1) holding the current x and g
+    int sweeps;         // sweeps that did work
+    unsigned int counter;  // last-block-done ticket (reset by the last block)
+    unsigned int counter2; // ticket of the theta kernel
+    int pad;
+};
+
+struct SweepArgs {
+    const float *data;  // T (xdim == 1)
+    const float *theta; // K
+    float *xb0, *xb1, *gb0, *gb1;
+    double *partials;   // gridDim.x * 4
+    SpgDevState *st;
+    long T;
+};
+
+struct ThetaArgs {
+    const float *data;
+    const float *xb0, *xb1;  // gamma lives in buffer st->cur
+    double *partials;         // gridDim.x * 2K
+    double *theta64;
+    float *theta32;
+    SpgDevState *st;          // counter2 is the last-block ticket
+    long T;
+    int cur;                  // buffer holding gamma
+};
+
+// Launchers (kernels_fused.cu).  Return a cudaError_t.
+int sweep_block_threads();
+int sweep_blocks_per_sm(int K, bool init);
+cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);
+cudaError_t launch_theta_f32(int K, int grid, const ThetaArgs &a, cudaStream_t s);
+cudaError_t launch_project_f32(float *x, long T, int K, cudaStream_t s);
+cudaError_t launch_matmult_f32(const float *x, float *y, long T, int K, float coeff, cudaStream_t s);
+cudaError_t launch_f64_to_f32(const double *src, float *dst, long n, cudaStream_t s);
+cudaError_t launch_f32_to_f64(const float *src, double *dst, long n, cudaStream_t s);
+
+// Plain FP64 kernels (kernels_plain.cu).
+cudaError_t launch_project_f64(double *x, long T, int K, cudaStream_t s);
+cudaError_t launch_matmult_f64(const double *x, double *y, long T, int K, double coeff, cudaStream_t s);
+cudaError_t launch_axpy_f64(double *y, double a, const double *x, long n, cudaStream_t s);
+cudaError_t launch_xmay_f64(double *d, const double *x, double a, const double *g, long n, cudaStream_t s);
+cudaError_t launch_residual_f64(const double *data, const double *theta, double *b, long T, int K,
+                                double bscale, cudaStream_t s);
+cudaError_t launch_permute_f64(const double *src, double *dst, long T, int K, cudaStream_t s);
+cudaError_t launch_permute_f32(const float *src, float *dst, long T, int K, cudaStream_t s);
+// Deterministic dot products: out[q] = sum_i a_q[i] * b_q[i] for q < nq (nq <= 3); a scratch
+// of dot_partials_size() doubles.  fxmode: out[0] = sum_i x_i * (g_i - b_i) (get_fx).
+size_t dot_partials_size();
+cudaError_t launch_dots_f64(int nq, const double *a0, const double *b0, const double *a1,
+                            const double *b1, const double *a2, const double *b2, long n,
+                            double *scratch, double *out, cudaStream_t s);
+cudaError_t launch_fx_f64(const double *x, const double *g, const double *b, long n,
+                          double *scratch, double *out, cudaStream_t s);
+cudaError_t launch_theta_f64(const double *gamma, const double *data, double *theta, long T, int K,
+                             double *scratch, cudaStream_t s);
+cudaError_t launch_recon_abserr(const double *gamma, const double *theta, const double *sol,
+                                long T, int K, double *scratch, double *out, cudaStream_t s);
+cudaError_t launch_argmax(const double *gamma, int *labels, long T, int K, cudaStream_t s);
+
+}  // namespace pasc

@@ -1,0 +1,471 @@
+// kernels_fused.cu -- mixed-precision (FP32 state, FP64 reductions) SPG-QP kernels.
+//
+// One HBM sweep per SPG iteration.  The reference iteration
+// (src/petscvector/solver/spgqpsolver.cpp:140-216)
+//     d = P(x - alpha g) - x ; Ad = coeff*A_hat d ; dd, dAd, gd ; beta (GLL) ;
+//     x += beta d ; g += beta Ad ; f = 1/2 (g - b)'x ; alpha = dd/dAd
+// is re-timed so that one pass over (x, g) finishes iteration c+1 and starts iteration c+2:
+// the sweep reads x^c, g^c, recomputes d_{c+1} (and Ad_{c+1} from a 2-timestep halo that is
+// recomputed, never stored), forms x^{c+1}, g^{c+1} and f^{c+1}, then d_{c+2}, Ad_{c+2} and
+// their dots.  x^{c+1}, g^{c+1} go to the other half of a ping-pong pair.  b is formed in
+// registers from the data and theta (b_tk = bscale*(x_t - theta_k)^2,
+// src/petscvector/model/graphh1fem.cpp:258-286) and never stored.  HBM traffic per
+// iteration: read x, g, data; write x, g = 16*K*T + 4*T bytes.
+//
+// Reductions: per thread in compensated FP32, per block and per grid in FP64 (fixed order,
+// deterministic for a fixed grid).  The last block applies the step-length and GLL rules in
+// FP64 and advances the device state; the host only polls the status word between chunks
+// of sweeps.  d'Ad is accumulated in the difference form 2*coeff*sum (d_{t+1}-d_t)^2, equal
+// to d'(A d) for the FEM-H1 matrix but free of the cancellation the dot form has in FP32.
+#include "common.cuh"
+#include "project.cuh"
+#include "internal.h"
+
+namespace pasc {
+
+constexpr int SWEEP_NT = 256;          // threads per block = timesteps per tile incl. halo
+constexpr int SWEEP_HALO = 2;
+constexpr int SWEEP_W = SWEEP_NT - 2 * SWEEP_HALO;  // owned timesteps per tile
+
+int sweep_block_threads() { return SWEEP_NT; }
+
+// Row sum of A_hat (FEM-H1, R = 1) at timestep t for component k from values staged in
+// shared memory at slots i-1, i, i+1 (stride K); the order of the assembled CSR row.
+template <int K>
+__device__ __forceinline__ float stencil_row(const float *s, int i, int k, long t, long T)
+{
+    if (T == 1) return 0.f;
+    const float w = (t == 0 || t == T - 1) ? 2.f : 4.f;
+    float sum = 0.f;
+    if (t > 0) sum = __fmul_rn(-2.f, s[(i - 1) * K + k]);
+    sum = __fadd_rn(sum, __fmul_rn(w, s[i * K + k]));
+    if (t < T - 1) sum = __fadd_rn(sum, __fmul_rn(-2.f, s[(i + 1) * K + k]));
+    return sum;
+}
+
+template <int K, bool INIT>
+__global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
+{
+    __shared__ float s_a[SWEEP_NT * K];
+    __shared__ float s_b[SWEEP_NT * K];
+    __shared__ double s_red[4 * (SWEEP_NT / 32)];
+
+    SpgDevState *st = a.st;
+    if (st->status != PASC_SPG_RUNNING) return;  // uniform across the grid
+
+    const int cur = st->cur;
+    const float *xin = cur ? a.xb1 : a.xb0;
+    const float *gin = cur ? a.gb1 : a.gb0;
+    float *xout = cur ? a.xb0 : a.xb1;
+    float *gout = cur ? a.gb0 : a.gb1;
+    const float a0 = (float)st->alpha_prev;
+    const float beta = (float)st->beta;
+    const float a1 = (float)st->alpha_cur;
+    const float coeff = (float)st->coeff;
+    const float bscale = (float)st->bscale;
+    const long T = a.T;
+
+    float theta[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) theta[k] = a.theta[k];
+
+    KahanF acc_f, acc_dd, acc_dAd, acc_gd;
+    const int i = threadIdx.x;
+    const long ntiles = (T + SWEEP_W - 1) / SWEEP_W;
+
+    for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long t = tile * SWEEP_W - SWEEP_HALO + i;
+        const bool in = (t >= 0 && t < T);
+
+        float xo[K], go[K];
+        float dv = 0.f;
+        if (in) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                xo[k] = __ldcs(xin + t * K + k);
+                go[k] = __ldcs(gin + t * K + k);
+            }
+            dv = __ldg(a.data + t);
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; k++) { xo[k] = 0.f; go[k] = 0.f; }
+        }
+
+        // phase 1: INIT projects the start point; otherwise recompute d_{c+1}
+        float p1[K];
+        if (INIT) {
+#pragma unroll
+            for (int k = 0; k < K; k++) p1[k] = xo[k];
+            project_reg<K>(p1);
+#pragma unroll
+            for (int k = 0; k < K; k++) s_a[i * K + k] = in ? p1[k] : 0.f;
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; k++) p1[k] = __fsub_rn(xo[k], __fmul_rn(a0, go[k]));
+            project_reg<K>(p1);
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                p1[k] = __fsub_rn(p1[k], xo[k]);  // d_{c+1}
+                s_a[i * K + k] = in ? p1[k] : 0.f;
+            }
+        }
+        __syncthreads();
+
+        // phase 2: x^{c+1}, g^{c+1}, f contribution, next direction d_{c+2}
+        const bool mid = in && i >= 1 && i <= SWEEP_NT - 2;
+        const bool own = in && i >= SWEEP_HALO && i < SWEEP_NT - SWEEP_HALO;
+        float x1[K], g1[K], d1[K];
+        if (mid) {
+            float fpart = 0.f;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float S = stencil_row<K>(s_a, i, k, t, T);
+                const float r = __fsub_rn(dv, theta[k]);
+                const float bk = __fmul_rn(bscale, __fmul_rn(r, r));
+                if (INIT) {
+                    x1[k] = p1[k];
+                    g1[k] = __fsub_rn(__fmul_rn(coeff, S), bk);
+                } else {
+                    x1[k] = __fadd_rn(xo[k], __fmul_rn(beta, p1[k]));
+                    g1[k] = __fadd_rn(go[k], __fmul_rn(beta, __fmul_rn(coeff, S)));
+                }
+                fpart = __fadd_rn(fpart, __fmul_rn(__fsub_rn(g1[k], bk), x1[k]));
+                d1[k] = __fsub_rn(x1[k], __fmul_rn(a1, g1[k]));
+            }
+            if (own) acc_f.add(fpart);
+            project_reg<K>(d1);
+#pragma unroll
+            for (int k = 0; k < K; k++) d1[k] = __fsub_rn(d1[k], x1[k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; k++) { x1[k] = 0.f; g1[k] = 0.f; d1[k] = 0.f; }
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) s_b[i * K + k] = d1[k];
+        __syncthreads();
+
+        // phase 3: dots of d_{c+2}; write x^{c+1}, g^{c+1}
+        if (own) {
+            float pdd = 0.f, pdiff = 0.f, pgd = 0.f;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                pdd = __fadd_rn(pdd, __fmul_rn(d1[k], d1[k]));
+                pgd = __fadd_rn(pgd, __fmul_rn(g1[k], d1[k]));
+                if (t < T - 1) {
+                    const float df = __fsub_rn(s_b[(i + 1) * K + k], d1[k]);
+                    pdiff = __fadd_rn(pdiff, __fmul_rn(df, df));
+                }
+            }
+            acc_dd.add(pdd);
+            acc_dAd.add(pdiff);
+            acc_gd.add(pgd);
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                __stcs(xout + t * K + k, x1[k]);
+                __stcs(gout + t * K + k, g1[k]);
+            }
+        }
+    }
+
+    // block and grid reductions
+    double v[4] = {acc_f.value(), acc_dd.value(), acc_dAd.value(), acc_gd.value()};
+    block_sum<4>(v, s_red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) a.partials[blockIdx.x * 4 + q] = v[q];
+    }
+    if (!last_block_done(&st->counter)) return;
+
+    double w[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += SWEEP_NT) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) w[q] += __ldcg(a.partials + b * 4 + q);
+    }
+    block_sum<4>(w, s_red);
+    if (threadIdx.x != 0) return;
+
+    st->counter = 0;
+    st->sweeps += 1;
+    const double fnew = 0.5 * w[0];
+    const double dd = w[1];
+    const double dAd = 2.0 * st->coeff * w[2];
+    const double gd = w[3];
+
+    if (INIT) {
+        // spgqpsolver.cpp:131-137: fs.init(fx), fx_old = max
+        st->fx = fnew;
+        st->fx_old = DBL_MAX;
+        for (int q = 0; q < st->m; q++) st->fs[q] = fnew;
+        st->fs_last = 0;
+        st->it = 0;
+        st->hessmult = 1;
+        st->cur = cur ^ 1;
+        if (st->maxit <= 0) { st->status = PASC_SPG_MAXIT; return; }
+        if (!isfinite(fnew)) { st->status = PASC_SPG_NONFINITE; return; }
+    } else {
+        st->it += 1;
+        st->hessmult += 1;
+        st->cur = cur ^ 1;
+        st->fx_old = st->fx;  // :207
+        st->fx = fnew;        // :209
+        int li = st->fs_last + 1;  // fs.update, spg_fs.cpp:52-63
+        if (li >= st->m) li = 0;
+        st->fs[li] = fnew;
+        st->fs_last = li;
+        if (!isfinite(fnew)) { st->status = PASC_SPG_NONFINITE; return; }
+        // stopping tests of iteration it on the direction it applied (:260-274)
+        const double ddo = st->dd, dAdo = st->dAd;
+        if ((st->stop_difff && fabs(st->fx - st->fx_old) < st->eps) ||
+            (st->stop_normgp && ddo < st->eps) ||
+            (st->stop_normgp_normb && ddo < st->eps * st->normb) ||
+            (st->stop_Anormgp && dAdo < st->eps) ||
+            (st->stop_Anormgp_normb && dAdo < st->eps * st->normb)) {
+            st->status = PASC_SPG_CONVERGED;
+            return;
+        }
+        if (st->it >= st->maxit) { st->status = PASC_SPG_MAXIT; return; }
+    }
+
+    // next direction: step length from the A-condition (:176-195) and BB step (:216)
+    if (!(isfinite(dd) && isfinite(dAd) && isfinite(gd))) { st->status = PASC_SPG_NONFINITE; return; }
+    if (!(dd > 0.0)) { st->status = PASC_SPG_DAD_ZERO; return; }  // projected step vanished
+    double nbeta, nalpha;
+    if (dAd > 0.0) {
+        double fx_max = st->fs[0];
+        for (int q = 0; q < st->m; q++) fx_max = st->fs[q] > fx_max ? st->fs[q] : fx_max;
+        const double xi = (fx_max - st->fx) / dAd;
+        const double beta_bar = -gd / dAd;
+        double beta_hat = st->gamma * beta_bar + sqrt(st->gamma * st->gamma * beta_bar * beta_bar + 2 * xi);
+        if (beta_hat < st->sigma1) beta_hat = st->sigma1;
+        nbeta = beta_hat < st->sigma2 ? beta_hat : st->sigma2;
+        nalpha = dd / dAd;
+    } else if (gd < 0.0) {
+        // d'Ad = 0 with d != 0: the objective is linear along d (A_hat d = 0, e.g. T == 1).
+        // The reference divides by zero here; its comparisons then fall through to
+        // beta = sigma2.  Take that step and keep the step length finite.
+        nbeta = st->sigma2;
+        nalpha = st->alpha_cur;
+    } else {
+        st->status = PASC_SPG_DAD_ZERO;
+        return;
+    }
+    st->alpha_prev = st->alpha_cur;
+    st->alpha_cur = nalpha;
+    st->beta = nbeta;
+    st->dd = dd;
+    st->dAd = dAd;
+    st->gd = gd;
+}
+
+template <int K, bool INIT>
+static int blocks_per_sm_t()
+{
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_kernel<K, INIT>, SWEEP_NT, 0);
+    return nb > 0 ? nb : 1;
+}
+
+int sweep_blocks_per_sm(int K, bool init)
+{
+    switch (K) {
+#define PASC_CASE(KK) case KK: return init ? blocks_per_sm_t<KK, true>() : blocks_per_sm_t<KK, false>();
+        PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
+        PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
+#undef PASC_CASE
+        default: return 1;
+    }
+}
+
+cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s)
+{
+    switch (K) {
+#define PASC_CASE(KK)                                                                   \
+    case KK:                                                                            \
+        if (init) spg_sweep_kernel<KK, true><<<grid, SWEEP_NT, 0, s>>>(a);              \
+        else spg_sweep_kernel<KK, false><<<grid, SWEEP_NT, 0, s>>>(a);                  \
+        break;
+        PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
+        PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
+#undef PASC_CASE
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// theta update (graphh1fem.cpp:347-380): theta_k = sum_t gamma_tk x_t / sum_t gamma_tk.
+// FP32 gamma/data, compensated FP32 per thread, FP64 per block and grid; the last block
+// writes theta in FP64 and FP32.
+// ---------------------------------------------------------------------------------------
+constexpr int THETA_NT = 256;
+
+template <int K>
+__global__ void __launch_bounds__(THETA_NT) theta_kernel(ThetaArgs a)
+{
+    __shared__ double s_red[2 * K * (THETA_NT / 32)];
+    const float *gam = a.cur ? a.xb1 : a.xb0;
+    KahanF sx[K], sg[K];
+    const long stride = (long)gridDim.x * THETA_NT;
+    for (long t = (long)blockIdx.x * THETA_NT + threadIdx.x; t < a.T; t += stride) {
+        const float x = __ldg(a.data + t);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const float gk = __ldcs(gam + t * K + k);
+            sg[k].add(gk);
+            sx[k].add(__fmul_rn(x, gk));
+        }
+    }
+    double v[2 * K];
+#pragma unroll
+    for (int k = 0; k < K; k++) { v[k] = sx[k].value(); v[K + k] = sg[k].value(); }
+    block_sum<2 * K>(v, s_red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < 2 * K; q++) a.partials[blockIdx.x * 2 * K + q] = v[q];
+    }
+    if (!last_block_done(&a.st->counter2)) return;
+    double w[2 * K];
+#pragma unroll
+    for (int q = 0; q < 2 * K; q++) w[q] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += THETA_NT) {
+#pragma unroll
+        for (int q = 0; q < 2 * K; q++) w[q] += __ldcg(a.partials + b * 2 * K + q);
+    }
+    block_sum<2 * K>(w, s_red);
+    if (threadIdx.x == 0) {
+        a.st->counter2 = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const double th = (w[K + k] != 0.0) ? w[k] / w[K + k] : 0.0;
+            a.theta64[k] = th;
+            a.theta32[k] = (float)th;
+        }
+    }
+}
+
+cudaError_t launch_theta_f32(int K, int grid, const ThetaArgs &a, cudaStream_t s)
+{
+    switch (K) {
+#define PASC_CASE(KK) case KK: theta_kernel<KK><<<grid, THETA_NT, 0, s>>>(a); break;
+        PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
+        PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
+#undef PASC_CASE
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// standalone FP32 projection and operator (device-pointer entry points)
+// ---------------------------------------------------------------------------------------
+template <int K>
+__global__ void project_f32_reg_kernel(float *x, long T)
+{
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < T; t += stride) {
+        float v[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = x[t * K + k];
+        project_reg<K>(v);
+#pragma unroll
+        for (int k = 0; k < K; k++) x[t * K + k] = v[k];
+    }
+}
+
+template <int G>
+__global__ void project_f32_group_kernel(float *x, long T, int K)
+{
+    const int per_warp = 32 / G;
+    const long warp_global = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    for (long w = warp_global; w * per_warp < T; w += nwarps) {
+        const long t = w * per_warp + lane / G;
+        const int k = lane & (G - 1);
+        const bool valid = t < T;
+        const bool act = valid && k < K;
+        float v = act ? x[t * K + k] : 0.f;
+        float r = project_group<G>(v, K, valid);
+        if (act) x[t * K + k] = r;
+    }
+}
+
+static int grid_for(long work, int threads)
+{
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long blocks = (work + threads - 1) / threads;
+    long cap = (long)sms * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    return (int)blocks;
+}
+
+cudaError_t launch_project_f32(float *x, long T, int K, cudaStream_t s)
+{
+    if (T <= 0) return cudaSuccess;
+    switch (K) {
+#define PASC_CASE(KK) case KK: project_f32_reg_kernel<KK><<<grid_for(T, 256), 256, 0, s>>>(x, T); break;
+        PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
+        PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
+#undef PASC_CASE
+        default:
+            if (K <= 16) project_f32_group_kernel<16><<<grid_for(T * 16, 256), 256, 0, s>>>(x, T, K);
+            else if (K <= 32) project_f32_group_kernel<32><<<grid_for(T * 32, 256), 256, 0, s>>>(x, T, K);
+            else return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+__global__ void matmult_f32_kernel(const float *x, float *y, long T, int K, float coeff)
+{
+    const long n = T * K;
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += stride) {
+        const long t = idx / K;
+        float sum = 0.f;
+        if (T > 1) {
+            const float w = (t == 0 || t == T - 1) ? 2.f : 4.f;
+            if (t > 0) sum = __fmul_rn(-2.f, x[idx - K]);
+            sum = __fadd_rn(sum, __fmul_rn(w, x[idx]));
+            if (t < T - 1) sum = __fadd_rn(sum, __fmul_rn(-2.f, x[idx + K]));
+        }
+        y[idx] = __fmul_rn(coeff, sum);
+    }
+}
+
+cudaError_t launch_matmult_f32(const float *x, float *y, long T, int K, float coeff, cudaStream_t s)
+{
+    if (T <= 0) return cudaSuccess;
+    matmult_f32_kernel<<<grid_for(T * K, 256), 256, 0, s>>>(x, y, T, K, coeff);
+    return cudaGetLastError();
+}
+
+__global__ void f64_to_f32_kernel(const double *src, float *dst, long n)
+{
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = (float)src[i];
+}
+
+__global__ void f32_to_f64_kernel(const float *src, double *dst, long n)
+{
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = (double)src[i];
+}
+
+cudaError_t launch_f64_to_f32(const double *src, float *dst, long n, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    f64_to_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_f32_to_f64(const float *src, double *dst, long n, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    f32_to_f64_kernel<<<grid_for(n, 256), 256, 0, s>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+}  // namespace pasc

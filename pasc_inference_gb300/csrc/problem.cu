@@ -1,0 +1,929 @@
+// problem.cu -- the C ABI (include/pasc_gb300.h): problem handles, the SPG-QP solve loops of
+// both precisions, the TSSolver outer loop and the device-pointer entry points.
+#include <math.h>
+#include <stdarg.h>
+#include <string.h>
+#include <chrono>
+#include <cstdio>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+using namespace pasc;
+
+// ---------------------------------------------------------------------------------------
+// error reporting
+// ---------------------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+static int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CU(call)                                                                               \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(PASC_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),        \
+                        __FILE__, __LINE__);                                                   \
+    } while (0)
+
+#define CHK(call)                                                                              \
+    do {                                                                                       \
+        int r_ = (call);                                                                       \
+        if (r_ != PASC_OK) return r_;                                                          \
+    } while (0)
+
+// ---------------------------------------------------------------------------------------
+// problem
+// ---------------------------------------------------------------------------------------
+
+// Host-side record of the current SPG solve (both paths; the fp64 path keeps its whole
+// scalar state here, the mixed path mirrors the device state after every poll).
+struct SpgRun {
+    pasc_gb300_spgqp_opts o{};
+    bool started = false;
+    int it = 0, hessmult = 0, status = PASC_SPG_RUNNING, launches = 0;
+    double fx = 0.0, fx_old = DBL_MAX, dd = 0.0, dAd = 0.0, normb = 0.0, alpha = 0.0;
+    double fs[MMAX_STATE] = {0};
+    int fs_last = 0;
+    double time_s = 0.0;
+    float last_iterate_ms = 0.f;
+    int last_iterate_launches = 0;
+};
+
+struct pasc_gb300_problem {
+    long T = 0;
+    int K = 0, xdim = 1, precision = 0, device = 0;
+    double epssqr = 0.0;
+    int scalef = 1;
+    double coeffA = 0.0, coeffB = 0.0;
+    long N = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    // shared
+    double *data64 = nullptr;     // T (fp64 path; mixed path uses it as upload staging)
+    double *theta64 = nullptr;    // K*xdim
+    double *stage64 = nullptr;    // N (mixed: conversions; fp64: permutation temp)
+    double *red = nullptr;        // reduction scratch (dot_partials_size doubles)
+    double *red_out = nullptr;    // 8 doubles
+    double *red_out_h = nullptr;  // pinned mirror
+    int *labels_d = nullptr;      // T
+
+    // fp64 path
+    double *x = nullptr, *g = nullptr, *d = nullptr, *Ad = nullptr, *b = nullptr;
+
+    // mixed path
+    float *data32 = nullptr, *theta32 = nullptr;
+    float *xb[2] = {nullptr, nullptr}, *gb[2] = {nullptr, nullptr};
+    SpgDevState *st = nullptr, *st_h = nullptr;
+    double *partials = nullptr;
+    int cur = 0;
+    int grid_sweep = 0, grid_sweep_init = 0, grid_theta = 0;
+    cudaGraphExec_t chunk_graph = nullptr;
+    int chunk_graph_len = 0;
+
+    SpgRun run;
+    double fx_last = 0.0;
+    bool have_fx = false;
+    bool have_data = false;
+};
+
+static void free_all(pasc_gb300_problem *p)
+{
+    if (!p) return;
+    cudaSetDevice(p->device);
+    if (p->chunk_graph) cudaGraphExecDestroy(p->chunk_graph);
+    void *dev[] = {p->data64, p->theta64, p->stage64, p->red, p->red_out, p->labels_d, p->x, p->g,
+                   p->d, p->Ad, p->b, p->data32, p->theta32, p->xb[0], p->xb[1], p->gb[0],
+                   p->gb[1], p->st, p->partials};
+    for (void *q : dev)
+        if (q) cudaFree(q);
+    if (p->st_h) cudaFreeHost(p->st_h);
+    if (p->red_out_h) cudaFreeHost(p->red_out_h);
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+template <typename T>
+static int dalloc(T **ptr, size_t count)
+{
+    cudaError_t e = cudaMalloc((void **)ptr, sizeof(T) * (count > 0 ? count : 1));
+    if (e != cudaSuccess)
+        return fail(PASC_ERR_ALLOC, "cudaMalloc of %zu bytes failed: %s", sizeof(T) * count,
+                    cudaGetErrorString(e));
+    return PASC_OK;
+}
+
+static void set_coeffs(pasc_gb300_problem *p)
+{
+    // graphh1fem.cpp:146-151 and :280-283 (not reduced: T_reduced == T)
+    double c = p->epssqr;
+    if (p->scalef) c *= (1.0 / ((double)p->T));
+    else c *= ((double)p->T / ((double)p->T));
+    p->coeffA = c;
+    double cb = -1.0;
+    if (p->scalef) cb *= (1.0 / ((double)p->T));
+    p->coeffB = cb;
+}
+
+extern "C" {
+
+void pasc_gb300_spgqp_default_opts(pasc_gb300_spgqp_opts *o)
+{
+    if (!o) return;
+    o->maxit = 1000;
+    o->eps = 1e-9;
+    o->m = 20;
+    o->gamma = 0.9;
+    o->sigma1 = 0.0;
+    o->sigma2 = 1.0;
+    o->alphainit = 2.0;
+    o->stop_difff = 1;
+    o->stop_normgp = 0;
+    o->stop_normgp_normb = 0;
+    o->stop_Anormgp = 0;
+    o->stop_Anormgp_normb = 0;
+}
+
+void pasc_gb300_ts_default_opts(pasc_gb300_ts_opts *o)
+{
+    if (!o) return;
+    o->maxit = 300;
+    o->eps = 1e-6;
+    o->init_permute = 1;
+    o->annealing = 1;
+    o->relative = 0;
+    o->thetasolved = 0;
+}
+
+int pasc_gb300_abi_version(void) { return PASC_GB300_ABI_VERSION; }
+
+const char *pasc_gb300_last_error(void) { return g_last_error.c_str(); }
+
+int pasc_gb300_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int precision,
+                      double epssqr, int device)
+{
+    if (!out) return fail(PASC_ERR_ARG, "create: out is NULL");
+    *out = nullptr;
+    if (T < 1) return fail(PASC_ERR_ARG, "create: T must be >= 1 (got %ld)", T);
+    if (xdim != 1) return fail(PASC_ERR_NOTSUPP, "create: xdim %d not supported (1-D signals only)", xdim);
+    if (precision != PASC_PREC_FP64 && precision != PASC_PREC_MIXED)
+        return fail(PASC_ERR_ARG, "create: unknown precision %d", precision);
+    const int kmax = precision == PASC_PREC_MIXED ? KMAX_FUSED : KMAX_PLAIN;
+    if (K < 1 || K > kmax)
+        return fail(PASC_ERR_ARG, "create: K must be in [1, %d] for this precision (got %d)", kmax, K);
+    if ((double)T * (double)K > 2.0e9) return fail(PASC_ERR_ARG, "create: K*T too large");
+    int ndev = pasc_gb300_device_count();
+    if (ndev <= 0) return fail(PASC_ERR_CUDA, "create: no CUDA device available");
+    if (device < 0 || device >= ndev) return fail(PASC_ERR_ARG, "create: device %d out of range", device);
+
+    pasc_gb300_problem *p = new (std::nothrow) pasc_gb300_problem();
+    if (!p) return fail(PASC_ERR_ALLOC, "create: host allocation failed");
+    p->T = T;
+    p->K = K;
+    p->xdim = xdim;
+    p->precision = precision;
+    p->device = device;
+    p->epssqr = epssqr;
+    p->N = T * (long)K;
+    set_coeffs(p);
+
+    int rc = PASC_OK;
+    auto bail = [&](int code) { free_all(p); return code; };
+    if (cudaSetDevice(device) != cudaSuccess) return bail(fail(PASC_ERR_CUDA, "cudaSetDevice failed"));
+    cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&p->ev0) != cudaSuccess || cudaEventCreate(&p->ev1) != cudaSuccess)
+        return bail(fail(PASC_ERR_CUDA, "create: stream/event creation failed"));
+
+    const long N = p->N;
+    if ((rc = dalloc(&p->data64, T)) || (rc = dalloc(&p->theta64, (size_t)K * xdim)) ||
+        (rc = dalloc(&p->stage64, N)) || (rc = dalloc(&p->red, dot_partials_size())) ||
+        (rc = dalloc(&p->red_out, 8)) || (rc = dalloc(&p->labels_d, T)))
+        return bail(rc);
+    if (cudaMallocHost((void **)&p->red_out_h, 8 * sizeof(double)) != cudaSuccess)
+        return bail(fail(PASC_ERR_ALLOC, "create: pinned allocation failed"));
+    cudaMemset(p->red, 0, dot_partials_size() * sizeof(double));
+    cudaMemset(p->theta64, 0, sizeof(double) * K * xdim);
+    cudaMemset(p->data64, 0, sizeof(double) * T);
+
+    if (precision == PASC_PREC_FP64) {
+        if ((rc = dalloc(&p->x, N)) || (rc = dalloc(&p->g, N)) || (rc = dalloc(&p->d, N)) ||
+            (rc = dalloc(&p->Ad, N)) || (rc = dalloc(&p->b, N)))
+            return bail(rc);
+        cudaMemset(p->x, 0, sizeof(double) * N);
+        cudaMemset(p->b, 0, sizeof(double) * N);
+    } else {
+        if ((rc = dalloc(&p->data32, T)) || (rc = dalloc(&p->theta32, K)) ||
+            (rc = dalloc(&p->xb[0], N)) || (rc = dalloc(&p->xb[1], N)) ||
+            (rc = dalloc(&p->gb[0], N)) || (rc = dalloc(&p->gb[1], N)) ||
+            (rc = dalloc(&p->st, 1)))
+            return bail(rc);
+        if (cudaMallocHost((void **)&p->st_h, sizeof(SpgDevState)) != cudaSuccess)
+            return bail(fail(PASC_ERR_ALLOC, "create: pinned allocation failed"));
+        memset(p->st_h, 0, sizeof(SpgDevState));
+        cudaMemset(p->st, 0, sizeof(SpgDevState));
+        cudaMemset(p->xb[0], 0, sizeof(float) * N);
+        cudaMemset(p->data32, 0, sizeof(float) * T);
+        cudaMemset(p->theta32, 0, sizeof(float) * K);
+        const long ntiles = (T + sweep_block_threads() - 5) / (sweep_block_threads() - 4);
+        long gs = (long)sweep_blocks_per_sm(K, false) * p->sms;
+        long gi = (long)sweep_blocks_per_sm(K, true) * p->sms;
+        p->grid_sweep = (int)(gs < ntiles ? gs : ntiles);
+        p->grid_sweep_init = (int)(gi < ntiles ? gi : ntiles);
+        long gt = (long)p->sms * 4;
+        long tb = (T + 255) / 256;
+        p->grid_theta = (int)(gt < tb ? gt : tb);
+        if (p->grid_sweep < 1) p->grid_sweep = 1;
+        if (p->grid_sweep_init < 1) p->grid_sweep_init = 1;
+        if (p->grid_theta < 1) p->grid_theta = 1;
+        long np = p->grid_sweep > p->grid_sweep_init ? p->grid_sweep : p->grid_sweep_init;
+        np = np * 4 > (long)p->grid_theta * 2 * K ? np * 4 : (long)p->grid_theta * 2 * K;
+        if ((rc = dalloc(&p->partials, np))) return bail(rc);
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        return bail(fail(PASC_ERR_CUDA, "create: initialisation failed"));
+    *out = p;
+    return PASC_OK;
+}
+
+int pasc_gb300_destroy(pasc_gb300_problem *p)
+{
+    if (!p) return PASC_OK;
+    free_all(p);
+    return PASC_OK;
+}
+
+int pasc_gb300_set_epssqr(pasc_gb300_problem *p, double epssqr, int scalef)
+{
+    if (!p) return fail(PASC_ERR_ARG, "set_epssqr: NULL problem");
+    p->run.started = false;
+    p->epssqr = epssqr;
+    p->scalef = scalef ? 1 : 0;
+    set_coeffs(p);
+    return PASC_OK;
+}
+
+int pasc_gb300_set_data(pasc_gb300_problem *p, const double *data)
+{
+    if (!p || !data) return fail(PASC_ERR_ARG, "set_data: NULL argument");
+    p->run.started = false;
+    CU(cudaSetDevice(p->device));
+    CU(cudaMemcpyAsync(p->data64, data, sizeof(double) * p->T * p->xdim, cudaMemcpyHostToDevice, p->stream));
+    if (p->precision == PASC_PREC_MIXED) CU(launch_f64_to_f32(p->data64, p->data32, p->T, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    p->have_data = true;
+    return PASC_OK;
+}
+
+int pasc_gb300_set_gamma(pasc_gb300_problem *p, const double *gamma)
+{
+    if (!p || !gamma) return fail(PASC_ERR_ARG, "set_gamma: NULL argument");
+    p->run.started = false;
+    CU(cudaSetDevice(p->device));
+    if (p->precision == PASC_PREC_FP64) {
+        CU(cudaMemcpyAsync(p->x, gamma, sizeof(double) * p->N, cudaMemcpyHostToDevice, p->stream));
+    } else {
+        CU(cudaMemcpyAsync(p->stage64, gamma, sizeof(double) * p->N, cudaMemcpyHostToDevice, p->stream));
+        CU(launch_f64_to_f32(p->stage64, p->xb[p->cur], p->N, p->stream));
+    }
+    CU(cudaStreamSynchronize(p->stream));
+    p->have_fx = false;
+    return PASC_OK;
+}
+
+// device FP64 view of gamma (mixed: converted into stage64)
+static int gamma64(pasc_gb300_problem *p, const double **out)
+{
+    if (p->precision == PASC_PREC_FP64) {
+        *out = p->x;
+        return PASC_OK;
+    }
+    CU(launch_f32_to_f64(p->xb[p->cur], p->stage64, p->N, p->stream));
+    *out = p->stage64;
+    return PASC_OK;
+}
+
+int pasc_gb300_get_gamma(pasc_gb300_problem *p, double *gamma)
+{
+    if (!p || !gamma) return fail(PASC_ERR_ARG, "get_gamma: NULL argument");
+    CU(cudaSetDevice(p->device));
+    const double *g64 = nullptr;
+    CHK(gamma64(p, &g64));
+    CU(cudaMemcpyAsync(gamma, g64, sizeof(double) * p->N, cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_set_theta(pasc_gb300_problem *p, const double *theta)
+{
+    if (!p || !theta) return fail(PASC_ERR_ARG, "set_theta: NULL argument");
+    p->run.started = false;
+    CU(cudaSetDevice(p->device));
+    CU(cudaMemcpyAsync(p->theta64, theta, sizeof(double) * p->K * p->xdim, cudaMemcpyHostToDevice, p->stream));
+    if (p->precision == PASC_PREC_MIXED) CU(launch_f64_to_f32(p->theta64, p->theta32, p->K, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_get_theta(pasc_gb300_problem *p, double *theta)
+{
+    if (!p || !theta) return fail(PASC_ERR_ARG, "get_theta: NULL argument");
+    CU(cudaSetDevice(p->device));
+    CU(cudaMemcpyAsync(theta, p->theta64, sizeof(double) * p->K * p->xdim, cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+static int permute_gamma_async(pasc_gb300_problem *p)
+{
+    if (p->precision == PASC_PREC_FP64) {
+        CU(launch_permute_f64(p->x, p->stage64, p->T, p->K, p->stream));
+        CU(cudaMemcpyAsync(p->x, p->stage64, sizeof(double) * p->N, cudaMemcpyDeviceToDevice, p->stream));
+    } else {
+        float *src = p->xb[p->cur], *dst = p->xb[p->cur ^ 1];
+        CU(launch_permute_f32(src, dst, p->T, p->K, p->stream));
+        p->cur ^= 1;
+    }
+    return PASC_OK;
+}
+
+int pasc_gb300_permute_gamma(pasc_gb300_problem *p)
+{
+    if (!p) return fail(PASC_ERR_ARG, "permute_gamma: NULL problem");
+    p->run.started = false;
+    CU(cudaSetDevice(p->device));
+    CHK(permute_gamma_async(p));
+    CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+static int update_theta_async(pasc_gb300_problem *p, int *launches)
+{
+    if (p->precision == PASC_PREC_FP64) {
+        CU(launch_theta_f64(p->x, p->data64, p->theta64, p->T, p->K, p->red, p->stream));
+        if (launches) *launches += (p->K + 7) / 8;
+    } else {
+        ThetaArgs a;
+        a.data = p->data32;
+        a.xb0 = p->xb[0];
+        a.xb1 = p->xb[1];
+        a.partials = p->partials;
+        a.theta64 = p->theta64;
+        a.theta32 = p->theta32;
+        a.st = p->st;
+        a.T = p->T;
+        a.cur = p->cur;
+        CU(launch_theta_f32(p->K, p->grid_theta, a, p->stream));
+        if (launches) *launches += 1;
+    }
+    return PASC_OK;
+}
+
+int pasc_gb300_update_theta(pasc_gb300_problem *p)
+{
+    if (!p) return fail(PASC_ERR_ARG, "update_theta: NULL problem");
+    p->run.started = false;
+    CU(cudaSetDevice(p->device));
+    CHK(update_theta_async(p, nullptr));
+    CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+static int update_b_async(pasc_gb300_problem *p, int *launches)
+{
+    if (p->precision == PASC_PREC_FP64) {
+        CU(launch_residual_f64(p->data64, p->theta64, p->b, p->T, p->K, p->coeffB, p->stream));
+        if (launches) *launches += 1;
+    }
+    // mixed: b is formed inside the sweep from data32 and theta32 (kept current by
+    // set_theta / update_theta)
+    return PASC_OK;
+}
+
+int pasc_gb300_update_b(pasc_gb300_problem *p)
+{
+    if (!p) return fail(PASC_ERR_ARG, "update_b: NULL problem");
+    p->run.started = false;
+    CU(cudaSetDevice(p->device));
+    CHK(update_b_async(p, nullptr));
+    CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// SPG-QP, FP64 plain path: the reference's loop (spgqpsolver.cpp:55-312) with host scalars.
+// ---------------------------------------------------------------------------------------
+static int read_red(pasc_gb300_problem *p, int n, double *vals)
+{
+    CU(cudaMemcpyAsync(p->red_out_h, p->red_out, sizeof(double) * n, cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    for (int i = 0; i < n; i++) vals[i] = p->red_out_h[i];
+    return PASC_OK;
+}
+
+static void fill_stats(const SpgRun &r, pasc_gb300_spgqp_stats *st)
+{
+    if (!st) return;
+    st->it = r.it;
+    st->hessmult = r.hessmult;
+    st->status = r.status;
+    st->kernel_launches = r.launches;
+    st->fx = r.fx;
+    st->gP = r.dd;
+    st->dAd = r.dAd;
+    st->time_s = r.time_s;
+}
+
+// spgqpsolver.cpp:104-137
+static int fp64_start(pasc_gb300_problem *p)
+{
+    SpgRun &r = p->run;
+    const long N = p->N, T = p->T;
+    const int K = p->K;
+    cudaStream_t s = p->stream;
+    double v[3];
+    CU(cudaEventRecord(p->ev0, s));
+    CU(launch_dots_f64(1, p->b, p->b, nullptr, nullptr, nullptr, nullptr, N, p->red, p->red_out, s));
+    r.launches++;
+    CHK(read_red(p, 1, v));
+    r.normb = sqrt(v[0]);             // :104
+    r.alpha = r.o.alphainit;          // :108
+    CU(launch_project_f64(p->x, T, K, s));                   // :116
+    CU(launch_matmult_f64(p->x, p->g, T, K, p->coeffA, s));  // :122-123
+    CU(launch_axpy_f64(p->g, -1.0, p->b, N, s));             // :128
+    CU(launch_fx_f64(p->x, p->g, p->b, N, p->red, p->red_out, s));  // :133
+    r.launches += 4;
+    CHK(read_red(p, 1, v));
+    r.fx = 0.5 * v[0];
+    r.fx_old = DBL_MAX;
+    for (int q = 0; q < r.o.m; q++) r.fs[q] = r.fx;
+    r.fs_last = 0;
+    r.it = 0;
+    r.hessmult = 1;
+    r.status = r.o.maxit <= 0 ? PASC_SPG_MAXIT : (isfinite(r.fx) ? PASC_SPG_RUNNING : PASC_SPG_NONFINITE);
+    CU(cudaEventRecord(p->ev1, s));
+    CU(cudaEventSynchronize(p->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+    r.time_s += ms * 1e-3;
+    return PASC_OK;
+}
+
+// spgqpsolver.cpp:140-297, at most n iterations
+static int fp64_iterate(pasc_gb300_problem *p, long n)
+{
+    SpgRun &r = p->run;
+    const pasc_gb300_spgqp_opts *o = &r.o;
+    const long N = p->N, T = p->T;
+    const int K = p->K;
+    cudaStream_t s = p->stream;
+    double v[3];
+    CU(cudaEventRecord(p->ev0, s));
+    for (long q = 0; q < n && r.status == PASC_SPG_RUNNING; q++) {
+        if (r.it >= o->maxit) { r.status = PASC_SPG_MAXIT; break; }
+        r.it += 1;
+        CU(launch_xmay_f64(p->d, p->x, r.alpha, p->g, N, s));    // :146-147
+        CU(launch_project_f64(p->d, T, K, s));                    // :153
+        CU(launch_axpy_f64(p->d, -1.0, p->x, N, s));              // :158
+        CU(launch_matmult_f64(p->d, p->Ad, T, K, p->coeffA, s));  // :164-165
+        r.hessmult += 1;
+        CU(launch_dots_f64(3, p->d, p->d, p->d, p->Ad, p->d, p->g, N, p->red, p->red_out, s));  // :357-363
+        r.launches += 5;
+        CHK(read_red(p, 3, v));
+        const double dd = v[0], dAd = v[1], gd = v[2];
+        if (!(isfinite(dd) && isfinite(dAd) && isfinite(gd))) { r.status = PASC_SPG_NONFINITE; r.it -= 1; break; }
+        if (!(dd > 0.0)) { r.status = PASC_SPG_DAD_ZERO; r.it -= 1; break; }
+        double beta, alpha_next;
+        if (dAd > 0.0) {
+            double fx_max = r.fs[0];
+            for (int i = 0; i < o->m; i++) fx_max = r.fs[i] > fx_max ? r.fs[i] : fx_max;  // :176
+            const double xi = (fx_max - r.fx) / dAd;  // :182-195
+            const double beta_bar = -gd / dAd;
+            double beta_hat = o->gamma * beta_bar + sqrt(o->gamma * o->gamma * beta_bar * beta_bar + 2 * xi);
+            if (beta_hat < o->sigma1) beta_hat = o->sigma1;
+            beta = beta_hat < o->sigma2 ? beta_hat : o->sigma2;
+            alpha_next = dd / dAd;  // :216
+        } else if (gd < 0.0) {
+            // linear along d (A_hat d = 0): the reference's division by zero falls through to
+            // beta = sigma2; take that step and keep alpha finite
+            beta = o->sigma2;
+            alpha_next = r.alpha;
+        } else {
+            r.status = PASC_SPG_DAD_ZERO;
+            r.it -= 1;
+            break;
+        }
+        CU(launch_axpy_f64(p->x, beta, p->d, N, s));   // :200
+        CU(launch_axpy_f64(p->g, beta, p->Ad, N, s));  // :201
+        CU(launch_fx_f64(p->x, p->g, p->b, N, p->red, p->red_out, s));  // :209
+        r.launches += 3;
+        CHK(read_red(p, 1, v));
+        r.fx_old = r.fx;
+        r.fx = 0.5 * v[0];
+        if (++r.fs_last >= o->m) r.fs_last = 0;  // :210
+        r.fs[r.fs_last] = r.fx;
+        r.alpha = alpha_next;
+        r.dd = dd;
+        r.dAd = dAd;
+        if (!isfinite(r.fx)) { r.status = PASC_SPG_NONFINITE; break; }
+        if ((o->stop_difff && fabs(r.fx - r.fx_old) < o->eps) || (o->stop_normgp && dd < o->eps) ||
+            (o->stop_normgp_normb && dd < o->eps * r.normb) || (o->stop_Anormgp && dAd < o->eps) ||
+            (o->stop_Anormgp_normb && dAd < o->eps * r.normb)) {
+            r.status = PASC_SPG_CONVERGED;
+        }
+    }
+    if (r.status == PASC_SPG_RUNNING && r.it >= o->maxit) r.status = PASC_SPG_MAXIT;
+    CU(cudaEventRecord(p->ev1, s));
+    CU(cudaEventSynchronize(p->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+    r.time_s += ms * 1e-3;
+    p->fx_last = r.fx;
+    p->have_fx = true;
+    return PASC_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// SPG-QP, mixed fused path: one sweep per iteration, state on the device, host polls.
+// ---------------------------------------------------------------------------------------
+static int sweep_args(pasc_gb300_problem *p, SweepArgs *a)
+{
+    a->data = p->data32;
+    a->theta = p->theta32;
+    a->xb0 = p->xb[0];
+    a->xb1 = p->xb[1];
+    a->gb0 = p->gb[0];
+    a->gb1 = p->gb[1];
+    a->partials = p->partials;
+    a->st = p->st;
+    a->T = p->T;
+    return PASC_OK;
+}
+
+static constexpr int GRAPH_CHUNK = 16;
+
+static int ensure_chunk_graph(pasc_gb300_problem *p)
+{
+    if (p->chunk_graph) return PASC_OK;
+    CU(cudaStreamSynchronize(p->stream));
+    SweepArgs a;
+    sweep_args(p, &a);
+    cudaGraph_t graph;
+    CU(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < GRAPH_CHUNK; i++) {
+        cudaError_t e = launch_sweep(p->K, false, p->grid_sweep, a, p->stream);
+        if (e != cudaSuccess) {
+            cudaStreamEndCapture(p->stream, &graph);
+            return fail(PASC_ERR_CUDA, "sweep capture: %s", cudaGetErrorString(e));
+        }
+    }
+    CU(cudaStreamEndCapture(p->stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&p->chunk_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        p->chunk_graph = nullptr;
+        return fail(PASC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+    p->chunk_graph_len = GRAPH_CHUNK;
+    return PASC_OK;
+}
+
+static void sync_run_from_device(pasc_gb300_problem *p)
+{
+    const SpgDevState *h = p->st_h;
+    SpgRun &r = p->run;
+    r.it = h->it;
+    r.hessmult = h->hessmult;
+    r.status = h->status;
+    r.fx = h->fx;
+    r.dd = h->dd;
+    r.dAd = h->dAd;
+    p->cur = h->cur;
+    p->fx_last = h->fx;
+    p->have_fx = true;
+}
+
+// spgqpsolver.cpp:104-137 plus the first direction (one INIT sweep)
+static int mixed_start(pasc_gb300_problem *p)
+{
+    const pasc_gb300_spgqp_opts *o = &p->run.o;
+    if (o->stop_normgp_normb || o->stop_Anormgp_normb)
+        return fail(PASC_ERR_NOTSUPP, "spgqp: ||b||-scaled stopping tests need the fp64 path");
+    cudaStream_t s = p->stream;
+    CHK(ensure_chunk_graph(p));
+    SpgDevState *h = p->st_h;
+    memset(h, 0, sizeof(SpgDevState));
+    h->alpha_prev = o->alphainit;
+    h->alpha_cur = o->alphainit;  // alpha of the first direction (:108)
+    h->coeff = p->coeffA;
+    h->bscale = p->coeffB;
+    h->eps = o->eps;
+    h->gamma = o->gamma;
+    h->sigma1 = o->sigma1;
+    h->sigma2 = o->sigma2;
+    h->maxit = o->maxit;
+    h->m = o->m;
+    h->stop_difff = o->stop_difff;
+    h->stop_normgp = o->stop_normgp;
+    h->stop_Anormgp = o->stop_Anormgp;
+    h->status = PASC_SPG_RUNNING;
+    h->cur = p->cur;
+    SweepArgs a;
+    sweep_args(p, &a);
+    CU(cudaEventRecord(p->ev0, s));
+    CU(cudaMemcpyAsync(p->st, h, sizeof(SpgDevState), cudaMemcpyHostToDevice, s));
+    CU(launch_sweep(p->K, true, p->grid_sweep_init, a, s));
+    CU(cudaEventRecord(p->ev1, s));
+    CU(cudaMemcpyAsync(h, p->st, sizeof(SpgDevState), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+    p->run.launches += 1;
+    p->run.time_s += ms * 1e-3;
+    sync_run_from_device(p);
+    return PASC_OK;
+}
+
+// Launches n regular sweeps.  With poll, the status word is read after chunks of growing
+// length and launching stops once the solve has ended; without poll exactly n sweeps are
+// launched back to back (sweeps after the end return at once) and timed as one region.
+static int mixed_iterate(pasc_gb300_problem *p, long n, int poll)
+{
+    cudaStream_t s = p->stream;
+    SweepArgs a;
+    sweep_args(p, &a);
+    SpgDevState *h = p->st_h;
+    if (p->run.status != PASC_SPG_RUNNING) return PASC_OK;
+    const long room = p->run.o.maxit - p->run.it;
+    if (n > room) n = room;
+    long done = 0;
+    int step = 0;
+    const int sched[] = {2, 4, 8};
+    CU(cudaEventRecord(p->ev0, s));
+    while (done < n) {
+        long want = poll ? (step < 3 ? sched[step] : GRAPH_CHUNK) : GRAPH_CHUNK;
+        step++;
+        if (want > n - done) want = n - done;
+        if (want == GRAPH_CHUNK) {
+            CU(cudaGraphLaunch(p->chunk_graph, s));
+        } else {
+            for (long q = 0; q < want; q++) CU(launch_sweep(p->K, false, p->grid_sweep, a, s));
+        }
+        done += want;
+        p->run.launches += (int)want;
+        if (poll) {
+            CU(cudaMemcpyAsync(h, p->st, sizeof(SpgDevState), cudaMemcpyDeviceToHost, s));
+            CU(cudaStreamSynchronize(s));
+            if (h->status != PASC_SPG_RUNNING) break;
+        }
+    }
+    CU(cudaEventRecord(p->ev1, s));
+    CU(cudaMemcpyAsync(h, p->st, sizeof(SpgDevState), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+    p->run.time_s += ms * 1e-3;
+    p->run.last_iterate_ms = ms;
+    p->run.last_iterate_launches = (int)done;
+    sync_run_from_device(p);
+    if (p->run.status == PASC_SPG_RUNNING && p->run.it >= p->run.o.maxit) p->run.status = PASC_SPG_MAXIT;
+    return PASC_OK;
+}
+
+static int check_opts(const pasc_gb300_spgqp_opts *o)
+{
+    if (!o) return fail(PASC_ERR_ARG, "spgqp: NULL options");
+    if (o->m < 1 || o->m > MMAX_STATE) return fail(PASC_ERR_ARG, "spgqp: m must be in [1, %d]", MMAX_STATE);
+    if (o->maxit < 0) return fail(PASC_ERR_ARG, "spgqp: maxit must be >= 0");
+    return PASC_OK;
+}
+
+static int spgqp_start(pasc_gb300_problem *p, const pasc_gb300_spgqp_opts *o)
+{
+    p->run = SpgRun();
+    p->run.o = *o;
+    p->run.started = true;
+    return p->precision == PASC_PREC_FP64 ? fp64_start(p) : mixed_start(p);
+}
+
+static int spgqp_iterate(pasc_gb300_problem *p, long n, int poll)
+{
+    return p->precision == PASC_PREC_FP64 ? fp64_iterate(p, n) : mixed_iterate(p, n, poll);
+}
+
+int pasc_gb300_spgqp_start(pasc_gb300_problem *p, const pasc_gb300_spgqp_opts *o)
+{
+    if (!p) return fail(PASC_ERR_ARG, "spgqp_start: NULL problem");
+    CHK(check_opts(o));
+    CU(cudaSetDevice(p->device));
+    return spgqp_start(p, o);
+}
+
+int pasc_gb300_spgqp_iterate(pasc_gb300_problem *p, long n, int poll, pasc_gb300_spgqp_stats *st)
+{
+    if (!p) return fail(PASC_ERR_ARG, "spgqp_iterate: NULL problem");
+    if (!p->run.started) return fail(PASC_ERR_STATE, "spgqp_iterate: call pasc_gb300_spgqp_start first");
+    if (n < 0) return fail(PASC_ERR_ARG, "spgqp_iterate: n must be >= 0");
+    CU(cudaSetDevice(p->device));
+    CHK(spgqp_iterate(p, n, poll));
+    fill_stats(p->run, st);
+    return PASC_OK;
+}
+
+int pasc_gb300_spgqp_last_iterate(pasc_gb300_problem *p, double *ms, int *launches)
+{
+    if (!p) return fail(PASC_ERR_ARG, "spgqp_last_iterate: NULL problem");
+    if (ms) *ms = p->run.last_iterate_ms;
+    if (launches) *launches = p->run.last_iterate_launches;
+    return PASC_OK;
+}
+
+int pasc_gb300_spgqp_solve(pasc_gb300_problem *p, const pasc_gb300_spgqp_opts *o, pasc_gb300_spgqp_stats *st)
+{
+    if (!p) return fail(PASC_ERR_ARG, "spgqp_solve: NULL problem");
+    CHK(check_opts(o));
+    CU(cudaSetDevice(p->device));
+    CHK(spgqp_start(p, o));
+    CHK(spgqp_iterate(p, o->maxit, 1));
+    if (p->run.status == PASC_SPG_RUNNING) p->run.status = PASC_SPG_MAXIT;
+    fill_stats(p->run, st);
+    return PASC_OK;
+}
+
+int pasc_gb300_get_fx(pasc_gb300_problem *p, double *fx)
+{
+    if (!p || !fx) return fail(PASC_ERR_ARG, "get_fx: NULL argument");
+    if (!p->have_fx) return fail(PASC_ERR_STATE, "get_fx: no solve since the last change of gamma");
+    *fx = p->fx_last;
+    return PASC_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// TSSolver::solve (include/general/solver/tssolver.h:492-715)
+// ---------------------------------------------------------------------------------------
+int pasc_gb300_ts_solve(pasc_gb300_problem *p, const pasc_gb300_ts_opts *ts,
+                        const pasc_gb300_spgqp_opts *spg, const double *gamma_restart,
+                        pasc_gb300_ts_stats *out)
+{
+    if (!p || !ts || !spg) return fail(PASC_ERR_ARG, "ts_solve: NULL argument");
+    CHK(check_opts(spg));
+    CU(cudaSetDevice(p->device));
+    auto t0 = std::chrono::steady_clock::now();
+    const int annealing = ts->annealing > 0 ? ts->annealing : 1;
+    std::vector<double> gbest, tbest;
+    double best_aic = DBL_MAX, keepL = DBL_MAX, keepdL = DBL_MAX, keepaic = DBL_MAX;
+    int keepit = 0, it_sum = 0, spg_it = 0, spg_hm = 0, launches = 0, increased = 0;
+
+    for (int an = 0; an < annealing; an++) {
+        if (ts->init_permute) {  // :528-530
+            CHK(permute_gamma_async(p));
+            launches += p->precision == PASC_PREC_FP64 ? 1 : 1;
+        }
+        double L = DBL_MAX, L_old, deltaL = DBL_MAX;
+        int it;
+        for (it = 0; it < ts->maxit; it++) {
+            if (!ts->thetasolved) CHK(update_theta_async(p, &launches));  // :550
+            CHK(update_b_async(p, &launches));                            // :586
+            pasc_gb300_spgqp_stats ss;
+            CHK(pasc_gb300_spgqp_solve(p, spg, &ss));                     // :590
+            spg_it += ss.it;
+            spg_hm += ss.hessmult;
+            launches += ss.kernel_launches;
+            L_old = L;  // :618-620
+            L = ss.fx;
+            deltaL = fabs(L - L_old);
+            if (L - L_old > 0) increased++;  // :637-639
+            if (ts->relative ? (deltaL < ts->eps * fabs(L)) : (deltaL < ts->eps)) break;  // :642
+        }
+        it_sum += it;
+        const double aic = 2 * log(L) + p->K;  // graphh1fem.h:444-447
+        if (annealing <= 1 || aic < best_aic) {
+            if (annealing > 1) {
+                gbest.resize(p->N);
+                tbest.resize((size_t)p->K * p->xdim);
+                CHK(pasc_gb300_get_gamma(p, gbest.data()));
+                CHK(pasc_gb300_get_theta(p, tbest.data()));
+            }
+            best_aic = aic;
+            keepL = L;
+            keepdL = deltaL;
+            keepaic = aic;
+            keepit = it;
+        }
+        if (an < annealing - 1 && gamma_restart) CHK(pasc_gb300_set_gamma(p, gamma_restart));  // :700-702
+    }
+    if (annealing > 1) {
+        CHK(pasc_gb300_set_gamma(p, gbest.data()));
+        CHK(pasc_gb300_set_theta(p, tbest.data()));
+        p->fx_last = keepL;
+        p->have_fx = true;
+    }
+    CU(cudaStreamSynchronize(p->stream));
+    if (out) {
+        out->it_last = keepit;
+        out->it_sum = it_sum;
+        out->spg_it_sum = spg_it;
+        out->spg_hessmult_sum = spg_hm;
+        out->kernel_launches = launches;
+        out->L_increased = increased;
+        out->L = keepL;
+        out->deltaL = keepdL;
+        out->aic = keepaic;
+        out->time_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return PASC_OK;
+}
+
+int pasc_gb300_abserr_reconstructed(pasc_gb300_problem *p, const double *solution, double *abserr)
+{
+    if (!p || !solution || !abserr) return fail(PASC_ERR_ARG, "abserr: NULL argument");
+    CU(cudaSetDevice(p->device));
+    const double *g64 = nullptr;
+    CHK(gamma64(p, &g64));
+    // the solution goes through the Ad buffer (fp64) or the tail of a scratch allocation
+    double *sol_d = nullptr;
+    CU(cudaMallocAsync((void **)&sol_d, sizeof(double) * p->T, p->stream));
+    CU(cudaMemcpyAsync(sol_d, solution, sizeof(double) * p->T, cudaMemcpyHostToDevice, p->stream));
+    cudaError_t e = launch_recon_abserr(g64, p->theta64, sol_d, p->T, p->K, p->red, p->red_out, p->stream);
+    cudaFreeAsync(sol_d, p->stream);
+    if (e != cudaSuccess) return fail(PASC_ERR_CUDA, "abserr kernel: %s", cudaGetErrorString(e));
+    double v[1];
+    CHK(read_red(p, 1, v));
+    *abserr = v[0];
+    return PASC_OK;
+}
+
+int pasc_gb300_argmax_labels(pasc_gb300_problem *p, int *labels)
+{
+    if (!p || !labels) return fail(PASC_ERR_ARG, "argmax: NULL argument");
+    CU(cudaSetDevice(p->device));
+    const double *g64 = nullptr;
+    CHK(gamma64(p, &g64));
+    CU(launch_argmax(g64, p->labels_d, p->T, p->K, p->stream));
+    CU(cudaMemcpyAsync(labels, p->labels_d, sizeof(int) * p->T, cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// device-pointer kernels
+// ---------------------------------------------------------------------------------------
+int pasc_gb300_project_f64(double *x_dev, long T, int K, void *stream)
+{
+    if (!x_dev && T > 0) return fail(PASC_ERR_ARG, "project_f64: NULL x");
+    if (T < 0 || K < 1 || K > KMAX_PLAIN) return fail(PASC_ERR_ARG, "project_f64: bad T/K (%ld, %d)", T, K);
+    CU(launch_project_f64(x_dev, T, K, (cudaStream_t)stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_project_f32(float *x_dev, long T, int K, void *stream)
+{
+    if (!x_dev && T > 0) return fail(PASC_ERR_ARG, "project_f32: NULL x");
+    if (T < 0 || K < 1 || K > KMAX_GROUP) return fail(PASC_ERR_ARG, "project_f32: bad T/K (%ld, %d)", T, K);
+    CU(launch_project_f32(x_dev, T, K, (cudaStream_t)stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_fem_h1_matmult_f64(const double *x_dev, double *y_dev, long T, int K, double coeff, void *stream)
+{
+    if ((!x_dev || !y_dev) && T > 0) return fail(PASC_ERR_ARG, "matmult_f64: NULL pointer");
+    if (T < 0 || K < 1) return fail(PASC_ERR_ARG, "matmult_f64: bad T/K");
+    CU(launch_matmult_f64(x_dev, y_dev, T, K, coeff, (cudaStream_t)stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_fem_h1_matmult_f32(const float *x_dev, float *y_dev, long T, int K, float coeff, void *stream)
+{
+    if ((!x_dev || !y_dev) && T > 0) return fail(PASC_ERR_ARG, "matmult_f32: NULL pointer");
+    if (T < 0 || K < 1) return fail(PASC_ERR_ARG, "matmult_f32: bad T/K");
+    CU(launch_matmult_f32(x_dev, y_dev, T, K, coeff, (cudaStream_t)stream));
+    return PASC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,67 @@
+"""Full-size workloads (T = 1e6 and the T = 1e7, K = 3 benchmark signal) on the GPU.
+
+At these sizes the FP64 CPU oracle is too slow for a test, so the mixed path is checked
+against the fp64 GPU path (itself pinned to the oracle at small sizes) and through
+size-independent properties: feasibility of every timestep, the reported objective equal to
+the objective recomputed on the host from the returned gamma, and label agreement."""
+import numpy as np
+import pytest
+
+from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Problem, capi, datagen
+
+pytestmark = pytest.mark.gpu
+
+
+def _objective(gamma, data, theta, T, K, eps2):
+    """1/2 x'Ax - b'x in FP64 on the host (A = eps2/T * A_hat, b = -(x_t - theta_k)^2 / T)."""
+    g = gamma.reshape(T, K)
+    dif = np.diff(g, axis=0)
+    quad = (eps2 / T) * np.sum(dif * dif)  # x'A_hat x = 2 sum (x_{t+1} - x_t)^2; times 1/2
+    b = -((data[:, None] - theta[None, :]) ** 2) / T
+    return quad - np.sum(b * g)
+
+
+def test_mixed_vs_fp64_gpu_1e6(gpulib):
+    sig = datagen.signal1d_cfg1(seed=5, T=1_000_000)
+    T, K, eps2 = sig.T, sig.K, 100.0
+    th = np.array([0.0, 1.0, 2.0])
+    res = {}
+    for prec in (PASC_PREC_FP64, PASC_PREC_MIXED):
+        with Problem(T, K, eps2, precision=prec) as p:
+            p.set_data(sig.data)
+            p.set_gamma(sig.gamma0)
+            p.set_theta(th)
+            p.permute_gamma()
+            p.update_b()
+            st = p.spgqp_solve(capi.spgqp_opts(maxit=3000, eps=1e-10, m=10))
+            res[prec] = (st, p.get_gamma())
+    st64, g64 = res[PASC_PREC_FP64]
+    st32, g32 = res[PASC_PREC_MIXED]
+    assert abs(st32.fx - st64.fx) <= 1e-6 * abs(st64.fx), (st32.fx, st64.fx, st32.it, st64.it)
+    lab64 = np.argmax(g64.reshape(T, K), axis=1)
+    lab32 = np.argmax(g32.reshape(T, K), axis=1)
+    assert np.mean(lab64 == lab32) >= 0.9999
+    f_host = _objective(g32, sig.data, th, T, K, eps2)
+    assert abs(f_host - st32.fx) <= 1e-6 * abs(st64.fx)
+
+
+def test_benchmark_signal_1e7_properties(gpulib):
+    sig = datagen.signal1d_cfg1()
+    T, K = sig.T, sig.K
+    with Problem(T, K, 10.0, precision=PASC_PREC_MIXED) as p:
+        p.set_data(sig.data)
+        p.set_gamma(sig.gamma0)
+        st = p.ts_solve(capi.ts_opts(maxit=30, relative=1, eps=1e-6), capi.spgqp_opts(m=10, eps=1e-6))
+        assert st.L > 0 and np.isfinite(st.L)
+        g = p.get_gamma()
+        th = p.get_theta()
+    G = g.reshape(T, K)
+    assert np.all(G >= 0.0)
+    assert np.max(np.abs(G.sum(axis=1) - 1.0)) <= 1e-5
+    f_host = _objective(g, sig.data, th, T, K, 10.0)
+    assert abs(f_host - st.L) <= 1e-6 * abs(st.L)
+    # clustering quality: thetas near the true levels, labels mostly right
+    order = np.argsort(th)
+    assert np.max(np.abs(th[order] - sig.levels)) < 0.05
+    lab = order.argsort()[np.argmax(G, axis=1)]
+    assert np.mean(lab == sig.labels) > 0.99

@@ -1,0 +1,109 @@
+"""Host-side logic without a GPU: seeded generators, PETSc binary I/O, the option mapping of
+the reference-style classes, and the replica timing helpers over two gloo ranks."""
+import os
+import socket
+import subprocess
+import sys
+import textwrap
+
+import numpy as np
+import pytest
+
+from pasc_inference_gb300 import datagen, petscio, spg_opts_from, ts_opts_from, Decomposition, PascError
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_generator_is_deterministic_and_shaped():
+    a = datagen.uniform(5, 1, 1000)
+    b = datagen.uniform(5, 1, 1000)
+    np.testing.assert_array_equal(a, b)
+    assert a.min() >= 0.0 and a.max() < 1.0
+    assert abs(a.mean() - 0.5) < 0.05
+    # counter-based: a window equals the slice of the full stream
+    np.testing.assert_array_equal(datagen.uniform(5, 1, 10, offset=500), a[500:510])
+    z = datagen.normal(9, 2, 200_000)
+    assert abs(z.mean()) < 0.01 and abs(z.std() - 1.0) < 0.01
+
+
+def test_signal_configs():
+    s0 = datagen.signal1d_cfg0()
+    assert s0.T == 10_000 and s0.K == 2 and s0.gamma0.size == 20_000
+    lens = np.diff(np.flatnonzero(np.diff(s0.labels)))
+    assert lens.min() >= 500 and lens.max() <= 2000
+    assert set(np.unique(s0.clean)) <= {1.0, 2.0}
+    s1 = datagen.signal1d_cfg1(T=200_000)
+    assert s1.K == 3 and set(np.unique(s1.clean)) <= {0.0, 1.0, 2.0}
+    assert abs(np.std(s1.data - s1.clean) - 0.5) < 0.01
+    b = datagen.batched(8)
+    assert all(1000 <= x.T <= 1_000_000 and 2 <= x.K <= 5 and 1 <= x.epssqr <= 1000 for x in b)
+    assert all(np.all(np.diff(x.levels) >= 0) for x in b)
+
+
+def test_normalised_gamma():
+    g0 = datagen.uniform(1, 0, 30)
+    g = datagen.normalised_gamma(g0, 10, 3).reshape(10, 3)
+    np.testing.assert_allclose(g.sum(axis=1), 1.0)
+
+
+def test_petsc_vec_roundtrip(tmp_path):
+    v = np.random.default_rng(0).normal(size=123)
+    p = str(tmp_path / "v.bin")
+    petscio.save_vec(p, v)
+    raw = open(p, "rb").read()
+    assert raw[:4] == (1211214).to_bytes(4, "big") and raw[4:8] == (123).to_bytes(4, "big")
+    np.testing.assert_array_equal(petscio.load_vec(p), v)
+
+
+def test_reference_option_names():
+    o = spg_opts_from({"spgqpsolver_m": 10, "spgqpsolver_eps": 1e-6, "spgqpsolver_stop_normgp": True})
+    assert (o.m, o.eps, o.stop_normgp) == (10, 1e-6, 1)
+    t = ts_opts_from({"tssolver_maxit": 5, "tssolver_init_permute": False})
+    assert (t.maxit, t.init_permute) == (5, 0)
+
+
+def test_decomposition_limits():
+    d = Decomposition(100, 1, 3, 1, 1)
+    assert (d.get_T(), d.get_K(), d.get_R()) == (100, 3, 1)
+    with pytest.raises(PascError):
+        Decomposition(100, 4, 3, 1, 1)
+    with pytest.raises(PascError):
+        Decomposition(100, 1, 3, 1, 2)
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def test_replica_timing_two_gloo_ranks(tmp_path):
+    """Two ranks: barrier, max and sum over ranks, as bench.py combines replica timings."""
+    pytest.importorskip("torch")
+    script = tmp_path / "w.py"
+    script.write_text(textwrap.dedent(f"""
+        import os, sys, json
+        sys.path.insert(0, {ROOT!r})
+        from pasc_inference_gb300 import dist
+        info = dist.init(timeout_s=60)
+        dist.barrier(info)
+        mx = dist.max_over_ranks(info, 10.0 + info.rank)
+        sm = dist.sum_over_ranks(info, 1.0)
+        print(json.dumps({{"rank": info.rank, "ws": info.world_size, "max": mx, "sum": sm}}))
+        dist.finalize(info)
+    """))
+    port = _free_port()
+    procs = []
+    for r in range(2):
+        env = dict(os.environ, RANK=str(r), WORLD_SIZE="2", LOCAL_RANK=str(r),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, str(script)], env=env, stdout=subprocess.PIPE,
+                                      stderr=subprocess.PIPE, text=True))
+    outs = [p.communicate(timeout=120) for p in procs]
+    for p, (o, e) in zip(procs, outs):
+        assert p.returncode == 0, e
+    import json
+    res = [json.loads(o.strip().splitlines()[-1]) for o, _ in outs]
+    assert all(r["ws"] == 2 and r["max"] == 11.0 and r["sum"] == 2.0 for r in res)

@@ -1,0 +1,68 @@
+"""The oracle against the reference's own code compiled here (oracle/_ref), on fresh random
+cases.  Skipped where the reference tree is not available (e.g. on the GPU machine)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pasc_oracle as O
+
+pytestmark = pytest.mark.skipif(
+    not os.path.exists(os.path.join(os.environ.get("PASC_REFERENCE", "/root/reference"),
+                                    "include/general/solver/spgqpsolver.h")),
+    reason="reference tree not available")
+
+
+@pytest.fixture(scope="module")
+def ref():
+    O.build()
+    if O.build_ref() is None:
+        pytest.skip("oracle/_ref not built")
+    return O
+
+
+@pytest.mark.parametrize("K", [1, 2, 3, 6, 9, 40])
+def test_projection_random(ref, K):
+    rng = np.random.default_rng(K)
+    T = 400
+    x = rng.normal(size=T * K) * rng.choice([0.01, 1.0, 100.0], size=T * K)
+    np.testing.assert_array_equal(ref.project(x, T, K), ref.ref_project(x, T, K))
+
+
+@pytest.mark.parametrize("T,K,eps2,m", [(700, 2, 3.0, 20), (900, 3, 300.0, 10), (50, 7, 30.0, 5)])
+def test_spgqp_random(ref, T, K, eps2, m):
+    rng = np.random.default_rng(T + K)
+    data = rng.normal(size=T) * 0.7 + rng.integers(0, K, size=T)
+    b = ref.residual_b(data, np.linspace(0, K - 1, K), T, K)
+    x0 = rng.random(T * K)
+    coeff = ref.A_coeff(eps2, T)
+    xr, it, hm, fx = ref.ref_spgqp_solve(b, x0, T, K, coeff, spgqpsolver_m=m)
+    xo, r, _ = ref.spgqp_solve(b, x0, T, K, coeff, ref.spg_opts(m=m))
+    assert (r.it, r.hessmult, r.fx) == (it, hm, fx)
+    np.testing.assert_array_equal(xo, xr)
+
+
+@pytest.mark.parametrize("eps2", [0.5, 20.0, 2000.0])
+def test_tssolver_random(ref, eps2):
+    rng = np.random.default_rng(int(eps2 * 10))
+    T, K = 1500, 3
+    data = np.repeat(rng.integers(0, 3, size=15), 100) + rng.normal(size=T) * 0.4
+    g0 = rng.random(T * K)
+    gr, thr, res = ref.ref_tssolver_solve(data, g0, np.zeros(K), T, K, eps2)
+    go, tho, r, _ = ref.tssolver_solve(data, g0, np.zeros(K), T, K, eps2)
+    assert r.L == res["L"] and r.it_last == res["it_last"] and r.aic == res["aic"]
+    np.testing.assert_array_equal(go, gr)
+    np.testing.assert_array_equal(tho, thr)
+
+
+def test_tssolver_given_theta(ref):
+    rng = np.random.default_rng(5)
+    T, K = 800, 2
+    data = np.repeat(rng.integers(1, 3, size=8), 100) + rng.normal(size=T) * 0.3
+    g0 = rng.random(T * K)
+    th0 = np.array([1.0, 2.0])
+    gr, thr, res = ref.ref_tssolver_solve(data, g0, th0, T, K, 10.0, theta_given=True)
+    go, tho, r, _ = ref.tssolver_solve(data, g0, th0, T, K, 10.0, ts=ref.ts_opts(thetasolved=1))
+    assert r.L == res["L"]
+    np.testing.assert_array_equal(go, gr)
+    np.testing.assert_array_equal(tho, th0)
