@@ -46,7 +46,7 @@ struct SpgDevState {
 struct SweepArgs {
     const float *data;  // T (xdim == 1)
     const float *theta; // K
-    float *xb0, *xb1, *gb0, *gb1;
+    float *xb0, *xb1;   // ping-pong pair holding x (gamma); buffer st->cur is current
     double *partials;   // gridDim.x * 4
     SpgDevState *st;
     long T;
@@ -65,6 +65,7 @@ struct ThetaArgs {
 
 // Launchers (kernels_fused.cu).  Return a cudaError_t.
 int sweep_block_threads();
+int sweep_tile_width();
 int sweep_blocks_per_sm(int K, bool init);
 cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);
 cudaError_t launch_theta_f32(int K, int grid, const ThetaArgs &a, cudaStream_t s);

@@ -1,16 +1,20 @@
 // kernels_fused.cu -- mixed-precision (FP32 state, FP64 reductions) SPG-QP kernels.
 //
-// One HBM sweep per SPG iteration.  The reference iteration
+// One HBM sweep per SPG iteration, and only gamma (x) is stored.  The reference iteration
 // (src/petscvector/solver/spgqpsolver.cpp:140-216)
 //     d = P(x - alpha g) - x ; Ad = coeff*A_hat d ; dd, dAd, gd ; beta (GLL) ;
 //     x += beta d ; g += beta Ad ; f = 1/2 (g - b)'x ; alpha = dd/dAd
-// is re-timed so that one pass over (x, g) finishes iteration c+1 and starts iteration c+2:
-// the sweep reads x^c, g^c, recomputes d_{c+1} (and Ad_{c+1} from a 2-timestep halo that is
-// recomputed, never stored), forms x^{c+1}, g^{c+1} and f^{c+1}, then d_{c+2}, Ad_{c+2} and
-// their dots.  x^{c+1}, g^{c+1} go to the other half of a ping-pong pair.  b is formed in
-// registers from the data and theta (b_tk = bscale*(x_t - theta_k)^2,
-// src/petscvector/model/graphh1fem.cpp:258-286) and never stored.  HBM traffic per
-// iteration: read x, g, data; write x, g = 16*K*T + 4*T bytes.
+// keeps the gradient in memory and updates it recursively.  Here the gradient is recomputed
+// on chip from x, g = coeff*A_hat x - b (the same value in exact arithmetic; the stencil has
+// the footprint the recursive update needs anyway), so nothing but x crosses HBM and FP32
+// rounding cannot accumulate in g over the iterations.  b is formed in registers from the
+// data and theta (b_tk = bscale*(x_t - theta_k)^2, src/petscvector/model/graphh1fem.cpp:258-286).
+//
+// The sweep is re-timed so that one pass finishes iteration c+1 and starts iteration c+2:
+// it reads x^c, forms g^c, d_{c+1}, x^{c+1} = x^c + beta_{c+1} d_{c+1}, g^{c+1}, f^{c+1},
+// then d_{c+2} and its dots.  The halo (2 timesteps before a tile, 3 after) is recomputed,
+// never stored; x^{c+1} goes to the other half of a ping-pong pair.  HBM traffic per
+// iteration: read x and the data, write x = 8*K*T + 4*T bytes.
 //
 // Reductions: per thread in compensated FP32, per block and per grid in FP64 (fixed order,
 // deterministic for a fixed grid).  The last block applies the step-length and GLL rules in
@@ -23,11 +27,13 @@
 
 namespace pasc {
 
-constexpr int SWEEP_NT = 256;          // threads per block = timesteps per tile incl. halo
-constexpr int SWEEP_HALO = 2;
-constexpr int SWEEP_W = SWEEP_NT - 2 * SWEEP_HALO;  // owned timesteps per tile
+constexpr int SWEEP_NT = 256;  // threads per block = timesteps per tile incl. halo
+constexpr int SWEEP_HL = 2;    // halo timesteps before the owned range
+constexpr int SWEEP_HR = 3;    // halo timesteps after it
+constexpr int SWEEP_W = SWEEP_NT - SWEEP_HL - SWEEP_HR;  // owned timesteps per tile
 
 int sweep_block_threads() { return SWEEP_NT; }
+int sweep_tile_width() { return SWEEP_W; }
 
 // Row sum of A_hat (FEM-H1, R = 1) at timestep t for component k from values staged in
 // shared memory at slots i-1, i, i+1 (stride K); the order of the assembled CSR row.
@@ -46,8 +52,9 @@ __device__ __forceinline__ float stencil_row(const float *s, int i, int k, long 
 template <int K, bool INIT>
 __global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
 {
-    __shared__ float s_a[SWEEP_NT * K];
-    __shared__ float s_b[SWEEP_NT * K];
+    __shared__ float s_x[SWEEP_NT * K];  // x^c
+    __shared__ float s_y[SWEEP_NT * K];  // x^{c+1}
+    __shared__ float s_d[SWEEP_NT * K];  // d_{c+2}
     __shared__ double s_red[4 * (SWEEP_NT / 32)];
 
     SpgDevState *st = a.st;
@@ -55,9 +62,7 @@ __global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
 
     const int cur = st->cur;
     const float *xin = cur ? a.xb1 : a.xb0;
-    const float *gin = cur ? a.gb1 : a.gb0;
     float *xout = cur ? a.xb0 : a.xb1;
-    float *gout = cur ? a.gb0 : a.gb1;
     const float a0 = (float)st->alpha_prev;
     const float beta = (float)st->beta;
     const float a1 = (float)st->alpha_cur;
@@ -74,62 +79,64 @@ __global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
     const long ntiles = (T + SWEEP_W - 1) / SWEEP_W;
 
     for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long t = tile * SWEEP_W - SWEEP_HALO + i;
+        const long t = tile * SWEEP_W - SWEEP_HL + i;
         const bool in = (t >= 0 && t < T);
 
-        float xo[K], go[K];
+        // phase A: x^c (INIT: the projected start point) and b_t in registers
+        float xc[K], bk[K];
         float dv = 0.f;
         if (in) {
 #pragma unroll
-            for (int k = 0; k < K; k++) {
-                xo[k] = __ldcs(xin + t * K + k);
-                go[k] = __ldcs(gin + t * K + k);
-            }
+            for (int k = 0; k < K; k++) xc[k] = __ldcs(xin + t * K + k);
             dv = __ldg(a.data + t);
         } else {
 #pragma unroll
-            for (int k = 0; k < K; k++) { xo[k] = 0.f; go[k] = 0.f; }
+            for (int k = 0; k < K; k++) xc[k] = 0.f;
         }
-
-        // phase 1: INIT projects the start point; otherwise recompute d_{c+1}
-        float p1[K];
-        if (INIT) {
+        if (INIT) project_reg<K>(xc);
 #pragma unroll
-            for (int k = 0; k < K; k++) p1[k] = xo[k];
-            project_reg<K>(p1);
-#pragma unroll
-            for (int k = 0; k < K; k++) s_a[i * K + k] = in ? p1[k] : 0.f;
-        } else {
-#pragma unroll
-            for (int k = 0; k < K; k++) p1[k] = __fsub_rn(xo[k], __fmul_rn(a0, go[k]));
-            project_reg<K>(p1);
-#pragma unroll
-            for (int k = 0; k < K; k++) {
-                p1[k] = __fsub_rn(p1[k], xo[k]);  // d_{c+1}
-                s_a[i * K + k] = in ? p1[k] : 0.f;
-            }
+        for (int k = 0; k < K; k++) {
+            const float r = __fsub_rn(dv, theta[k]);
+            bk[k] = __fmul_rn(bscale, __fmul_rn(r, r));
+            s_x[i * K + k] = in ? xc[k] : 0.f;
         }
         __syncthreads();
 
-        // phase 2: x^{c+1}, g^{c+1}, f contribution, next direction d_{c+2}
-        const bool mid = in && i >= 1 && i <= SWEEP_NT - 2;
-        const bool own = in && i >= SWEEP_HALO && i < SWEEP_NT - SWEEP_HALO;
-        float x1[K], g1[K], d1[K];
-        if (mid) {
+        // phase B: g^c = coeff*A_hat x^c - b, d_{c+1} = P(x^c - alpha g^c) - x^c,
+        //          x^{c+1} = x^c + beta d_{c+1}    (INIT: x^{c+1} = x^c)
+        float x1[K];
+        const bool inB = in && i >= 1 && i <= SWEEP_NT - 2;
+        if (INIT) {
+#pragma unroll
+            for (int k = 0; k < K; k++) x1[k] = xc[k];
+        } else if (inB) {
+            float z[K];
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float g = __fsub_rn(__fmul_rn(coeff, stencil_row<K>(s_x, i, k, t, T)), bk[k]);
+                z[k] = __fsub_rn(xc[k], __fmul_rn(a0, g));
+            }
+            project_reg<K>(z);
+#pragma unroll
+            for (int k = 0; k < K; k++) x1[k] = __fadd_rn(xc[k], __fmul_rn(beta, __fsub_rn(z[k], xc[k])));
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; k++) x1[k] = 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) s_y[i * K + k] = (INIT ? in : inB) ? x1[k] : 0.f;
+        __syncthreads();
+
+        // phase C: g^{c+1}, objective contribution, d_{c+2} = P(x^{c+1} - alpha' g^{c+1}) - x^{c+1}
+        const bool inC = in && i >= 2 && i <= SWEEP_NT - 3;
+        const bool own = in && i >= SWEEP_HL && i < SWEEP_NT - SWEEP_HR;
+        float g1[K], d1[K];
+        if (inC) {
             float fpart = 0.f;
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                const float S = stencil_row<K>(s_a, i, k, t, T);
-                const float r = __fsub_rn(dv, theta[k]);
-                const float bk = __fmul_rn(bscale, __fmul_rn(r, r));
-                if (INIT) {
-                    x1[k] = p1[k];
-                    g1[k] = __fsub_rn(__fmul_rn(coeff, S), bk);
-                } else {
-                    x1[k] = __fadd_rn(xo[k], __fmul_rn(beta, p1[k]));
-                    g1[k] = __fadd_rn(go[k], __fmul_rn(beta, __fmul_rn(coeff, S)));
-                }
-                fpart = __fadd_rn(fpart, __fmul_rn(__fsub_rn(g1[k], bk), x1[k]));
+                g1[k] = __fsub_rn(__fmul_rn(coeff, stencil_row<K>(s_y, i, k, t, T)), bk[k]);
+                fpart = __fadd_rn(fpart, __fmul_rn(__fsub_rn(g1[k], bk[k]), x1[k]));
                 d1[k] = __fsub_rn(x1[k], __fmul_rn(a1, g1[k]));
             }
             if (own) acc_f.add(fpart);
@@ -138,13 +145,13 @@ __global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
             for (int k = 0; k < K; k++) d1[k] = __fsub_rn(d1[k], x1[k]);
         } else {
 #pragma unroll
-            for (int k = 0; k < K; k++) { x1[k] = 0.f; g1[k] = 0.f; d1[k] = 0.f; }
+            for (int k = 0; k < K; k++) { g1[k] = 0.f; d1[k] = 0.f; }
         }
 #pragma unroll
-        for (int k = 0; k < K; k++) s_b[i * K + k] = d1[k];
+        for (int k = 0; k < K; k++) s_d[i * K + k] = d1[k];
         __syncthreads();
 
-        // phase 3: dots of d_{c+2}; write x^{c+1}, g^{c+1}
+        // phase D: dots of d_{c+2}; write x^{c+1}
         if (own) {
             float pdd = 0.f, pdiff = 0.f, pgd = 0.f;
 #pragma unroll
@@ -152,7 +159,7 @@ __global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
                 pdd = __fadd_rn(pdd, __fmul_rn(d1[k], d1[k]));
                 pgd = __fadd_rn(pgd, __fmul_rn(g1[k], d1[k]));
                 if (t < T - 1) {
-                    const float df = __fsub_rn(s_b[(i + 1) * K + k], d1[k]);
+                    const float df = __fsub_rn(s_d[(i + 1) * K + k], d1[k]);
                     pdiff = __fadd_rn(pdiff, __fmul_rn(df, df));
                 }
             }
@@ -160,10 +167,7 @@ __global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
             acc_dAd.add(pdiff);
             acc_gd.add(pgd);
 #pragma unroll
-            for (int k = 0; k < K; k++) {
-                __stcs(xout + t * K + k, x1[k]);
-                __stcs(gout + t * K + k, g1[k]);
-            }
+            for (int k = 0; k < K; k++) __stcs(xout + t * K + k, x1[k]);
         }
     }
 

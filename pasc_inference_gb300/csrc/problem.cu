@@ -87,7 +87,7 @@ struct pasc_gb300_problem {
 
     // mixed path
     float *data32 = nullptr, *theta32 = nullptr;
-    float *xb[2] = {nullptr, nullptr}, *gb[2] = {nullptr, nullptr};
+    float *xb[2] = {nullptr, nullptr};
     SpgDevState *st = nullptr, *st_h = nullptr;
     double *partials = nullptr;
     int cur = 0;
@@ -107,8 +107,7 @@ static void free_all(pasc_gb300_problem *p)
     cudaSetDevice(p->device);
     if (p->chunk_graph) cudaGraphExecDestroy(p->chunk_graph);
     void *dev[] = {p->data64, p->theta64, p->stage64, p->red, p->red_out, p->labels_d, p->x, p->g,
-                   p->d, p->Ad, p->b, p->data32, p->theta32, p->xb[0], p->xb[1], p->gb[0],
-                   p->gb[1], p->st, p->partials};
+                   p->d, p->Ad, p->b, p->data32, p->theta32, p->xb[0], p->xb[1], p->st, p->partials};
     for (void *q : dev)
         if (q) cudaFree(q);
     if (p->st_h) cudaFreeHost(p->st_h);
@@ -241,7 +240,6 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
     } else {
         if ((rc = dalloc(&p->data32, T)) || (rc = dalloc(&p->theta32, K)) ||
             (rc = dalloc(&p->xb[0], N)) || (rc = dalloc(&p->xb[1], N)) ||
-            (rc = dalloc(&p->gb[0], N)) || (rc = dalloc(&p->gb[1], N)) ||
             (rc = dalloc(&p->st, 1)))
             return bail(rc);
         if (cudaMallocHost((void **)&p->st_h, sizeof(SpgDevState)) != cudaSuccess)
@@ -251,7 +249,7 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
         cudaMemset(p->xb[0], 0, sizeof(float) * N);
         cudaMemset(p->data32, 0, sizeof(float) * T);
         cudaMemset(p->theta32, 0, sizeof(float) * K);
-        const long ntiles = (T + sweep_block_threads() - 5) / (sweep_block_threads() - 4);
+        const long ntiles = (T + sweep_tile_width() - 1) / sweep_tile_width();
         long gs = (long)sweep_blocks_per_sm(K, false) * p->sms;
         long gi = (long)sweep_blocks_per_sm(K, true) * p->sms;
         p->grid_sweep = (int)(gs < ntiles ? gs : ntiles);
@@ -578,8 +576,6 @@ static int sweep_args(pasc_gb300_problem *p, SweepArgs *a)
     a->theta = p->theta32;
     a->xb0 = p->xb[0];
     a->xb1 = p->xb[1];
-    a->gb0 = p->gb[0];
-    a->gb1 = p->gb[1];
     a->partials = p->partials;
     a->st = p->st;
     a->T = p->T;

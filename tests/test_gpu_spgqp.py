@@ -61,29 +61,40 @@ def _golden_spg(golden):
 
 @pytest.mark.parametrize("prec", [PASC_PREC_FP64, PASC_PREC_MIXED])
 def test_golden_solves(gpulib, golden, oracle, prec):
-    """The reference-produced SPG solves: the GPU's b (formed from the same data and theta)
-    equals the golden b, and the converged objective agrees (1e-7 relative for fp64, where
-    only the stopping iteration may differ; 1e-6 relative for mixed)."""
+    """The reference-produced SPG solves.  The GPU forms the same b from the same data and
+    theta.  Fixed-length runs (maxit < 100) must follow the reference's trajectory
+    (1e-12 relative fp64, 2e-6 mixed).  Runs the reference stopped on |f - f_old| < eps sit
+    somewhere short of the optimum, so there the check is that the GPU driven to the optimum
+    matches the oracle's optimum (1e-9 fp64, 1e-6 mixed) and is no worse than the
+    reference's stopped objective."""
     for i, T, K, eps2, kw in _golden_spg(golden):
         data, theta = golden[f"spg_{i}_data"], golden[f"spg_{i}_theta"]
-        np.testing.assert_array_equal(oracle.residual_b(data, theta, T, K), golden[f"spg_{i}_b"])
+        b = golden[f"spg_{i}_b"]
+        np.testing.assert_array_equal(oracle.residual_b(data, theta, T, K), b)
         it_ref, _, fx_ref = golden[f"spg_{i}_res"]
-        with _problem(T, K, eps2, data, theta, golden[f"spg_{i}_x0"], prec) as p:
-            if prec == PASC_PREC_MIXED and kw.get("stop_normgp"):
-                kw = dict(kw, eps=1e-9)  # ||d||^2 < 1e-10 is below FP32 resolution
-            st = p.spgqp_solve(capi.spgqp_opts(**kw))
-            if kw.get("maxit", 1000) < 100:  # fixed-length trajectory
+        x0 = golden[f"spg_{i}_x0"]
+        fixed = kw.get("maxit", 1000) < 100
+        with _problem(T, K, eps2, data, theta, x0, prec) as p:
+            if fixed:
+                st = p.spgqp_solve(capi.spgqp_opts(**kw))
                 assert st.it == int(it_ref)
-            tol = 1e-7 if prec == PASC_PREC_FP64 else 1e-6
-            if kw.get("maxit", 1000) < 100 and prec == PASC_PREC_FP64:
-                tol = 1e-12
-            assert abs(st.fx - fx_ref) <= tol * max(abs(fx_ref), 1e-12), (i, st.fx, fx_ref, st.it, it_ref)
+                tol = 1e-12 if prec == PASC_PREC_FP64 else 2e-6
+                assert abs(st.fx - fx_ref) <= tol * abs(fx_ref), (i, st.fx, fx_ref)
+                continue
+            tight = {k: v for k, v in kw.items() if k not in ("eps", "stop_normgp", "stop_difff", "maxit")}
+            st = p.spgqp_solve(capi.spgqp_opts(maxit=4000, stop_difff=0, **tight))
+        coeff = oracle.A_coeff(eps2, T)
+        _, ro, _ = oracle.spgqp_solve(b, x0, T, K, coeff, oracle.spg_opts(maxit=4000, stop_difff=0, **tight))
+        tol = 1e-9 if prec == PASC_PREC_FP64 else 1e-6
+        assert abs(st.fx - ro.fx) <= tol * abs(ro.fx), (i, st.fx, ro.fx)
+        assert ro.fx <= fx_ref + 1e-12 * abs(fx_ref)
+        assert st.fx <= fx_ref + tol * abs(fx_ref), (i, st.fx, fx_ref)
 
 
 @pytest.mark.parametrize("T,K,eps2", [(1000, 2, 10.0), (2000, 3, 100.0), (500, 4, 1.0)])
 def test_fp64_converged_objective(gpulib, oracle, T, K, eps2):
     data, theta, x0, b, coeff = _qp(T, K, eps2, 7 * T + K, oracle)
-    opts = dict(maxit=3000, eps=1e-12)
+    opts = dict(maxit=3000, stop_difff=0)
     xo, ro, _ = oracle.spgqp_solve(b, x0, T, K, coeff, oracle.spg_opts(**opts))
     with _problem(T, K, eps2, data, theta, x0, PASC_PREC_FP64) as p:
         st = p.spgqp_solve(capi.spgqp_opts(**opts))
@@ -154,13 +165,25 @@ def test_edge_sizes(gpulib, oracle, prec):
 
 @pytest.mark.parametrize("prec", [PASC_PREC_FP64, PASC_PREC_MIXED])
 def test_nonfinite_input_reports_status(gpulib, oracle, prec):
+    """A NaN in the data makes b and the objective NaN: the solve stops with NONFINITE
+    instead of iterating on garbage.  (A NaN in gamma does not propagate: the reference's
+    projection maps such a block to zeros, and so does the GPU's.)"""
     T, K = 500, 2
     data, theta, x0, b, coeff = _qp(T, K, 5.0, 3, oracle)
-    x0 = x0.copy()
-    x0[10] = np.nan
+    data = data.copy()
+    data[10] = np.nan
     with _problem(T, K, 5.0, data, theta, x0, prec) as p:
         st = p.spgqp_solve(capi.spgqp_opts(maxit=50))
         assert st.status == capi.PASC_SPG_NONFINITE
+    x0 = x0.copy()
+    x0[10] = np.nan
+    data, theta, _, b, coeff = _qp(T, K, 5.0, 3, oracle)
+    xo, ro, _ = oracle.spgqp_solve(b, x0, T, K, coeff, oracle.spg_opts(maxit=20))
+    with _problem(T, K, 5.0, data, theta, x0, prec) as p:
+        st = p.spgqp_solve(capi.spgqp_opts(maxit=20))
+        assert st.status == capi.PASC_SPG_MAXIT and np.isfinite(st.fx)
+        tol = 1e-12 if prec == PASC_PREC_FP64 else 1e-5
+        assert abs(st.fx - ro.fx) <= tol * abs(ro.fx)
 
 
 def test_bad_arguments(gpulib):

@@ -34,20 +34,56 @@ def _labels(g, T, K):
     return np.argmax(g.reshape(T, K), axis=1)
 
 
+def _threl(th, ref):
+    """theta error relative to the scale of theta: max_k |dtheta_k| / max_k |theta_k|."""
+    return float(np.max(np.abs(th - ref)) / np.max(np.abs(ref)))
+
+
 @pytest.mark.parametrize("prec", [PASC_PREC_FP64, PASC_PREC_MIXED])
-def test_golden_tssolver(gpulib, golden, prec):
+def test_golden_tssolver_reference_settings(gpulib, golden, prec):
+    """The reference's runs with its default settings (SPG stops on |f - f_old| < 1e-9, the
+    outer loop on |L - L_old| < 1e-6 absolute).  Those rules stop short of the fixed point,
+    and where they stop depends on rounding, so two correct implementations agree only to
+    the accuracy the rules leave: L to 1e-4 relative, theta to 5e-3 of its scale, labels on
+    >= 99.9% of timesteps.  The tight comparison is test_tssolver_tight_vs_oracle."""
     for i, name, T, K, eps2 in _golden_ts(golden):
-        L_ref, it_last, _, aic_ref = golden[f"ts_{i}_res"]
+        L_ref = golden[f"ts_{i}_res"][0]
         th_ref, g_ref = golden[f"ts_{i}_theta"], golden[f"ts_{i}_gamma"]
         p, st = _run_ts(T, K, eps2, golden[f"ts_{i}_data"], golden[f"ts_{i}_gamma0"], prec)
         with p:
             th = p.get_theta()
             g = p.get_gamma()
-        tol_L, tol_th = (1e-9, 1e-7) if prec == PASC_PREC_FP64 else (1e-6, 1e-5)
-        assert abs(st.L - L_ref) <= tol_L * abs(L_ref), (name, st.L, L_ref)
-        assert np.max(np.abs(th - th_ref) / np.maximum(np.abs(th_ref), 1e-3)) <= tol_th, (name, th, th_ref)
-        agree = np.mean(_labels(g, T, K) == _labels(g_ref, T, K))
-        assert agree >= 0.9999, (name, agree)
+        assert abs(st.L - L_ref) <= 1e-4 * abs(L_ref), (name, st.L, L_ref)
+        assert _threl(th, th_ref) <= 5e-3, (name, th, th_ref)
+        assert np.mean(_labels(g, T, K) == _labels(g_ref, T, K)) >= 0.999, name
+
+
+TIGHT_CASES = [("k3_sigma05", dict(T=4000, K=3, levels=[0.0, 1.0, 2.0], smin=200, smax=800, sigma=0.5, seed=3), 20.0),
+               ("k2_sigma08", dict(T=3000, K=2, levels=[1.0, 2.0], smin=200, smax=600, sigma=0.8, seed=21), 10.0),
+               ("k3_eps1000", dict(T=3000, K=3, levels=[0.0, 1.0, 2.0], smin=100, smax=600, sigma=0.5, seed=7), 1000.0)]
+
+
+@pytest.mark.parametrize("case", TIGHT_CASES, ids=[c[0] for c in TIGHT_CASES])
+@pytest.mark.parametrize("prec", [PASC_PREC_FP64, PASC_PREC_MIXED])
+def test_tssolver_tight_vs_oracle(gpulib, oracle, case, prec):
+    """TSSolver driven to its fixed point (SPG |f - f_old| < 1e-13, outer |L - L_old| < 1e-13)
+    on the GPU and in the FP64 oracle from identical inputs: L within 1e-6 relative (1e-9 for
+    fp64), theta within 1e-5 of its scale, argmax labels equal on >= 99.99% of timesteps."""
+    name, g, eps2 = case
+    sig = datagen.signal1d(g["T"], g["K"], g["levels"], g["smin"], g["smax"], g["sigma"], g["seed"])
+    T, K = sig.T, sig.K
+    g_o, th_o, r_o, _ = oracle.tssolver_solve(sig.data, sig.gamma0, np.zeros(K), T, K, eps2,
+                                              ts=oracle.ts_opts(maxit=300, eps=1e-13),
+                                              spg=oracle.spg_opts(m=10, eps=1e-13, maxit=20000))
+    p, st = _run_ts(T, K, eps2, sig.data, sig.gamma0, prec, capi.ts_opts(maxit=300, eps=1e-13),
+                    capi.spgqp_opts(m=10, eps=1e-13, maxit=20000))
+    with p:
+        th = p.get_theta()
+        gam = p.get_gamma()
+    tol_L = 1e-9 if prec == PASC_PREC_FP64 else 1e-6
+    assert abs(st.L - r_o.L) <= tol_L * abs(r_o.L), (name, st.L, r_o.L)
+    assert _threl(th, th_o) <= 1e-5, (name, th, th_o)
+    assert np.mean(_labels(gam, T, K) == _labels(g_o, T, K)) >= 0.9999, name
 
 
 def test_mirror_classes_cfg0(gpulib, oracle):
@@ -64,7 +100,7 @@ def test_mirror_classes_cfg0(gpulib, oracle):
                                               spg=oracle.spg_opts(m=10, eps=1e-6))
     assert abs(solver.get_L() - r_o.L) <= 1e-6 * abs(r_o.L)
     th = mydata.get_thetavector()
-    assert np.max(np.abs(th - th_o) / np.abs(th_o)) <= 1e-5
+    assert _threl(th, th_o) <= 1e-5
     agree = np.mean(_labels(mydata.get_gammavector(), T, K) == _labels(g_o, T, K))
     assert agree >= 0.9999
     # recovered signal error, as the driver reports it
