@@ -18,8 +18,9 @@ Besides the headline line it measures, on rank 0:
              host<->device copies inside the timed region.
   tts        time to an objective within 1e-6 relative of the converged FP64 objective, for the
              mixed path and for the plain FP64 GPU path on the same problem.
-  roofline   the sweep kernel's algorithmic bytes (16*K*T + 4*T per iteration) over its
-             CUDA-event time, against the measured HBM copy bandwidth.
+  roofline   the sweep kernel's algorithmic bytes (8*K*T + 4*T per iteration: gamma read and
+             written in FP32, the data read once) over its CUDA-event time, against the
+             measured HBM copy bandwidth.
   cpu_baseline  the FP64 CPU oracle (a port of the reference's CPU path) on all host cores.
 """
 from __future__ import annotations
@@ -218,7 +219,7 @@ def main():
     sig = datagen.signal1d_cfg1(T=args.T)
     T, K = sig.T, sig.K
     theta = np.array([0.0, 1.0, 2.0])
-    B_it = 16.0 * K * T + 4.0 * T
+    B_it = 8.0 * K * T + 4.0 * T  # read x, data; write x (FP32): the sweep's algorithmic bytes
 
     p = Problem(T, K, args.eps2, precision=PASC_PREC_MIXED, device=dev)
     p.set_data(sig.data)
@@ -274,7 +275,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "T": T, "K": K, "epssqr": args.eps2,
                    "parallelism": f"replicas x{info.world_size}",
-                   "l2": "inputs larger than L2 (x,g,data = 280 MB read per step)",
+                   "l2": "inputs larger than L2 (x 120 MB + data 40 MB read, x 120 MB written per step)",
                    "wall_s_timed": t_wall, "restarts": restarts},
         "gpu_launches": launches,
         "roofline": roofline,

@@ -35,24 +35,10 @@ constexpr int SWEEP_W = SWEEP_NT - SWEEP_HL - SWEEP_HR;  // owned timesteps per 
 int sweep_block_threads() { return SWEEP_NT; }
 int sweep_tile_width() { return SWEEP_W; }
 
-// Row sum of A_hat (FEM-H1, R = 1) at timestep t for component k from values staged in
-// shared memory at slots i-1, i, i+1 (stride K); the order of the assembled CSR row.
-template <int K>
-__device__ __forceinline__ float stencil_row(const float *s, int i, int k, long t, long T)
-{
-    if (T == 1) return 0.f;
-    const float w = (t == 0 || t == T - 1) ? 2.f : 4.f;
-    float sum = 0.f;
-    if (t > 0) sum = __fmul_rn(-2.f, s[(i - 1) * K + k]);
-    sum = __fadd_rn(sum, __fmul_rn(w, s[i * K + k]));
-    if (t < T - 1) sum = __fadd_rn(sum, __fmul_rn(-2.f, s[(i + 1) * K + k]));
-    return sum;
-}
-
 template <int K, bool INIT>
-__global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
+__global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_sweep_kernel(SweepArgs a)
 {
-    __shared__ float s_x[SWEEP_NT * K];  // x^c
+    __shared__ float s_x[SWEEP_NT * K];  // x^c (zero outside 0 <= t < T)
     __shared__ float s_y[SWEEP_NT * K];  // x^{c+1}
     __shared__ float s_d[SWEEP_NT * K];  // d_{c+2}
     __shared__ double s_red[4 * (SWEEP_NT / 32)];
@@ -61,43 +47,61 @@ __global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
     if (st->status != PASC_SPG_RUNNING) return;  // uniform across the grid
 
     const int cur = st->cur;
-    const float *xin = cur ? a.xb1 : a.xb0;
-    float *xout = cur ? a.xb0 : a.xb1;
+    const float *__restrict__ xin = cur ? a.xb1 : a.xb0;
+    float *__restrict__ xout = cur ? a.xb0 : a.xb1;
     const float a0 = (float)st->alpha_prev;
     const float beta = (float)st->beta;
     const float a1 = (float)st->alpha_cur;
     const float coeff = (float)st->coeff;
     const float bscale = (float)st->bscale;
-    const long T = a.T;
+    const int T = (int)a.T;  // K*T < 2^31 (checked at creation)
 
     float theta[K];
 #pragma unroll
     for (int k = 0; k < K; k++) theta[k] = a.theta[k];
 
-    KahanF acc_f, acc_dd, acc_dAd, acc_gd;
+    KahanF acc_f;  // the objective keeps a compensated sum; the dots need less
+    float acc_dd = 0.f, acc_dAd = 0.f, acc_gd = 0.f;
     const int i = threadIdx.x;
-    const long ntiles = (T + SWEEP_W - 1) / SWEEP_W;
+    // neighbour slots, clamped so that the edge threads (whose results are discarded) stay
+    // inside the shared arrays
+    const int il = (i > 0 ? i - 1 : 0) * K, ir = (i < SWEEP_NT - 1 ? i + 1 : i) * K;
+    const int ntiles = (T + SWEEP_W - 1) / SWEEP_W;
 
-    for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long t = tile * SWEEP_W - SWEEP_HL + i;
-        const bool in = (t >= 0 && t < T);
+    // the next tile's x and data are loaded into registers while the current one is computed
+    float xn[K], dvn = 0.f;
+    {
+        const int t = blockIdx.x * SWEEP_W - SWEEP_HL + i;
+        const bool in = (int)blockIdx.x < ntiles && (unsigned)t < (unsigned)T;
+#pragma unroll
+        for (int k = 0; k < K; k++) xn[k] = in ? __ldcs(xin + t * K + k) : 0.f;
+        if (in) dvn = __ldg(a.data + t);
+    }
+
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int t = tile * SWEEP_W - SWEEP_HL + i;
+        const bool in = (unsigned)t < (unsigned)T;
+        // FEM-H1 row (blockgraphsparse.cpp:51-109, R = 1): centre 4, 2 at an end, 0 for T == 1;
+        // neighbours -2, entering through zero-padded shared memory
+        const float wc = 4.f - (t == 0 ? 2.f : 0.f) - (t == T - 1 ? 2.f : 0.f);
 
         // phase A: x^c (INIT: the projected start point) and b_t in registers
         float xc[K], bk[K];
-        float dv = 0.f;
-        if (in) {
+        const float dv = dvn;
 #pragma unroll
-            for (int k = 0; k < K; k++) xc[k] = __ldcs(xin + t * K + k);
-            dv = __ldg(a.data + t);
-        } else {
+        for (int k = 0; k < K; k++) xc[k] = xn[k];
+        {
+            const int tn = t + (int)gridDim.x * SWEEP_W;
+            const bool inn = tile + (int)gridDim.x < ntiles && (unsigned)tn < (unsigned)T;
 #pragma unroll
-            for (int k = 0; k < K; k++) xc[k] = 0.f;
+            for (int k = 0; k < K; k++) xn[k] = inn ? __ldcs(xin + tn * K + k) : 0.f;
+            dvn = inn ? __ldg(a.data + tn) : 0.f;
         }
         if (INIT) project_reg<K>(xc);
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const float r = __fsub_rn(dv, theta[k]);
-            bk[k] = __fmul_rn(bscale, __fmul_rn(r, r));
+            const float r = dv - theta[k];
+            bk[k] = bscale * (r * r);
             s_x[i * K + k] = in ? xc[k] : 0.f;
         }
         __syncthreads();
@@ -109,19 +113,17 @@ __global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
         if (INIT) {
 #pragma unroll
             for (int k = 0; k < K; k++) x1[k] = xc[k];
-        } else if (inB) {
+        } else {
             float z[K];
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                const float g = __fsub_rn(__fmul_rn(coeff, stencil_row<K>(s_x, i, k, t, T)), bk[k]);
-                z[k] = __fsub_rn(xc[k], __fmul_rn(a0, g));
+                const float S = wc * xc[k] - 2.f * (s_x[il + k] + s_x[ir + k]);
+                const float g = coeff * S - bk[k];
+                z[k] = xc[k] - a0 * g;
             }
             project_reg<K>(z);
 #pragma unroll
-            for (int k = 0; k < K; k++) x1[k] = __fadd_rn(xc[k], __fmul_rn(beta, __fsub_rn(z[k], xc[k])));
-        } else {
-#pragma unroll
-            for (int k = 0; k < K; k++) x1[k] = 0.f;
+            for (int k = 0; k < K; k++) x1[k] = xc[k] + beta * (z[k] - xc[k]);
         }
 #pragma unroll
         for (int k = 0; k < K; k++) s_y[i * K + k] = (INIT ? in : inB) ? x1[k] : 0.f;
@@ -131,48 +133,41 @@ __global__ void __launch_bounds__(SWEEP_NT) spg_sweep_kernel(SweepArgs a)
         const bool inC = in && i >= 2 && i <= SWEEP_NT - 3;
         const bool own = in && i >= SWEEP_HL && i < SWEEP_NT - SWEEP_HR;
         float g1[K], d1[K];
-        if (inC) {
+        {
             float fpart = 0.f;
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                g1[k] = __fsub_rn(__fmul_rn(coeff, stencil_row<K>(s_y, i, k, t, T)), bk[k]);
-                fpart = __fadd_rn(fpart, __fmul_rn(__fsub_rn(g1[k], bk[k]), x1[k]));
-                d1[k] = __fsub_rn(x1[k], __fmul_rn(a1, g1[k]));
+                const float S = wc * x1[k] - 2.f * (s_y[il + k] + s_y[ir + k]);
+                g1[k] = coeff * S - bk[k];
+                fpart += (g1[k] - bk[k]) * x1[k];
+                d1[k] = x1[k] - a1 * g1[k];
             }
             if (own) acc_f.add(fpart);
             project_reg<K>(d1);
 #pragma unroll
-            for (int k = 0; k < K; k++) d1[k] = __fsub_rn(d1[k], x1[k]);
-        } else {
-#pragma unroll
-            for (int k = 0; k < K; k++) { g1[k] = 0.f; d1[k] = 0.f; }
+            for (int k = 0; k < K; k++) {
+                d1[k] = inC ? d1[k] - x1[k] : 0.f;
+                s_d[i * K + k] = d1[k];
+            }
         }
-#pragma unroll
-        for (int k = 0; k < K; k++) s_d[i * K + k] = d1[k];
         __syncthreads();
 
         // phase D: dots of d_{c+2}; write x^{c+1}
         if (own) {
-            float pdd = 0.f, pdiff = 0.f, pgd = 0.f;
+            const bool right = t < T - 1;
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                pdd = __fadd_rn(pdd, __fmul_rn(d1[k], d1[k]));
-                pgd = __fadd_rn(pgd, __fmul_rn(g1[k], d1[k]));
-                if (t < T - 1) {
-                    const float df = __fsub_rn(s_d[(i + 1) * K + k], d1[k]);
-                    pdiff = __fadd_rn(pdiff, __fmul_rn(df, df));
-                }
+                acc_dd += d1[k] * d1[k];
+                acc_gd += g1[k] * d1[k];
+                const float df = right ? s_d[ir + k] - d1[k] : 0.f;
+                acc_dAd += df * df;
+                __stcs(xout + t * K + k, x1[k]);
             }
-            acc_dd.add(pdd);
-            acc_dAd.add(pdiff);
-            acc_gd.add(pgd);
-#pragma unroll
-            for (int k = 0; k < K; k++) __stcs(xout + t * K + k, x1[k]);
         }
     }
 
     // block and grid reductions
-    double v[4] = {acc_f.value(), acc_dd.value(), acc_dAd.value(), acc_gd.value()};
+    double v[4] = {acc_f.value(), (double)acc_dd, (double)acc_dAd, (double)acc_gd};
     block_sum<4>(v, s_red);
     if (threadIdx.x == 0) {
 #pragma unroll

@@ -91,40 +91,46 @@ __device__ __forceinline__ void sort_net(float (&s)[K])
     }
 }
 
+// The reference's threshold (the first t_i from the top with t_i >= y_{i-1}) equals the
+// largest of all candidates t_i = (sum of the K-i largest entries - 1)/(K-i): every candidate
+// is a lower bound of the threshold (sum_k max(y_k - t, 0) >= 1 at t = t_i) and the one of the
+// active set attains it.  Taking the maximum needs no search and no branch; for K <= 3 it
+// needs no sort either (the largest, the sum minus the smallest, the sum).  An already
+// feasible block yields t = 0 and is returned unchanged, as in the reference's early exit.
+// The divisions are multiplications by compile-time reciprocals (within one ulp).
 template <int K>
 __device__ __forceinline__ void project_reg(float (&x)[K])
 {
-    bool inside = true;
     float sum = 0.f;
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        inside = inside && !(x[k] < 0.f);
-        sum = __fadd_rn(sum, x[k]);
-    }
-    if (inside && sum == 1.f) return;
-
-    float s[K];
+    for (int k = 0; k < K; k++) sum += x[k];
+    float tau;
+    if (K == 1) {
+        tau = sum - 1.f;
+    } else if (K == 2) {
+        tau = fmaxf(fmaxf(x[0], x[1]) - 1.f, (sum - 1.f) * 0.5f);
+    } else if (K == 3) {
+        const float mx = fmaxf(fmaxf(x[0], x[1]), x[2]);
+        const float mn = fminf(fminf(x[0], x[1]), x[2]);
+        tau = fmaxf(fmaxf(mx - 1.f, (sum - mn - 1.f) * 0.5f), (sum - 1.f) * (1.f / 3.f));
+    } else {
+        float s[K];
 #pragma unroll
-    for (int k = 0; k < K; k++) s[k] = x[k];
-    sort_net<K>(s);
-
-    float tau = __fdiv_rn(__fsub_rn(sum, 1.f), (float)K);
-    float acc = 0.f;
-    bool found = false;
+        for (int k = 0; k < K; k++) s[k] = x[k];
+        sort_net<K>(s);
+        float acc = 0.f;
+        tau = -FLT_MAX;
 #pragma unroll
-    for (int i = K - 1; i >= 1; i--) {
-        acc = __fadd_rn(acc, s[i]);
-        float ti = __fdiv_rn(__fsub_rn(acc, 1.f), (float)(K - i));
-        if (!found && ti >= s[i - 1]) {
-            tau = ti;
-            found = true;
+        for (int i = K - 1; i >= 0; i--) {
+            acc += s[i];
+            tau = fmaxf(tau, (acc - 1.f) * (1.f / (float)(K - i)));
         }
     }
+    // fmaxf drops NaN operands; a block holding a NaN gets a NaN threshold and so becomes all
+    // zeros, as in the reference (whose comparisons with NaN all fail)
+    if (sum != sum) tau = sum;
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        float v = __fsub_rn(x[k], tau);
-        x[k] = v > 0.f ? v : 0.f;
-    }
+    for (int k = 0; k < K; k++) x[k] = fmaxf(x[k] - tau, 0.f);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -60,14 +60,20 @@ def _golden_spg(golden):
 
 
 @pytest.mark.parametrize("prec", [PASC_PREC_FP64, PASC_PREC_MIXED])
-def test_golden_solves(gpulib, golden, oracle, prec):
+def test_golden_solves(gpulib, golden, oracle, qp_optimum, prec):
     """The reference-produced SPG solves.  The GPU forms the same b from the same data and
     theta.  Fixed-length runs (maxit < 100) must follow the reference's trajectory
     (1e-12 relative fp64, 2e-6 mixed).  Runs the reference stopped on |f - f_old| < eps sit
     somewhere short of the optimum, so there the check is that the GPU driven to the optimum
     matches the oracle's optimum (1e-9 fp64, 1e-6 mixed) and is no worse than the
-    reference's stopped objective."""
+    reference's stopped objective.  The optimum is an independent FP64 solve (accelerated
+    projected gradient): on the 2-timestep case the reference's iteration, continued past
+    convergence, leaves the optimum (its BB step blows up as d'Ad -> 0)."""
     for i, T, K, eps2, kw in _golden_spg(golden):
+        if T == 1:
+            # A = 0: the reference divides by d'Ad = 0 and ends at an infeasible point; the GPU
+            # answer is checked against the analytic optimum in test_edge_sizes
+            continue
         data, theta = golden[f"spg_{i}_data"], golden[f"spg_{i}_theta"]
         b = golden[f"spg_{i}_b"]
         np.testing.assert_array_equal(oracle.residual_b(data, theta, T, K), b)
@@ -84,11 +90,10 @@ def test_golden_solves(gpulib, golden, oracle, prec):
             tight = {k: v for k, v in kw.items() if k not in ("eps", "stop_normgp", "stop_difff", "maxit")}
             st = p.spgqp_solve(capi.spgqp_opts(maxit=4000, stop_difff=0, **tight))
         coeff = oracle.A_coeff(eps2, T)
-        _, ro, _ = oracle.spgqp_solve(b, x0, T, K, coeff, oracle.spg_opts(maxit=4000, stop_difff=0, **tight))
+        f_opt, _ = qp_optimum(b, x0, T, K, coeff)
         tol = 1e-9 if prec == PASC_PREC_FP64 else 1e-6
-        assert abs(st.fx - ro.fx) <= tol * abs(ro.fx), (i, st.fx, ro.fx)
-        assert ro.fx <= fx_ref + 1e-12 * abs(fx_ref)
-        assert st.fx <= fx_ref + tol * abs(fx_ref), (i, st.fx, fx_ref)
+        assert abs(st.fx - f_opt) <= tol * abs(f_opt), (i, st.fx, f_opt)
+        assert fx_ref >= f_opt - 1e-12 * abs(f_opt)  # the reference's stopped objective
 
 
 @pytest.mark.parametrize("T,K,eps2", [(1000, 2, 10.0), (2000, 3, 100.0), (500, 4, 1.0)])
@@ -108,7 +113,7 @@ def test_mixed_converged_objective(gpulib, oracle, T, K, eps2):
     data, theta, x0, b, coeff = _qp(T, K, eps2, 11 * T + K, oracle)
     xo, ro, _ = oracle.spgqp_solve(b, x0, T, K, coeff, oracle.spg_opts(maxit=5000, eps=1e-13))
     with _problem(T, K, eps2, data, theta, x0, PASC_PREC_MIXED) as p:
-        st = p.spgqp_solve(capi.spgqp_opts(maxit=3000, eps=1e-10))
+        st = p.spgqp_solve(capi.spgqp_opts(maxit=3000, stop_difff=0))
         assert st.status != capi.PASC_SPG_NONFINITE
         assert abs(st.fx - ro.fx) <= 1e-6 * abs(ro.fx), (st.fx, ro.fx, st.it, st.status)
         g = p.get_gamma().reshape(T, K)
