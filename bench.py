@@ -230,6 +230,7 @@ def main():
     total_steps = args.warmup + args.steps
     opts = capi.spgqp_opts(maxit=10 * total_steps + 100, m=10, stop_difff=0)
     p.spgqp_start(opts)
+    variant = p.get_sweep_variant()
     if args.warmup:
         p.spgqp_iterate(args.warmup, poll=False)
 
@@ -266,7 +267,8 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": profile_traffic(),
                 "peak_source": peak_kind,
-                "bytes_per_launch": B_it, "kernel": "spg_sweep_kernel<3,false>"}
+                "bytes_per_launch": B_it,
+                "kernel": "spg_sweep_tma_kernel<3,128,false>" if variant == 1 else "spg_sweep_kernel<3,false>"}
 
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": info.world_size,
@@ -276,7 +278,8 @@ def main():
         "config": {"workload": WORKLOAD, "T": T, "K": K, "epssqr": args.eps2,
                    "parallelism": f"replicas x{info.world_size}",
                    "l2": "inputs larger than L2 (x 120 MB + data 40 MB read, x 120 MB written per step)",
-                   "wall_s_timed": t_wall, "restarts": restarts},
+                   "wall_s_timed": t_wall, "restarts": restarts,
+                   "sweep_kernel": {0: "one timestep per thread", 1: "bulk-copy tiles, 4 timesteps per thread"}[variant]},
         "gpu_launches": launches,
         "roofline": roofline,
         "clocks": clocks,

@@ -193,6 +193,13 @@ int pasc_gb300_spgqp_iterate(pasc_gb300_problem *p, long n, int poll, pasc_gb300
  * spgqp_iterate call. */
 int pasc_gb300_spgqp_last_iterate(pasc_gb300_problem *p, double *ms, int *launches);
 
+/* Sweep kernel of the mixed path (no reference counterpart: the reference has one SpMV and
+ * separate vector kernels).  0 = one timestep per thread; 1 = tiles of 4 timesteps per
+ * thread brought in by bulk asynchronous copies; -1 (default) = whichever is faster on the
+ * first solve, measured on the solve's own first sweep. */
+int pasc_gb300_set_sweep_variant(pasc_gb300_problem *p, int variant);
+int pasc_gb300_get_sweep_variant(pasc_gb300_problem *p, int *variant);
+
 /* SPGQPSolver<PetscVector>::get_fx (spgqpsolver.cpp:316-345): 1/2 (g - b)'x of the last solve. */
 int pasc_gb300_get_fx(pasc_gb300_problem *p, double *fx);
 

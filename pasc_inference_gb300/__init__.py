@@ -135,6 +135,14 @@ class Problem:
         check(load().pasc_gb300_spgqp_last_iterate(self._h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
+    def set_sweep_variant(self, variant: int):
+        check(load().pasc_gb300_set_sweep_variant(self._h, int(variant)))
+
+    def get_sweep_variant(self) -> int:
+        v = C.c_int()
+        check(load().pasc_gb300_get_sweep_variant(self._h, C.byref(v)))
+        return v.value
+
     def get_fx(self) -> float:
         v = C.c_double()
         check(load().pasc_gb300_get_fx(self._h, C.byref(v)))

@@ -40,7 +40,7 @@ struct SpgDevState {
     int sweeps;         // sweeps that did work
     unsigned int counter;  // last-block-done ticket (reset by the last block)
     unsigned int counter2; // ticket of the theta kernel
-    int pad;
+    int error;             // set when a bounded device wait gave up
 };
 
 struct SweepArgs {
@@ -68,6 +68,12 @@ int sweep_block_threads();
 int sweep_tile_width();
 int sweep_blocks_per_sm(int K, bool init);
 cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);
+// Bulk-copy (TMA) form of the sweep: 4 timesteps per thread, double-buffered tiles.
+bool sweep_tma_supported(int K);
+int sweep_tma_tile_width();
+int sweep_tma_max_tile();
+int sweep_tma_blocks_per_sm(int K, bool init);
+cudaError_t launch_sweep_tma(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);
 cudaError_t launch_theta_f32(int K, int grid, const ThetaArgs &a, cudaStream_t s);
 cudaError_t launch_project_f32(float *x, long T, int K, cudaStream_t s);
 cudaError_t launch_matmult_f32(const float *x, float *y, long T, int K, float coeff, cudaStream_t s);

@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "project.cuh"
 #include "internal.h"
+#include "sweep_common.cuh"
 
 namespace pasc {
 
@@ -81,9 +82,10 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int t = tile * SWEEP_W - SWEEP_HL + i;
         const bool in = (unsigned)t < (unsigned)T;
-        // FEM-H1 row (blockgraphsparse.cpp:51-109, R = 1): centre 4, 2 at an end, 0 for T == 1;
-        // neighbours -2, entering through zero-padded shared memory
-        const float wc = 4.f - (t == 0 ? 2.f : 0.f) - (t == T - 1 ? 2.f : 0.f);
+        // FEM-H1 row (blockgraphsparse.cpp:51-109, R = 1) in difference form:
+        // (A_hat x)_t = 2 [t > 0] (x_t - x_{t-1}) + 2 [t < T-1] (x_t - x_{t+1}), equal to the
+        // assembled row (centre 4, 2 at an end, neighbours -2) but exact where neighbours agree
+        const float ml = t > 0 ? 2.f : 0.f, mr = t < T - 1 ? 2.f : 0.f;
 
         // phase A: x^c (INIT: the projected start point) and b_t in registers
         float xc[K], bk[K];
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
             float z[K];
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                const float S = wc * xc[k] - 2.f * (s_x[il + k] + s_x[ir + k]);
+                const float S = ml * (xc[k] - s_x[il + k]) + mr * (xc[k] - s_x[ir + k]);
                 const float g = coeff * S - bk[k];
                 z[k] = xc[k] - a0 * g;
             }
@@ -137,7 +139,7 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
             float fpart = 0.f;
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                const float S = wc * x1[k] - 2.f * (s_y[il + k] + s_y[ir + k]);
+                const float S = ml * (x1[k] - s_y[il + k]) + mr * (x1[k] - s_y[ir + k]);
                 g1[k] = coeff * S - bk[k];
                 fpart += (g1[k] - bk[k]) * x1[k];
                 d1[k] = x1[k] - a1 * g1[k];
@@ -183,77 +185,7 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
     block_sum<4>(w, s_red);
     if (threadIdx.x != 0) return;
 
-    st->counter = 0;
-    st->sweeps += 1;
-    const double fnew = 0.5 * w[0];
-    const double dd = w[1];
-    const double dAd = 2.0 * st->coeff * w[2];
-    const double gd = w[3];
-
-    if (INIT) {
-        // spgqpsolver.cpp:131-137: fs.init(fx), fx_old = max
-        st->fx = fnew;
-        st->fx_old = DBL_MAX;
-        for (int q = 0; q < st->m; q++) st->fs[q] = fnew;
-        st->fs_last = 0;
-        st->it = 0;
-        st->hessmult = 1;
-        st->cur = cur ^ 1;
-        if (st->maxit <= 0) { st->status = PASC_SPG_MAXIT; return; }
-        if (!isfinite(fnew)) { st->status = PASC_SPG_NONFINITE; return; }
-    } else {
-        st->it += 1;
-        st->hessmult += 1;
-        st->cur = cur ^ 1;
-        st->fx_old = st->fx;  // :207
-        st->fx = fnew;        // :209
-        int li = st->fs_last + 1;  // fs.update, spg_fs.cpp:52-63
-        if (li >= st->m) li = 0;
-        st->fs[li] = fnew;
-        st->fs_last = li;
-        if (!isfinite(fnew)) { st->status = PASC_SPG_NONFINITE; return; }
-        // stopping tests of iteration it on the direction it applied (:260-274)
-        const double ddo = st->dd, dAdo = st->dAd;
-        if ((st->stop_difff && fabs(st->fx - st->fx_old) < st->eps) ||
-            (st->stop_normgp && ddo < st->eps) ||
-            (st->stop_normgp_normb && ddo < st->eps * st->normb) ||
-            (st->stop_Anormgp && dAdo < st->eps) ||
-            (st->stop_Anormgp_normb && dAdo < st->eps * st->normb)) {
-            st->status = PASC_SPG_CONVERGED;
-            return;
-        }
-        if (st->it >= st->maxit) { st->status = PASC_SPG_MAXIT; return; }
-    }
-
-    // next direction: step length from the A-condition (:176-195) and BB step (:216)
-    if (!(isfinite(dd) && isfinite(dAd) && isfinite(gd))) { st->status = PASC_SPG_NONFINITE; return; }
-    if (!(dd > 0.0)) { st->status = PASC_SPG_DAD_ZERO; return; }  // projected step vanished
-    double nbeta, nalpha;
-    if (dAd > 0.0) {
-        double fx_max = st->fs[0];
-        for (int q = 0; q < st->m; q++) fx_max = st->fs[q] > fx_max ? st->fs[q] : fx_max;
-        const double xi = (fx_max - st->fx) / dAd;
-        const double beta_bar = -gd / dAd;
-        double beta_hat = st->gamma * beta_bar + sqrt(st->gamma * st->gamma * beta_bar * beta_bar + 2 * xi);
-        if (beta_hat < st->sigma1) beta_hat = st->sigma1;
-        nbeta = beta_hat < st->sigma2 ? beta_hat : st->sigma2;
-        nalpha = dd / dAd;
-    } else if (gd < 0.0) {
-        // d'Ad = 0 with d != 0: the objective is linear along d (A_hat d = 0, e.g. T == 1).
-        // The reference divides by zero here; its comparisons then fall through to
-        // beta = sigma2.  Take that step and keep the step length finite.
-        nbeta = st->sigma2;
-        nalpha = st->alpha_cur;
-    } else {
-        st->status = PASC_SPG_DAD_ZERO;
-        return;
-    }
-    st->alpha_prev = st->alpha_cur;
-    st->alpha_cur = nalpha;
-    st->beta = nbeta;
-    st->dd = dd;
-    st->dAd = dAd;
-    st->gd = gd;
+    spg_finish_sweep<INIT>(st, cur, w);
 }
 
 template <int K, bool INIT>

@@ -14,6 +14,10 @@
 
 using namespace pasc;
 
+// zero pads around the mixed path's gamma and data buffers (timesteps)
+static constexpr long PAD_FRONT = 4;
+static constexpr long PAD_BACK = 1024;
+
 // ---------------------------------------------------------------------------------------
 // error reporting
 // ---------------------------------------------------------------------------------------
@@ -86,14 +90,17 @@ struct pasc_gb300_problem {
     double *x = nullptr, *g = nullptr, *d = nullptr, *Ad = nullptr, *b = nullptr;
 
     // mixed path
-    float *data32 = nullptr, *theta32 = nullptr;
-    float *xb[2] = {nullptr, nullptr};
+    float *data32 = nullptr, *theta32 = nullptr;  // data32 points past the front pad
+    float *xb[2] = {nullptr, nullptr};            // past the front pad of xb_raw
+    float *xb_raw[2] = {nullptr, nullptr}, *data32_raw = nullptr;
     SpgDevState *st = nullptr, *st_h = nullptr;
     double *partials = nullptr;
     int cur = 0;
-    int grid_sweep = 0, grid_sweep_init = 0, grid_theta = 0;
+    // sweep kernels: 0 = one timestep per thread, 1 = bulk-copy tiles, 4 timesteps per thread
+    int grid_sweep[2] = {0, 0}, grid_sweep_init[2] = {0, 0}, grid_theta = 0;
+    int variant = -1;             // -1: chosen by timing at the first solve
     cudaGraphExec_t chunk_graph = nullptr;
-    int chunk_graph_len = 0;
+    int chunk_graph_len = 0, chunk_graph_variant = -1;
 
     SpgRun run;
     double fx_last = 0.0;
@@ -107,7 +114,8 @@ static void free_all(pasc_gb300_problem *p)
     cudaSetDevice(p->device);
     if (p->chunk_graph) cudaGraphExecDestroy(p->chunk_graph);
     void *dev[] = {p->data64, p->theta64, p->stage64, p->red, p->red_out, p->labels_d, p->x, p->g,
-                   p->d, p->Ad, p->b, p->data32, p->theta32, p->xb[0], p->xb[1], p->st, p->partials};
+                   p->d, p->Ad, p->b, p->data32_raw, p->theta32, p->xb_raw[0], p->xb_raw[1], p->st,
+                   p->partials};
     for (void *q : dev)
         if (q) cudaFree(q);
     if (p->st_h) cudaFreeHost(p->st_h);
@@ -238,29 +246,45 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
         cudaMemset(p->x, 0, sizeof(double) * N);
         cudaMemset(p->b, 0, sizeof(double) * N);
     } else {
-        if ((rc = dalloc(&p->data32, T)) || (rc = dalloc(&p->theta32, K)) ||
-            (rc = dalloc(&p->xb[0], N)) || (rc = dalloc(&p->xb[1], N)) ||
+        // gamma and data carry zero pads (PAD_FRONT timesteps before, PAD_BACK after) so that
+        // the bulk-copy sweep can copy whole tiles at the ends of the signal; the pads stay
+        // zero because every kernel writes only 0 <= t < T
+        const size_t nx = (size_t)(T + PAD_FRONT + PAD_BACK) * K, nd = (size_t)(T + PAD_FRONT + PAD_BACK);
+        if ((rc = dalloc(&p->data32_raw, nd)) || (rc = dalloc(&p->theta32, K)) ||
+            (rc = dalloc(&p->xb_raw[0], nx)) || (rc = dalloc(&p->xb_raw[1], nx)) ||
             (rc = dalloc(&p->st, 1)))
             return bail(rc);
+        cudaMemset(p->xb_raw[0], 0, sizeof(float) * nx);
+        cudaMemset(p->xb_raw[1], 0, sizeof(float) * nx);
+        cudaMemset(p->data32_raw, 0, sizeof(float) * nd);
+        p->xb[0] = p->xb_raw[0] + (size_t)PAD_FRONT * K;
+        p->xb[1] = p->xb_raw[1] + (size_t)PAD_FRONT * K;
+        p->data32 = p->data32_raw + PAD_FRONT;
         if (cudaMallocHost((void **)&p->st_h, sizeof(SpgDevState)) != cudaSuccess)
             return bail(fail(PASC_ERR_ALLOC, "create: pinned allocation failed"));
         memset(p->st_h, 0, sizeof(SpgDevState));
         cudaMemset(p->st, 0, sizeof(SpgDevState));
-        cudaMemset(p->xb[0], 0, sizeof(float) * N);
-        cudaMemset(p->data32, 0, sizeof(float) * T);
         cudaMemset(p->theta32, 0, sizeof(float) * K);
-        const long ntiles = (T + sweep_tile_width() - 1) / sweep_tile_width();
-        long gs = (long)sweep_blocks_per_sm(K, false) * p->sms;
-        long gi = (long)sweep_blocks_per_sm(K, true) * p->sms;
-        p->grid_sweep = (int)(gs < ntiles ? gs : ntiles);
-        p->grid_sweep_init = (int)(gi < ntiles ? gi : ntiles);
+        auto grid = [&](long per_sm, long ntiles) {
+            long g = per_sm * p->sms;
+            g = g < ntiles ? g : ntiles;
+            return (int)(g < 1 ? 1 : g);
+        };
+        const long nt_thread = (T + sweep_tile_width() - 1) / sweep_tile_width();
+        p->grid_sweep[0] = grid(sweep_blocks_per_sm(K, false), nt_thread);
+        p->grid_sweep_init[0] = grid(sweep_blocks_per_sm(K, true), nt_thread);
+        const long nt_tma = (T + sweep_tma_tile_width() - 1) / sweep_tma_tile_width();
+        p->grid_sweep[1] = grid(sweep_tma_blocks_per_sm(K, false), nt_tma);
+        p->grid_sweep_init[1] = grid(sweep_tma_blocks_per_sm(K, true), nt_tma);
         long gt = (long)p->sms * 4;
         long tb = (T + 255) / 256;
         p->grid_theta = (int)(gt < tb ? gt : tb);
-        if (p->grid_sweep < 1) p->grid_sweep = 1;
-        if (p->grid_sweep_init < 1) p->grid_sweep_init = 1;
         if (p->grid_theta < 1) p->grid_theta = 1;
-        long np = p->grid_sweep > p->grid_sweep_init ? p->grid_sweep : p->grid_sweep_init;
+        long np = 0;
+        for (int v = 0; v < 2; v++) {
+            np = np > p->grid_sweep[v] ? np : p->grid_sweep[v];
+            np = np > p->grid_sweep_init[v] ? np : p->grid_sweep_init[v];
+        }
         np = np * 4 > (long)p->grid_theta * 2 * K ? np * 4 : (long)p->grid_theta * 2 * K;
         if ((rc = dalloc(&p->partials, np))) return bail(rc);
     }
@@ -584,16 +608,26 @@ static int sweep_args(pasc_gb300_problem *p, SweepArgs *a)
 
 static constexpr int GRAPH_CHUNK = 16;
 
+static cudaError_t launch_variant(pasc_gb300_problem *p, int v, bool init, const SweepArgs &a)
+{
+    if (v == 1) return launch_sweep_tma(p->K, init, init ? p->grid_sweep_init[1] : p->grid_sweep[1], a, p->stream);
+    return launch_sweep(p->K, init, init ? p->grid_sweep_init[0] : p->grid_sweep[0], a, p->stream);
+}
+
 static int ensure_chunk_graph(pasc_gb300_problem *p)
 {
-    if (p->chunk_graph) return PASC_OK;
+    if (p->chunk_graph && p->chunk_graph_variant == p->variant) return PASC_OK;
+    if (p->chunk_graph) {
+        cudaGraphExecDestroy(p->chunk_graph);
+        p->chunk_graph = nullptr;
+    }
     CU(cudaStreamSynchronize(p->stream));
     SweepArgs a;
     sweep_args(p, &a);
     cudaGraph_t graph;
     CU(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < GRAPH_CHUNK; i++) {
-        cudaError_t e = launch_sweep(p->K, false, p->grid_sweep, a, p->stream);
+        cudaError_t e = launch_variant(p, p->variant, false, a);
         if (e != cudaSuccess) {
             cudaStreamEndCapture(p->stream, &graph);
             return fail(PASC_ERR_CUDA, "sweep capture: %s", cudaGetErrorString(e));
@@ -607,6 +641,14 @@ static int ensure_chunk_graph(pasc_gb300_problem *p)
         return fail(PASC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
     }
     p->chunk_graph_len = GRAPH_CHUNK;
+    p->chunk_graph_variant = p->variant;
+    return PASC_OK;
+}
+
+static int check_device_error(pasc_gb300_problem *p)
+{
+    if (p->st_h->error)
+        return fail(PASC_ERR_TIMEOUT, "spgqp: a bounded wait for a bulk copy gave up inside the sweep");
     return PASC_OK;
 }
 
@@ -625,15 +667,9 @@ static void sync_run_from_device(pasc_gb300_problem *p)
     p->have_fx = true;
 }
 
-// spgqpsolver.cpp:104-137 plus the first direction (one INIT sweep)
-static int mixed_start(pasc_gb300_problem *p)
+static void fill_device_state(pasc_gb300_problem *p, SpgDevState *h)
 {
     const pasc_gb300_spgqp_opts *o = &p->run.o;
-    if (o->stop_normgp_normb || o->stop_Anormgp_normb)
-        return fail(PASC_ERR_NOTSUPP, "spgqp: ||b||-scaled stopping tests need the fp64 path");
-    cudaStream_t s = p->stream;
-    CHK(ensure_chunk_graph(p));
-    SpgDevState *h = p->st_h;
     memset(h, 0, sizeof(SpgDevState));
     h->alpha_prev = o->alphainit;
     h->alpha_cur = o->alphainit;  // alpha of the first direction (:108)
@@ -650,11 +686,64 @@ static int mixed_start(pasc_gb300_problem *p)
     h->stop_Anormgp = o->stop_Anormgp;
     h->status = PASC_SPG_RUNNING;
     h->cur = p->cur;
+}
+
+// Chooses the sweep kernel by timing.  The INIT sweep reads only buffer `cur` and the data
+// and writes the other buffer and the state, so it can be repeated with either kernel
+// without changing the solve; the faster kernel is kept for the problem's lifetime.
+static int autotune_variant(pasc_gb300_problem *p)
+{
+    if (p->variant >= 0) return PASC_OK;
+    if (!sweep_tma_supported(p->K)) {
+        p->variant = 0;
+        return PASC_OK;
+    }
+    cudaStream_t s = p->stream;
+    SweepArgs a;
+    sweep_args(p, &a);
+    float best = 1e30f;
+    int bestv = 0;
+    for (int v = 0; v < 2; v++) {
+        float tot = 0.f;
+        for (int rep = 0; rep < 4; rep++) {
+            fill_device_state(p, p->st_h);
+            CU(cudaMemcpyAsync(p->st, p->st_h, sizeof(SpgDevState), cudaMemcpyHostToDevice, s));
+            CU(cudaEventRecord(p->ev0, s));
+            CU(launch_variant(p, v, true, a));
+            CU(cudaEventRecord(p->ev1, s));
+            CU(cudaEventSynchronize(p->ev1));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+            if (rep > 0) tot += ms;  // the first launch also pays one-time set-up
+        }
+        CU(cudaMemcpyAsync(p->st_h, p->st, sizeof(SpgDevState), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        CHK(check_device_error(p));
+        if (tot < best) {
+            best = tot;
+            bestv = v;
+        }
+    }
+    p->variant = bestv;
+    return PASC_OK;
+}
+
+// spgqpsolver.cpp:104-137 plus the first direction (one INIT sweep)
+static int mixed_start(pasc_gb300_problem *p)
+{
+    const pasc_gb300_spgqp_opts *o = &p->run.o;
+    if (o->stop_normgp_normb || o->stop_Anormgp_normb)
+        return fail(PASC_ERR_NOTSUPP, "spgqp: ||b||-scaled stopping tests need the fp64 path");
+    cudaStream_t s = p->stream;
+    CHK(autotune_variant(p));
+    CHK(ensure_chunk_graph(p));
+    SpgDevState *h = p->st_h;
+    fill_device_state(p, h);
     SweepArgs a;
     sweep_args(p, &a);
     CU(cudaEventRecord(p->ev0, s));
     CU(cudaMemcpyAsync(p->st, h, sizeof(SpgDevState), cudaMemcpyHostToDevice, s));
-    CU(launch_sweep(p->K, true, p->grid_sweep_init, a, s));
+    CU(launch_variant(p, p->variant, true, a));
     CU(cudaEventRecord(p->ev1, s));
     CU(cudaMemcpyAsync(h, p->st, sizeof(SpgDevState), cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
@@ -662,6 +751,7 @@ static int mixed_start(pasc_gb300_problem *p)
     cudaEventElapsedTime(&ms, p->ev0, p->ev1);
     p->run.launches += 1;
     p->run.time_s += ms * 1e-3;
+    CHK(check_device_error(p));
     sync_run_from_device(p);
     return PASC_OK;
 }
@@ -676,6 +766,7 @@ static int mixed_iterate(pasc_gb300_problem *p, long n, int poll)
     sweep_args(p, &a);
     SpgDevState *h = p->st_h;
     if (p->run.status != PASC_SPG_RUNNING) return PASC_OK;
+    CHK(ensure_chunk_graph(p));
     const long room = p->run.o.maxit - p->run.it;
     if (n > room) n = room;
     long done = 0;
@@ -689,14 +780,14 @@ static int mixed_iterate(pasc_gb300_problem *p, long n, int poll)
         if (want == GRAPH_CHUNK) {
             CU(cudaGraphLaunch(p->chunk_graph, s));
         } else {
-            for (long q = 0; q < want; q++) CU(launch_sweep(p->K, false, p->grid_sweep, a, s));
+            for (long q = 0; q < want; q++) CU(launch_variant(p, p->variant, false, a));
         }
         done += want;
         p->run.launches += (int)want;
         if (poll) {
             CU(cudaMemcpyAsync(h, p->st, sizeof(SpgDevState), cudaMemcpyDeviceToHost, s));
             CU(cudaStreamSynchronize(s));
-            if (h->status != PASC_SPG_RUNNING) break;
+            if (h->status != PASC_SPG_RUNNING || h->error) break;
         }
     }
     CU(cudaEventRecord(p->ev1, s));
@@ -707,6 +798,7 @@ static int mixed_iterate(pasc_gb300_problem *p, long n, int poll)
     p->run.time_s += ms * 1e-3;
     p->run.last_iterate_ms = ms;
     p->run.last_iterate_launches = (int)done;
+    CHK(check_device_error(p));
     sync_run_from_device(p);
     if (p->run.status == PASC_SPG_RUNNING && p->run.it >= p->run.o.maxit) p->run.status = PASC_SPG_MAXIT;
     return PASC_OK;
@@ -919,6 +1011,28 @@ int pasc_gb300_fem_h1_matmult_f32(const float *x_dev, float *y_dev, long T, int 
     if ((!x_dev || !y_dev) && T > 0) return fail(PASC_ERR_ARG, "matmult_f32: NULL pointer");
     if (T < 0 || K < 1) return fail(PASC_ERR_ARG, "matmult_f32: bad T/K");
     CU(launch_matmult_f32(x_dev, y_dev, T, K, coeff, (cudaStream_t)stream));
+    return PASC_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int pasc_gb300_set_sweep_variant(pasc_gb300_problem *p, int variant)
+{
+    if (!p) return fail(PASC_ERR_ARG, "set_sweep_variant: NULL problem");
+    if (variant < -1 || variant > 1) return fail(PASC_ERR_ARG, "set_sweep_variant: variant must be -1, 0 or 1");
+    if (p->precision != PASC_PREC_MIXED) return fail(PASC_ERR_STATE, "set_sweep_variant: mixed precision only");
+    if (variant == 1 && !sweep_tma_supported(p->K)) return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: K not supported");
+    p->variant = variant;
+    p->run.started = false;
+    return PASC_OK;
+}
+
+int pasc_gb300_get_sweep_variant(pasc_gb300_problem *p, int *variant)
+{
+    if (!p || !variant) return fail(PASC_ERR_ARG, "get_sweep_variant: NULL argument");
+    *variant = p->variant;
     return PASC_OK;
 }
 

@@ -1,0 +1,105 @@
+"""Both sweep kernels of the mixed path (0: one timestep per thread; 1: bulk-copy tiles of four
+timesteps per thread) against the FP64 oracle, with sizes around their tile boundaries
+(251 owned timesteps per tile for kernel 0, 504 for kernel 1) and every K they support.
+
+Tolerances: fixed-length trajectories within 2e-6 relative of the oracle's objective (FP32
+state, FP64 reductions); converged objectives within 1e-6 relative; the two kernels agree
+with each other to 1e-6 relative (they differ only in the grouping of FP32 sums)."""
+import numpy as np
+import pytest
+
+from pasc_inference_gb300 import PASC_PREC_MIXED, Problem, capi
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [1, 2, 3, 4, 5, 7, 250, 251, 252, 503, 504, 505, 508, 1007, 1008, 1009, 5000, 100003]
+
+
+def _qp(T, K, eps2, seed, oracle):
+    rng = np.random.default_rng(seed)
+    data = rng.normal(size=T) * 0.5 + rng.integers(0, K, size=T)
+    theta = np.arange(K, dtype=float)
+    x0 = rng.random(T * K)
+    return data, theta, x0, oracle.residual_b(data, theta, T, K), oracle.A_coeff(eps2, T)
+
+
+def _solve(T, K, eps2, data, theta, x0, variant, opts):
+    with Problem(T, K, eps2, precision=PASC_PREC_MIXED) as p:
+        p.set_sweep_variant(variant)
+        p.set_data(data)
+        p.set_theta(theta)
+        p.set_gamma(x0)
+        p.update_b()
+        st = p.spgqp_solve(opts)
+        assert p.get_sweep_variant() == variant
+        return st, p.get_gamma()
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("K", [1, 2, 3, 4, 5, 8])
+def test_trajectory_all_sizes(gpulib, oracle, variant, K):
+    for T in SIZES:
+        data, theta, x0, b, coeff = _qp(T, K, 10.0, 1000 * K + T, oracle)
+        x0r = x0.astype(np.float32).astype(np.float64)
+        for maxit in (0, 3):
+            if T == 1 and maxit > 0:
+                continue  # A = 0: the reference's step is a division by zero (see test_edge_sizes)
+            xo, ro, _ = oracle.spgqp_solve(b, x0r, T, K, coeff, oracle.spg_opts(maxit=maxit, m=10))
+            st, g = _solve(T, K, 10.0, data, theta, x0, variant, capi.spgqp_opts(maxit=maxit, m=10))
+            if ro.it != maxit:  # the oracle met a degenerate step (T == 1): nothing to compare
+                continue
+            assert st.it == maxit, (T, K, st.it, st.status)
+            assert abs(st.fx - ro.fx) <= 2e-6 * max(abs(ro.fx), 1e-9), (T, K, maxit, st.fx, ro.fx)
+            G = g.reshape(T, K)
+            assert np.all(G >= 0) and np.max(np.abs(G.sum(axis=1) - 1)) <= 1e-5, (T, K)
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("T,K,eps2", [(2000, 3, 30.0), (7777, 2, 5.0), (3001, 5, 100.0), (999, 8, 20.0)])
+def test_converged_objective(gpulib, oracle, qp_optimum, variant, T, K, eps2):
+    data, theta, x0, b, coeff = _qp(T, K, eps2, T + 17 * K, oracle)
+    f_opt, _ = qp_optimum(b, x0, T, K, coeff)
+    st, g = _solve(T, K, eps2, data, theta, x0, variant, capi.spgqp_opts(maxit=3000, stop_difff=0, m=10))
+    assert abs(st.fx - f_opt) <= 1e-6 * abs(f_opt), (st.fx, f_opt, st.it)
+    f_host = 0.5 * g @ oracle.matmult(g, T, K, coeff) - b @ g
+    assert abs(f_host - st.fx) <= 1e-6 * abs(f_opt)
+
+
+def test_variants_agree_and_autotune(gpulib, oracle):
+    T, K, eps2 = 300_001, 3, 10.0
+    data, theta, x0, b, coeff = _qp(T, K, eps2, 5, oracle)
+    res = {}
+    for v in (0, 1):
+        st, g = _solve(T, K, eps2, data, theta, x0, v, capi.spgqp_opts(maxit=200, stop_difff=0, m=10))
+        res[v] = (st, g)
+    # mid-trajectory iterates on a flat landscape may differ; the objective and the hard
+    # labels must not
+    assert abs(res[0][0].fx - res[1][0].fx) <= 1e-6 * abs(res[0][0].fx)
+    lab = [np.argmax(res[v][1].reshape(T, K), axis=1) for v in (0, 1)]
+    assert np.mean(lab[0] == lab[1]) >= 0.999
+    with Problem(T, K, eps2, precision=PASC_PREC_MIXED) as p:
+        assert p.get_sweep_variant() == -1
+        p.set_data(data)
+        p.set_theta(theta)
+        p.set_gamma(x0)
+        st = p.spgqp_solve(capi.spgqp_opts(maxit=200, stop_difff=0, m=10))
+        assert p.get_sweep_variant() in (0, 1)
+        assert abs(st.fx - res[0][0].fx) <= 1e-6 * abs(res[0][0].fx)
+
+
+def test_pads_stay_zero_and_buffers_untouched_outside(gpulib, oracle):
+    """Many solves on one handle: results stay identical to a fresh handle's (the zero pads
+    the bulk-copy kernel reads beyond the signal are never written)."""
+    T, K, eps2 = 1009, 3, 10.0
+    data, theta, x0, b, coeff = _qp(T, K, eps2, 9, oracle)
+    opts = capi.spgqp_opts(maxit=50, stop_difff=0, m=10)
+    st_ref, g_ref = _solve(T, K, eps2, data, theta, x0, 1, opts)
+    with Problem(T, K, eps2, precision=PASC_PREC_MIXED) as p:
+        p.set_sweep_variant(1)
+        p.set_data(data)
+        p.set_theta(theta)
+        for _ in range(5):
+            p.set_gamma(x0)
+            st = p.spgqp_solve(opts)
+            np.testing.assert_array_equal(p.get_gamma(), g_ref)
+            assert st.fx == st_ref.fx
