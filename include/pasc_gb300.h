@@ -240,6 +240,22 @@ int pasc_gb300_fem_h1_matmult_f64(const double *x_dev, double *y_dev, long T, in
 int pasc_gb300_fem_h1_matmult_f32(const float *x_dev, float *y_dev, long T, int K,
                                   float coeff, void *stream);
 
+/* Theta update for callers that cannot allocate device memory when they need it: code
+ * running while a stream is captured into a CUDA graph, hosts whose device memory belongs
+ * to another framework's allocator, real-time loops that allow no allocation (nor the
+ * device synchronisation cudaMalloc/cudaFree can imply) after start-up.  No counterpart in
+ * the reference; it computes what pasc_gb300_update_theta computes
+ * (theta_k = sum_t gamma_tk x_t / sum_t gamma_tk) on caller-owned device buffers: gamma_dev
+ * (T*K floats, t*K + k), data_dev (T floats), theta_dev (K doubles, written).  It calls no
+ * cudaMalloc, cudaFree or allocating library routine; its reduction scratch is a static
+ * device array of the library (about 128 KiB, held on every GPU that loads the library until
+ * the process exits), which limits K to 8.  The first call on a device looks up that array's
+ * address (cudaGetSymbolAddress), so make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (other streams, or before the previous call has
+ * finished) race and must be avoided.  Asynchronous on `stream`. */
+int pasc_gb300_theta_update_noalloc(const float *gamma_dev, const float *data_dev, long T, int K,
+                                    double *theta_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,6 +94,8 @@ PROTOTYPES = {
                                                 C.c_void_p]),
     "pasc_gb300_fem_h1_matmult_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_float,
                                                 C.c_void_p]),
+    "pasc_gb300_theta_update_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p,
+                                                  C.c_void_p]),
 }
 
 _lib = None

@@ -63,6 +63,9 @@ struct ThetaArgs {
     int cur;                  // buffer holding gamma
 };
 
+// Sets the message pasc_gb300_last_error() returns on the calling thread.
+void record_error(const char *msg);
+
 // Launchers (kernels_fused.cu).  Return a cudaError_t.
 int sweep_block_threads();
 int sweep_tile_width();

@@ -1037,3 +1037,8 @@ int pasc_gb300_get_sweep_variant(pasc_gb300_problem *p, int *variant)
 }
 
 }  // extern "C"
+
+namespace pasc {
+// lets other translation units report through pasc_gb300_last_error()
+void record_error(const char *msg) { g_last_error = msg; }
+}  // namespace pasc
