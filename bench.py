@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tts", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--variant", type=int, default=-1, choices=[-1, 0, 1],
+                    help="sweep kernel: -1 chosen by timing (default), 0 one timestep per thread, "
+                         "1 bulk-copy tiles (pin it when profiling: a profiler distorts the timing)")
     return ap.parse_args()
 
 
@@ -69,7 +72,7 @@ def measured_peaks():
 
 def profile_traffic():
     """DRAM bytes per sweep launch from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", "spg_sweep_k3_t1e7.md")
+    path = os.path.join(ROOT, "profiles", "spg_sweep_tma_k3_t1e7.md")
     try:
         with open(path) as f:
             for line in f:
@@ -222,6 +225,8 @@ def main():
     B_it = 8.0 * K * T + 4.0 * T  # read x, data; write x (FP32): the sweep's algorithmic bytes
 
     p = Problem(T, K, args.eps2, precision=PASC_PREC_MIXED, device=dev)
+    if args.variant >= 0:
+        p.set_sweep_variant(args.variant)
     p.set_data(sig.data)
     p.set_gamma(sig.gamma0)
     p.permute_gamma()
