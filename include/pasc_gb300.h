@@ -256,6 +256,37 @@ int pasc_gb300_fem_h1_matmult_f32(const float *x_dev, float *y_dev, long T, int 
 int pasc_gb300_theta_update_noalloc(const float *gamma_dev, const float *data_dev, long T, int K,
                                     double *theta_dev, void *stream);
 
+/* ---------------------------------------------------------------------------------------
+ * batch handle: n independent signals (each with its own T, K and epssqr) solved together on
+ * one device, mixed precision.  The reference solves such problems one run at a time (one
+ * TSSolver per signal, examples/test_signal1D/test_signal1D.cpp:188-353); here one launch
+ * per SPG iteration advances every signal whose solve is still running, and each signal
+ * keeps its own step lengths, GLL memory and stopping decision.
+ * ------------------------------------------------------------------------------------- */
+typedef struct pasc_gb300_batch pasc_gb300_batch;
+
+/* T[i] >= 1, 1 <= K[i] <= 8, epssqr[i] as in pasc_gb300_create (xdim == 1, scalef = 1). */
+int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const int *K,
+                            const double *epssqr, int device);
+int pasc_gb300_batch_destroy(pasc_gb300_batch *b);
+int pasc_gb300_batch_size(pasc_gb300_batch *b, int *n);
+/* Host buffers of signal i, FP64, with the meaning of pasc_gb300_set_data/set_gamma/
+ * get_gamma/set_theta/get_theta (T[i], T[i]*K[i] and K[i] values). */
+int pasc_gb300_batch_set_data(pasc_gb300_batch *b, int i, const double *data);
+int pasc_gb300_batch_set_gamma(pasc_gb300_batch *b, int i, const double *gamma);
+int pasc_gb300_batch_get_gamma(pasc_gb300_batch *b, int i, double *gamma);
+int pasc_gb300_batch_set_theta(pasc_gb300_batch *b, int i, const double *theta);
+int pasc_gb300_batch_get_theta(pasc_gb300_batch *b, int i, double *theta);
+/* pasc_gb300_spgqp_solve for every signal at once; st: n entries (nullable).  The
+ * ||b||-scaled stopping tests are not supported (PASC_ERR_NOTSUPP). */
+int pasc_gb300_batch_spgqp_solve(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o,
+                                 pasc_gb300_spgqp_stats *st);
+/* pasc_gb300_ts_solve for every signal at once (annealing <= 1): every signal runs its own
+ * outer loop and leaves the batch when its |L - L_old| test holds; st: n entries
+ * (nullable), kernel_launches and time_s are those of the whole batch. */
+int pasc_gb300_batch_ts_solve(pasc_gb300_batch *b, const pasc_gb300_ts_opts *ts,
+                              const pasc_gb300_spgqp_opts *spg, pasc_gb300_ts_stats *st);
+
 #ifdef __cplusplus
 }
 #endif

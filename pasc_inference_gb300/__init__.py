@@ -21,7 +21,7 @@ from . import capi
 from .capi import (PASC_PREC_FP64, PASC_PREC_MIXED, PascError, SpgqpOpts, SpgqpStats, TsOpts,
                    TsStats, check, load)
 
-__all__ = ["Problem", "Decomposition", "Signal1DData", "TSData", "GraphH1FEMModel", "TSSolver",
+__all__ = ["Problem", "Batch", "Decomposition", "Signal1DData", "TSData", "GraphH1FEMModel", "TSSolver",
            "SPGQPSolver", "PascError", "PASC_PREC_FP64", "PASC_PREC_MIXED", "capi"]
 
 _SPG_KEYS = {"spgqpsolver_maxit": "maxit", "spgqpsolver_eps": "eps", "spgqpsolver_m": "m",
@@ -169,6 +169,69 @@ class Problem:
         out = np.empty(self.T, dtype=np.int32)
         check(load().pasc_gb300_argmax_labels(self._h, out))
         return out
+
+
+class Batch:
+    """n independent signals (own T, K, epssqr) solved together on one GPU (a
+    pasc_gb300_batch handle): one launch per SPG iteration for all signals still running."""
+
+    def __init__(self, T, K, epssqr, device: int = 0):
+        self.T = np.ascontiguousarray(T, dtype=capi.LONG_DTYPE)
+        self.K = np.ascontiguousarray(K, dtype=np.int32)
+        eps = np.ascontiguousarray(epssqr, dtype=np.float64)
+        if not (len(self.T) == len(self.K) == len(eps)):
+            raise ValueError("T, K and epssqr need one entry per signal")
+        self.n = len(self.T)
+        h = C.c_void_p()
+        check(load().pasc_gb300_batch_create(C.byref(h), self.n, self.T, self.K, eps, int(device)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().pasc_gb300_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_data(self, i: int, data):
+        check(load().pasc_gb300_batch_set_data(self._h, int(i), np.ascontiguousarray(data, dtype=np.float64)))
+
+    def set_gamma(self, i: int, gamma):
+        check(load().pasc_gb300_batch_set_gamma(self._h, int(i), np.ascontiguousarray(gamma, dtype=np.float64)))
+
+    def get_gamma(self, i: int) -> np.ndarray:
+        out = np.empty(int(self.T[i]) * int(self.K[i]))
+        check(load().pasc_gb300_batch_get_gamma(self._h, int(i), out))
+        return out
+
+    def set_theta(self, i: int, theta):
+        check(load().pasc_gb300_batch_set_theta(self._h, int(i), np.ascontiguousarray(theta, dtype=np.float64)))
+
+    def get_theta(self, i: int) -> np.ndarray:
+        out = np.empty(int(self.K[i]))
+        check(load().pasc_gb300_batch_get_theta(self._h, int(i), out))
+        return out
+
+    def spgqp_solve(self, opts: SpgqpOpts | None = None) -> list:
+        st = (SpgqpStats * self.n)()
+        check(load().pasc_gb300_batch_spgqp_solve(self._h, C.byref(opts or capi.spgqp_opts()), st))
+        return list(st)
+
+    def ts_solve(self, ts: TsOpts | None = None, spg: SpgqpOpts | None = None) -> list:
+        st = (TsStats * self.n)()
+        check(load().pasc_gb300_batch_ts_solve(self._h, C.byref(ts or capi.ts_opts()),
+                                               C.byref(spg or capi.spgqp_opts()), st))
+        return list(st)
 
 
 # ------------------------------------------------------------------------------------------

@@ -57,6 +57,8 @@ class PascError(RuntimeError):
 
 _dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+LONG_DTYPE = np.int64 if C.sizeof(C.c_long) == 8 else np.int32
+_lp = np.ctypeslib.ndpointer(LONG_DTYPE, flags="C_CONTIGUOUS")
 _h = C.c_void_p
 
 # name -> (restype, argtypes); the complete list of exported symbols of include/pasc_gb300.h
@@ -96,6 +98,16 @@ PROTOTYPES = {
                                                 C.c_void_p]),
     "pasc_gb300_theta_update_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p,
                                                   C.c_void_p]),
+    "pasc_gb300_batch_create": (C.c_int, [C.POINTER(_h), C.c_int, _lp, _ip, _dp, C.c_int]),
+    "pasc_gb300_batch_destroy": (C.c_int, [_h]),
+    "pasc_gb300_batch_size": (C.c_int, [_h, C.POINTER(C.c_int)]),
+    "pasc_gb300_batch_set_data": (C.c_int, [_h, C.c_int, _dp]),
+    "pasc_gb300_batch_set_gamma": (C.c_int, [_h, C.c_int, _dp]),
+    "pasc_gb300_batch_get_gamma": (C.c_int, [_h, C.c_int, _dp]),
+    "pasc_gb300_batch_set_theta": (C.c_int, [_h, C.c_int, _dp]),
+    "pasc_gb300_batch_get_theta": (C.c_int, [_h, C.c_int, _dp]),
+    "pasc_gb300_batch_spgqp_solve": (C.c_int, [_h, C.POINTER(SpgqpOpts), C.c_void_p]),
+    "pasc_gb300_batch_ts_solve": (C.c_int, [_h, C.POINTER(TsOpts), C.POINTER(SpgqpOpts), C.c_void_p]),
 }
 
 _lib = None

@@ -1,0 +1,461 @@
+// batch.cu -- C ABI of the batched solver: many independent FEM-H1 signals on one GPU, one
+// launch per SPG iteration for all of them (kernels_batch.cu), each signal with its own
+// T, K, epssqr, step lengths, GLL memory and stopping decision.
+#include <math.h>
+#include <string.h>
+#include <algorithm>
+#include <chrono>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+using namespace pasc;
+
+namespace {
+
+constexpr int IDLE = 99;  // status of a signal that takes no part in the current solve
+constexpr long BPAD_FRONT = 4;
+
+int bfail(int code, const std::string &msg)
+{
+    record_error(msg.c_str());
+    return code;
+}
+
+}  // namespace
+
+#define BCU(call)                                                                                  \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return bfail(PASC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+#define BCHK(call)                     \
+    do {                               \
+        int r_ = (call);               \
+        if (r_ != PASC_OK) return r_;  \
+    } while (0)
+
+struct pasc_gb300_batch {
+    int n = 0, device = 0, sms = 0, KB = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<long> T;
+    std::vector<int> K;
+    std::vector<double> epssqr, coeffA, coeffB;
+    std::vector<BatchInstDev> inst_h;
+    std::vector<int> cur;  // buffer holding each signal's gamma
+    BatchInstDev *inst_d = nullptr;
+    int *seg_inst_d = nullptr;
+    int nseg = 0;
+    long nx = 0, nd = 0, maxN = 0;
+    float *xb[2] = {nullptr, nullptr}, *data = nullptr;
+    double *stage64 = nullptr;
+    SpgDevState *st_d = nullptr, *st_h = nullptr;
+    double *partials = nullptr, *theta64 = nullptr;
+    unsigned int *ticket = nullptr, *next_job = nullptr;
+    int *active_d = nullptr, *active_h = nullptr;
+    int grid = 0, grid_init = 0, grid_theta = 0;
+    cudaGraphExec_t chunk = nullptr;
+    pasc_gb300_spgqp_opts o{};
+    int launches = 0;
+};
+
+static constexpr int BATCH_CHUNK = 16;
+
+static void batch_free(pasc_gb300_batch *b)
+{
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->chunk) cudaGraphExecDestroy(b->chunk);
+    void *dev[] = {b->inst_d, b->seg_inst_d, b->xb[0], b->xb[1], b->data, b->stage64, b->st_d, b->partials,
+                   b->theta64, b->ticket, b->next_job, b->active_d};
+    for (void *p : dev)
+        if (p) cudaFree(p);
+    if (b->st_h) cudaFreeHost(b->st_h);
+    if (b->active_h) cudaFreeHost(b->active_h);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+static BatchArgs batch_args(pasc_gb300_batch *b)
+{
+    BatchArgs a;
+    a.inst = b->inst_d;
+    a.seg_inst = b->seg_inst_d;
+    a.nseg = b->nseg;
+    a.ninst = b->n;
+    a.xb0 = b->xb[0];
+    a.xb1 = b->xb[1];
+    a.data = b->data;
+    a.st = b->st_d;
+    a.partials = b->partials;
+    a.ticket = b->ticket;
+    a.next_job = b->next_job;
+    a.active = b->active_d;
+    a.theta64 = b->theta64;
+    return a;
+}
+
+static int batch_check_index(pasc_gb300_batch *b, int i)
+{
+    if (!b) return bfail(PASC_ERR_ARG, "batch: NULL handle");
+    if (i < 0 || i >= b->n) return bfail(PASC_ERR_ARG, "batch: signal index out of range");
+    return PASC_OK;
+}
+
+extern "C" {
+
+int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const int *K, const double *epssqr,
+                            int device)
+{
+    if (!out || !T || !K || !epssqr) return bfail(PASC_ERR_ARG, "batch_create: NULL argument");
+    *out = nullptr;
+    if (n < 1) return bfail(PASC_ERR_ARG, "batch_create: n must be >= 1");
+    int ndev = pasc_gb300_device_count();
+    if (ndev <= 0) return bfail(PASC_ERR_CUDA, "batch_create: no CUDA device available");
+    if (device < 0 || device >= ndev) return bfail(PASC_ERR_ARG, "batch_create: device out of range");
+    pasc_gb300_batch *b = new pasc_gb300_batch();
+    auto bail = [&](int code) { batch_free(b); return code; };
+    b->n = n;
+    b->device = device;
+    b->T.assign(T, T + n);
+    b->K.assign(K, K + n);
+    b->epssqr.assign(epssqr, epssqr + n);
+    b->cur.assign(n, 0);
+    const int W = batch_tile_width(), ST = batch_segment_timesteps();
+    const long PADB = batch_max_tile();
+    std::vector<int> seg_inst;
+    b->inst_h.resize(n);
+    long xo = 0, doff = 0;
+    for (int i = 0; i < n; i++) {
+        if (T[i] < 1 || K[i] < 1 || K[i] > 8)
+            return bail(bfail(PASC_ERR_ARG, "batch_create: signal " + std::to_string(i) + " needs T >= 1 and 1 <= K <= 8"));
+        if ((double)T[i] * K[i] > 1.0e9) return bail(bfail(PASC_ERR_ARG, "batch_create: signal too long"));
+        b->KB = std::max(b->KB, K[i]);
+        BatchInstDev &I = b->inst_h[i];
+        memset(&I, 0, sizeof I);
+        I.T = (int)T[i];
+        I.K = K[i];
+        I.xoff = xo + BPAD_FRONT * K[i];
+        I.doff = doff + BPAD_FRONT;
+        xo += ((BPAD_FRONT + T[i] + PADB) * K[i] + 3) / 4 * 4;  // next signal starts 16-byte aligned
+        doff += (BPAD_FRONT + T[i] + PADB + 3) / 4 * 4;
+        I.tiles = (int)((T[i] + W - 1) / W);
+        I.seg0 = (int)seg_inst.size();
+        I.nseg = (int)((T[i] + ST - 1) / ST);
+        for (int s = 0; s < I.nseg; s++) seg_inst.push_back(i);
+        b->maxN = std::max(b->maxN, T[i] * (long)K[i]);
+        double c = epssqr[i] * (1.0 / (double)T[i]);  // graphh1fem.cpp:146-151
+        b->coeffA.push_back(c);
+        b->coeffB.push_back(-1.0 * (1.0 / (double)T[i]));  // graphh1fem.cpp:280-283
+    }
+    b->nx = xo;
+    b->nd = doff;
+    b->nseg = (int)seg_inst.size();
+    if (cudaSetDevice(device) != cudaSuccess) return bail(bfail(PASC_ERR_CUDA, "cudaSetDevice failed"));
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
+        return bail(bfail(PASC_ERR_CUDA, "batch_create: stream/event creation failed"));
+    auto dal = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes > 0 ? bytes : 1) == cudaSuccess; };
+    if (!dal((void **)&b->inst_d, sizeof(BatchInstDev) * n) || !dal((void **)&b->seg_inst_d, sizeof(int) * b->nseg) ||
+        !dal((void **)&b->xb[0], sizeof(float) * b->nx) || !dal((void **)&b->xb[1], sizeof(float) * b->nx) ||
+        !dal((void **)&b->data, sizeof(float) * b->nd) || !dal((void **)&b->stage64, sizeof(double) * b->maxN) ||
+        !dal((void **)&b->st_d, sizeof(SpgDevState) * n) || !dal((void **)&b->partials, sizeof(double) * 16 * b->nseg) ||
+        !dal((void **)&b->theta64, sizeof(double) * 8 * n) || !dal((void **)&b->ticket, sizeof(unsigned int) * n) ||
+        !dal((void **)&b->next_job, sizeof(unsigned int)) || !dal((void **)&b->active_d, sizeof(int) * n))
+        return bail(bfail(PASC_ERR_ALLOC, "batch_create: device allocation failed"));
+    if (cudaMallocHost((void **)&b->st_h, sizeof(SpgDevState) * n) != cudaSuccess ||
+        cudaMallocHost((void **)&b->active_h, sizeof(int) * n) != cudaSuccess)
+        return bail(bfail(PASC_ERR_ALLOC, "batch_create: pinned allocation failed"));
+    memset(b->st_h, 0, sizeof(SpgDevState) * n);
+    cudaMemset(b->xb[0], 0, sizeof(float) * b->nx);  // pads stay zero: kernels write 0 <= t < T only
+    cudaMemset(b->xb[1], 0, sizeof(float) * b->nx);
+    cudaMemset(b->data, 0, sizeof(float) * b->nd);
+    cudaMemset(b->st_d, 0, sizeof(SpgDevState) * n);
+    cudaMemset(b->ticket, 0, sizeof(unsigned int) * n);
+    cudaMemset(b->theta64, 0, sizeof(double) * 8 * n);
+    cudaMemcpy(b->inst_d, b->inst_h.data(), sizeof(BatchInstDev) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(b->seg_inst_d, seg_inst.data(), sizeof(int) * b->nseg, cudaMemcpyHostToDevice);
+    b->grid = std::max(1, std::min(batch_blocks_per_sm(b->KB, false) * b->sms, b->nseg));
+    b->grid_init = std::max(1, std::min(batch_blocks_per_sm(b->KB, true) * b->sms, b->nseg));
+    b->grid_theta = std::max(1, std::min(b->sms * 4, b->nseg));
+    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        return bail(bfail(PASC_ERR_CUDA, "batch_create: initialisation failed"));
+    *out = b;
+    return PASC_OK;
+}
+
+int pasc_gb300_batch_destroy(pasc_gb300_batch *b)
+{
+    batch_free(b);
+    return PASC_OK;
+}
+
+int pasc_gb300_batch_size(pasc_gb300_batch *b, int *n)
+{
+    if (!b || !n) return bfail(PASC_ERR_ARG, "batch_size: NULL argument");
+    *n = b->n;
+    return PASC_OK;
+}
+
+int pasc_gb300_batch_set_data(pasc_gb300_batch *b, int i, const double *data)
+{
+    BCHK(batch_check_index(b, i));
+    if (!data) return bfail(PASC_ERR_ARG, "batch_set_data: NULL data");
+    BCU(cudaSetDevice(b->device));
+    BCU(cudaMemcpyAsync(b->stage64, data, sizeof(double) * b->T[i], cudaMemcpyHostToDevice, b->stream));
+    BCU(launch_f64_to_f32(b->stage64, b->data + b->inst_h[i].doff, b->T[i], b->stream));
+    BCU(cudaStreamSynchronize(b->stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_batch_set_gamma(pasc_gb300_batch *b, int i, const double *gamma)
+{
+    BCHK(batch_check_index(b, i));
+    if (!gamma) return bfail(PASC_ERR_ARG, "batch_set_gamma: NULL gamma");
+    BCU(cudaSetDevice(b->device));
+    const long N = b->T[i] * b->K[i];
+    BCU(cudaMemcpyAsync(b->stage64, gamma, sizeof(double) * N, cudaMemcpyHostToDevice, b->stream));
+    BCU(launch_f64_to_f32(b->stage64, b->xb[b->cur[i]] + b->inst_h[i].xoff, N, b->stream));
+    BCU(cudaStreamSynchronize(b->stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_batch_get_gamma(pasc_gb300_batch *b, int i, double *gamma)
+{
+    BCHK(batch_check_index(b, i));
+    if (!gamma) return bfail(PASC_ERR_ARG, "batch_get_gamma: NULL gamma");
+    BCU(cudaSetDevice(b->device));
+    const long N = b->T[i] * b->K[i];
+    BCU(launch_f32_to_f64(b->xb[b->cur[i]] + b->inst_h[i].xoff, b->stage64, N, b->stream));
+    BCU(cudaMemcpyAsync(gamma, b->stage64, sizeof(double) * N, cudaMemcpyDeviceToHost, b->stream));
+    BCU(cudaStreamSynchronize(b->stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_batch_set_theta(pasc_gb300_batch *b, int i, const double *theta)
+{
+    BCHK(batch_check_index(b, i));
+    if (!theta) return bfail(PASC_ERR_ARG, "batch_set_theta: NULL theta");
+    BCU(cudaSetDevice(b->device));
+    BatchInstDev &I = b->inst_h[i];
+    for (int k = 0; k < b->K[i]; k++) I.theta[k] = (float)theta[k];
+    BCU(cudaMemcpyAsync(b->theta64 + 8 * i, theta, sizeof(double) * b->K[i], cudaMemcpyHostToDevice, b->stream));
+    BCU(cudaMemcpyAsync(b->inst_d + i, &I, sizeof(BatchInstDev), cudaMemcpyHostToDevice, b->stream));
+    BCU(cudaStreamSynchronize(b->stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_batch_get_theta(pasc_gb300_batch *b, int i, double *theta)
+{
+    BCHK(batch_check_index(b, i));
+    if (!theta) return bfail(PASC_ERR_ARG, "batch_get_theta: NULL theta");
+    BCU(cudaSetDevice(b->device));
+    BCU(cudaMemcpyAsync(theta, b->theta64 + 8 * i, sizeof(double) * b->K[i], cudaMemcpyDeviceToHost, b->stream));
+    BCU(cudaStreamSynchronize(b->stream));
+    return PASC_OK;
+}
+
+}  // extern "C"
+
+// blocked k*T+t -> interleaved t*K+k for every signal (TSSolver::gammavector_permute)
+static int batch_permute(pasc_gb300_batch *b)
+{
+    for (int i = 0; i < b->n; i++) {
+        const long off = b->inst_h[i].xoff;
+        BCU(launch_permute_f32(b->xb[b->cur[i]] + off, b->xb[b->cur[i] ^ 1] + off, b->T[i], b->K[i], b->stream));
+        b->cur[i] ^= 1;
+    }
+    return PASC_OK;
+}
+
+static int ensure_batch_graph(pasc_gb300_batch *b)
+{
+    if (b->chunk) return PASC_OK;
+    BCU(cudaStreamSynchronize(b->stream));
+    BatchArgs a = batch_args(b);
+    cudaGraph_t g;
+    BCU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    for (int q = 0; q < BATCH_CHUNK; q++) {
+        cudaError_t e = cudaMemsetAsync(b->next_job, 0, sizeof(unsigned int), b->stream);
+        if (e == cudaSuccess) e = launch_batch_sweep(b->KB, false, b->grid, a, b->stream);
+        if (e != cudaSuccess) {
+            cudaStreamEndCapture(b->stream, &g);
+            return bfail(PASC_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+        }
+    }
+    BCU(cudaStreamEndCapture(b->stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&b->chunk, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        b->chunk = nullptr;
+        return bfail(PASC_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+    }
+    return PASC_OK;
+}
+
+// SPG solves of the signals with active_h[i] != 0 (the others stay untouched).
+static int batch_spgqp(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o, double *elapsed_ms)
+{
+    if (o->stop_normgp_normb || o->stop_Anormgp_normb)
+        return bfail(PASC_ERR_NOTSUPP, "batch: ||b||-scaled stopping tests are not supported");
+    if (o->m < 1 || o->m > MMAX_STATE) return bfail(PASC_ERR_ARG, "batch: m must be in [1, 64]");
+    BCHK(ensure_batch_graph(b));
+    cudaStream_t s = b->stream;
+    int nact = 0;
+    for (int i = 0; i < b->n; i++) {
+        SpgDevState &h = b->st_h[i];
+        memset(&h, 0, sizeof h);
+        h.alpha_prev = h.alpha_cur = o->alphainit;
+        h.coeff = b->coeffA[i];
+        h.bscale = b->coeffB[i];
+        h.eps = o->eps;
+        h.gamma = o->gamma;
+        h.sigma1 = o->sigma1;
+        h.sigma2 = o->sigma2;
+        h.maxit = o->maxit;
+        h.m = o->m;
+        h.stop_difff = o->stop_difff;
+        h.stop_normgp = o->stop_normgp;
+        h.stop_Anormgp = o->stop_Anormgp;
+        h.cur = b->cur[i];
+        h.status = b->active_h[i] ? PASC_SPG_RUNNING : IDLE;
+        nact += b->active_h[i] ? 1 : 0;
+    }
+    if (nact == 0) return PASC_OK;
+    BatchArgs a = batch_args(b);
+    BCU(cudaEventRecord(b->ev0, s));
+    BCU(cudaMemcpyAsync(b->st_d, b->st_h, sizeof(SpgDevState) * b->n, cudaMemcpyHostToDevice, s));
+    BCU(cudaMemsetAsync(b->ticket, 0, sizeof(unsigned int) * b->n, s));
+    BCU(cudaMemsetAsync(b->next_job, 0, sizeof(unsigned int), s));
+    BCU(launch_batch_sweep(b->KB, true, b->grid_init, a, s));
+    b->launches++;
+    long done = 0;
+    while (done < o->maxit) {
+        BCU(cudaGraphLaunch(b->chunk, s));
+        done += BATCH_CHUNK;
+        b->launches += BATCH_CHUNK;
+        BCU(cudaMemcpyAsync(b->st_h, b->st_d, sizeof(SpgDevState) * b->n, cudaMemcpyDeviceToHost, s));
+        BCU(cudaStreamSynchronize(s));
+        bool running = false, err = false;
+        for (int i = 0; i < b->n; i++) {
+            running = running || b->st_h[i].status == PASC_SPG_RUNNING;
+            err = err || b->st_h[i].error;
+        }
+        if (err) return bfail(PASC_ERR_TIMEOUT, "batch: a bounded wait for a bulk copy gave up");
+        if (!running) break;
+    }
+    BCU(cudaEventRecord(b->ev1, s));
+    BCU(cudaMemcpyAsync(b->st_h, b->st_d, sizeof(SpgDevState) * b->n, cudaMemcpyDeviceToHost, s));
+    BCU(cudaEventSynchronize(b->ev1));
+    BCU(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    if (elapsed_ms) *elapsed_ms += ms;
+    for (int i = 0; i < b->n; i++) {
+        if (!b->active_h[i]) continue;
+        b->cur[i] = b->st_h[i].cur;
+        if (b->st_h[i].status == PASC_SPG_RUNNING) b->st_h[i].status = PASC_SPG_MAXIT;
+    }
+    return PASC_OK;
+}
+
+extern "C" {
+
+int pasc_gb300_batch_spgqp_solve(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o, pasc_gb300_spgqp_stats *st)
+{
+    if (!b || !o) return bfail(PASC_ERR_ARG, "batch_spgqp_solve: NULL argument");
+    BCU(cudaSetDevice(b->device));
+    for (int i = 0; i < b->n; i++) b->active_h[i] = 1;
+    double ms = 0.0;
+    b->launches = 0;
+    BCHK(batch_spgqp(b, o, &ms));
+    if (st) {
+        for (int i = 0; i < b->n; i++) {
+            const SpgDevState &h = b->st_h[i];
+            st[i].it = h.it;
+            st[i].hessmult = h.hessmult;
+            st[i].status = h.status;
+            st[i].kernel_launches = b->launches;
+            st[i].fx = h.fx;
+            st[i].gP = h.dd;
+            st[i].dAd = h.dAd;
+            st[i].time_s = ms * 1e-3;
+        }
+    }
+    return PASC_OK;
+}
+
+// TSSolver::solve (include/general/solver/tssolver.h:492-715) for every signal of the batch at
+// once: each signal has its own outer loop (theta step, gamma step, |L - L_old| test); a
+// signal that has stopped takes no further part.  No annealing.
+int pasc_gb300_batch_ts_solve(pasc_gb300_batch *b, const pasc_gb300_ts_opts *ts, const pasc_gb300_spgqp_opts *spg,
+                              pasc_gb300_ts_stats *st)
+{
+    if (!b || !ts || !spg) return bfail(PASC_ERR_ARG, "batch_ts_solve: NULL argument");
+    if (ts->annealing > 1) return bfail(PASC_ERR_NOTSUPP, "batch_ts_solve: annealing is not supported");
+    BCU(cudaSetDevice(b->device));
+    auto t0 = std::chrono::steady_clock::now();
+    const int n = b->n;
+    std::vector<double> L(n, DBL_MAX), dL(n, DBL_MAX);
+    std::vector<int> done(n, 0), it_last(n, 0), spg_it(n, 0), spg_hm(n, 0), incr(n, 0);
+    b->launches = 0;
+    if (ts->init_permute) BCHK(batch_permute(b));
+    BatchArgs a = batch_args(b);
+    for (int it = 0; it < ts->maxit; it++) {
+        int nact = 0;
+        for (int i = 0; i < n; i++) {
+            b->active_h[i] = !done[i];
+            nact += b->active_h[i];
+        }
+        if (nact == 0) break;
+        if (!ts->thetasolved) {
+            // the theta kernel reads each signal's buffer index from its state
+            for (int i = 0; i < n; i++) b->st_h[i].cur = b->cur[i];
+            BCU(cudaMemcpyAsync(b->st_d, b->st_h, sizeof(SpgDevState) * n, cudaMemcpyHostToDevice, b->stream));
+            BCU(cudaMemcpyAsync(b->active_d, b->active_h, sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
+            BCU(cudaMemsetAsync(b->ticket, 0, sizeof(unsigned int) * n, b->stream));
+            BCU(cudaMemsetAsync(b->next_job, 0, sizeof(unsigned int), b->stream));
+            BCU(launch_theta_batch(b->grid_theta, a, b->stream));
+            b->launches++;
+        }
+        BCHK(batch_spgqp(b, spg, nullptr));
+        for (int i = 0; i < n; i++) {
+            if (done[i]) continue;
+            const SpgDevState &h = b->st_h[i];
+            spg_it[i] += h.it;
+            spg_hm[i] += h.hessmult;
+            const double L_old = L[i];
+            L[i] = h.fx;
+            dL[i] = fabs(L[i] - L_old);
+            if (L[i] - L_old > 0) incr[i]++;
+            it_last[i] = it;
+            if (ts->relative ? (dL[i] < ts->eps * fabs(L[i])) : (dL[i] < ts->eps)) done[i] = 1;
+            else if (it == ts->maxit - 1) it_last[i] = ts->maxit;
+        }
+    }
+    BCU(cudaStreamSynchronize(b->stream));
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (st) {
+        for (int i = 0; i < n; i++) {
+            st[i].it_last = it_last[i];
+            st[i].it_sum = it_last[i];
+            st[i].spg_it_sum = spg_it[i];
+            st[i].spg_hessmult_sum = spg_hm[i];
+            st[i].kernel_launches = b->launches;
+            st[i].L_increased = incr[i];
+            st[i].L = L[i];
+            st[i].deltaL = dL[i];
+            st[i].aic = 2 * log(L[i]) + b->K[i];
+            st[i].time_s = secs;
+        }
+    }
+    return PASC_OK;
+}
+
+}  // extern "C"

@@ -82,4 +82,17 @@ __device__ __forceinline__ bool last_block_done(unsigned int *counter)
     return am_last;
 }
 
+// Same for a counter shared by n participants (e.g. the segments of one signal): true in the
+// block that arrives n-th.
+__device__ __forceinline__ bool last_block_done_count(unsigned int *counter, unsigned int n)
+{
+    __shared__ bool am_last_n;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) am_last_n = (atomicAdd(counter, 1u) == n - 1);
+    __syncthreads();
+    if (am_last_n) __threadfence();
+    return am_last_n;
+}
+
 }  // namespace pasc

@@ -63,6 +63,38 @@ struct ThetaArgs {
     int cur;                  // buffer holding gamma
 };
 
+// One signal of a batch (device copy).
+struct BatchInstDev {
+    long xoff;       // gamma of t = 0 in the packed gamma buffers (floats)
+    long doff;       // data of t = 0 in the packed data buffer
+    int T, K;
+    int seg0, nseg;  // its segments in the work list
+    int tiles;       // bulk-copy tiles covering it
+    int pad;
+    float theta[8];
+};
+
+struct BatchArgs {
+    BatchInstDev *inst;
+    const int *seg_inst;     // segment -> signal
+    int nseg, ninst;
+    float *xb0, *xb1;        // packed gamma, ping-pong (each signal's half given by its state's cur)
+    const float *data;       // packed data
+    SpgDevState *st;         // one per signal
+    double *partials;        // 16 per segment
+    unsigned int *ticket;    // one per signal
+    unsigned int *next_job;  // work-list counter (zeroed before every launch)
+    const int *active;       // theta step: signals still in their outer loop
+    double *theta64;         // 8 per signal
+};
+
+int batch_tile_width();
+int batch_segment_timesteps();
+int batch_max_tile();
+int batch_blocks_per_sm(int KB, bool init);
+cudaError_t launch_batch_sweep(int KB, bool init, int grid, const BatchArgs &a, cudaStream_t s);
+cudaError_t launch_theta_batch(int grid, const BatchArgs &a, cudaStream_t s);
+
 // Sets the message pasc_gb300_last_error() returns on the calling thread.
 void record_error(const char *msg);
 
