@@ -22,6 +22,12 @@ Besides the headline line it measures, on rank 0:
              written in FP32, the data read once) over its CUDA-event time, against the
              measured HBM copy bandwidth.
   cpu_baseline  the FP64 CPU oracle (a port of the reference's CPU path) on all host cores.
+  batched    the 256-signal uneven workload (T log-uniform in [1e3, 1e6], K in 2..5, epssqr
+             log-uniform in [1, 1000]): every signal's TSSolver (SPG eps 1e-6, m 10; outer loop
+             to 1e-6 relative change of L) solved by one batch handle (one launch per SPG
+             iteration for all running signals) and, for comparison, one signal at a time with
+             the plain FP64 GPU path and with the single-signal mixed path; plus the batch
+             sweep's HBM throughput with all 256 signals running.
 """
 from __future__ import annotations
 
@@ -55,6 +61,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tts", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--variant", type=int, default=-1, choices=[-1, 0, 1],
                     help="sweep kernel: -1 chosen by timing (default), 0 one timestep per thread, "
                          "1 bulk-copy tiles (pin it when profiling: a profiler distorts the timing)")
@@ -295,6 +302,8 @@ def main():
         result["e2e"] = measure_e2e(sig, theta, args.eps2, dev)
     if info.rank == 0 and not args.no_tts:
         result["time_to_1e-6_rel_obj"] = measure_tts(sig, theta, args.eps2, dev)
+    if info.rank == 0 and not args.no_batched:
+        result["batched"] = measure_batched(dev, peak)
     if info.rank == 0 and not args.no_cpu:
         rate, dt = oracle_iter_rate(sig, theta, args.eps2, T, 5, 0)
         result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
@@ -369,6 +378,76 @@ def measure_tts(sig, theta, eps2, dev):
     a, b = res["fp64_plain"]["seconds"], res["mixed_fused"]["seconds"]
     res["speedup_vs_fp64_plain"] = (a / b) if (a and b) else None
     return res
+
+
+def measure_batched(dev, peak):
+    from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Batch, Problem, capi, datagen
+    inst = datagen.batched()
+    n = len(inst)
+    ts = capi.ts_opts(eps=1e-6, relative=1)
+    spg = capi.spgqp_opts(m=10, eps=1e-6)
+
+    def load_batch(theta0):
+        bt = Batch([s.T for s in inst], [s.K for s in inst], [s.epssqr for s in inst], device=dev)
+        for i, s in enumerate(inst):
+            bt.set_data(i, s.data)
+            bt.set_gamma(i, s.gamma0)
+            bt.set_theta(i, theta0(s))
+        return bt
+
+    # sweep throughput with every signal running: 200 iterations, stopping tests off
+    B_sweep = float(sum((8 * s.K + 4) * s.T for s in inst))
+    with load_batch(lambda s: np.linspace(0.0, 4.0, s.K)) as bt:
+        bt.spgqp_solve(capi.spgqp_opts(maxit=20, stop_difff=0))
+        for i, s in enumerate(inst):
+            bt.set_gamma(i, s.gamma0)
+        st = bt.spgqp_solve(capi.spgqp_opts(maxit=200, stop_difff=0))
+        running = sum(1 for x in st if x.status == capi.PASC_SPG_MAXIT)
+        sweep_s = st[0].time_s / (200 + 1)
+    gbs = B_sweep / sweep_s / 1e9
+
+    walls, L_b = [], None
+    for rep in range(2):
+        with load_batch(lambda s: np.zeros(s.K)) as bt:
+            t0 = time.perf_counter()
+            st = bt.ts_solve(ts, spg)
+            walls.append(time.perf_counter() - t0)
+            L_b = np.array([x.L for x in st])
+            spg_it_b = int(sum(x.spg_it_sum for x in st))
+            launches_b = st[0].kernel_launches
+    seq = {}
+    for name, prec in (("fp64_plain", PASC_PREC_FP64), ("mixed_single", PASC_PREC_MIXED)):
+        tot, its, Ls = 0.0, 0, []
+        for s in inst:
+            with Problem(s.T, s.K, s.epssqr, precision=prec, device=dev) as p:
+                p.set_data(s.data)
+                p.set_gamma(s.gamma0)
+                p.set_theta(np.zeros(s.K))
+                t0 = time.perf_counter()
+                r = p.ts_solve(ts, spg)
+                tot += time.perf_counter() - t0
+                its += r.spg_it_sum
+                Ls.append(r.L)
+        seq[name] = (tot, its, np.array(Ls))
+    wall_b = min(walls)
+    rel = np.abs(L_b - seq["fp64_plain"][2]) / np.abs(seq["fp64_plain"][2])
+    return {
+        "workload": "256 signals, T log-U[1e3,1e6], K U{2..5}, epssqr log-U[1,1000], sorted levels U[0,4], "
+                    "segments U[T/50,T/5], sigma U[0.2,1]; TSSolver SPG eps 1e-6 m 10, outer 1e-6 relative",
+        "signals": n, "timesteps": int(sum(s.T for s in inst)),
+        "batch_s": wall_b, "batch_spg_it_sum": spg_it_b, "batch_gpu_launches": launches_b,
+        "fp64_plain_sequential_s": seq["fp64_plain"][0], "fp64_plain_spg_it_sum": int(seq["fp64_plain"][1]),
+        "mixed_single_sequential_s": seq["mixed_single"][0],
+        "mixed_single_spg_it_sum": int(seq["mixed_single"][1]),
+        "speedup_vs_fp64_plain_sequential": seq["fp64_plain"][0] / wall_b,
+        "speedup_vs_mixed_single_sequential": seq["mixed_single"][0] / wall_b,
+        "L_rel_diff_vs_fp64": {"median": float(np.median(rel)), "max": float(np.max(rel)),
+                               "frac_within_1e-6": float(np.mean(rel <= 1e-6)),
+                               "frac_within_1e-4": float(np.mean(rel <= 1e-4))},
+        "sweep_all_running": {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                              "us_per_sweep": sweep_s * 1e6, "bytes_per_sweep": B_sweep,
+                              "signals_running_at_end": running},
+    }
 
 
 if __name__ == "__main__":

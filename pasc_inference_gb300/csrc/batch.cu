@@ -49,6 +49,9 @@ struct pasc_gb300_batch {
     BatchInstDev *inst_d = nullptr;
     int *seg_inst_d = nullptr;
     int nseg = 0;
+    // work list: the segments of the signals taking part in the next launches
+    int *work_d = nullptr, *nwork_d = nullptr, *work_h = nullptr;
+    std::vector<char> in_work;  // signals in the uploaded list
     long nx = 0, nd = 0, maxN = 0;
     float *xb[2] = {nullptr, nullptr}, *data = nullptr;
     double *stage64 = nullptr;
@@ -69,12 +72,13 @@ static void batch_free(pasc_gb300_batch *b)
     if (!b) return;
     cudaSetDevice(b->device);
     if (b->chunk) cudaGraphExecDestroy(b->chunk);
-    void *dev[] = {b->inst_d, b->seg_inst_d, b->xb[0], b->xb[1], b->data, b->stage64, b->st_d, b->partials,
+    void *dev[] = {b->inst_d, b->seg_inst_d, b->work_d, b->nwork_d, b->xb[0], b->xb[1], b->data, b->stage64, b->st_d, b->partials,
                    b->theta64, b->ticket, b->next_job, b->active_d};
     for (void *p : dev)
         if (p) cudaFree(p);
     if (b->st_h) cudaFreeHost(b->st_h);
     if (b->active_h) cudaFreeHost(b->active_h);
+    if (b->work_h) cudaFreeHost(b->work_h);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -86,6 +90,8 @@ static BatchArgs batch_args(pasc_gb300_batch *b)
     BatchArgs a;
     a.inst = b->inst_d;
     a.seg_inst = b->seg_inst_d;
+    a.work = b->work_d;
+    a.nwork = b->nwork_d;
     a.nseg = b->nseg;
     a.ninst = b->n;
     a.xb0 = b->xb[0];
@@ -167,10 +173,12 @@ int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const 
         !dal((void **)&b->data, sizeof(float) * b->nd) || !dal((void **)&b->stage64, sizeof(double) * b->maxN) ||
         !dal((void **)&b->st_d, sizeof(SpgDevState) * n) || !dal((void **)&b->partials, sizeof(double) * 16 * b->nseg) ||
         !dal((void **)&b->theta64, sizeof(double) * 8 * n) || !dal((void **)&b->ticket, sizeof(unsigned int) * n) ||
-        !dal((void **)&b->next_job, sizeof(unsigned int)) || !dal((void **)&b->active_d, sizeof(int) * n))
+        !dal((void **)&b->next_job, sizeof(unsigned int)) || !dal((void **)&b->active_d, sizeof(int) * n) ||
+        !dal((void **)&b->work_d, sizeof(int) * b->nseg) || !dal((void **)&b->nwork_d, sizeof(int)))
         return bail(bfail(PASC_ERR_ALLOC, "batch_create: device allocation failed"));
     if (cudaMallocHost((void **)&b->st_h, sizeof(SpgDevState) * n) != cudaSuccess ||
-        cudaMallocHost((void **)&b->active_h, sizeof(int) * n) != cudaSuccess)
+        cudaMallocHost((void **)&b->active_h, sizeof(int) * n) != cudaSuccess ||
+        cudaMallocHost((void **)&b->work_h, sizeof(int) * (b->nseg + 1)) != cudaSuccess)
         return bail(bfail(PASC_ERR_ALLOC, "batch_create: pinned allocation failed"));
     memset(b->st_h, 0, sizeof(SpgDevState) * n);
     cudaMemset(b->xb[0], 0, sizeof(float) * b->nx);  // pads stay zero: kernels write 0 <= t < T only
@@ -179,6 +187,8 @@ int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const 
     cudaMemset(b->st_d, 0, sizeof(SpgDevState) * n);
     cudaMemset(b->ticket, 0, sizeof(unsigned int) * n);
     cudaMemset(b->theta64, 0, sizeof(double) * 8 * n);
+    cudaMemset(b->nwork_d, 0, sizeof(int));
+    b->in_work.assign(n, 0);
     cudaMemcpy(b->inst_d, b->inst_h.data(), sizeof(BatchInstDev) * n, cudaMemcpyHostToDevice);
     cudaMemcpy(b->seg_inst_d, seg_inst.data(), sizeof(int) * b->nseg, cudaMemcpyHostToDevice);
     b->grid = std::max(1, std::min(batch_blocks_per_sm(b->KB, false) * b->sms, b->nseg));
@@ -274,6 +284,28 @@ static int batch_permute(pasc_gb300_batch *b)
     return PASC_OK;
 }
 
+// Rebuilds the work list from take[i] (signal i takes part) when that set changed since the
+// last upload; the list holds all segments of every signal taking part, in signal order.
+template <class Pred>
+static int update_worklist(pasc_gb300_batch *b, Pred take)
+{
+    bool same = true;
+    for (int i = 0; i < b->n && same; i++) same = (b->in_work[i] != 0) == take(i);
+    if (same) return PASC_OK;
+    BCU(cudaStreamSynchronize(b->stream));  // the pinned list may still be feeding an upload
+    int cnt = 0;
+    for (int i = 0; i < b->n; i++) {
+        b->in_work[i] = take(i) ? 1 : 0;
+        if (!b->in_work[i]) continue;
+        const BatchInstDev &I = b->inst_h[i];
+        for (int s = 0; s < I.nseg; s++) b->work_h[1 + cnt++] = I.seg0 + s;
+    }
+    b->work_h[0] = cnt;
+    BCU(cudaMemcpyAsync(b->nwork_d, b->work_h, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    if (cnt) BCU(cudaMemcpyAsync(b->work_d, b->work_h + 1, sizeof(int) * cnt, cudaMemcpyHostToDevice, b->stream));
+    return PASC_OK;
+}
+
 static int ensure_batch_graph(pasc_gb300_batch *b)
 {
     if (b->chunk) return PASC_OK;
@@ -307,6 +339,7 @@ static int batch_spgqp(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o, doub
     if (o->m < 1 || o->m > MMAX_STATE) return bfail(PASC_ERR_ARG, "batch: m must be in [1, 64]");
     BCHK(ensure_batch_graph(b));
     cudaStream_t s = b->stream;
+    BCU(cudaStreamSynchronize(s));  // the pinned state mirror may still be feeding an upload
     int nact = 0;
     for (int i = 0; i < b->n; i++) {
         SpgDevState &h = b->st_h[i];
@@ -329,17 +362,32 @@ static int batch_spgqp(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o, doub
     }
     if (nact == 0) return PASC_OK;
     BatchArgs a = batch_args(b);
+    BCHK(update_worklist(b, [&](int i) { return b->active_h[i] != 0; }));
     BCU(cudaEventRecord(b->ev0, s));
     BCU(cudaMemcpyAsync(b->st_d, b->st_h, sizeof(SpgDevState) * b->n, cudaMemcpyHostToDevice, s));
     BCU(cudaMemsetAsync(b->ticket, 0, sizeof(unsigned int) * b->n, s));
     BCU(cudaMemsetAsync(b->next_job, 0, sizeof(unsigned int), s));
     BCU(launch_batch_sweep(b->KB, true, b->grid_init, a, s));
     b->launches++;
+    // the states are read after 2, 4, 8 and then every BATCH_CHUNK sweeps (solves that end
+    // within a few iterations do not pay for a whole chunk); after each read the work list
+    // drops the signals whose solve has ended
     long done = 0;
+    int step = 0;
+    const int sched[] = {2, 4, 8};
     while (done < o->maxit) {
-        BCU(cudaGraphLaunch(b->chunk, s));
-        done += BATCH_CHUNK;
-        b->launches += BATCH_CHUNK;
+        const int want = step < 3 ? sched[step] : BATCH_CHUNK;
+        step++;
+        if (want == BATCH_CHUNK) {
+            BCU(cudaGraphLaunch(b->chunk, s));
+        } else {
+            for (int q = 0; q < want; q++) {
+                BCU(cudaMemsetAsync(b->next_job, 0, sizeof(unsigned int), s));
+                BCU(launch_batch_sweep(b->KB, false, b->grid, a, s));
+            }
+        }
+        done += want;
+        b->launches += want;
         BCU(cudaMemcpyAsync(b->st_h, b->st_d, sizeof(SpgDevState) * b->n, cudaMemcpyDeviceToHost, s));
         BCU(cudaStreamSynchronize(s));
         bool running = false, err = false;
@@ -349,6 +397,7 @@ static int batch_spgqp(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o, doub
         }
         if (err) return bfail(PASC_ERR_TIMEOUT, "batch: a bounded wait for a bulk copy gave up");
         if (!running) break;
+        BCHK(update_worklist(b, [&](int i) { return b->st_h[i].status == PASC_SPG_RUNNING; }));
     }
     BCU(cudaEventRecord(b->ev1, s));
     BCU(cudaMemcpyAsync(b->st_h, b->st_d, sizeof(SpgDevState) * b->n, cudaMemcpyDeviceToHost, s));
@@ -419,6 +468,7 @@ int pasc_gb300_batch_ts_solve(pasc_gb300_batch *b, const pasc_gb300_ts_opts *ts,
             for (int i = 0; i < n; i++) b->st_h[i].cur = b->cur[i];
             BCU(cudaMemcpyAsync(b->st_d, b->st_h, sizeof(SpgDevState) * n, cudaMemcpyHostToDevice, b->stream));
             BCU(cudaMemcpyAsync(b->active_d, b->active_h, sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
+            BCHK(update_worklist(b, [&](int i) { return b->active_h[i] != 0; }));
             BCU(cudaMemsetAsync(b->ticket, 0, sizeof(unsigned int) * n, b->stream));
             BCU(cudaMemsetAsync(b->next_job, 0, sizeof(unsigned int), b->stream));
             BCU(launch_theta_batch(b->grid_theta, a, b->stream));

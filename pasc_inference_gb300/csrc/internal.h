@@ -77,6 +77,8 @@ struct BatchInstDev {
 struct BatchArgs {
     BatchInstDev *inst;
     const int *seg_inst;     // segment -> signal
+    const int *work;         // segments to visit in this launch (those of signals still taking part)
+    const int *nwork;        // length of work (device memory: rewritten between captured launches)
     int nseg, ninst;
     float *xb0, *xb1;        // packed gamma, ping-pong (each signal's half given by its state's cur)
     const float *data;       // packed data

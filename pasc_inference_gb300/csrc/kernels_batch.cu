@@ -6,8 +6,9 @@
 // tssolver.h:522-698; independent signals are separate runs).  Here all of them share a
 // persistent grid:
 //   - each signal is cut into segments of SEG_TILES bulk-copy tiles (sweep_tma.cuh); the
-//     segments of all signals form one work list, and blocks take segments in turn from an
-//     atomic counter, so long and short signals balance across the GPU;
+//     segments of the signals still running form one work list (rebuilt by the host whenever
+//     it reads the signals' states), and blocks take segments in turn from an atomic counter,
+//     so long and short signals balance across the GPU;
 //   - a segment is computed by one block with the tile pipeline of the single-signal kernel
 //     (K dispatched at run time) and leaves its four partial sums in its own slot, so the
 //     sums do not depend on which block took which segment (deterministic);
@@ -95,8 +96,12 @@ __device__ __forceinline__ bool batch_segment(TmaSmem<KB, BATCH_NT> &sm, const B
     return true;
 }
 
+// resident blocks per SM the register allocation is held to: the run-time K switch makes the
+// compiler allocate for the largest case, above what any single K needs
+constexpr int batch_min_blocks(int KB) { return KB <= 3 ? 5 : KB <= 5 ? 4 : KB <= 7 ? 3 : 2; }
+
 template <int KB, bool INIT>
-__global__ void __launch_bounds__(BATCH_NT) spg_batch_sweep_kernel(BatchArgs a)
+__global__ void __launch_bounds__(BATCH_NT, batch_min_blocks(KB)) spg_batch_sweep_kernel(BatchArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TmaSmem<KB, BATCH_NT> &sm = *reinterpret_cast<TmaSmem<KB, BATCH_NT> *>(smem_raw);
@@ -111,10 +116,11 @@ __global__ void __launch_bounds__(BATCH_NT) spg_batch_sweep_kernel(BatchArgs a)
         __syncthreads();
         if (threadIdx.x == 0) sm.job = (int)atomicAdd(a.next_job, 1u);
         __syncthreads();
-        const int seg = sm.job;
-        if (seg >= a.nseg) break;
+        const int job = sm.job;
+        if (job >= *a.nwork) break;
+        const int seg = a.work[job];
         const int q = a.seg_inst[seg];
-        if (a.st[q].status != PASC_SPG_RUNNING) continue;  // this signal's solve has ended
+        if (a.st[q].status != PASC_SPG_RUNNING) continue;  // this signal's solve ended in this chunk
         bool ok = true;
         switch (a.inst[q].K) {
 #define PASC_CASE(KK) \
@@ -193,8 +199,9 @@ __global__ void __launch_bounds__(BATCH_THETA_NT) theta_batch_kernel(BatchArgs a
         __syncthreads();
         if (threadIdx.x == 0) s_job = (int)atomicAdd(a.next_job, 1u);
         __syncthreads();
-        const int seg = s_job;
-        if (seg >= a.nseg) break;
+        const int job = s_job;
+        if (job >= *a.nwork) break;
+        const int seg = a.work[job];
         const int q = a.seg_inst[seg];
         if (!a.active[q]) continue;
         switch (a.inst[q].K) {
