@@ -220,6 +220,45 @@ int pasc_gb300_abserr_reconstructed(pasc_gb300_problem *p, const double *solutio
 int pasc_gb300_argmax_labels(pasc_gb300_problem *p, int *labels);
 
 /* ---------------------------------------------------------------------------------------
+ * derivatives through the converged gamma step (no counterpart in the reference, which only
+ * solves).  With the free set F_t = {k : gamma_tk > act_tol} held fixed, the solution of the
+ * QP moves inside S = {v : v_tk = 0 for k outside F_t, sum_k v_tk = 0}; the adjoint lambda in
+ * S solves P A P lambda = P dloss/dgamma (P the orthogonal projection onto S, A = coeff *
+ * A_hat) by conjugate gradients in FP64, and
+ *   dloss/d epssqr  = -(d coeff/d epssqr) lambda'(A_hat gamma)
+ *   dloss/d x_t     =  sum_k lambda_tk d b_tk/d x_t       (b_tk = bscale (x_t - theta_k)^2)
+ *   dloss/d theta_k =  sum_t lambda_tk d b_tk/d theta_k  (+ the loss's own theta term, below)
+ * theta is a given input here (the theta step is not differentiated).
+ * ------------------------------------------------------------------------------------- */
+typedef struct {
+    double act_tol;         /* gamma_tk > act_tol is free (1e-7) */
+    double cg_tol;          /* stop when ||r|| <= cg_tol * ||r_0|| (1e-10) */
+    int cg_maxit;           /* (20000) */
+} pasc_gb300_adjoint_opts;
+
+typedef struct {
+    int cg_it;              /* conjugate-gradient iterations */
+    int status;             /* 1 converged, 2 cg_maxit reached */
+    int kernel_launches;
+    long free_dims;         /* dimension of S: sum_t max(|F_t| - 1, 0) */
+    double cg_relres;       /* ||r|| / ||r_0|| at the end */
+    double time_s;          /* device time (CUDA events) */
+} pasc_gb300_adjoint_stats;
+
+void pasc_gb300_adjoint_default_opts(pasc_gb300_adjoint_opts *o);
+/* loss = 1/T sum_t (sum_k gamma_tk theta_k - clean_t)^2 of the current gamma and theta (clean: T
+ * host values); dloss/dgamma and the loss's own dloss/dtheta are kept on the device for the
+ * next pasc_gb300_adjoint call with dloss_dgamma == NULL. */
+int pasc_gb300_recon_mse(pasc_gb300_problem *p, const double *clean, double *loss);
+/* dloss_dgamma: N host values, or NULL for the gradient kept by pasc_gb300_recon_mse (then
+ * dloss_dtheta includes that loss's direct theta term).  Outputs are nullable host buffers:
+ * dloss_depssqr (1), dloss_ddata (T), dloss_dtheta (K).  K <= 8.  PASC_ERR_STATE if conjugate
+ * gradients break down (the right-hand side has a part in the null space of P A P). */
+int pasc_gb300_adjoint(pasc_gb300_problem *p, const double *dloss_dgamma, const pasc_gb300_adjoint_opts *o,
+                       double *dloss_depssqr, double *dloss_ddata, double *dloss_dtheta,
+                       pasc_gb300_adjoint_stats *st);
+
+/* ---------------------------------------------------------------------------------------
  * device-pointer kernels: the reference's GPU-side operations, usable on caller buffers
  * ------------------------------------------------------------------------------------- */
 

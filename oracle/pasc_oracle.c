@@ -570,3 +570,149 @@ void pasc_oracle_argmax_labels(const double *gamma, int *labels, long T, int K)
         labels[t] = best;
     }
 }
+
+/* ------------------------------------------------------------------------------------
+ * adjoint (no reference counterpart; see the header)
+ * ---------------------------------------------------------------------------------- */
+
+double pasc_oracle_recon_mse(const double *gamma, const double *theta, const double *clean, long T,
+                             int K, double *dgamma, double *dtheta)
+{
+    double loss = 0.0;
+    if (dtheta)
+        for (int k = 0; k < K; k++) dtheta[k] = 0.0;
+    for (long t = 0; t < T; t++) {
+        double rec = 0.0;
+        for (int k = 0; k < K; k++) rec += gamma[t * (long)K + k] * theta[k];
+        double e = rec - clean[t];
+        loss += e * e;
+        for (int k = 0; k < K; k++) {
+            if (dgamma) dgamma[t * (long)K + k] = 2.0 / (double)T * e * theta[k];
+            if (dtheta) dtheta[k] += 2.0 / (double)T * e * gamma[t * (long)K + k];
+        }
+    }
+    return loss / (double)T;
+}
+
+/* P at one timestep, in place */
+static void adj_proj(double *v, const unsigned char *fr, int K)
+{
+    int nf = 0;
+    double s = 0.0;
+    for (int k = 0; k < K; k++)
+        if (fr[k]) {
+            nf++;
+            s += v[k];
+        }
+    if (nf <= 1) {
+        for (int k = 0; k < K; k++) v[k] = 0.0;
+        return;
+    }
+    double mean = s / nf;
+    for (int k = 0; k < K; k++) v[k] = fr[k] ? v[k] - mean : 0.0;
+}
+
+/* y = P (coeff A_hat) v for v in S */
+static void adj_apply(const double *v, double *y, const unsigned char *fr, long T, int K, double coeff)
+{
+    for (long t = 0; t < T; t++) {
+        for (int k = 0; k < K; k++) {
+            long i = t * (long)K + k;
+            double a = 0.0;
+            if (t > 0) a += 2.0 * (v[i] - v[i - K]);
+            if (t < T - 1) a += 2.0 * (v[i] - v[i + K]);
+            y[i] = coeff * a;
+        }
+        adj_proj(y + t * (long)K, fr + t * (long)K, K);
+    }
+}
+
+int pasc_oracle_adjoint(const double *gamma, const double *data, const double *theta,
+                        const double *dloss_dgamma, long T, int K, double coeff, double dcoeff,
+                        double bscale, const pasc_oracle_adj_opts *o, double *lambda,
+                        double *dloss_depssqr, double *dloss_ddata, double *dloss_dtheta,
+                        pasc_oracle_adj_result *res)
+{
+    const long N = T * (long)K;
+    unsigned char *fr = (unsigned char *)malloc((size_t)N);
+    double *lam = (double *)calloc((size_t)N, sizeof(double));
+    double *r = (double *)malloc(sizeof(double) * (size_t)N);
+    double *p = (double *)malloc(sizeof(double) * (size_t)N);
+    double *q = (double *)malloc(sizeof(double) * (size_t)N);
+    if (!fr || !lam || !r || !p || !q) {
+        free(fr); free(lam); free(r); free(p); free(q);
+        return -1;
+    }
+    long free_dims = 0;
+    double rr = 0.0;
+    for (long t = 0; t < T; t++) {
+        int nf = 0;
+        for (int k = 0; k < K; k++) {
+            long i = t * (long)K + k;
+            fr[i] = gamma[i] > o->act_tol;
+            nf += fr[i];
+            r[i] = dloss_dgamma[i];
+        }
+        free_dims += nf > 1 ? nf - 1 : 0;
+        adj_proj(r + t * (long)K, fr + t * (long)K, K);
+        for (int k = 0; k < K; k++) rr += r[t * (long)K + k] * r[t * (long)K + k];
+    }
+    const double rr0 = rr;
+    int it = 0, status = rr0 > 0.0 ? 0 : 1;
+    for (long i = 0; i < N; i++) p[i] = r[i];
+    while (status == 0) {
+        if (it >= o->cg_maxit) {
+            status = 2;
+            break;
+        }
+        adj_apply(p, q, fr, T, K, coeff);
+        double pq = 0.0;
+        for (long i = 0; i < N; i++) pq += p[i] * q[i];
+        if (!(pq > 0.0) || !isfinite(pq)) {
+            status = 4;
+            break;
+        }
+        double alpha = rr / pq, rrn = 0.0;
+        for (long i = 0; i < N; i++) {
+            lam[i] += alpha * p[i];
+            r[i] -= alpha * q[i];
+            rrn += r[i] * r[i];
+        }
+        it++;
+        double beta = rrn / rr;
+        rr = rrn;
+        if (rr <= o->cg_tol * o->cg_tol * rr0) {
+            status = 1;
+            break;
+        }
+        for (long i = 0; i < N; i++) p[i] = r[i] + beta * p[i];
+    }
+    double deps = 0.0;
+    if (dloss_dtheta)
+        for (int k = 0; k < K; k++) dloss_dtheta[k] = 0.0;
+    for (long t = 0; t < T; t++) {
+        double dx = 0.0;
+        for (int k = 0; k < K; k++) {
+            long i = t * (long)K + k;
+            double ag = 0.0;
+            if (t > 0) ag += 2.0 * (gamma[i] - gamma[i - K]);
+            if (t < T - 1) ag += 2.0 * (gamma[i] - gamma[i + K]);
+            deps += lam[i] * ag;
+            double db = 2.0 * bscale * (data[t] - theta[k]);
+            dx += lam[i] * db;
+            if (dloss_dtheta) dloss_dtheta[k] -= lam[i] * db;
+        }
+        if (dloss_ddata) dloss_ddata[t] = dx;
+    }
+    if (dloss_depssqr) *dloss_depssqr = -dcoeff * deps;
+    if (lambda)
+        for (long i = 0; i < N; i++) lambda[i] = lam[i];
+    if (res) {
+        res->cg_it = it;
+        res->status = status;
+        res->free_dims = free_dims;
+        res->cg_relres = rr0 > 0.0 ? sqrt(rr / rr0) : 0.0;
+    }
+    free(fr); free(lam); free(r); free(p); free(q);
+    return status == 4 ? 1 : 0;
+}

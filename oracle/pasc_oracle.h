@@ -118,6 +118,42 @@ double pasc_oracle_abserr_reconstructed(const double *gamma, const double *theta
 /* Hard labels: true argmax per t, lowest k wins ties. */
 void pasc_oracle_argmax_labels(const double *gamma, int *labels, long T, int K);
 
+/* ------------------------------------------------------------------------------------
+ * Derivatives through the converged gamma step.  The reference has no such code: this is
+ * the FP64 statement of active-set implicit differentiation of the QP above, the checker of
+ * the GPU adjoint.  Free set F_t = {k : gamma_tk > act_tol}; S = {v : v_tk = 0 off F_t,
+ * sum_k v_tk = 0}; P = orthogonal projection onto S (per t: zero off F_t, subtract the mean
+ * over F_t).  lambda in S solves P A P lambda = P dl/dgamma (conjugate gradients from 0,
+ * stop at ||r|| <= cg_tol ||r_0||), A = coeff * A_hat, and
+ *   dl/d epssqr  = -dcoeff * lambda'(A_hat gamma)           (dcoeff = d coeff / d epssqr)
+ *   dl/d x_t     =  sum_k lambda_tk * 2 bscale (x_t - theta_k)
+ *   dl/d theta_k = -sum_t lambda_tk * 2 bscale (x_t - theta_k)
+ * ---------------------------------------------------------------------------------- */
+typedef struct {
+    double act_tol;
+    double cg_tol;
+    int    cg_maxit;
+} pasc_oracle_adj_opts;
+
+typedef struct {
+    int    cg_it;
+    int    status;         /* 1 converged, 2 maxit, 4 breakdown */
+    long   free_dims;
+    double cg_relres;
+} pasc_oracle_adj_result;
+
+/* loss = 1/T sum_t (sum_k gamma_tk theta_k - clean_t)^2; dgamma (N, nullable) = dl/dgamma,
+ * dtheta (K, nullable) = the loss's direct dl/dtheta. */
+double pasc_oracle_recon_mse(const double *gamma, const double *theta, const double *clean, long T,
+                             int K, double *dgamma, double *dtheta);
+
+/* lambda (N, nullable), dloss_ddata (T, nullable), dloss_dtheta (K, nullable). */
+int pasc_oracle_adjoint(const double *gamma, const double *data, const double *theta,
+                        const double *dloss_dgamma, long T, int K, double coeff, double dcoeff,
+                        double bscale, const pasc_oracle_adj_opts *o, double *lambda,
+                        double *dloss_depssqr, double *dloss_ddata, double *dloss_dtheta,
+                        pasc_oracle_adj_result *r);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,6 +66,14 @@ def build_ref() -> str | None:
     return REF_LIB_PATH if os.path.exists(REF_LIB_PATH) else None
 
 
+class AdjOpts(C.Structure):
+    _fields_ = [("act_tol", C.c_double), ("cg_tol", C.c_double), ("cg_maxit", C.c_int)]
+
+
+class AdjResult(C.Structure):
+    _fields_ = [("cg_it", C.c_int), ("status", C.c_int), ("free_dims", C.c_long), ("cg_relres", C.c_double)]
+
+
 _lib = None
 
 
@@ -95,6 +103,11 @@ def lib():
         L.pasc_oracle_abserr_reconstructed.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int]
         L.pasc_oracle_abserr_reconstructed.restype = C.c_double
         L.pasc_oracle_argmax_labels.argtypes = [_dp, _ip, C.c_long, C.c_int]
+        L.pasc_oracle_recon_mse.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_void_p, C.c_void_p]
+        L.pasc_oracle_recon_mse.restype = C.c_double
+        L.pasc_oracle_adjoint.argtypes = [_dp, _dp, _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_double,
+                                          C.c_double, C.POINTER(AdjOpts), C.c_void_p, C.POINTER(C.c_double),
+                                          C.c_void_p, C.c_void_p, C.POINTER(AdjResult)]
         _lib = L
     return _lib
 
@@ -200,6 +213,33 @@ def argmax_labels(gamma, T, K):
     lab = np.empty(T, dtype=np.int32)
     lib().pasc_oracle_argmax_labels(_f64(gamma), lab, T, K)
     return lab
+
+
+def recon_mse(gamma, theta, clean, T, K):
+    """Returns (loss, dloss/dgamma [N], direct dloss/dtheta [K])."""
+    dg = np.empty(T * K)
+    dth = np.empty(K)
+    loss = lib().pasc_oracle_recon_mse(_f64(gamma), _f64(theta), _f64(clean), T, K, dg.ctypes.data,
+                                       dth.ctypes.data)
+    return loss, dg, dth
+
+
+def adjoint(gamma, data, theta, dloss_dgamma, T, K, epssqr, scalef=1, act_tol=1e-7, cg_tol=1e-10,
+            cg_maxit=20000):
+    """Returns (dloss/d epssqr, dloss/d data [T], dloss/d theta [K] (through b only), lambda [N],
+    AdjResult)."""
+    o = AdjOpts(act_tol=act_tol, cg_tol=cg_tol, cg_maxit=cg_maxit)
+    r = AdjResult()
+    lam = np.empty(T * K)
+    dX = np.empty(T)
+    dth = np.empty(K)
+    deps = C.c_double()
+    coeff = A_coeff(epssqr, T, scalef)
+    dcoeff = (1.0 / T) if scalef else 1.0
+    lib().pasc_oracle_adjoint(_f64(gamma), _f64(data), _f64(theta), _f64(dloss_dgamma), T, K, coeff, dcoeff,
+                              b_coeff(T, scalef), C.byref(o), lam.ctypes.data, C.byref(deps), dX.ctypes.data,
+                              dth.ctypes.data, C.byref(r))
+    return deps.value, dX, dth, lam, r
 
 
 # --------------------------------------------------------------------------------------

@@ -170,6 +170,24 @@ class Problem:
         check(load().pasc_gb300_argmax_labels(self._h, out))
         return out
 
+    # derivatives through the converged gamma step
+    def recon_mse(self, clean) -> float:
+        v = C.c_double()
+        check(load().pasc_gb300_recon_mse(self._h, np.ascontiguousarray(clean, dtype=np.float64), C.byref(v)))
+        return v.value
+
+    def adjoint(self, dloss_dgamma=None, opts: capi.AdjointOpts | None = None):
+        """Returns (dloss/d epssqr, dloss/d data [T], dloss/d theta [K], AdjointStats)."""
+        deps = C.c_double()
+        ddata = np.empty(self.T)
+        dtheta = np.empty(self.K)
+        st = capi.AdjointStats()
+        g = None if dloss_dgamma is None else np.ascontiguousarray(dloss_dgamma, dtype=np.float64)
+        check(load().pasc_gb300_adjoint(self._h, g.ctypes.data if g is not None else None,
+                                        C.byref(opts or capi.adjoint_opts()), C.byref(deps),
+                                        ddata.ctypes.data, dtheta.ctypes.data, C.byref(st)))
+        return deps.value, ddata, dtheta, st
+
 
 class Batch:
     """n independent signals (own T, K, epssqr) solved together on one GPU (a

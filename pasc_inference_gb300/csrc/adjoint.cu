@@ -1,0 +1,549 @@
+// adjoint.cu -- derivatives of a loss through the converged gamma-step QP (no counterpart in
+// the reference, which only solves).
+//
+// The QP  min 1/2 x'Ax - b'x  over the product of K-simplices has A = coeff * (A_hat (x) I_K)
+// (coeff = epssqr/T) and b_tk = bscale * (x_t - theta_k)^2 (bscale = -1/T), as formed by
+// GraphH1FEMModel (src/petscvector/model/graphh1fem.cpp:146-151, 237-289).  At a solution
+// gamma the free set of timestep t is F_t = {k : gamma_tk > act_tol}; S = {v : v_tk = 0 for k
+// outside F_t, sum_k v_tk = 0} is the space gamma can move in without changing the active
+// set, and P (per timestep: zero outside F_t, subtract the mean over F_t) is the orthogonal
+// projection onto it.  The optimality conditions on S, P(A gamma - b) = 0, differentiated at
+// a fixed active set give  P A P gamma' = -P(A' gamma - b'),  so for a loss l(gamma)
+//     l' = -lambda'(A' gamma - b'),   lambda in S solving  P A P lambda = P dl/dgamma.
+// lambda is found by conjugate gradients on S in FP64: two kernels per CG iteration (apply
+// P A P to the search direction and reduce p'q; update lambda and r and reduce r'r), the
+// scalars kept on the device (last block of each launch), launched in CUDA-graph chunks with
+// the host polling a status word in between.  The gradients then follow in one pass:
+//     dl/d epssqr  = -(d coeff/d epssqr) * sum_tk lambda_tk (A_hat gamma)_tk
+//     dl/d x_t     =  sum_k lambda_tk * 2 bscale (x_t - theta_k)
+//     dl/d theta_k = -sum_t lambda_tk * 2 bscale (x_t - theta_k)      (through b only)
+// All reductions sum fixed per-block partials in block order (deterministic).
+#include <math.h>
+#include <string.h>
+#include <algorithm>
+#include <string>
+
+#include "common.cuh"
+#include "internal.h"
+#include "problem.h"
+
+namespace pasc {
+
+constexpr int ADJ_NT = 256;
+constexpr int ADJ_CHUNK = 16;  // CG iterations per captured graph
+
+enum { ADJ_RUNNING = 0, ADJ_CONVERGED = 1, ADJ_MAXIT = 2, ADJ_BREAKDOWN = 4 };
+
+struct AdjDevState {
+    double rr, rr0, pq, alpha, beta, tol;
+    double free_dims;
+    int it, maxit, status, pcur;
+    unsigned int counter;
+};
+
+struct AdjointWork {
+    int K = 0, grid = 0;
+    long T = 0;
+    double *gam = nullptr;           // N: FP64 gamma (the mixed path converts into it)
+    double *gl = nullptr;            // N: dl/dgamma
+    double *lam = nullptr, *r = nullptr, *pb[2] = {nullptr, nullptr}, *q = nullptr;  // N each
+    unsigned int *mask = nullptr;    // T: free clusters of each timestep (bit k)
+    double *clean = nullptr, *dX = nullptr;  // T each
+    double *partials = nullptr;      // grid * 16
+    double *out = nullptr;           // 16: results of the one-pass kernels
+    double *out_h = nullptr;         // pinned mirror
+    AdjDevState *st = nullptr, *st_h = nullptr;
+    unsigned int *ticket = nullptr;  // last-block ticket of the one-pass kernels
+    cudaGraphExec_t chunk = nullptr;
+    double gtheta_direct[8] = {0};   // direct d loss/d theta of the last recon_mse
+    bool have_gl = false;
+};
+
+void adjoint_free(AdjointWork *w)
+{
+    if (!w) return;
+    if (w->chunk) cudaGraphExecDestroy(w->chunk);
+    void *dev[] = {w->gam, w->gl, w->lam, w->r, w->pb[0], w->pb[1], w->q, w->mask, w->clean, w->dX,
+                   w->partials, w->out, w->st, w->ticket};
+    for (void *p : dev)
+        if (p) cudaFree(p);
+    if (w->out_h) cudaFreeHost(w->out_h);
+    if (w->st_h) cudaFreeHost(w->st_h);
+    delete w;
+}
+
+// ---------------------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------------------
+
+// orthogonal projection onto S at one timestep (free clusters: bits of m)
+template <int K>
+__device__ __forceinline__ void proj_free(double (&v)[K], unsigned int m)
+{
+    const int nf = __popc(m);
+    if (nf <= 1) {
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = 0.0;
+        return;
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < K; k++) s += ((m >> k) & 1u) ? v[k] : 0.0;
+    const double mean = s / nf;
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = ((m >> k) & 1u) ? v[k] - mean : 0.0;
+}
+
+// Writes the block's NV sums to partials[blockIdx.x * 16 + j]; the last block to finish
+// (ticket) sums them in block order and returns true with the totals in w (thread 0).
+template <int NV>
+__device__ __forceinline__ bool grid_sum(double (&v)[NV], double *partials, unsigned int *ticket,
+                                         double *scratch, double (&w)[NV])
+{
+    block_sum<NV>(v, scratch);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int j = 0; j < NV; j++) partials[blockIdx.x * 16 + j] = v[j];
+    }
+    if (!last_block_done(ticket)) return false;
+#pragma unroll
+    for (int j = 0; j < NV; j++) w[j] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+#pragma unroll
+        for (int j = 0; j < NV; j++) w[j] += __ldcg(partials + b * 16 + j);
+    }
+    block_sum<NV>(w, scratch);
+    if (threadIdx.x == 0) *ticket = 0;
+    return true;
+}
+
+// ---------------------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------------------
+
+// l = 1/T sum_t (sum_k gamma_tk theta_k - c_t)^2, dl/dgamma_tk = 2/T e_t theta_k and the
+// direct dl/dtheta_k = 2/T sum_t e_t gamma_tk (e = reconstruction - clean).
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) recon_mse_kernel(const double *gam, const double *theta,
+                                                           const double *clean, long T, double *gl,
+                                                           double *partials, unsigned int *ticket, double *out)
+{
+    __shared__ double scratch[(K + 1) * (ADJ_NT / 32)];
+    const double invT = 1.0 / (double)T;
+    double th[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) th[k] = theta[k];
+    double v[K + 1];
+#pragma unroll
+    for (int j = 0; j <= K; j++) v[j] = 0.0;
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        double g[K], rec = 0.0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            g[k] = gam[t * K + k];
+            rec += g[k] * th[k];
+        }
+        const double e = rec - clean[t];
+        v[0] += e * e;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            gl[t * K + k] = 2.0 * invT * e * th[k];
+            v[1 + k] += 2.0 * invT * e * g[k];
+        }
+    }
+    double w[K + 1];
+    if (!grid_sum<K + 1>(v, partials, ticket, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        out[0] = w[0] * invT;
+#pragma unroll
+        for (int k = 0; k < K; k++) out[1 + k] = w[1 + k];
+    }
+}
+
+// free sets, r = P dl/dgamma, lambda = 0, both search-direction buffers 0, r'r and dim S.
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_setup_kernel(const double *gam, const double *gl, long T,
+                                                           double act_tol, unsigned int *mask, double *lam,
+                                                           double *r, double *p0, double *p1,
+                                                           double *partials, AdjDevState *st)
+{
+    __shared__ double scratch[2 * (ADJ_NT / 32)];
+    double v2[2] = {0.0, 0.0};
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        unsigned int m = 0u;
+        double v[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            m |= (gam[t * K + k] > act_tol ? 1u : 0u) << k;
+            v[k] = gl[t * K + k];
+        }
+        mask[t] = m;
+        proj_free<K>(v, m);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            r[t * K + k] = v[k];
+            lam[t * K + k] = 0.0;
+            p0[t * K + k] = 0.0;
+            p1[t * K + k] = 0.0;
+            v2[0] += v[k] * v[k];
+        }
+        const int nf = __popc(m);
+        v2[1] += nf > 1 ? (double)(nf - 1) : 0.0;
+    }
+    double w[2];
+    if (!grid_sum<2>(v2, partials, &st->counter, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        st->rr = st->rr0 = w[0];
+        st->free_dims = w[1];
+        st->it = 0;
+        st->beta = 0.0;
+        st->pcur = 0;
+        st->status = (w[0] > 0.0) ? ADJ_RUNNING : ADJ_CONVERGED;
+        if (!isfinite(w[0])) st->status = ADJ_BREAKDOWN;
+    }
+}
+
+// p_new = r + beta p_old (at t and its neighbours), q = P A p_new, p'q; alpha = r'r / p'q.
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_apply_kernel(const unsigned int *mask, const double *r,
+                                                           double *pb0, double *pb1, double *q, long T,
+                                                           double coeff, double *partials, AdjDevState *st)
+{
+    __shared__ double scratch[1 * (ADJ_NT / 32)];
+    if (st->status != ADJ_RUNNING) return;  // uniform
+    const int pc = st->pcur;
+    const double beta = st->beta;
+    const double *pold = pc ? pb1 : pb0;
+    double *pnew = pc ? pb0 : pb1;
+    double v[1] = {0.0};
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        double pc_[K], y[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            pc_[k] = r[t * K + k] + beta * pold[t * K + k];
+            y[k] = 0.0;
+        }
+        if (t > 0) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const double pl = r[(t - 1) * K + k] + beta * pold[(t - 1) * K + k];
+                y[k] += 2.0 * (pc_[k] - pl);
+            }
+        }
+        if (t < T - 1) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const double pr = r[(t + 1) * K + k] + beta * pold[(t + 1) * K + k];
+                y[k] += 2.0 * (pc_[k] - pr);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) y[k] *= coeff;
+        proj_free<K>(y, mask[t]);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            pnew[t * K + k] = pc_[k];
+            q[t * K + k] = y[k];
+            v[0] += pc_[k] * y[k];
+        }
+    }
+    double w[1];
+    if (!grid_sum<1>(v, partials, &st->counter, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        st->pq = w[0];
+        if (w[0] > 0.0 && isfinite(w[0])) {
+            st->alpha = st->rr / w[0];
+        } else {
+            st->alpha = 0.0;
+            st->status = ADJ_BREAKDOWN;  // P A P is only semi-definite: r left its range
+        }
+    }
+}
+
+// lambda += alpha p, r -= alpha q, r'r; beta, convergence.
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_update_kernel(double *lam, double *r, const double *pb0,
+                                                            const double *pb1, const double *q, long T,
+                                                            double *partials, AdjDevState *st)
+{
+    __shared__ double scratch[1 * (ADJ_NT / 32)];
+    if (st->status != ADJ_RUNNING) return;
+    const double alpha = st->alpha;
+    const double *p = st->pcur ? pb0 : pb1;  // written by the apply kernel
+    double v[1] = {0.0};
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const long i = t * K + k;
+            lam[i] += alpha * p[i];
+            const double rn = r[i] - alpha * q[i];
+            r[i] = rn;
+            v[0] += rn * rn;
+        }
+    }
+    double w[1];
+    if (!grid_sum<1>(v, partials, &st->counter, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        const double rr = w[0];
+        st->beta = rr / st->rr;
+        st->rr = rr;
+        st->it += 1;
+        st->pcur ^= 1;
+        if (!isfinite(rr)) st->status = ADJ_BREAKDOWN;
+        else if (rr <= st->tol * st->tol * st->rr0) st->status = ADJ_CONVERGED;
+        else if (st->it >= st->maxit) st->status = ADJ_MAXIT;
+    }
+}
+
+// gradients from lambda (see the head of the file).  dX may be null.
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_output_kernel(const double *lam, const double *gam,
+                                                            const double *data, const double *theta, long T,
+                                                            double dcoeff, double bscale, double *dX,
+                                                            double *partials, unsigned int *ticket, double *out)
+{
+    __shared__ double scratch[(K + 1) * (ADJ_NT / 32)];
+    double th[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) th[k] = theta[k];
+    double v[K + 1];
+#pragma unroll
+    for (int j = 0; j <= K; j++) v[j] = 0.0;
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        const double x = data[t];
+        double dx = 0.0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const double lk = lam[t * K + k];
+            const double gc = gam[t * K + k];
+            double ag = 0.0;
+            if (t > 0) ag += 2.0 * (gc - gam[(t - 1) * K + k]);
+            if (t < T - 1) ag += 2.0 * (gc - gam[(t + 1) * K + k]);
+            v[0] += lk * ag;
+            const double db = 2.0 * bscale * (x - th[k]);  // d b_tk / d x_t = -d b_tk / d theta_k
+            dx += lk * db;
+            v[1 + k] -= lk * db;
+        }
+        if (dX) dX[t] = dx;
+    }
+    double w[K + 1];
+    if (!grid_sum<K + 1>(v, partials, ticket, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        out[0] = -dcoeff * w[0];
+#pragma unroll
+        for (int k = 0; k < K; k++) out[1 + k] = w[1 + k];
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------------
+
+static int afail(int code, const std::string &msg)
+{
+    record_error(msg.c_str());
+    return code;
+}
+
+#define ACU(call)                                                                                  \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return afail(PASC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+#define ACHK(call)                     \
+    do {                               \
+        int r_ = (call);               \
+        if (r_ != PASC_OK) return r_;  \
+    } while (0)
+
+#define PASC_ADJ_DISPATCH(K, ...)                                             \
+    switch (K) {                                                              \
+        case 1: { constexpr int KK = 1; __VA_ARGS__; } break;                 \
+        case 2: { constexpr int KK = 2; __VA_ARGS__; } break;                 \
+        case 3: { constexpr int KK = 3; __VA_ARGS__; } break;                 \
+        case 4: { constexpr int KK = 4; __VA_ARGS__; } break;                 \
+        case 5: { constexpr int KK = 5; __VA_ARGS__; } break;                 \
+        case 6: { constexpr int KK = 6; __VA_ARGS__; } break;                 \
+        case 7: { constexpr int KK = 7; __VA_ARGS__; } break;                 \
+        case 8: { constexpr int KK = 8; __VA_ARGS__; } break;                 \
+        default: break;                                                       \
+    }
+
+static int ensure_work(pasc_gb300_problem *p)
+{
+    if (p->adj) return PASC_OK;
+    if (p->K > 8) return afail(PASC_ERR_NOTSUPP, "adjoint: K > 8 is not supported");
+    AdjointWork *w = new AdjointWork();
+    w->K = p->K;
+    w->T = p->T;
+    const long N = p->N, T = p->T;
+    w->grid = (int)std::max(1L, std::min((T + ADJ_NT - 1) / ADJ_NT, (long)p->sms * 4));
+    auto dal = [&](void **ptr, size_t bytes) { return cudaMalloc(ptr, bytes > 0 ? bytes : 1) == cudaSuccess; };
+    bool ok = dal((void **)&w->gl, sizeof(double) * N) && dal((void **)&w->lam, sizeof(double) * N) &&
+              dal((void **)&w->r, sizeof(double) * N) && dal((void **)&w->pb[0], sizeof(double) * N) &&
+              dal((void **)&w->pb[1], sizeof(double) * N) && dal((void **)&w->q, sizeof(double) * N) &&
+              dal((void **)&w->mask, sizeof(unsigned int) * T) && dal((void **)&w->clean, sizeof(double) * T) &&
+              dal((void **)&w->dX, sizeof(double) * T) && dal((void **)&w->partials, sizeof(double) * 16 * w->grid) &&
+              dal((void **)&w->out, sizeof(double) * 16) && dal((void **)&w->st, sizeof(AdjDevState)) &&
+              dal((void **)&w->ticket, sizeof(unsigned int));
+    if (ok && p->precision == PASC_PREC_MIXED) ok = dal((void **)&w->gam, sizeof(double) * N);
+    if (ok) ok = cudaMallocHost((void **)&w->out_h, sizeof(double) * 16) == cudaSuccess &&
+                 cudaMallocHost((void **)&w->st_h, sizeof(AdjDevState)) == cudaSuccess;
+    if (!ok) {
+        adjoint_free(w);
+        return afail(PASC_ERR_ALLOC, "adjoint: device allocation failed");
+    }
+    cudaMemsetAsync(w->ticket, 0, sizeof(unsigned int), p->stream);
+    cudaMemsetAsync(w->st, 0, sizeof(AdjDevState), p->stream);
+    p->adj = w;
+    return PASC_OK;
+}
+
+// FP64 gamma of the problem (converted from the FP32 state on the mixed path)
+static int adj_gamma(pasc_gb300_problem *p, const double **g)
+{
+    if (p->precision == PASC_PREC_FP64) {
+        *g = p->x;
+        return PASC_OK;
+    }
+    ACU(launch_f32_to_f64(p->xb[p->cur], p->adj->gam, p->N, p->stream));
+    *g = p->adj->gam;
+    return PASC_OK;
+}
+
+static int ensure_adj_graph(pasc_gb300_problem *p)
+{
+    AdjointWork *w = p->adj;
+    if (w->chunk) return PASC_OK;
+    ACU(cudaStreamSynchronize(p->stream));
+    cudaGraph_t g;
+    ACU(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    const double coeff = p->coeffA;
+    for (int i = 0; i < ADJ_CHUNK; i++) {
+        PASC_ADJ_DISPATCH(p->K, {
+            adj_apply_kernel<KK><<<w->grid, ADJ_NT, 0, p->stream>>>(w->mask, w->r, w->pb[0], w->pb[1], w->q,
+                                                                    p->T, coeff, w->partials, w->st);
+            adj_update_kernel<KK><<<w->grid, ADJ_NT, 0, p->stream>>>(w->lam, w->r, w->pb[0], w->pb[1], w->q,
+                                                                     p->T, w->partials, w->st);
+        });
+    }
+    cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+    if (e != cudaSuccess) return afail(PASC_ERR_CUDA, std::string("adjoint capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&w->chunk, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        w->chunk = nullptr;
+        return afail(PASC_ERR_CUDA, std::string("adjoint graph: ") + cudaGetErrorString(e));
+    }
+    return PASC_OK;
+}
+
+}  // namespace pasc
+
+using namespace pasc;
+
+extern "C" {
+
+void pasc_gb300_adjoint_default_opts(pasc_gb300_adjoint_opts *o)
+{
+    if (!o) return;
+    o->act_tol = 1e-7;
+    o->cg_tol = 1e-10;
+    o->cg_maxit = 20000;
+}
+
+int pasc_gb300_recon_mse(pasc_gb300_problem *p, const double *clean, double *loss)
+{
+    if (!p || !clean || !loss) return afail(PASC_ERR_ARG, "recon_mse: NULL argument");
+    ACU(cudaSetDevice(p->device));
+    ACHK(ensure_work(p));
+    AdjointWork *w = p->adj;
+    const double *g = nullptr;
+    ACHK(adj_gamma(p, &g));
+    ACU(cudaMemcpyAsync(w->clean, clean, sizeof(double) * p->T, cudaMemcpyHostToDevice, p->stream));
+    PASC_ADJ_DISPATCH(p->K, (recon_mse_kernel<KK><<<w->grid, ADJ_NT, 0, p->stream>>>(
+                                g, p->theta64, w->clean, p->T, w->gl, w->partials, w->ticket, w->out)));
+    ACU(cudaGetLastError());
+    ACU(cudaMemcpyAsync(w->out_h, w->out, sizeof(double) * (1 + p->K), cudaMemcpyDeviceToHost, p->stream));
+    ACU(cudaStreamSynchronize(p->stream));
+    *loss = w->out_h[0];
+    for (int k = 0; k < p->K; k++) w->gtheta_direct[k] = w->out_h[1 + k];
+    w->have_gl = true;
+    return PASC_OK;
+}
+
+int pasc_gb300_adjoint(pasc_gb300_problem *p, const double *dloss_dgamma, const pasc_gb300_adjoint_opts *o,
+                       double *dloss_depssqr, double *dloss_ddata, double *dloss_dtheta,
+                       pasc_gb300_adjoint_stats *stats)
+{
+    if (!p) return afail(PASC_ERR_ARG, "adjoint: NULL problem");
+    pasc_gb300_adjoint_opts od;
+    pasc_gb300_adjoint_default_opts(&od);
+    if (!o) o = &od;
+    if (o->cg_maxit < 0 || !(o->cg_tol >= 0.0)) return afail(PASC_ERR_ARG, "adjoint: bad options");
+    ACU(cudaSetDevice(p->device));
+    ACHK(ensure_work(p));
+    AdjointWork *w = p->adj;
+    cudaStream_t s = p->stream;
+    const bool stored = dloss_dgamma == nullptr;
+    if (stored && !w->have_gl)
+        return afail(PASC_ERR_STATE, "adjoint: no dloss/dgamma given and none stored by recon_mse");
+    if (!stored) {
+        ACU(cudaMemcpyAsync(w->gl, dloss_dgamma, sizeof(double) * p->N, cudaMemcpyHostToDevice, s));
+        w->have_gl = false;  // the stored MSE gradient is overwritten
+    }
+    const double *g = nullptr;
+    ACHK(adj_gamma(p, &g));
+    ACHK(ensure_adj_graph(p));
+    ACU(cudaEventRecord(p->ev0, s));
+
+    AdjDevState *h = w->st_h;
+    memset(h, 0, sizeof *h);
+    h->tol = o->cg_tol;
+    h->maxit = o->cg_maxit;
+    ACU(cudaMemcpyAsync(w->st, h, sizeof *h, cudaMemcpyHostToDevice, s));
+    PASC_ADJ_DISPATCH(p->K, (adj_setup_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(
+                                g, w->gl, p->T, o->act_tol, w->mask, w->lam, w->r, w->pb[0], w->pb[1],
+                                w->partials, w->st)));
+    ACU(cudaGetLastError());
+    int launches = 1;
+    ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
+    ACU(cudaStreamSynchronize(s));
+    if (h->status == ADJ_RUNNING && o->cg_maxit == 0) h->status = ADJ_MAXIT;
+    while (h->status == ADJ_RUNNING) {
+        ACU(cudaGraphLaunch(w->chunk, s));
+        launches += 2 * ADJ_CHUNK;
+        ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
+        ACU(cudaStreamSynchronize(s));
+    }
+    const double dcoeff = p->scalef ? 1.0 / (double)p->T : 1.0;  // d coeff / d epssqr
+    PASC_ADJ_DISPATCH(p->K, (adj_output_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(
+                                w->lam, g, p->data64, p->theta64, p->T, dcoeff, p->coeffB, w->dX, w->partials,
+                                w->ticket, w->out)));
+    ACU(cudaGetLastError());
+    launches++;
+    ACU(cudaMemcpyAsync(w->out_h, w->out, sizeof(double) * (1 + p->K), cudaMemcpyDeviceToHost, s));
+    if (dloss_ddata) ACU(cudaMemcpyAsync(dloss_ddata, w->dX, sizeof(double) * p->T, cudaMemcpyDeviceToHost, s));
+    ACU(cudaEventRecord(p->ev1, s));
+    ACU(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+    if (dloss_depssqr) *dloss_depssqr = w->out_h[0];
+    if (dloss_dtheta) {
+        for (int k = 0; k < p->K; k++) dloss_dtheta[k] = w->out_h[1 + k] + (stored ? w->gtheta_direct[k] : 0.0);
+    }
+    if (stats) {
+        stats->cg_it = h->it;
+        stats->status = h->status;
+        stats->kernel_launches = launches;
+        stats->free_dims = (long)h->free_dims;
+        stats->cg_relres = h->rr0 > 0.0 ? sqrt(h->rr / h->rr0) : 0.0;
+        stats->time_s = ms * 1e-3;
+    }
+    if (h->status == ADJ_BREAKDOWN)
+        return afail(PASC_ERR_STATE, "adjoint: conjugate gradients broke down (non-finite values, or the "
+                                     "right-hand side has a component in the null space of P A P)");
+    return PASC_OK;
+}
+
+}  // extern "C"

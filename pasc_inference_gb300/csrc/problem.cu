@@ -11,6 +11,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "problem.h"
 
 using namespace pasc;
 
@@ -52,66 +53,11 @@ static int fail(int code, const char *fmt, ...)
 // problem
 // ---------------------------------------------------------------------------------------
 
-// Host-side record of the current SPG solve (both paths; the fp64 path keeps its whole
-// scalar state here, the mixed path mirrors the device state after every poll).
-struct SpgRun {
-    pasc_gb300_spgqp_opts o{};
-    bool started = false;
-    int it = 0, hessmult = 0, status = PASC_SPG_RUNNING, launches = 0;
-    double fx = 0.0, fx_old = DBL_MAX, dd = 0.0, dAd = 0.0, normb = 0.0, alpha = 0.0;
-    double fs[MMAX_STATE] = {0};
-    int fs_last = 0;
-    double time_s = 0.0;
-    float last_iterate_ms = 0.f;
-    int last_iterate_launches = 0;
-};
-
-struct pasc_gb300_problem {
-    long T = 0;
-    int K = 0, xdim = 1, precision = 0, device = 0;
-    double epssqr = 0.0;
-    int scalef = 1;
-    double coeffA = 0.0, coeffB = 0.0;
-    long N = 0;
-    int sms = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-
-    // shared
-    double *data64 = nullptr;     // T (fp64 path; mixed path uses it as upload staging)
-    double *theta64 = nullptr;    // K*xdim
-    double *stage64 = nullptr;    // N (mixed: conversions; fp64: permutation temp)
-    double *red = nullptr;        // reduction scratch (dot_partials_size doubles)
-    double *red_out = nullptr;    // 8 doubles
-    double *red_out_h = nullptr;  // pinned mirror
-    int *labels_d = nullptr;      // T
-
-    // fp64 path
-    double *x = nullptr, *g = nullptr, *d = nullptr, *Ad = nullptr, *b = nullptr;
-
-    // mixed path
-    float *data32 = nullptr, *theta32 = nullptr;  // data32 points past the front pad
-    float *xb[2] = {nullptr, nullptr};            // past the front pad of xb_raw
-    float *xb_raw[2] = {nullptr, nullptr}, *data32_raw = nullptr;
-    SpgDevState *st = nullptr, *st_h = nullptr;
-    double *partials = nullptr;
-    int cur = 0;
-    // sweep kernels: 0 = one timestep per thread, 1 = bulk-copy tiles, 4 timesteps per thread
-    int grid_sweep[2] = {0, 0}, grid_sweep_init[2] = {0, 0}, grid_theta = 0;
-    int variant = -1;             // -1: chosen by timing at the first solve
-    cudaGraphExec_t chunk_graph = nullptr;
-    int chunk_graph_len = 0, chunk_graph_variant = -1;
-
-    SpgRun run;
-    double fx_last = 0.0;
-    bool have_fx = false;
-    bool have_data = false;
-};
-
 static void free_all(pasc_gb300_problem *p)
 {
     if (!p) return;
     cudaSetDevice(p->device);
+    if (p->adj) adjoint_free(p->adj);
     if (p->chunk_graph) cudaGraphExecDestroy(p->chunk_graph);
     void *dev[] = {p->data64, p->theta64, p->stage64, p->red, p->red_out, p->labels_d, p->x, p->g,
                    p->d, p->Ad, p->b, p->data32_raw, p->theta32, p->xb_raw[0], p->xb_raw[1], p->st,
