@@ -28,6 +28,11 @@ Besides the headline line it measures, on rank 0:
              iteration for all running signals) and, for comparison, one signal at a time with
              the plain FP64 GPU path and with the single-signal mixed path; plus the batch
              sweep's HBM throughput with all 256 signals running.
+  adjoint    derivatives through the converged gamma step at T = 1e6, K = 3 (the benchmark
+             signal generator, clean copy kept): dloss/d epssqr of the reconstruction MSE from
+             the adjoint, checked against central differences (1e-4 relative) through FP64 GPU
+             solves and against the FP64 oracle's gradient (timed: the CPU baseline), then 20
+             gradient steps on log epssqr.
 """
 from __future__ import annotations
 
@@ -62,6 +67,7 @@ def parse():
     ap.add_argument("--no-tts", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--variant", type=int, default=-1, choices=[-1, 0, 1],
                     help="sweep kernel: -1 chosen by timing (default), 0 one timestep per thread, "
                          "1 bulk-copy tiles (pin it when profiling: a profiler distorts the timing)")
@@ -304,6 +310,8 @@ def main():
         result["time_to_1e-6_rel_obj"] = measure_tts(sig, theta, args.eps2, dev)
     if info.rank == 0 and not args.no_batched:
         result["batched"] = measure_batched(dev, peak)
+    if info.rank == 0 and not args.no_adjoint:
+        result["adjoint"] = measure_adjoint(dev, peak)
     if info.rank == 0 and not args.no_cpu:
         rate, dt = oracle_iter_rate(sig, theta, args.eps2, T, 5, 0)
         result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
@@ -377,6 +385,86 @@ def measure_tts(sig, theta, eps2, dev):
                      "status": capi.STATUS_NAMES.get(st.status, st.status)}
     a, b = res["fp64_plain"]["seconds"], res["mixed_fused"]["seconds"]
     res["speedup_vs_fp64_plain"] = (a / b) if (a and b) else None
+    return res
+
+
+def measure_adjoint(dev, peak, eps0=300.0):
+    from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Problem, capi, datagen, learn
+    sys.path.insert(0, ROOT)
+    from oracle import pasc_oracle as orc
+    sig = datagen.signal1d_cfg1(T=1_000_000)
+    T, K = sig.T, sig.K
+    theta = np.array([0.0, 1.0, 2.0])
+    spg_mixed = capi.spgqp_opts(m=10, eps=1e-12, maxit=20000)
+    spg64 = capi.spgqp_opts(m=10, eps=1e-26, maxit=40000, stop_difff=0, stop_normgp=1)
+
+    def loaded(prec, eps2, gamma=None):
+        p = Problem(T, K, eps2, precision=prec, device=dev)
+        p.set_data(sig.data)
+        p.set_theta(theta)
+        if gamma is None:
+            p.set_gamma(sig.gamma0)
+            p.permute_gamma()
+        else:
+            p.set_gamma(gamma)
+        p.update_b()
+        return p
+
+    res = {"workload": "signal1d T=1e6 K=3 levels {0,1,2} sigma=0.5 (clean copy kept), theta fixed at the "
+                       "levels, loss = MSE(sum_k gamma_k theta_k, clean)", "T": T, "K": K, "epssqr0": eps0}
+    # gradient on the mixed path (timed) and its CG throughput
+    with loaded(PASC_PREC_MIXED, eps0) as p:
+        t0 = time.perf_counter()
+        st = p.spgqp_solve(spg_mixed)
+        t1 = time.perf_counter()
+        loss = p.recon_mse(sig.clean)
+        deps, dX, dth, a = p.adjoint()
+        t2 = time.perf_counter()
+    N = T * K
+    B_cg = 80.0 * N + 4.0 * T  # per CG iteration: apply (r, p read; p, q written; mask) + update
+    cg_s = a.time_s / max(a.cg_it, 1)
+    res.update({"loss": loss, "dloss_depssqr": deps, "solve_s": t1 - t0, "spg_it": st.it,
+                "adjoint_s": t2 - t1, "adjoint_device_s": a.time_s, "cg_it": a.cg_it,
+                "free_dims": a.free_dims,
+                "cg_iteration": {"us": cg_s * 1e6, "bytes": B_cg, "achieved": B_cg / cg_s / 1e9, "unit": "GB/s",
+                                 "peak": peak, "frac": B_cg / cg_s / 1e9 / peak}})
+    # FP64 GPU: gradient and central differences
+    with loaded(PASC_PREC_FP64, eps0) as p:
+        p.spgqp_solve(spg64)
+        x0 = p.get_gamma()
+        p.recon_mse(sig.clean)
+        deps64, _, _, _ = p.adjoint()
+        h = 1e-4
+        lo = []
+        for e in (eps0 * (1 + h), eps0 * (1 - h)):
+            p.set_epssqr(e)
+            p.set_gamma(x0)
+            p.update_b()
+            p.spgqp_solve(spg64)
+            lo.append(p.recon_mse(sig.clean))
+    fd = (lo[0] - lo[1]) / (2 * h * eps0)
+    # FP64 oracle on the host: solve + adjoint (the CPU baseline of the gradient)
+    t0 = time.perf_counter()
+    b = orc.residual_b(sig.data, theta, T, K, nthreads=cpu_cores())
+    xo, _, _ = orc.spgqp_solve(b, orc.permute_blocked_to_interleaved(sig.gamma0, T, K), T, K,
+                               orc.A_coeff(eps0, T), orc.spg_opts(m=10, eps=1e-12, maxit=20000),
+                               nthreads=cpu_cores())
+    _, dgo, _ = orc.recon_mse(xo, theta, sig.clean, T, K)
+    deps_o = orc.adjoint(xo, sig.data, theta, dgo, T, K, eps0)[0]
+    t_cpu = time.perf_counter() - t0
+    res["checks"] = {"fd_central_h1e-4_fp64": fd, "adjoint_fp64": deps64, "oracle_fp64": deps_o,
+                     "rel_mixed_vs_fd": abs(deps - fd) / abs(fd), "rel_fp64_vs_fd": abs(deps64 - fd) / abs(fd),
+                     "rel_mixed_vs_oracle": abs(deps - deps_o) / abs(deps_o)}
+    res["cpu_baseline_gradient_s"] = t_cpu
+    res["cpu_baseline_cores"] = cpu_cores()
+    # 20 gradient steps on log epssqr
+    with loaded(PASC_PREC_MIXED, eps0) as p:
+        t0 = time.perf_counter()
+        rec = learn.descend_log_epssqr(p, sig.clean, steps=20, spg=spg_mixed)
+        t_gd = time.perf_counter() - t0
+    res["descent"] = {"steps": 20, "wall_s": t_gd, "loss_first": rec[0]["loss"], "loss_last": rec[-1]["loss"],
+                      "epssqr_last": rec[-1]["epssqr"],
+                      "epssqr": [r["epssqr"] for r in rec], "loss": [r["loss"] for r in rec]}
     return res
 
 

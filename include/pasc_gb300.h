@@ -221,7 +221,9 @@ int pasc_gb300_argmax_labels(pasc_gb300_problem *p, int *labels);
 
 /* ---------------------------------------------------------------------------------------
  * derivatives through the converged gamma step (no counterpart in the reference, which only
- * solves).  With the free set F_t = {k : gamma_tk > act_tol} held fixed, the solution of the
+ * solves).  The free set F_t = {k : z_tk > act_tol} is read from one projected-gradient step
+ * z = Proj(gamma - a (A gamma - b)), a = 1/(8 coeff + |bscale|) (z = gamma at an exact solution;
+ * on an FP32 end point it drops entries held at zero by their multiplier).  With F held fixed, the solution of the
  * QP moves inside S = {v : v_tk = 0 for k outside F_t, sum_k v_tk = 0}; the adjoint lambda in
  * S solves P A P lambda = P dloss/dgamma (P the orthogonal projection onto S, A = coeff *
  * A_hat) by conjugate gradients in FP64, and
@@ -231,7 +233,7 @@ int pasc_gb300_argmax_labels(pasc_gb300_problem *p, int *labels);
  * theta is a given input here (the theta step is not differentiated).
  * ------------------------------------------------------------------------------------- */
 typedef struct {
-    double act_tol;         /* gamma_tk > act_tol is free (1e-7) */
+    double act_tol;         /* z_tk > act_tol is free (1e-7) */
     double cg_tol;          /* stop when ||r|| <= cg_tol * ||r_0|| (1e-10) */
     int cg_maxit;           /* (20000) */
 } pasc_gb300_adjoint_opts;

@@ -643,13 +643,30 @@ int pasc_oracle_adjoint(const double *gamma, const double *data, const double *t
         free(fr); free(lam); free(r); free(p); free(q);
         return -1;
     }
+    /* free sets from one projected-gradient step z = Proj(gamma - a (A gamma - b)),
+     * a = 1/(8 coeff + |bscale|); z = gamma at an exact solution */
+    const double a = 1.0 / (8.0 * coeff + fabs(bscale));
+    double z[64], zs[64];
     long free_dims = 0;
     double rr = 0.0;
+    if (K > 64) {
+        free(fr); free(lam); free(r); free(p); free(q);
+        return -1;
+    }
     for (long t = 0; t < T; t++) {
         int nf = 0;
         for (int k = 0; k < K; k++) {
             long i = t * (long)K + k;
-            fr[i] = gamma[i] > o->act_tol;
+            double ag = 0.0;
+            if (t > 0) ag += 2.0 * (gamma[i] - gamma[i - K]);
+            if (t < T - 1) ag += 2.0 * (gamma[i] - gamma[i + K]);
+            double res = data[t] - theta[k];
+            z[k] = gamma[i] - a * (coeff * ag - bscale * res * res);
+        }
+        project_block(z, K, zs);
+        for (int k = 0; k < K; k++) {
+            long i = t * (long)K + k;
+            fr[i] = z[k] > o->act_tol;
             nf += fr[i];
             r[i] = dloss_dgamma[i];
         }

@@ -121,7 +121,8 @@ void pasc_oracle_argmax_labels(const double *gamma, int *labels, long T, int K);
 /* ------------------------------------------------------------------------------------
  * Derivatives through the converged gamma step.  The reference has no such code: this is
  * the FP64 statement of active-set implicit differentiation of the QP above, the checker of
- * the GPU adjoint.  Free set F_t = {k : gamma_tk > act_tol}; S = {v : v_tk = 0 off F_t,
+ * the GPU adjoint.  Free set F_t = {k : z_tk > act_tol} with z = Proj(gamma - a (A gamma - b)),
+ * a = 1/(8 coeff + |bscale|) (z = gamma at an exact solution); S = {v : v_tk = 0 off F_t,
  * sum_k v_tk = 0}; P = orthogonal projection onto S (per t: zero off F_t, subtract the mean
  * over F_t).  lambda in S solves P A P lambda = P dl/dgamma (conjugate gradients from 0,
  * stop at ||r|| <= cg_tol ||r_0||), A = coeff * A_hat, and

@@ -7,7 +7,11 @@
 // gamma the free set of timestep t is F_t = {k : gamma_tk > act_tol}; S = {v : v_tk = 0 for k
 // outside F_t, sum_k v_tk = 0} is the space gamma can move in without changing the active
 // set, and P (per timestep: zero outside F_t, subtract the mean over F_t) is the orthogonal
-// projection onto it.  The optimality conditions on S, P(A gamma - b) = 0, differentiated at
+// projection onto it.  The free set is read from one projected-gradient step,
+// z = Proj(gamma - a (A gamma - b)) with a = 1/(8 coeff + |bscale|) (1/||A|| when A dominates):
+// at an exact solution z = gamma, and on an FP32 end point (x^c + beta d, not exactly on the
+// active face) entries held at zero by a positive multiplier are projected away instead of
+// being mistaken for free ones.  The optimality conditions on S, P(A gamma - b) = 0, differentiated at
 // a fixed active set give  P A P gamma' = -P(A' gamma - b'),  so for a loss l(gamma)
 //     l' = -lambda'(A' gamma - b'),   lambda in S solving  P A P lambda = P dl/dgamma.
 // lambda is found by conjugate gradients on S in FP64: two kernels per CG iteration (apply
@@ -26,6 +30,7 @@
 #include "common.cuh"
 #include "internal.h"
 #include "problem.h"
+#include "project.cuh"
 
 namespace pasc {
 
@@ -160,21 +165,36 @@ __global__ void __launch_bounds__(ADJ_NT) recon_mse_kernel(const double *gam, co
     }
 }
 
-// free sets, r = P dl/dgamma, lambda = 0, both search-direction buffers 0, r'r and dim S.
+// free sets (from z = Proj(gamma - a g), see the head of the file), r = P dl/dgamma,
+// lambda = 0, both search-direction buffers 0, r'r and dim S.
 template <int K>
-__global__ void __launch_bounds__(ADJ_NT) adj_setup_kernel(const double *gam, const double *gl, long T,
+__global__ void __launch_bounds__(ADJ_NT) adj_setup_kernel(const double *gam, const double *gl, const double *data,
+                                                           const double *theta, long T, double coeff, double bscale,
                                                            double act_tol, unsigned int *mask, double *lam,
                                                            double *r, double *p0, double *p1,
                                                            double *partials, AdjDevState *st)
 {
     __shared__ double scratch[2 * (ADJ_NT / 32)];
+    const double a = 1.0 / (8.0 * coeff + fabs(bscale));
     double v2[2] = {0.0, 0.0};
     for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        const double x = data[t];
+        double z[K], zs[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const double gc = gam[t * K + k];
+            double ag = 0.0;
+            if (t > 0) ag += 2.0 * (gc - gam[(t - 1) * K + k]);
+            if (t < T - 1) ag += 2.0 * (gc - gam[(t + 1) * K + k]);
+            const double res = x - theta[k];
+            z[k] = gc - a * (coeff * ag - bscale * res * res);
+        }
+        project_ref_f64(z, K, zs);
         unsigned int m = 0u;
         double v[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            m |= (gam[t * K + k] > act_tol ? 1u : 0u) << k;
+            m |= (z[k] > act_tol ? 1u : 0u) << k;
             v[k] = gl[t * K + k];
         }
         mask[t] = m;
@@ -503,8 +523,8 @@ int pasc_gb300_adjoint(pasc_gb300_problem *p, const double *dloss_dgamma, const 
     h->maxit = o->cg_maxit;
     ACU(cudaMemcpyAsync(w->st, h, sizeof *h, cudaMemcpyHostToDevice, s));
     PASC_ADJ_DISPATCH(p->K, (adj_setup_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(
-                                g, w->gl, p->T, o->act_tol, w->mask, w->lam, w->r, w->pb[0], w->pb[1],
-                                w->partials, w->st)));
+                                g, w->gl, p->data64, p->theta64, p->T, p->coeffA, p->coeffB, o->act_tol,
+                                w->mask, w->lam, w->r, w->pb[0], w->pb[1], w->partials, w->st)));
     ACU(cudaGetLastError());
     int launches = 1;
     ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));

@@ -8,7 +8,7 @@ differences (step 1e-4 relative) through tightly converged FP64 GPU solves agree
 import numpy as np
 import pytest
 
-from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Problem, capi, datagen
+from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Problem, capi, datagen, learn
 
 pytestmark = pytest.mark.gpu
 
@@ -120,6 +120,26 @@ def test_adjoint_finite_differences_fp64(gpulib, oracle):
             lo.append(p.recon_mse(sig.clean))
         fd = (lo[0] - lo[1]) / (2 * hx)
         assert abs(fd - dX @ v) <= 1e-4 * np.abs(dX).sum(), (fd, dX @ v)
+
+
+def test_descent_on_log_epssqr_lowers_the_loss(gpulib, oracle):
+    """20 gradient steps on log epssqr from an over-regularised start: the loss falls, and the
+    FP64 oracle's own solves agree that the end point is better than the start."""
+    T, K = 20000, 3
+    sig = _signal(T, K, 21)
+    theta = np.array([0.0, 1.0, 2.0])
+    with Problem(T, K, 3000.0, precision=PASC_PREC_MIXED) as p:
+        p.set_data(sig.data)
+        p.set_theta(theta)
+        p.set_gamma(sig.gamma0)
+        p.permute_gamma()
+        rec = learn.descend_log_epssqr(p, sig.clean, steps=20)
+    assert len(rec) == 21
+    losses = [r["loss"] for r in rec]
+    assert losses[-1] < 0.8 * losses[0], losses
+    lo = [oracle.recon_mse(_converged(oracle, sig, theta, r["epssqr"]), theta, sig.clean, T, K)[0]
+          for r in (rec[0], rec[-1])]
+    assert lo[1] < 0.8 * lo[0], lo
 
 
 def test_adjoint_errors(gpulib):

@@ -134,14 +134,33 @@ def test_adjoint_gradients_match_finite_differences(oracle, T, K, eps2, seed):
 
 
 def test_adjoint_vertex_solution_has_zero_gradient(oracle):
-    """Every timestep at a vertex: no free direction, so the QP solution is locally constant
-    and every derivative through it is zero."""
-    T, K = 20, 3
-    gamma = np.zeros(T * K)
-    gamma[np.arange(T) * K + (np.arange(T) % K)] = 1.0
-    data = np.linspace(0, 2, T)
+    """A solution with every timestep at a vertex (noise-free data, long segments, weak
+    regularisation): no free direction, so the QP solution is locally constant and every
+    derivative through it is zero."""
+    T, K, eps2 = 30, 3, 0.01
+    labels = np.repeat([0, 1, 2], 10)
     theta = np.array([0.0, 1.0, 2.0])
+    data = theta[labels]
+    b = oracle.residual_b(data, theta, T, K)
+    gamma = exact_qp(oracle, b, np.full(T * K, 1.0 / K), T, K, oracle.A_coeff(eps2, T))
+    assert np.array_equal(gamma, np.eye(K)[labels].ravel())
     dg = np.random.default_rng(0).normal(size=T * K)
-    deps, dX, dth, lam, r = oracle.adjoint(gamma, data, theta, dg, T, K, 10.0)
+    deps, dX, dth, lam, r = oracle.adjoint(gamma, data, theta, dg, T, K, eps2)
     assert r.free_dims == 0 and r.status == 1
     assert deps == 0.0 and np.all(dX == 0.0) and np.all(dth == 0.0)
+
+
+@pytest.mark.parametrize("T,K,eps2,seed", [(40, 3, 20.0, 1), (60, 2, 50.0, 2)])
+def test_free_set_read_through_a_projected_step(oracle, T, K, eps2, seed):
+    """An inexact end point whose active entries are small positives (as an FP32 iterate
+    x^c + beta d leaves them) yields the free set of the exact solution, and nearly its
+    gradient: the free set is taken from Proj(gamma - a g), not from gamma itself."""
+    sig, theta, b, coeff, x = _case(T, K, eps2, seed, oracle)
+    _, dg, _ = oracle.recon_mse(x, theta, sig.clean, T, K)
+    deps, dX, _, _, r = oracle.adjoint(x, sig.data, theta, dg, T, K, eps2)
+    xn = x.copy()
+    xn[x == 0.0] = 1e-6
+    xn = (xn.reshape(T, K) / xn.reshape(T, K).sum(axis=1, keepdims=True)).ravel()
+    deps_n, dX_n, _, _, r_n = oracle.adjoint(xn, sig.data, theta, dg, T, K, eps2)
+    assert r_n.free_dims == r.free_dims
+    assert abs(deps_n - deps) <= 1e-3 * abs(deps)
