@@ -33,6 +33,11 @@ Besides the headline line it measures, on rank 0:
              the adjoint, checked against central differences (1e-4 relative) through FP64 GPU
              solves and against the FP64 oracle's gradient (timed: the CPU baseline), then 20
              gradient steps on log epssqr.
+  multichannel  T = 1e6 timesteps of n = 128 channels, K = 8 (Markov labels, centroids N(0, I),
+             noise 0.8; X in BF16): the TSSolver wall time, and per kernel its device time and
+             bytes: the residual on the tensor cores and on the CUDA cores, the theta update,
+             the SPG sweep reading the materialised b; the oracle's residual and theta update
+             on the host cores for comparison.
 """
 from __future__ import annotations
 
@@ -68,6 +73,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-multichannel", action="store_true")
     ap.add_argument("--variant", type=int, default=-1, choices=[-1, 0, 1],
                     help="sweep kernel: -1 chosen by timing (default), 0 one timestep per thread, "
                          "1 bulk-copy tiles (pin it when profiling: a profiler distorts the timing)")
@@ -310,6 +316,8 @@ def main():
         result["time_to_1e-6_rel_obj"] = measure_tts(sig, theta, args.eps2, dev)
     if info.rank == 0 and not args.no_batched:
         result["batched"] = measure_batched(dev, peak)
+    if info.rank == 0 and not args.no_multichannel:
+        result["multichannel"] = measure_multichannel(dev, peak)
     if info.rank == 0 and not args.no_adjoint:
         result["adjoint"] = measure_adjoint(dev, peak)
     if info.rank == 0 and not args.no_cpu:
@@ -385,6 +393,64 @@ def measure_tts(sig, theta, eps2, dev):
                      "status": capi.STATUS_NAMES.get(st.status, st.status)}
     a, b = res["fp64_plain"]["seconds"], res["mixed_fused"]["seconds"]
     res["speedup_vs_fp64_plain"] = (a / b) if (a and b) else None
+    return res
+
+
+def measure_multichannel(dev, peak):
+    from pasc_inference_gb300 import PASC_PREC_MIXED, Problem, capi, datagen
+    sys.path.insert(0, ROOT)
+    from oracle import pasc_oracle as orc
+    t0 = time.perf_counter()
+    mc = datagen.multichannel()
+    t_gen = time.perf_counter() - t0
+    T, n, K = mc.T, mc.n, mc.K
+    res = {"workload": "multichannel T=1e6 n=128 K=8, Markov labels (stay 0.999), centroids N(0,I), noise 0.8, "
+                       "epssqr=50, X in BF16", "T": T, "n": n, "K": K, "datagen_s": t_gen}
+    with Problem(T, K, mc.epssqr, precision=PASC_PREC_MIXED, xdim=n, device=dev) as p:
+        p.set_data(mc.data)
+        p.set_gamma(mc.gamma0)
+        p.set_theta(np.zeros(K * n))
+        t0 = time.perf_counter()
+        st = p.ts_solve(capi.ts_opts(), capi.spgqp_opts(m=10))
+        res["tssolver"] = {"wall_s": time.perf_counter() - t0, "L": st.L, "outer_it": st.it_last,
+                           "spg_it": st.spg_it_sum, "gpu_launches": st.kernel_launches,
+                           "settings": "reference defaults (SPG eps 1e-9, outer |dL| < 1e-6), m 10"}
+        kernels = {}
+        B_res = 2.0 * T * n + 4.0 * T + 4.0 * T * K  # X (BF16), ||X_t||^2, b written
+        for eng, name in ((0, "residual_tcgen05"), (1, "residual_cuda_cores")):
+            p.set_residual_engine(eng)
+            p.time_model_kernels(2, 3)
+            ms = p.time_model_kernels(2, 20)
+            kernels[name] = {"us": ms * 1e3, "bytes": B_res, "achieved": B_res / (ms * 1e-3) / 1e9, "unit": "GB/s",
+                             "frac": B_res / (ms * 1e-3) / 1e9 / peak,
+                             "tflops_useful": 2.0 * T * n * K / (ms * 1e-3) / 1e12}
+        p.set_residual_engine(0)
+        B_th = 2.0 * T * n + 4.0 * T * K
+        p.time_model_kernels(1, 3)
+        ms = p.time_model_kernels(1, 20)
+        kernels["theta_update"] = {"us": ms * 1e3, "bytes": B_th, "achieved": B_th / (ms * 1e-3) / 1e9, "unit": "GB/s",
+                                   "frac": B_th / (ms * 1e-3) / 1e9 / peak}
+        p.update_b()
+        p.spgqp_start(capi.spgqp_opts(m=10, maxit=100000, stop_difff=0))
+        p.spgqp_iterate(20, poll=False)
+        p.spgqp_iterate(200, poll=False)
+        ms, nl = p.spgqp_last_iterate()
+        B_sw = 12.0 * K * T  # x read, b read, x written (FP32)
+        kernels["spg_sweep_bmat"] = {"us": ms / nl * 1e3, "bytes": B_sw, "achieved": B_sw / (ms / nl * 1e-3) / 1e9,
+                                     "unit": "GB/s", "frac": B_sw / (ms / nl * 1e-3) / 1e9 / peak}
+        res["kernels"] = kernels
+        th = p.get_theta()
+        g = p.get_gamma()
+    res["peak"] = peak
+    # host FP64 oracle: residual (all cores) and theta update (one core)
+    t0 = time.perf_counter()
+    orc.residual_b(mc.data, th, T, K, xdim=n, nthreads=cpu_cores())
+    t_res = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    orc.theta_update(g, mc.data, T, K, xdim=n)
+    t_th = time.perf_counter() - t0
+    res["cpu_oracle"] = {"residual_s": t_res, "residual_cores": cpu_cores(), "theta_update_s": t_th,
+                         "theta_update_cores": 1}
     return res
 
 

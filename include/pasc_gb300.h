@@ -141,7 +141,12 @@ int pasc_gb300_device_count(void);
  * ------------------------------------------------------------------------------------- */
 typedef struct pasc_gb300_problem pasc_gb300_problem;
 
-/* T >= 1, 1 <= K <= 32 (mixed) or <= 128 (fp64), xdim == 1.  epssqr as in
+/* Multichannel data (xdim = n > 1, each X_t in R^n; b_tk = bscale ||X_t - theta_k||^2 and
+ * theta_k = sum_t gamma_tk X_t / sum_t gamma_tk, the extension of the scalar model whose theta
+ * the reference already sizes K*xdim, graphh1fem.cpp:23): mixed path only, K <= 8, n <= 256;
+ * X is held on the device in BF16 (rounded to nearest) and b is formed once per update_b /
+ * outer iteration. */
+/* T >= 1, 1 <= K <= 32 (mixed) or <= 128 (fp64), xdim >= 1.  epssqr as in
  * GraphH1FEMModel(tsdata, epssqr) (src/petscvector/model/graphh1fem.cpp:8-65). */
 int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int precision,
                       double epssqr, int device);
@@ -199,6 +204,24 @@ int pasc_gb300_spgqp_last_iterate(pasc_gb300_problem *p, double *ms, int *launch
  * first solve, measured on the solve's own first sweep. */
 int pasc_gb300_set_sweep_variant(pasc_gb300_problem *p, int variant);
 int pasc_gb300_get_sweep_variant(pasc_gb300_problem *p, int *variant);
+
+/* Measurement: device time per call (CUDA events on the handle's stream) of `reps`
+ * back-to-back launches of the theta update (which = 1, as pasc_gb300_update_theta) or of the
+ * residual b (which = 2, as pasc_gb300_update_b).  Changes theta / b as those calls do. */
+int pasc_gb300_time_model_kernels(pasc_gb300_problem *p, int which, int reps, double *ms_per_call);
+
+/* QPData::get_b (include/general/data/qpdata.h:23-112): the gamma problem's linear term
+ * b_tk = bscale ||X_t - theta_k||^2 (N host values).  fp64 path: the stored b; multichannel:
+ * the FP32 b the residual kernel wrote; 1-D mixed path (b formed inside the sweep): the same
+ * formula evaluated in FP64 from the stored data and theta. */
+int pasc_gb300_get_b(pasc_gb300_problem *p, double *b);
+
+/* Residual kernel of multichannel data (xdim > 1): 0 = tensor cores (tcgen05, BF16 X and a
+ * three-part BF16 theta, FP32 accumulation; xdim in {64, 128, 256}; the default there),
+ * 1 = CUDA cores (FP32; any xdim, the default otherwise).  No reference counterpart: the
+ * reference's GraphH1FEM takes scalar data. */
+int pasc_gb300_set_residual_engine(pasc_gb300_problem *p, int engine);
+int pasc_gb300_get_residual_engine(pasc_gb300_problem *p, int *engine);
 
 /* SPGQPSolver<PetscVector>::get_fx (spgqpsolver.cpp:316-345): 1/2 (g - b)'x of the last solve. */
 int pasc_gb300_get_fx(pasc_gb300_problem *p, double *fx);

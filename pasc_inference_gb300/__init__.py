@@ -143,6 +143,26 @@ class Problem:
         check(load().pasc_gb300_get_sweep_variant(self._h, C.byref(v)))
         return v.value
 
+    def time_model_kernels(self, which: int, reps: int = 10) -> float:
+        """ms per call of the theta update (which=1) or the residual (which=2)."""
+        v = C.c_double()
+        check(load().pasc_gb300_time_model_kernels(self._h, int(which), int(reps), C.byref(v)))
+        return v.value
+
+    def get_b(self) -> np.ndarray:
+        out = np.empty(self.T * self.K)
+        check(load().pasc_gb300_get_b(self._h, out))
+        return out
+
+    def set_residual_engine(self, engine: int):
+        """Multichannel data: 0 = tensor cores, 1 = CUDA cores."""
+        check(load().pasc_gb300_set_residual_engine(self._h, int(engine)))
+
+    def get_residual_engine(self) -> int:
+        v = C.c_int()
+        check(load().pasc_gb300_get_residual_engine(self._h, C.byref(v)))
+        return v.value
+
     def get_fx(self) -> float:
         v = C.c_double()
         check(load().pasc_gb300_get_fx(self._h, C.byref(v)))

@@ -94,6 +94,10 @@ PROTOTYPES = {
     "pasc_gb300_spgqp_last_iterate": (C.c_int, [_h, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "pasc_gb300_set_sweep_variant": (C.c_int, [_h, C.c_int]),
     "pasc_gb300_get_sweep_variant": (C.c_int, [_h, C.POINTER(C.c_int)]),
+    "pasc_gb300_get_b": (C.c_int, [_h, _dp]),
+    "pasc_gb300_time_model_kernels": (C.c_int, [_h, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "pasc_gb300_set_residual_engine": (C.c_int, [_h, C.c_int]),
+    "pasc_gb300_get_residual_engine": (C.c_int, [_h, C.POINTER(C.c_int)]),
     "pasc_gb300_get_fx": (C.c_int, [_h, C.POINTER(C.c_double)]),
     "pasc_gb300_ts_solve": (C.c_int, [_h, C.POINTER(TsOpts), C.POINTER(SpgqpOpts), C.c_void_p,
                                       C.POINTER(TsStats)]),

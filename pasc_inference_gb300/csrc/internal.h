@@ -1,6 +1,7 @@
 // internal.h -- types shared by the library's translation units (not part of the ABI).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -44,6 +45,7 @@ struct SpgDevState {
 };
 
 struct SweepArgs {
+    const float *bmat;  // T*K: b materialised (multichannel data); null: b formed from data, theta
     const float *data;  // T (xdim == 1)
     const float *theta; // K
     float *xb0, *xb1;   // ping-pong pair holding x (gamma); buffer st->cur is current
@@ -90,6 +92,32 @@ struct BatchArgs {
     double *theta64;         // 8 per signal
 };
 
+// Multichannel data (kernels_mc.cu).
+struct McArgs {
+    long T;
+    int n;                          // channels (xdim)
+    const unsigned short *xbf;      // T*n BF16, row-major
+    const float *xnorm;             // T: ||X_t||^2 of the BF16 values
+    float *bmat;                    // T*K: b_tk = bscale ||X_t - theta_k||^2
+    unsigned short *theta_split;    // 32*n BF16: rows k, K+k, 2K+k = three parts of theta_k
+    float *theta_f32;               // K*n
+    float *tnorm;                   // K: ||theta_k||^2
+    double *theta64;                // K*n
+    double *partials;               // theta-update partial sums
+    float bscale;
+    int *err;                       // set by a bounded wait that gave up
+};
+cudaError_t launch_mc_convert(const double *x64, unsigned short *xbf, float *xnorm, long T, int n, cudaStream_t s);
+int mc_tc_supported(int n);
+cudaError_t mc_make_tmap(CUtensorMap *map, const unsigned short *xbf, long T, int n);
+cudaError_t prepare_mc_residual_tc(int K, int n);
+cudaError_t launch_mc_residual_tc(const CUtensorMap &map, int K, int n, int grid, const McArgs &a, cudaStream_t s);
+cudaError_t launch_mc_residual_simt(int K, int grid, const McArgs &a, cudaStream_t s);
+// gamma != null: theta from gamma (partial kernel on `grid` blocks + per-cluster finish);
+// gamma == null: only the preparation of the current theta64 (split, FP32 copy, norms)
+cudaError_t launch_mc_theta(int K, int grid, const McArgs &a, const float *gamma, cudaStream_t s);
+size_t mc_partials_size(int K, int n, int grid);
+
 int batch_tile_width();
 int batch_segment_timesteps();
 int batch_max_tile();
@@ -104,7 +132,7 @@ void record_error(const char *msg);
 int sweep_block_threads();
 int sweep_tile_width();
 int sweep_blocks_per_sm(int K, bool init);
-cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);
+cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);  // a.bmat selects the b source
 // Bulk-copy (TMA) form of the sweep: 4 timesteps per thread, double-buffered tiles.
 bool sweep_tma_supported(int K);
 int sweep_tma_tile_width();

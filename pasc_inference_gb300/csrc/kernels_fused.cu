@@ -8,7 +8,9 @@
 // on chip from x, g = coeff*A_hat x - b (the same value in exact arithmetic; the stencil has
 // the footprint the recursive update needs anyway), so nothing but x crosses HBM and FP32
 // rounding cannot accumulate in g over the iterations.  b is formed in registers from the
-// data and theta (b_tk = bscale*(x_t - theta_k)^2, src/petscvector/model/graphh1fem.cpp:258-286).
+// data and theta (b_tk = bscale*(x_t - theta_k)^2, src/petscvector/model/graphh1fem.cpp:258-286),
+// or, for multichannel data (BMAT), read from the T x K array the residual kernel wrote once per
+// outer iteration (K values per timestep instead of n channels).
 //
 // The sweep is re-timed so that one pass finishes iteration c+1 and starts iteration c+2:
 // it reads x^c, forms g^c, d_{c+1}, x^{c+1} = x^c + beta_{c+1} d_{c+1}, g^{c+1}, f^{c+1},
@@ -36,7 +38,7 @@ constexpr int SWEEP_W = SWEEP_NT - SWEEP_HL - SWEEP_HR;  // owned timesteps per 
 int sweep_block_threads() { return SWEEP_NT; }
 int sweep_tile_width() { return SWEEP_W; }
 
-template <int K, bool INIT>
+template <int K, bool INIT, bool BMAT>
 __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_sweep_kernel(SweepArgs a)
 {
     __shared__ float s_x[SWEEP_NT * K];  // x^c (zero outside 0 <= t < T)
@@ -59,7 +61,7 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
 
     float theta[K];
 #pragma unroll
-    for (int k = 0; k < K; k++) theta[k] = a.theta[k];
+    for (int k = 0; k < K; k++) theta[k] = BMAT ? 0.f : a.theta[k];
 
     KahanF acc_f;  // the objective keeps a compensated sum; the dots need less
     float acc_dd = 0.f, acc_dAd = 0.f, acc_gd = 0.f;
@@ -70,13 +72,18 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
     const int ntiles = (T + SWEEP_W - 1) / SWEEP_W;
 
     // the next tile's x and data are loaded into registers while the current one is computed
-    float xn[K], dvn = 0.f;
+    float xn[K], dvn = 0.f, bn[BMAT ? K : 1];
     {
         const int t = blockIdx.x * SWEEP_W - SWEEP_HL + i;
         const bool in = (int)blockIdx.x < ntiles && (unsigned)t < (unsigned)T;
 #pragma unroll
         for (int k = 0; k < K; k++) xn[k] = in ? __ldcs(xin + t * K + k) : 0.f;
-        if (in) dvn = __ldg(a.data + t);
+        if (BMAT) {
+#pragma unroll
+            for (int k = 0; k < K; k++) bn[k] = in ? __ldg(a.bmat + t * K + k) : 0.f;
+        } else if (in) {
+            dvn = __ldg(a.data + t);
+        }
     }
 
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -91,19 +98,29 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
         float xc[K], bk[K];
         const float dv = dvn;
 #pragma unroll
-        for (int k = 0; k < K; k++) xc[k] = xn[k];
+        for (int k = 0; k < K; k++) {
+            xc[k] = xn[k];
+            if (BMAT) bk[k] = bn[BMAT ? k : 0];
+        }
         {
             const int tn = t + (int)gridDim.x * SWEEP_W;
             const bool inn = tile + (int)gridDim.x < ntiles && (unsigned)tn < (unsigned)T;
 #pragma unroll
             for (int k = 0; k < K; k++) xn[k] = inn ? __ldcs(xin + tn * K + k) : 0.f;
-            dvn = inn ? __ldg(a.data + tn) : 0.f;
+            if (BMAT) {
+#pragma unroll
+                for (int k = 0; k < K; k++) bn[BMAT ? k : 0] = inn ? __ldg(a.bmat + tn * K + k) : 0.f;
+            } else {
+                dvn = inn ? __ldg(a.data + tn) : 0.f;
+            }
         }
         if (INIT) project_reg<K>(xc);
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const float r = dv - theta[k];
-            bk[k] = bscale * (r * r);
+            if (!BMAT) {
+                const float r = dv - theta[k];
+                bk[k] = bscale * (r * r);
+            }
             s_x[i * K + k] = in ? xc[k] : 0.f;
         }
         __syncthreads();
@@ -192,7 +209,7 @@ template <int K, bool INIT>
 static int blocks_per_sm_t()
 {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_kernel<K, INIT>, SWEEP_NT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_kernel<K, INIT, false>, SWEEP_NT, 0);
     return nb > 0 ? nb : 1;
 }
 
@@ -212,8 +229,13 @@ cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStr
     switch (K) {
 #define PASC_CASE(KK)                                                                   \
     case KK:                                                                            \
-        if (init) spg_sweep_kernel<KK, true><<<grid, SWEEP_NT, 0, s>>>(a);              \
-        else spg_sweep_kernel<KK, false><<<grid, SWEEP_NT, 0, s>>>(a);                  \
+        if (a.bmat) {                                                                   \
+            if (init) spg_sweep_kernel<KK, true, true><<<grid, SWEEP_NT, 0, s>>>(a);    \
+            else spg_sweep_kernel<KK, false, true><<<grid, SWEEP_NT, 0, s>>>(a);        \
+        } else {                                                                        \
+            if (init) spg_sweep_kernel<KK, true, false><<<grid, SWEEP_NT, 0, s>>>(a);   \
+            else spg_sweep_kernel<KK, false, false><<<grid, SWEEP_NT, 0, s>>>(a);       \
+        }                                                                               \
         break;
         PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
         PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)

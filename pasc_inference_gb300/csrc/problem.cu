@@ -61,7 +61,8 @@ static void free_all(pasc_gb300_problem *p)
     if (p->chunk_graph) cudaGraphExecDestroy(p->chunk_graph);
     void *dev[] = {p->data64, p->theta64, p->stage64, p->red, p->red_out, p->labels_d, p->x, p->g,
                    p->d, p->Ad, p->b, p->data32_raw, p->theta32, p->xb_raw[0], p->xb_raw[1], p->st,
-                   p->partials};
+                   p->partials, p->xbf, p->xnorm, p->bmat, p->theta_split, p->theta_f32, p->tnorm,
+                   p->mc_partials, p->mc_err};
     for (void *q : dev)
         if (q) cudaFree(q);
     if (p->st_h) cudaFreeHost(p->st_h);
@@ -144,7 +145,10 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
     if (!out) return fail(PASC_ERR_ARG, "create: out is NULL");
     *out = nullptr;
     if (T < 1) return fail(PASC_ERR_ARG, "create: T must be >= 1 (got %ld)", T);
-    if (xdim != 1) return fail(PASC_ERR_NOTSUPP, "create: xdim %d not supported (1-D signals only)", xdim);
+    if (xdim < 1) return fail(PASC_ERR_ARG, "create: xdim must be >= 1 (got %d)", xdim);
+    if (xdim > 1 && precision != PASC_PREC_MIXED)
+        return fail(PASC_ERR_NOTSUPP, "create: multichannel data (xdim %d) needs the mixed path", xdim);
+    if (xdim > 256) return fail(PASC_ERR_NOTSUPP, "create: xdim %d > 256 not supported", xdim);
     if (precision != PASC_PREC_FP64 && precision != PASC_PREC_MIXED)
         return fail(PASC_ERR_ARG, "create: unknown precision %d", precision);
     const int kmax = precision == PASC_PREC_MIXED ? KMAX_FUSED : KMAX_PLAIN;
@@ -175,7 +179,7 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
         return bail(fail(PASC_ERR_CUDA, "create: stream/event creation failed"));
 
     const long N = p->N;
-    if ((rc = dalloc(&p->data64, T)) || (rc = dalloc(&p->theta64, (size_t)K * xdim)) ||
+    if ((rc = dalloc(&p->data64, (size_t)T * xdim)) || (rc = dalloc(&p->theta64, (size_t)K * xdim)) ||
         (rc = dalloc(&p->stage64, N)) || (rc = dalloc(&p->red, dot_partials_size())) ||
         (rc = dalloc(&p->red_out, 8)) || (rc = dalloc(&p->labels_d, T)))
         return bail(rc);
@@ -183,7 +187,7 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
         return bail(fail(PASC_ERR_ALLOC, "create: pinned allocation failed"));
     cudaMemset(p->red, 0, dot_partials_size() * sizeof(double));
     cudaMemset(p->theta64, 0, sizeof(double) * K * xdim);
-    cudaMemset(p->data64, 0, sizeof(double) * T);
+    cudaMemset(p->data64, 0, sizeof(double) * T * xdim);
 
     if (precision == PASC_PREC_FP64) {
         if ((rc = dalloc(&p->x, N)) || (rc = dalloc(&p->g, N)) || (rc = dalloc(&p->d, N)) ||
@@ -233,6 +237,34 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
         }
         np = np * 4 > (long)p->grid_theta * 2 * K ? np * 4 : (long)p->grid_theta * 2 * K;
         if ((rc = dalloc(&p->partials, np))) return bail(rc);
+        if (xdim > 1) {
+            long gm = (long)p->sms * 4, tb64 = (T + 63) / 64;
+            p->mc_grid_theta = (int)(gm < tb64 ? gm : tb64);
+            if (p->mc_grid_theta < 1) p->mc_grid_theta = 1;
+            long nt = (T + 127) / 128;
+            p->mc_grid_res = (int)((long)p->sms < nt ? p->sms : nt);
+            if ((rc = dalloc(&p->xbf, (size_t)T * xdim)) || (rc = dalloc(&p->xnorm, T)) ||
+                (rc = dalloc(&p->bmat, (size_t)T * K)) || (rc = dalloc(&p->theta_split, (size_t)32 * xdim)) ||
+                (rc = dalloc(&p->theta_f32, (size_t)K * xdim)) || (rc = dalloc(&p->tnorm, K)) ||
+                (rc = dalloc(&p->mc_err, 1)) ||
+                (rc = dalloc(&p->mc_partials, mc_partials_size(K, xdim, p->mc_grid_theta))))
+                return bail(rc);
+            cudaMemset(p->xbf, 0, sizeof(unsigned short) * T * xdim);
+            cudaMemset(p->xnorm, 0, sizeof(float) * T);
+            cudaMemset(p->bmat, 0, sizeof(float) * T * K);
+            cudaMemset(p->theta_split, 0, sizeof(unsigned short) * 32 * xdim);
+            cudaMemset(p->theta_f32, 0, sizeof(float) * K * xdim);
+            cudaMemset(p->tnorm, 0, sizeof(float) * K);
+            cudaMemset(p->mc_err, 0, sizeof(int));
+            p->variant = 0;  // the bulk-copy sweep forms b from 1-D data only
+            p->mc_engine = mc_tc_supported(xdim) ? 0 : 1;
+            if (p->mc_engine == 0) {
+                cudaError_t e = mc_make_tmap(&p->mc_tmap, p->xbf, T, xdim);
+                if (e == cudaSuccess) e = prepare_mc_residual_tc(K, xdim);
+                if (e != cudaSuccess)
+                    return bail(fail(PASC_ERR_CUDA, "create: tensor map / kernel set-up failed: %s", cudaGetErrorString(e)));
+            }
+        }
     }
     if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess)
         return bail(fail(PASC_ERR_CUDA, "create: initialisation failed"));
@@ -257,14 +289,67 @@ int pasc_gb300_set_epssqr(pasc_gb300_problem *p, double epssqr, int scalef)
     return PASC_OK;
 }
 
+}  // extern "C"
+
+static McArgs mc_args(pasc_gb300_problem *p)
+{
+    McArgs a;
+    a.T = p->T;
+    a.n = p->xdim;
+    a.xbf = p->xbf;
+    a.xnorm = p->xnorm;
+    a.bmat = p->bmat;
+    a.theta_split = p->theta_split;
+    a.theta_f32 = p->theta_f32;
+    a.tnorm = p->tnorm;
+    a.theta64 = p->theta64;
+    a.partials = p->mc_partials;
+    a.bscale = (float)p->coeffB;
+    a.err = p->mc_err;
+    return a;
+}
+
+// b_tk = bscale ||X_t - theta_k||^2 into bmat (multichannel)
+static int mc_residual_async(pasc_gb300_problem *p, int *launches)
+{
+    const McArgs a = mc_args(p);
+    if (p->mc_engine == 0) CU(launch_mc_residual_tc(p->mc_tmap, p->K, p->xdim, p->mc_grid_res, a, p->stream));
+    else CU(launch_mc_residual_simt(p->K, p->sms * 4, a, p->stream));
+    if (launches) *launches += 1;
+    return PASC_OK;
+}
+
+static int mc_check_error(pasc_gb300_problem *p)
+{
+    if (p->xdim == 1) return PASC_OK;
+    int e = 0;
+    CU(cudaMemcpyAsync(&e, p->mc_err, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    if (e) {
+        cudaMemsetAsync(p->mc_err, 0, sizeof(int), p->stream);
+        return fail(PASC_ERR_TIMEOUT, "residual kernel: a bounded wait for a tile copy or the tensor cores gave up (%d)", e);
+    }
+    return PASC_OK;
+}
+
+extern "C" {
+
 int pasc_gb300_set_data(pasc_gb300_problem *p, const double *data)
 {
     if (!p || !data) return fail(PASC_ERR_ARG, "set_data: NULL argument");
     p->run.started = false;
     CU(cudaSetDevice(p->device));
     CU(cudaMemcpyAsync(p->data64, data, sizeof(double) * p->T * p->xdim, cudaMemcpyHostToDevice, p->stream));
-    if (p->precision == PASC_PREC_MIXED) CU(launch_f64_to_f32(p->data64, p->data32, p->T, p->stream));
+    if (p->xdim > 1) {
+        // multichannel: X is kept in BF16 (rounded to nearest), with ||X_t||^2 of the rounded
+        // values; b follows from the current theta
+        CU(launch_mc_convert(p->data64, p->xbf, p->xnorm, p->T, p->xdim, p->stream));
+        CHK(mc_residual_async(p, nullptr));
+    } else if (p->precision == PASC_PREC_MIXED) {
+        CU(launch_f64_to_f32(p->data64, p->data32, p->T, p->stream));
+    }
     CU(cudaStreamSynchronize(p->stream));
+    CHK(mc_check_error(p));
     p->have_data = true;
     return PASC_OK;
 }
@@ -314,8 +399,14 @@ int pasc_gb300_set_theta(pasc_gb300_problem *p, const double *theta)
     p->run.started = false;
     CU(cudaSetDevice(p->device));
     CU(cudaMemcpyAsync(p->theta64, theta, sizeof(double) * p->K * p->xdim, cudaMemcpyHostToDevice, p->stream));
-    if (p->precision == PASC_PREC_MIXED) CU(launch_f64_to_f32(p->theta64, p->theta32, p->K, p->stream));
+    if (p->xdim > 1) {
+        CU(launch_mc_theta(p->K, p->mc_grid_theta, mc_args(p), nullptr, p->stream));
+        if (p->have_data) CHK(mc_residual_async(p, nullptr));
+    } else if (p->precision == PASC_PREC_MIXED) {
+        CU(launch_f64_to_f32(p->theta64, p->theta32, p->K, p->stream));
+    }
     CU(cudaStreamSynchronize(p->stream));
+    CHK(mc_check_error(p));
     return PASC_OK;
 }
 
@@ -353,6 +444,11 @@ int pasc_gb300_permute_gamma(pasc_gb300_problem *p)
 
 static int update_theta_async(pasc_gb300_problem *p, int *launches)
 {
+    if (p->xdim > 1) {
+        CU(launch_mc_theta(p->K, p->mc_grid_theta, mc_args(p), p->xb[p->cur], p->stream));
+        if (launches) *launches += 2;
+        return PASC_OK;
+    }
     if (p->precision == PASC_PREC_FP64) {
         CU(launch_theta_f64(p->x, p->data64, p->theta64, p->T, p->K, p->red, p->stream));
         if (launches) *launches += (p->K + 7) / 8;
@@ -385,6 +481,7 @@ int pasc_gb300_update_theta(pasc_gb300_problem *p)
 
 static int update_b_async(pasc_gb300_problem *p, int *launches)
 {
+    if (p->xdim > 1) return mc_residual_async(p, launches);
     if (p->precision == PASC_PREC_FP64) {
         CU(launch_residual_f64(p->data64, p->theta64, p->b, p->T, p->K, p->coeffB, p->stream));
         if (launches) *launches += 1;
@@ -401,6 +498,7 @@ int pasc_gb300_update_b(pasc_gb300_problem *p)
     CU(cudaSetDevice(p->device));
     CHK(update_b_async(p, nullptr));
     CU(cudaStreamSynchronize(p->stream));
+    CHK(mc_check_error(p));
     return PASC_OK;
 }
 
@@ -542,6 +640,7 @@ static int fp64_iterate(pasc_gb300_problem *p, long n)
 // ---------------------------------------------------------------------------------------
 static int sweep_args(pasc_gb300_problem *p, SweepArgs *a)
 {
+    a->bmat = p->xdim > 1 ? p->bmat : nullptr;
     a->data = p->data32;
     a->theta = p->theta32;
     a->xb0 = p->xb[0];
@@ -879,6 +978,7 @@ int pasc_gb300_ts_solve(pasc_gb300_problem *p, const pasc_gb300_ts_opts *ts,
         p->have_fx = true;
     }
     CU(cudaStreamSynchronize(p->stream));
+    CHK(mc_check_error(p));
     if (out) {
         out->it_last = keepit;
         out->it_sum = it_sum;
@@ -897,6 +997,7 @@ int pasc_gb300_ts_solve(pasc_gb300_problem *p, const pasc_gb300_ts_opts *ts,
 int pasc_gb300_abserr_reconstructed(pasc_gb300_problem *p, const double *solution, double *abserr)
 {
     if (!p || !solution || !abserr) return fail(PASC_ERR_ARG, "abserr: NULL argument");
+    if (p->xdim > 1) return fail(PASC_ERR_NOTSUPP, "abserr: 1-D signals only (Signal1DData)");
     CU(cudaSetDevice(p->device));
     const double *g64 = nullptr;
     CHK(gamma64(p, &g64));
@@ -970,8 +1071,74 @@ int pasc_gb300_set_sweep_variant(pasc_gb300_problem *p, int variant)
     if (variant < -1 || variant > 1) return fail(PASC_ERR_ARG, "set_sweep_variant: variant must be -1, 0 or 1");
     if (p->precision != PASC_PREC_MIXED) return fail(PASC_ERR_STATE, "set_sweep_variant: mixed precision only");
     if (variant == 1 && !sweep_tma_supported(p->K)) return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: K not supported");
+    if (variant != 0 && p->xdim > 1)
+        return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: multichannel data runs the one-timestep-per-thread sweep");
     p->variant = variant;
     p->run.started = false;
+    return PASC_OK;
+}
+
+int pasc_gb300_time_model_kernels(pasc_gb300_problem *p, int which, int reps, double *ms_per_call)
+{
+    if (!p || !ms_per_call) return fail(PASC_ERR_ARG, "time_model_kernels: NULL argument");
+    if ((which != 1 && which != 2) || reps < 1) return fail(PASC_ERR_ARG, "time_model_kernels: which 1 or 2, reps >= 1");
+    CU(cudaSetDevice(p->device));
+    CU(cudaStreamSynchronize(p->stream));
+    CU(cudaEventRecord(p->ev0, p->stream));
+    for (int r = 0; r < reps; r++) {
+        if (which == 1) CHK(update_theta_async(p, nullptr));
+        else CHK(update_b_async(p, nullptr));
+    }
+    CU(cudaEventRecord(p->ev1, p->stream));
+    CU(cudaEventSynchronize(p->ev1));
+    CHK(mc_check_error(p));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, p->ev0, p->ev1));
+    *ms_per_call = (double)ms / reps;
+    return PASC_OK;
+}
+
+int pasc_gb300_get_b(pasc_gb300_problem *p, double *b)
+{
+    if (!p || !b) return fail(PASC_ERR_ARG, "get_b: NULL argument");
+    CU(cudaSetDevice(p->device));
+    const double *src = nullptr;
+    if (p->precision == PASC_PREC_FP64) {
+        src = p->b;
+    } else if (p->xdim > 1) {
+        CU(launch_f32_to_f64(p->bmat, p->stage64, p->N, p->stream));
+        src = p->stage64;
+    } else {
+        CU(launch_residual_f64(p->data64, p->theta64, p->stage64, p->T, p->K, p->coeffB, p->stream));
+        src = p->stage64;
+    }
+    CU(cudaMemcpyAsync(b, src, sizeof(double) * p->N, cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_set_residual_engine(pasc_gb300_problem *p, int engine)
+{
+    if (!p) return fail(PASC_ERR_ARG, "set_residual_engine: NULL problem");
+    if (p->xdim == 1) return fail(PASC_ERR_STATE, "set_residual_engine: multichannel data only");
+    if (engine != 0 && engine != 1) return fail(PASC_ERR_ARG, "set_residual_engine: engine must be 0 or 1");
+    if (engine == 0 && !mc_tc_supported(p->xdim))
+        return fail(PASC_ERR_NOTSUPP, "set_residual_engine: tensor cores need xdim in {64, 128, 256}");
+    CU(cudaSetDevice(p->device));
+    p->mc_engine = engine;
+    p->run.started = false;
+    if (p->have_data) {
+        CHK(mc_residual_async(p, nullptr));
+        CU(cudaStreamSynchronize(p->stream));
+        CHK(mc_check_error(p));
+    }
+    return PASC_OK;
+}
+
+int pasc_gb300_get_residual_engine(pasc_gb300_problem *p, int *engine)
+{
+    if (!p || !engine) return fail(PASC_ERR_ARG, "get_residual_engine: NULL argument");
+    *engine = p->xdim > 1 ? p->mc_engine : -1;
     return PASC_OK;
 }
 

@@ -63,6 +63,20 @@ struct pasc_gb300_problem {
     cudaGraphExec_t chunk_graph = nullptr;
     int chunk_graph_len = 0, chunk_graph_variant = -1;
 
+    // multichannel data (xdim > 1, mixed path): X in BF16, b materialised once per outer
+    // iteration by the residual kernel (kernels_mc.cu)
+    unsigned short *xbf = nullptr;         // T*xdim
+    float *xnorm = nullptr;                // T
+    float *bmat = nullptr;                 // T*K
+    unsigned short *theta_split = nullptr; // 32*xdim
+    float *theta_f32 = nullptr;            // K*xdim
+    float *tnorm = nullptr;                // K
+    double *mc_partials = nullptr;
+    int *mc_err = nullptr;
+    int mc_grid_theta = 0, mc_grid_res = 0;
+    int mc_engine = 0;                     // residual: 0 tensor cores (when xdim allows), 1 CUDA cores
+    CUtensorMap mc_tmap;
+
     pasc::SpgRun run;
     pasc::AdjointWork *adj = nullptr;  // allocated by the first adjoint call
     double fx_last = 0.0;

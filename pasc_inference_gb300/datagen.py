@@ -11,6 +11,9 @@ Workloads (sizes and distributions of the benchmark configurations):
                   U[1e3, 1e5], noise N(0, 0.5^2), epssqr in {1, 10, 100, 1000}
   batched         256 signals, T log-uniform [1e3, 1e6], K U{2..5}, epssqr log-uniform [1, 1000],
                   sorted levels U[0, 4], segments U[T/50, T/5], noise sigma U[0.2, 1]
+  multichannel    T=1e6, n=128 channels, K=8: centroids N(0, I_n), hidden labels a Markov chain
+                  with self-transition 0.999 and uniform jumps to another state, X_t = theta_label +
+                  N(0, 0.8^2 I), epssqr=50; values rounded to BF16 (the device's storage format)
 The initial gamma follows the reference: uniform [0, 1) values written in the blocked order
 k*T + t (GeneralVector::set_random, src/petscvector/algebra/vector/generalvector.cpp:7-28),
 permuted to t*K + k by the TSSolver and projected when the SPG solve starts.
@@ -151,3 +154,36 @@ def batched(n: int = 256, seed: int = 3, tmin: int = 1000, tmax: int = 1_000_000
         out.append(BatchInstance(T=T, K=K, epssqr=eps, sigma=sigma, levels=levels, data=s.data,
                                  clean=s.clean, gamma0=s.gamma0))
     return out
+
+
+def bf16_round(x: np.ndarray) -> np.ndarray:
+    """FP64 values rounded to the nearest BF16 value (ties to even), returned as FP64: the
+    rounding the device applies to multichannel data (one rounding from FP64, no FP32 step)."""
+    x = np.asarray(x, dtype=np.float64)
+    f, e = np.frexp(x)  # |x| = |f| 2^e, |f| in [0.5, 1)
+    ulp_exp = e - 8     # BF16 keeps 8 significant bits
+    return np.ldexp(np.round(np.ldexp(x, -ulp_exp)), ulp_exp)
+
+
+@dataclass
+class Multichannel:
+    T: int
+    n: int
+    K: int
+    data: np.ndarray       # T*n row-major, BF16-representable values
+    centroids: np.ndarray  # K*n
+    labels: np.ndarray     # T
+    gamma0: np.ndarray     # K*T, uniform [0,1) in blocked order
+    epssqr: float = 50.0
+
+
+def multichannel(T: int = 1_000_000, n: int = 128, K: int = 8, seed: int = 2, stay: float = 0.999,
+                 sigma: float = 0.8, epssqr: float = 50.0) -> Multichannel:
+    centroids = normal(seed, 1, K * n)
+    jump = uniform(seed, 2, T) >= stay
+    jump[0] = False
+    step = randint(seed, 3, T, 1, K - 1) * jump
+    labels = ((randint(seed, 6, 1, 0, K - 1)[0] + np.cumsum(step)) % K).astype(np.int32)
+    data = centroids.reshape(K, n)[labels].ravel() + sigma * normal(seed, 4, T * n)
+    return Multichannel(T=T, n=n, K=K, data=bf16_round(data), centroids=centroids, labels=labels,
+                        gamma0=uniform(seed, 5, K * T), epssqr=epssqr)

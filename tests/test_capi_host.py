@@ -61,7 +61,9 @@ def test_argument_errors_without_device(lib):
     assert lib.pasc_gb300_create(C.byref(h), 0, 3, 1, 1, 1.0, 0) == capi.PASC_ERR_ARG
     assert b"T must be" in lib.pasc_gb300_last_error()
     assert lib.pasc_gb300_create(C.byref(h), 100, 9, 1, 1, 1.0, 0) == capi.PASC_ERR_ARG
-    assert lib.pasc_gb300_create(C.byref(h), 100, 3, 2, 1, 1.0, 0) == capi.PASC_ERR_NOTSUPP
+    assert lib.pasc_gb300_create(C.byref(h), 100, 3, 2, 0, 1.0, 0) == capi.PASC_ERR_NOTSUPP  # multichannel fp64
+    assert lib.pasc_gb300_create(C.byref(h), 100, 3, 300, 1, 1.0, 0) == capi.PASC_ERR_NOTSUPP  # xdim > 256
+    assert lib.pasc_gb300_create(C.byref(h), 100, 3, 0, 1, 1.0, 0) == capi.PASC_ERR_ARG
     assert lib.pasc_gb300_destroy(None) == capi.PASC_OK
     assert lib.pasc_gb300_spgqp_solve(None, None, None) == capi.PASC_ERR_ARG
 
