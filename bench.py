@@ -431,13 +431,18 @@ def measure_multichannel(dev, peak):
         kernels["theta_update"] = {"us": ms * 1e3, "bytes": B_th, "achieved": B_th / (ms * 1e-3) / 1e9, "unit": "GB/s",
                                    "frac": B_th / (ms * 1e-3) / 1e9 / peak}
         p.update_b()
-        p.spgqp_start(capi.spgqp_opts(m=10, maxit=100000, stop_difff=0))
-        p.spgqp_iterate(20, poll=False)
-        p.spgqp_iterate(200, poll=False)
-        ms, nl = p.spgqp_last_iterate()
+        chosen = p.get_sweep_variant()
+        res["tssolver"]["sweep_kernel_chosen"] = chosen
         B_sw = 12.0 * K * T  # x read, b read, x written (FP32)
-        kernels["spg_sweep_bmat"] = {"us": ms / nl * 1e3, "bytes": B_sw, "achieved": B_sw / (ms / nl * 1e-3) / 1e9,
-                                     "unit": "GB/s", "frac": B_sw / (ms / nl * 1e-3) / 1e9 / peak}
+        for v, name in ((0, "spg_sweep_bmat_thread_per_timestep"), (1, "spg_sweep_bmat_bulk_copy")):
+            p.set_sweep_variant(v)
+            p.spgqp_start(capi.spgqp_opts(m=10, maxit=100000, stop_difff=0))
+            p.spgqp_iterate(20, poll=False)
+            p.spgqp_iterate(200, poll=False)
+            ms, nl = p.spgqp_last_iterate()
+            kernels[name] = {"us": ms / nl * 1e3, "bytes": B_sw, "achieved": B_sw / (ms / nl * 1e-3) / 1e9,
+                             "unit": "GB/s", "frac": B_sw / (ms / nl * 1e-3) / 1e9 / peak}
+        p.set_sweep_variant(chosen)
         res["kernels"] = kernels
         th = p.get_theta()
         g = p.get_gamma()

@@ -116,7 +116,7 @@ cudaError_t launch_mc_residual_simt(int K, int grid, const McArgs &a, cudaStream
 // gamma != null: theta from gamma (partial kernel on `grid` blocks + per-cluster finish);
 // gamma == null: only the preparation of the current theta64 (split, FP32 copy, norms)
 cudaError_t launch_mc_theta(int K, int grid, const McArgs &a, const float *gamma, cudaStream_t s);
-size_t mc_partials_size(int K, int n, int grid);
+size_t mc_partials_size(int K, int n, int grid, long T);
 
 int batch_tile_width();
 int batch_segment_timesteps();
@@ -137,7 +137,7 @@ cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStr
 bool sweep_tma_supported(int K);
 int sweep_tma_tile_width();
 int sweep_tma_max_tile();
-int sweep_tma_blocks_per_sm(int K, bool init);
+int sweep_tma_blocks_per_sm(int K, bool init, bool bmat = false);  // bmat: the materialised-b form
 cudaError_t launch_sweep_tma(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);
 cudaError_t launch_theta_f32(int K, int grid, const ThetaArgs &a, cudaStream_t s);
 cudaError_t launch_project_f32(float *x, long T, int K, cudaStream_t s);

@@ -30,6 +30,47 @@
 
 namespace pasc {
 
+// K consecutive floats of one timestep: 16-byte loads when K % 4 == 0, 8-byte when K % 2 == 0
+// (the buffers are 16-byte aligned and t*K*4 bytes keeps that alignment).  STREAM: evict-first.
+template <int K, bool STREAM>
+__device__ __forceinline__ void load_row(const float *p, float (&v)[K])
+{
+    if (K % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < K / 4; q++) {
+            const float4 w = STREAM ? __ldcs(reinterpret_cast<const float4 *>(p) + q)
+                                    : __ldg(reinterpret_cast<const float4 *>(p) + q);
+            v[4 * q] = w.x; v[4 * q + 1] = w.y; v[4 * q + 2] = w.z; v[4 * q + 3] = w.w;
+        }
+    } else if (K % 2 == 0) {
+#pragma unroll
+        for (int q = 0; q < K / 2; q++) {
+            const float2 w = STREAM ? __ldcs(reinterpret_cast<const float2 *>(p) + q)
+                                    : __ldg(reinterpret_cast<const float2 *>(p) + q);
+            v[2 * q] = w.x; v[2 * q + 1] = w.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = STREAM ? __ldcs(p + k) : __ldg(p + k);
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void store_row(float *p, const float (&v)[K])
+{
+    if (K % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < K / 4; q++)
+            __stcs(reinterpret_cast<float4 *>(p) + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
+    } else if (K % 2 == 0) {
+#pragma unroll
+        for (int q = 0; q < K / 2; q++) __stcs(reinterpret_cast<float2 *>(p) + q, make_float2(v[2 * q], v[2 * q + 1]));
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; k++) __stcs(p + k, v[k]);
+    }
+}
+
 constexpr int SWEEP_NT = 256;  // threads per block = timesteps per tile incl. halo
 constexpr int SWEEP_HL = 2;    // halo timesteps before the owned range
 constexpr int SWEEP_HR = 3;    // halo timesteps after it
@@ -72,17 +113,20 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
     const int ntiles = (T + SWEEP_W - 1) / SWEEP_W;
 
     // the next tile's x and data are loaded into registers while the current one is computed
-    float xn[K], dvn = 0.f, bn[BMAT ? K : 1];
+    float xn[K], dvn = 0.f, bn[K];
     {
         const int t = blockIdx.x * SWEEP_W - SWEEP_HL + i;
         const bool in = (int)blockIdx.x < ntiles && (unsigned)t < (unsigned)T;
+        if (in) {
+            load_row<K, true>(xin + t * K, xn);
+            if (BMAT) load_row<K, false>(a.bmat + t * K, bn);
+            else dvn = __ldg(a.data + t);
+        } else {
 #pragma unroll
-        for (int k = 0; k < K; k++) xn[k] = in ? __ldcs(xin + t * K + k) : 0.f;
-        if (BMAT) {
-#pragma unroll
-            for (int k = 0; k < K; k++) bn[k] = in ? __ldg(a.bmat + t * K + k) : 0.f;
-        } else if (in) {
-            dvn = __ldg(a.data + t);
+            for (int k = 0; k < K; k++) {
+                xn[k] = 0.f;
+                bn[k] = 0.f;
+            }
         }
     }
 
@@ -100,18 +144,22 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
 #pragma unroll
         for (int k = 0; k < K; k++) {
             xc[k] = xn[k];
-            if (BMAT) bk[k] = bn[BMAT ? k : 0];
+            if (BMAT) bk[k] = bn[k];
         }
         {
             const int tn = t + (int)gridDim.x * SWEEP_W;
             const bool inn = tile + (int)gridDim.x < ntiles && (unsigned)tn < (unsigned)T;
-#pragma unroll
-            for (int k = 0; k < K; k++) xn[k] = inn ? __ldcs(xin + tn * K + k) : 0.f;
-            if (BMAT) {
-#pragma unroll
-                for (int k = 0; k < K; k++) bn[BMAT ? k : 0] = inn ? __ldg(a.bmat + tn * K + k) : 0.f;
+            if (inn) {
+                load_row<K, true>(xin + tn * K, xn);
+                if (BMAT) load_row<K, false>(a.bmat + tn * K, bn);
+                else dvn = __ldg(a.data + tn);
             } else {
-                dvn = inn ? __ldg(a.data + tn) : 0.f;
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    xn[k] = 0.f;
+                    bn[k] = 0.f;
+                }
+                dvn = 0.f;
             }
         }
         if (INIT) project_reg<K>(xc);
@@ -180,8 +228,8 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
                 acc_gd += g1[k] * d1[k];
                 const float df = right ? s_d[ir + k] - d1[k] : 0.f;
                 acc_dAd += df * df;
-                __stcs(xout + t * K + k, x1[k]);
             }
+            store_row<K>(xout + t * K, x1);
         }
     }
 

@@ -425,6 +425,91 @@ __global__ void __launch_bounds__(MC_THETA_NT) mc_theta_partial_kernel(McArgs a,
         for (int k = 0; k < K; k++) P[K * n + k] = den[k];
 }
 
+// Vectorised form for n in {8, 16, 32, 64, 128, 256}: a thread owns 8 consecutive channels of a
+// row (one 16-byte load of BF16) and holds their K sums in FP32 over its 64 rows; TPR = n/8
+// threads share a row and a block of 256 threads covers MC_THETA_ROWS consecutive rows.
+// Clusters with gamma_tk == 0 contribute nothing and are skipped (near convergence most
+// timesteps sit at a vertex of the simplex, so this removes most of the multiply-adds).
+// Block sums: shuffles across the rows of a warp, then warps in a fixed order through shared
+// memory in FP64 (deterministic); one partial per block in the layout of the kernel above.
+constexpr int MC_THETA_VNT = 256;
+constexpr int MC_THETA_ROWS = 1024;
+
+template <int K, int TPR>
+__global__ void __launch_bounds__(MC_THETA_VNT, K >= 7 ? 1 : 2) mc_theta_partial_vec_kernel(McArgs a, const float *gamma)
+{
+    constexpr int RPB = MC_THETA_VNT / TPR;  // rows per step
+    constexpr int NW = MC_THETA_VNT / 32;
+    const int n = TPR * 8;
+    __shared__ double s_sum[TPR * 8 * K + K];
+    const int tid = threadIdx.x, c = tid % TPR, r0 = tid / TPR;
+    const long t0 = (long)blockIdx.x * MC_THETA_ROWS;
+    const long t1 = t0 + MC_THETA_ROWS < a.T ? t0 + MC_THETA_ROWS : a.T;
+    float acc[8][K], den[K];
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+#pragma unroll
+        for (int k = 0; k < K; k++) acc[q][k] = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; k++) den[k] = 0.f;
+#pragma unroll 2
+    for (long t = t0 + r0; t < t1; t += RPB) {
+        const uint4 xv = __ldcs(reinterpret_cast<const uint4 *>(a.xbf + t * n) + c);
+        float g[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) g[k] = __ldg(gamma + t * K + k);
+        float x[8];
+        const unsigned int w[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            x[2 * q] = __uint_as_float(w[q] << 16);
+            x[2 * q + 1] = __uint_as_float(w[q] & 0xFFFF0000u);
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            den[k] += g[k];
+            if (g[k] != 0.f) {
+#pragma unroll
+                for (int q = 0; q < 8; q++) acc[q][k] = fmaf(g[k], x[q], acc[q][k]);
+            }
+        }
+    }
+    // rows of a warp that share channel chunk c: lanes c, c + TPR, ...
+#pragma unroll
+    for (int off = TPR; off < 32; off <<= 1) {
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+#pragma unroll
+            for (int k = 0; k < K; k++) acc[q][k] += __shfl_xor_sync(0xffffffffu, acc[q][k], off);
+#pragma unroll
+        for (int k = 0; k < K; k++) den[k] += __shfl_xor_sync(0xffffffffu, den[k], off);
+    }
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int w = 0; w < NW; w++) {
+        if (warp == w && lane < TPR) {
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    double &dst = s_sum[k * n + c * 8 + q];
+                    dst = (w == 0 ? 0.0 : dst) + (double)acc[q][k];
+                }
+            if (c == 0)
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    double &dst = s_sum[K * n + k];
+                    dst = (w == 0 ? 0.0 : dst) + (double)den[k];
+                }
+        }
+        __syncthreads();
+    }
+    double *P = a.partials + (long)blockIdx.x * (K * n + K);
+    for (int i = tid; i < K * n + K; i += MC_THETA_VNT) P[i] = s_sum[i];
+}
+
+int mc_theta_vec_supported(int n) { return n == 8 || n == 16 || n == 32 || n == 64 || n == 128 || n == 256; }
+int mc_theta_vec_grid(long T) { return (int)((T + MC_THETA_ROWS - 1) / MC_THETA_ROWS); }
+
 // One block per cluster k (blockDim >= n, a multiple of 32).  from_partials: theta_k from the
 // partial sums of `nparts` blocks (summed in block order); otherwise theta64 as given.  Then:
 // the FP32 copy, the three BF16 parts (rows k, K + k, 2K + k of theta_split) and ||theta_k||^2.
@@ -473,7 +558,19 @@ template <int NKA, int K>
 static cudaError_t launch_theta_t(int grid, const McArgs &a, const float *gamma, cudaStream_t s)
 {
     const int nb = ((a.n + 31) / 32) * 32;
-    if (gamma) {
+    if (gamma && mc_theta_vec_supported(a.n)) {
+        const int g = mc_theta_vec_grid(a.T);
+        switch (a.n / 8) {
+            case 1: mc_theta_partial_vec_kernel<K, 1><<<g, MC_THETA_VNT, 0, s>>>(a, gamma); break;
+            case 2: mc_theta_partial_vec_kernel<K, 2><<<g, MC_THETA_VNT, 0, s>>>(a, gamma); break;
+            case 4: mc_theta_partial_vec_kernel<K, 4><<<g, MC_THETA_VNT, 0, s>>>(a, gamma); break;
+            case 8: mc_theta_partial_vec_kernel<K, 8><<<g, MC_THETA_VNT, 0, s>>>(a, gamma); break;
+            case 16: mc_theta_partial_vec_kernel<K, 16><<<g, MC_THETA_VNT, 0, s>>>(a, gamma); break;
+            case 32: mc_theta_partial_vec_kernel<K, 32><<<g, MC_THETA_VNT, 0, s>>>(a, gamma); break;
+            default: return cudaErrorInvalidValue;
+        }
+        mc_theta_prepare_kernel<K><<<K, nb, 0, s>>>(a, g, 1);
+    } else if (gamma) {
         if (a.n <= 128) mc_theta_partial_kernel<1, K><<<grid, MC_THETA_NT, 0, s>>>(a, gamma);
         else mc_theta_partial_kernel<2, K><<<grid, MC_THETA_NT, 0, s>>>(a, gamma);
         mc_theta_prepare_kernel<K><<<K, nb, 0, s>>>(a, grid, 1);
@@ -489,6 +586,10 @@ cudaError_t launch_mc_theta(int K, int grid, const McArgs &a, const float *gamma
     PASC_MC_K_SWITCH(K, 0, launch_theta_t, grid, a, gamma, s)
 }
 
-size_t mc_partials_size(int K, int n, int grid) { return (size_t)grid * (K * n + K); }
+size_t mc_partials_size(int K, int n, int grid, long T)
+{
+    const long g = mc_theta_vec_supported(n) && mc_theta_vec_grid(T) > grid ? mc_theta_vec_grid(T) : grid;
+    return (size_t)g * (K * n + K);
+}
 
 }  // namespace pasc

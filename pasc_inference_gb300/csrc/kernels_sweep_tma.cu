@@ -22,13 +22,13 @@
 
 namespace pasc {
 
-template <int K, int NT, bool INIT>
+template <int K, int NT, bool INIT, bool BM>
 __global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
 {
     constexpr int P = NT * TMA_R;
     constexpr int W = P - 2 * TMA_HALO;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    TmaSmem<K, NT> &sm = *reinterpret_cast<TmaSmem<K, NT> *>(smem_raw);
+    TmaSmem<K, NT, BM> &sm = *reinterpret_cast<TmaSmem<K, NT, BM> *>(smem_raw);
 
     SpgDevState *st = a.st;
     if (st->status != PASC_SPG_RUNNING) return;  // uniform across the grid
@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
     TileScalars<K> sc;
     sc.xin = cur ? a.xb1 : a.xb0;
     sc.xout = cur ? a.xb0 : a.xb1;
-    sc.data = a.data;
+    sc.data = BM ? a.bmat : a.data;
     sc.a0 = (float)st->alpha_prev;
     sc.beta = (float)st->beta;
     sc.a1 = (float)st->alpha_cur;
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
         }
         parity ^= 1u << s;
         const int next2 = tile + 2 * (int)gridDim.x;
-        tma_tile<K, K, NT, INIT>(sm, s, tile * W - TMA_HALO, sc, acc,
+        tma_tile<K, K, NT, INIT, BM>(sm, s, tile * W - TMA_HALO, sc, acc,
                                  next2 < ntiles ? next2 * W - TMA_HALO : TMA_NO_REFILL);
     }
 
@@ -107,20 +107,30 @@ static cudaError_t launch_tma_t(int grid, const SweepArgs &a, cudaStream_t s)
 {
     // the dynamic shared memory limit was raised by tma_blocks_per_sm_t at problem creation
     // (no attribute call here: launches may be inside a stream capture)
-    const size_t smem = sizeof(TmaSmem<K, NT>);
-    spg_sweep_tma_kernel<K, NT, INIT><<<grid, NT, smem, s>>>(a);
+    if (a.bmat) spg_sweep_tma_kernel<K, NT, INIT, true><<<grid, NT, sizeof(TmaSmem<K, NT, true>), s>>>(a);
+    else spg_sweep_tma_kernel<K, NT, INIT, false><<<grid, NT, sizeof(TmaSmem<K, NT, false>), s>>>(a);
     return cudaGetLastError();
 }
 
-template <int K, int NT, bool INIT>
-static int tma_blocks_per_sm_t()
+template <int K, int NT, bool INIT, bool BM>
+static int tma_blocks_per_sm_bm()
 {
-    const size_t smem = sizeof(TmaSmem<K, NT>);
-    cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const size_t smem = sizeof(TmaSmem<K, NT, BM>);
+    cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_tma_kernel<K, NT, INIT>, NT, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_tma_kernel<K, NT, INIT, BM>, NT, smem);
     return nb > 0 ? nb : 1;
+}
+
+// sets the shared-memory limit of both forms (data / materialised b); returns the occupancy
+// of the form `bm` selects
+template <int K, int NT, bool INIT>
+static int tma_blocks_per_sm_t(bool bm)
+{
+    const int n0 = tma_blocks_per_sm_bm<K, NT, INIT, false>();
+    const int n1 = tma_blocks_per_sm_bm<K, NT, INIT, true>();
+    return bm ? n1 : n0;
 }
 
 constexpr int TMA_NT = 128;
@@ -130,11 +140,11 @@ int sweep_tma_max_tile() { return TMA_NT * TMA_R; }
 
 bool sweep_tma_supported(int K) { return K >= 1 && K <= 8; }
 
-int sweep_tma_blocks_per_sm(int K, bool init)
+int sweep_tma_blocks_per_sm(int K, bool init, bool bmat)
 {
     switch (K) {
 #define PASC_CASE(KK) \
-    case KK: return init ? tma_blocks_per_sm_t<KK, TMA_NT, true>() : tma_blocks_per_sm_t<KK, TMA_NT, false>();
+    case KK: return init ? tma_blocks_per_sm_t<KK, TMA_NT, true>(bmat) : tma_blocks_per_sm_t<KK, TMA_NT, false>(bmat);
         PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
         PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
 #undef PASC_CASE

@@ -61,7 +61,7 @@ static void free_all(pasc_gb300_problem *p)
     if (p->chunk_graph) cudaGraphExecDestroy(p->chunk_graph);
     void *dev[] = {p->data64, p->theta64, p->stage64, p->red, p->red_out, p->labels_d, p->x, p->g,
                    p->d, p->Ad, p->b, p->data32_raw, p->theta32, p->xb_raw[0], p->xb_raw[1], p->st,
-                   p->partials, p->xbf, p->xnorm, p->bmat, p->theta_split, p->theta_f32, p->tnorm,
+                   p->partials, p->xbf, p->xnorm, p->bmat_raw, p->theta_split, p->theta_f32, p->tnorm,
                    p->mc_partials, p->mc_err};
     for (void *q : dev)
         if (q) cudaFree(q);
@@ -224,8 +224,8 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
         p->grid_sweep[0] = grid(sweep_blocks_per_sm(K, false), nt_thread);
         p->grid_sweep_init[0] = grid(sweep_blocks_per_sm(K, true), nt_thread);
         const long nt_tma = (T + sweep_tma_tile_width() - 1) / sweep_tma_tile_width();
-        p->grid_sweep[1] = grid(sweep_tma_blocks_per_sm(K, false), nt_tma);
-        p->grid_sweep_init[1] = grid(sweep_tma_blocks_per_sm(K, true), nt_tma);
+        p->grid_sweep[1] = grid(sweep_tma_blocks_per_sm(K, false, xdim > 1), nt_tma);
+        p->grid_sweep_init[1] = grid(sweep_tma_blocks_per_sm(K, true, xdim > 1), nt_tma);
         long gt = (long)p->sms * 4;
         long tb = (T + 255) / 256;
         p->grid_theta = (int)(gt < tb ? gt : tb);
@@ -244,19 +244,19 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
             long nt = (T + 127) / 128;
             p->mc_grid_res = (int)((long)p->sms < nt ? p->sms : nt);
             if ((rc = dalloc(&p->xbf, (size_t)T * xdim)) || (rc = dalloc(&p->xnorm, T)) ||
-                (rc = dalloc(&p->bmat, (size_t)T * K)) || (rc = dalloc(&p->theta_split, (size_t)32 * xdim)) ||
+                (rc = dalloc(&p->bmat_raw, nx)) || (rc = dalloc(&p->theta_split, (size_t)32 * xdim)) ||
                 (rc = dalloc(&p->theta_f32, (size_t)K * xdim)) || (rc = dalloc(&p->tnorm, K)) ||
                 (rc = dalloc(&p->mc_err, 1)) ||
-                (rc = dalloc(&p->mc_partials, mc_partials_size(K, xdim, p->mc_grid_theta))))
+                (rc = dalloc(&p->mc_partials, mc_partials_size(K, xdim, p->mc_grid_theta, T))))
                 return bail(rc);
             cudaMemset(p->xbf, 0, sizeof(unsigned short) * T * xdim);
             cudaMemset(p->xnorm, 0, sizeof(float) * T);
-            cudaMemset(p->bmat, 0, sizeof(float) * T * K);
+            cudaMemset(p->bmat_raw, 0, sizeof(float) * nx);
+            p->bmat = p->bmat_raw + (size_t)PAD_FRONT * K;
             cudaMemset(p->theta_split, 0, sizeof(unsigned short) * 32 * xdim);
             cudaMemset(p->theta_f32, 0, sizeof(float) * K * xdim);
             cudaMemset(p->tnorm, 0, sizeof(float) * K);
             cudaMemset(p->mc_err, 0, sizeof(int));
-            p->variant = 0;  // the bulk-copy sweep forms b from 1-D data only
             p->mc_engine = mc_tc_supported(xdim) ? 0 : 1;
             if (p->mc_engine == 0) {
                 cudaError_t e = mc_make_tmap(&p->mc_tmap, p->xbf, T, xdim);
@@ -1071,8 +1071,6 @@ int pasc_gb300_set_sweep_variant(pasc_gb300_problem *p, int variant)
     if (variant < -1 || variant > 1) return fail(PASC_ERR_ARG, "set_sweep_variant: variant must be -1, 0 or 1");
     if (p->precision != PASC_PREC_MIXED) return fail(PASC_ERR_STATE, "set_sweep_variant: mixed precision only");
     if (variant == 1 && !sweep_tma_supported(p->K)) return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: K not supported");
-    if (variant != 0 && p->xdim > 1)
-        return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: multichannel data runs the one-timestep-per-thread sweep");
     p->variant = variant;
     p->run.started = false;
     return PASC_OK;

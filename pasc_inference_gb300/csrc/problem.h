@@ -67,7 +67,8 @@ struct pasc_gb300_problem {
     // iteration by the residual kernel (kernels_mc.cu)
     unsigned short *xbf = nullptr;         // T*xdim
     float *xnorm = nullptr;                // T
-    float *bmat = nullptr;                 // T*K
+    float *bmat = nullptr;                 // T*K, past the front pad of bmat_raw
+    float *bmat_raw = nullptr;             // zero pads as the gamma buffers (bulk-copy tiles)
     unsigned short *theta_split = nullptr; // 32*xdim
     float *theta_f32 = nullptr;            // K*xdim
     float *tnorm = nullptr;                // K

@@ -75,12 +75,13 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned int 
     return false;
 }
 
-// Shared memory of a block, sized for up to KB clusters.
-template <int KB, int NT>
+// Shared memory of a block, sized for up to KB clusters.  BM: the stages carry the tile's b
+// (P*K values, materialised for multichannel data) instead of its data values.
+template <int KB, int NT, bool BM = false>
 struct TmaSmem {
     static constexpr int P = NT * TMA_R;
     alignas(16) float x[2][P * KB];  // gamma tile, two stages (stride K for K <= KB)
-    alignas(16) float dat[2][P];     // data tile, two stages
+    alignas(16) float dat[2][BM ? P * KB : P];  // data tile (BM: b tile), two stages
     float yl[NT * KB], yr[NT * KB];  // x^{c+1} of each thread's first / last timestep
     float dl[NT * KB];               // d_{c+2} of each thread's first timestep
     double red[4 * (NT / 32)];
@@ -96,7 +97,7 @@ struct TileScalars {
     int T;
     const float *xin;
     float *xout;
-    const float *data;
+    const float *data;  // BM: the materialised b (T*K, zero pads like gamma)
 };
 
 struct TileAcc {
@@ -105,21 +106,22 @@ struct TileAcc {
 };
 
 // Thread 0: bring the tile starting at timestep t0 into stage s.
-template <int K, int KB, int NT>
-__device__ __forceinline__ void tma_issue(TmaSmem<KB, NT> &sm, int s, const float *xin, const float *data, int t0)
+template <int K, int KB, int NT, bool BM>
+__device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM> &sm, int s, const float *xin, const float *data, int t0)
 {
     constexpr int P = NT * TMA_R;
-    const unsigned int bytes_x = P * K * sizeof(float), bytes_d = P * sizeof(float);
+    const unsigned int bytes_x = P * K * sizeof(float), bytes_d = (BM ? P * K : P) * sizeof(float);
     mbar_expect_tx(&sm.bar[s], bytes_x + bytes_d);
     bulk_g2s(sm.x[s], xin + (long)t0 * K, bytes_x, &sm.bar[s]);
-    bulk_g2s(sm.dat[s], data + t0, bytes_d, &sm.bar[s]);
+    bulk_g2s(sm.dat[s], data + (long)t0 * (BM ? K : 1), bytes_d, &sm.bar[s]);
 }
 
-// One tile whose stage s has arrived: phases A-D of the sweep.  After phase B (the stage's
-// last read) thread 0 refills stage s with the tile at refill_t0 unless it is TMA_NO_REFILL.
-// Contains three __syncthreads(); all threads of the block must call it.
-template <int K, int KB, int NT, bool INIT>
-__device__ __forceinline__ void tma_tile(TmaSmem<KB, NT> &sm, int s, int t0, const TileScalars<K> &sc,
+// One tile whose stage s has arrived: phases A-D of the sweep.  After the stage's last read
+// (phase B; phase C when b comes from the stage) thread 0 refills stage s with the tile at
+// refill_t0 unless it is TMA_NO_REFILL.  Contains three __syncthreads(); all threads of the
+// block must call it.
+template <int K, int KB, int NT, bool INIT, bool BM = false>
+__device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0, const TileScalars<K> &sc,
                                          TileAcc &acc, int refill_t0)
 {
     constexpr int R = TMA_R;
@@ -131,9 +133,12 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT> &sm, int s, int t0, con
 
     // phase A: this thread's 4 timesteps of x^c and data, plus the neighbours' edge values
     float xc[R][K], dv[R], xlft[K], xrgt[K];
-    {
+    const float *bt = &sm.dat[s][i * R * K];  // BM: this thread's R*K values of b
+    if (!BM) {
         const float4 d4 = *reinterpret_cast<const float4 *>(&sm.dat[s][i * R]);
         dv[0] = d4.x; dv[1] = d4.y; dv[2] = d4.z; dv[3] = d4.w;
+    }
+    {
         const float4 *src = reinterpret_cast<const float4 *>(&sm.x[s][i * R * K]);
 #pragma unroll
         for (int q = 0; q < K; q++) {
@@ -196,8 +201,14 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT> &sm, int s, int t0, con
                 const float left = r == 0 ? xlft[k] : xc[r > 0 ? r - 1 : 0][k];
                 const float right = r == R - 1 ? xrgt[k] : xc[r < R - 1 ? r + 1 : R - 1][k];
                 const float S = ml[r] * (xc[r][k] - left) + mr[r] * (xc[r][k] - right);
-                const float rr = dv[r] - sc.theta[k];
-                const float g = sc.coeff * S - sc.bscale * (rr * rr);
+                float bk;
+                if (BM) {
+                    bk = bt[r * K + k];
+                } else {
+                    const float rr = dv[r] - sc.theta[k];
+                    bk = sc.bscale * (rr * rr);
+                }
+                const float g = sc.coeff * S - bk;
                 z[k] = xc[r][k] - sc.a0 * g;
             }
             project_reg<K>(z);
@@ -213,7 +224,7 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT> &sm, int s, int t0, con
     __syncthreads();
 
     // the stage is free (phase A was its last reader): refill it
-    if (i == 0 && refill_t0 != TMA_NO_REFILL) {
+    if (!BM && i == 0 && refill_t0 != TMA_NO_REFILL) {
         fence_proxy_async_smem();
         tma_issue<K>(sm, s, sc.xin, sc.data, refill_t0);
     }
@@ -235,8 +246,13 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT> &sm, int s, int t0, con
                 const float left = r == 0 ? yl[k] : x1[r > 0 ? r - 1 : 0][k];
                 const float right = r == R - 1 ? yr[k] : x1[r < R - 1 ? r + 1 : R - 1][k];
                 const float S = ml[r] * (x1[r][k] - left) + mr[r] * (x1[r][k] - right);
-                const float rr = dv[r] - sc.theta[k];
-                const float bk = sc.bscale * (rr * rr);
+                float bk;
+                if (BM) {
+                    bk = bt[r * K + k];
+                } else {
+                    const float rr = dv[r] - sc.theta[k];
+                    bk = sc.bscale * (rr * rr);
+                }
                 g1[r][k] = sc.coeff * S - bk;
                 fpart += in[r] ? (g1[r][k] - bk) * x1[r][k] : 0.f;
                 d1[r][k] = x1[r][k] - sc.a1 * g1[r][k];
@@ -250,6 +266,11 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT> &sm, int s, int t0, con
 #pragma unroll
     for (int k = 0; k < K; k++) sm.dl[i * K + k] = d1[0][k];
     __syncthreads();
+    // BM: phase C was the stage's last reader
+    if (BM && i == 0 && refill_t0 != TMA_NO_REFILL) {
+        fence_proxy_async_smem();
+        tma_issue<K>(sm, s, sc.xin, sc.data, refill_t0);
+    }
 
     // phase D: dots of d_{c+2} and the store of x^{c+1}
     if (owner) {

@@ -59,12 +59,17 @@ def test_adjoint_matches_oracle_on_same_gamma(gpulib, oracle, T, K, eps2, prec):
 
 
 def test_adjoint_end_to_end_mixed_vs_oracle(gpulib, oracle):
-    """Solve on the GPU (mixed path, tight) and differentiate, against the oracle's FP64 solve
-    and adjoint from the same inputs."""
+    """Solve on the GPU (mixed path, run to FP32 stagnation) and differentiate, against the
+    oracle's FP64 solve (converged to ||d||^2 < 1e-28) and adjoint from the same inputs.  The
+    gradient jumps where the free set changes: an oracle solve stopped at |f - f_old| < 1e-14
+    (f within 2e-10 of the optimum) keeps one extra free entry and moves d loss/d epssqr by 1%,
+    so both solves must reach the fixed point."""
     T, K, eps2 = 20000, 3, 50.0
     sig = _signal(T, K, 5)
     theta = np.array([0.0, 1.0, 2.0])
-    x = _converged(oracle, sig, theta, eps2)
+    b = oracle.residual_b(sig.data, theta, T, K)
+    x, _, _ = oracle.spgqp_solve(b, oracle.project(sig.gamma0.copy(), T, K), T, K, oracle.A_coeff(eps2, T),
+                                 oracle.spg_opts(m=10, eps=1e-28, maxit=60000, stop_difff=0, stop_normgp=1))
     _, dg, dth_direct = oracle.recon_mse(x, theta, sig.clean, T, K)
     deps_o, dX_o, dth_o, _, _ = oracle.adjoint(x, sig.data, theta, dg, T, K, eps2)
     with Problem(T, K, eps2, precision=PASC_PREC_MIXED) as p:
@@ -73,7 +78,7 @@ def test_adjoint_end_to_end_mixed_vs_oracle(gpulib, oracle):
         p.set_gamma(sig.gamma0)
         p.permute_gamma()
         p.update_b()
-        p.spgqp_solve(capi.spgqp_opts(m=10, eps=1e-13, maxit=20000))
+        p.spgqp_solve(capi.spgqp_opts(m=10, maxit=3000, stop_difff=0))
         p.recon_mse(sig.clean)
         deps, dX, dth, st = p.adjoint()
     assert _rel(deps, deps_o) <= 1e-4, (deps, deps_o)

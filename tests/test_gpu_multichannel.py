@@ -56,9 +56,10 @@ def test_theta_update_matches_fp64(gpulib, oracle, T, n, K):
     assert _scale_rel(th, th_o) <= 5e-6, _scale_rel(th, th_o)
 
 
+@pytest.mark.parametrize("variant", [0, 1])
 @pytest.mark.parametrize("T,n,K,eps2,stay", [(4000, 64, 4, 50.0, 0.99), (3000, 128, 8, 50.0, 0.995),
                                              (2500, 48, 3, 20.0, 0.99)])
-def test_tssolver_tight_vs_oracle(gpulib, oracle, T, n, K, eps2, stay):
+def test_tssolver_tight_vs_oracle(gpulib, oracle, T, n, K, eps2, stay, variant):
     """From a uniform random gamma0 the first theta step makes the K centroids nearly equal,
     and (as in K-means) which fixed point the alternating loop then reaches depends on
     rounding; parity is checked from an informative start (true labels weighted 1 plus
@@ -71,6 +72,7 @@ def test_tssolver_tight_vs_oracle(gpulib, oracle, T, n, K, eps2, stay):
                                               ts=oracle.ts_opts(maxit=300, eps=1e-13),
                                               spg=oracle.spg_opts(m=10, eps=1e-13, maxit=20000))
     with Problem(T, K, eps2, precision=PASC_PREC_MIXED, xdim=n) as p:
+        p.set_sweep_variant(variant)  # both sweep kernels read the materialised b
         p.set_data(mc.data)
         p.set_gamma(mc.gamma0)
         p.set_theta(np.zeros(K * n))
@@ -109,8 +111,6 @@ def test_multichannel_argument_errors(gpulib):
     with Problem(100, 3, 1.0, precision=PASC_PREC_MIXED, xdim=48) as p:
         with pytest.raises(capi.PascError):
             p.set_residual_engine(0)  # tensor cores need xdim in {64, 128, 256}
-        with pytest.raises(capi.PascError):
-            p.set_sweep_variant(1)
         with pytest.raises(capi.PascError):
             p.abserr_reconstructed(np.zeros(100))
     with Problem(100, 3, 1.0, precision=PASC_PREC_MIXED) as p:

@@ -197,7 +197,9 @@ def test_bad_arguments(gpulib):
     with pytest.raises(capi.PascError):
         Problem(100, 9, precision=PASC_PREC_MIXED)
     with pytest.raises(capi.PascError):
-        Problem(100, 3, xdim=2)
+        Problem(100, 3, xdim=2, precision=PASC_PREC_FP64)  # multichannel data: mixed path only
+    with pytest.raises(capi.PascError):
+        Problem(100, 3, xdim=300)
     with Problem(10, 2) as p:
         with pytest.raises(capi.PascError):
             p.spgqp_solve(capi.spgqp_opts(m=0))
