@@ -42,9 +42,15 @@ __device__ __forceinline__ void spg_finish_sweep(SpgDevState *st, int cur, const
         st->fs[li] = fnew;
         st->fs_last = li;
         if (!isfinite(fnew)) { st->status = PASC_SPG_NONFINITE; return; }
-        // stopping tests of iteration it on the direction it applied (:260-274)
+        // stopping tests of iteration it on the direction it applied (:260-274).  f - f_old
+        // is taken in the incremental form f(x + beta d) - f(x) = beta g'd + beta^2 d'Ad / 2
+        // (SPGQPSolver::get_fx(fx_old, beta, gd, dAd), include/general/solver/
+        // spgqpsolver.h:809-842): equal in exact arithmetic, and free of the cancellation of
+        // two objectives summed from FP32 terms (their difference is resolved only to ~1e-7
+        // of f, far above the usual eps, so the explicit form would stop on rounding noise)
         const double ddo = st->dd, dAdo = st->dAd;
-        if ((st->stop_difff && fabs(st->fx - st->fx_old) < st->eps) ||
+        const double dfx = st->beta * st->gd + 0.5 * st->beta * st->beta * dAdo;
+        if ((st->stop_difff && fabs(dfx) < st->eps) ||
             (st->stop_normgp && ddo < st->eps) ||
             (st->stop_normgp_normb && ddo < st->eps * st->normb) ||
             (st->stop_Anormgp && dAdo < st->eps) ||

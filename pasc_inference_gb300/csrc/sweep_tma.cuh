@@ -116,13 +116,20 @@ __device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM> &sm, int s, const 
     bulk_g2s(sm.dat[s], data + (long)t0 * (BM ? K : 1), bytes_d, &sm.bar[s]);
 }
 
-// One tile whose stage s has arrived: phases A-D of the sweep.  After the stage's last read
-// (phase B; phase C when b comes from the stage) thread 0 refills stage s with the tile at
-// refill_t0 unless it is TMA_NO_REFILL.  Contains three __syncthreads(); all threads of the
-// block must call it.
-template <int K, int KB, int NT, bool INIT, bool BM = false>
-__device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0, const TileScalars<K> &sc,
-                                         TileAcc &acc, int refill_t0)
+// One tile whose stage s has arrived: phases A-D of the sweep.  After phase B (the stage's
+// last read: b values, when they come from the stage, are read into registers in phase A)
+// thread 0 refills stage s with the tile at refill_t0 unless it is TMA_NO_REFILL.  Contains
+// three __syncthreads(); all threads of the block must call it.
+//
+// The FEM-H1 row is formed from shared neighbour differences: with D_j = x_{tb+j} -
+// x_{tb+j-1} (zero when the pair crosses an end of the signal, t_j <= 0 or t_j > T-1),
+// (A_hat x)_r = 2 (D_r - D_{r+1}), which is bit for bit the difference form
+// 2[t>0](x_t - x_{t-1}) + 2[t<T-1](x_t - x_{t+1}) and needs one subtraction per neighbour
+// pair.  EDGE: the tile touches t <= 0 or t >= T-1 and needs the range masks; interior tiles
+// (all but the first and last of a signal) run without them.
+template <int K, int KB, int NT, bool INIT, bool BM, bool EDGE>
+__device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM> &sm, int s, int t0, const TileScalars<K> &sc,
+                                              TileAcc &acc, int refill_t0)
 {
     constexpr int R = TMA_R;
     const int i = threadIdx.x;
@@ -130,15 +137,24 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0,
     const bool owner = i >= 1 && i <= NT - 2;                        // owns its 4 timesteps
     const int T = sc.T;
     const int tb = t0 + i * R;  // first timestep of this thread
+    const float c2 = 2.f * sc.coeff;
 
-    // phase A: this thread's 4 timesteps of x^c and data, plus the neighbours' edge values
-    float xc[R][K], dv[R], xlft[K], xrgt[K];
-    const float *bt = &sm.dat[s][i * R * K];  // BM: this thread's R*K values of b
-    if (!BM) {
-        const float4 d4 = *reinterpret_cast<const float4 *>(&sm.dat[s][i * R]);
-        dv[0] = d4.x; dv[1] = d4.y; dv[2] = d4.z; dv[3] = d4.w;
-    }
+    // range masks: in[r] (0 <= t_r < T) and dm[j] (the pair (t_j - 1, t_j) lies in the signal)
+    bool in[R], dm[R + 1];
+#pragma unroll
+    for (int r = 0; r < R; r++) in[r] = EDGE ? (unsigned)(tb + r) < (unsigned)T : true;
+#pragma unroll
+    for (int j = 0; j <= R; j++) dm[j] = EDGE ? (unsigned)(tb + j - 1) < (unsigned)(T - 1) : true;
+
+    // phase A: this thread's 4 timesteps of x^c and b, plus the neighbours' edge values
+    float xc[R][K], bk[R][K], xlft[K], xrgt[K];
     {
+        const float *bt = &sm.dat[s][i * R * K];  // BM: this thread's R*K values of b
+        float dv[R];
+        if (!BM) {
+            const float4 d4 = *reinterpret_cast<const float4 *>(&sm.dat[s][i * R]);
+            dv[0] = d4.x; dv[1] = d4.y; dv[2] = d4.z; dv[3] = d4.w;
+        }
         const float4 *src = reinterpret_cast<const float4 *>(&sm.x[s][i * R * K]);
 #pragma unroll
         for (int q = 0; q < K; q++) {
@@ -154,15 +170,17 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0,
             xlft[k] = sm.x[s][(li * R + R - 1) * K + k];
             xrgt[k] = sm.x[s][(ri * R) * K + k];
         }
-    }
-    bool in[R];
-    float ml[R], mr[R];  // FEM-H1 row in difference form: 2[t>0](x_t-x_{t-1}) + 2[t<T-1](x_t-x_{t+1})
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-        const int t = tb + r;
-        in[r] = (unsigned)t < (unsigned)T;
-        ml[r] = t > 0 ? 2.f : 0.f;
-        mr[r] = t < T - 1 ? 2.f : 0.f;
+        for (int r = 0; r < R; r++)
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                if (BM) {
+                    bk[r][k] = bt[r * K + k];
+                } else {
+                    const float rr = dv[r] - sc.theta[k];
+                    bk[r][k] = sc.bscale * (rr * rr);
+                }
+            }
     }
     if (INIT) {
         // the start point is projected; its neighbours are projected the same way
@@ -171,12 +189,12 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0,
         project_reg<K>(xlft);
         project_reg<K>(xrgt);
     }
-    // zero outside the signal (the pads hold zeros; projection of a zero block does not)
+    if (EDGE) {
+        // zero outside the signal (the pads hold zeros; projection of a zero block does not)
 #pragma unroll
-    for (int r = 0; r < R; r++)
+        for (int r = 0; r < R; r++)
 #pragma unroll
-        for (int k = 0; k < K; k++) xc[r][k] = in[r] ? xc[r][k] : 0.f;
-    {
+            for (int k = 0; k < K; k++) xc[r][k] = in[r] ? xc[r][k] : 0.f;
         const bool inl = (unsigned)(tb - 1) < (unsigned)T, inr = (unsigned)(tb + R) < (unsigned)T;
 #pragma unroll
         for (int k = 0; k < K; k++) {
@@ -194,26 +212,28 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0,
             for (int k = 0; k < K; k++) x1[r][k] = xc[r][k];
     } else {
 #pragma unroll
+        for (int k = 0; k < K; k++) {
+            float D[R + 1];
+            D[0] = xc[0][k] - xlft[k];
+#pragma unroll
+            for (int r = 1; r < R; r++) D[r] = xc[r][k] - xc[r - 1][k];
+            D[R] = xrgt[k] - xc[R - 1][k];
+#pragma unroll
+            for (int j = 0; j <= R; j++) D[j] = dm[j] ? D[j] : 0.f;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const float g = fmaf(c2, D[r] - D[r + 1], -bk[r][k]);
+                x1[r][k] = fmaf(-sc.a0, g, xc[r][k]);  // z before the projection
+            }
+        }
+#pragma unroll
         for (int r = 0; r < R; r++) {
-            float z[K];
+            project_reg<K>(x1[r]);
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                const float left = r == 0 ? xlft[k] : xc[r > 0 ? r - 1 : 0][k];
-                const float right = r == R - 1 ? xrgt[k] : xc[r < R - 1 ? r + 1 : R - 1][k];
-                const float S = ml[r] * (xc[r][k] - left) + mr[r] * (xc[r][k] - right);
-                float bk;
-                if (BM) {
-                    bk = bt[r * K + k];
-                } else {
-                    const float rr = dv[r] - sc.theta[k];
-                    bk = sc.bscale * (rr * rr);
-                }
-                const float g = sc.coeff * S - bk;
-                z[k] = xc[r][k] - sc.a0 * g;
+                const float v = fmaf(sc.beta, x1[r][k] - xc[r][k], xc[r][k]);
+                x1[r][k] = in[r] ? v : 0.f;
             }
-            project_reg<K>(z);
-#pragma unroll
-            for (int k = 0; k < K; k++) x1[r][k] = in[r] ? xc[r][k] + sc.beta * (z[k] - xc[r][k]) : 0.f;
         }
     }
 #pragma unroll
@@ -224,7 +244,7 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0,
     __syncthreads();
 
     // the stage is free (phase A was its last reader): refill it
-    if (!BM && i == 0 && refill_t0 != TMA_NO_REFILL) {
+    if (i == 0 && refill_t0 != TMA_NO_REFILL) {
         fence_proxy_async_smem();
         tma_issue<K>(sm, s, sc.xin, sc.data, refill_t0);
     }
@@ -232,64 +252,51 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0,
     // phase C: g^{c+1}, objective, d_{c+2}
     float g1[R][K], d1[R][K];
     {
-        float yl[K], yr[K];
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            yl[k] = sm.yr[li * K + k];
-            yr[k] = sm.yl[ri * K + k];
-        }
         float fpart = 0.f;
 #pragma unroll
-        for (int r = 0; r < R; r++) {
+        for (int k = 0; k < K; k++) {
+            float E[R + 1];
+            E[0] = x1[0][k] - sm.yr[li * K + k];
 #pragma unroll
-            for (int k = 0; k < K; k++) {
-                const float left = r == 0 ? yl[k] : x1[r > 0 ? r - 1 : 0][k];
-                const float right = r == R - 1 ? yr[k] : x1[r < R - 1 ? r + 1 : R - 1][k];
-                const float S = ml[r] * (x1[r][k] - left) + mr[r] * (x1[r][k] - right);
-                float bk;
-                if (BM) {
-                    bk = bt[r * K + k];
-                } else {
-                    const float rr = dv[r] - sc.theta[k];
-                    bk = sc.bscale * (rr * rr);
-                }
-                g1[r][k] = sc.coeff * S - bk;
-                fpart += in[r] ? (g1[r][k] - bk) * x1[r][k] : 0.f;
-                d1[r][k] = x1[r][k] - sc.a1 * g1[r][k];
+            for (int r = 1; r < R; r++) E[r] = x1[r][k] - x1[r - 1][k];
+            E[R] = sm.yl[ri * K + k] - x1[R - 1][k];
+#pragma unroll
+            for (int j = 0; j <= R; j++) E[j] = dm[j] ? E[j] : 0.f;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                g1[r][k] = fmaf(c2, E[r] - E[r + 1], -bk[r][k]);
+                const float fk = (g1[r][k] - bk[r][k]) * x1[r][k];
+                fpart += in[r] ? fk : 0.f;
+                d1[r][k] = fmaf(-sc.a1, g1[r][k], x1[r][k]);
             }
+        }
+        if (owner) acc.f.add(fpart);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
             project_reg<K>(d1[r]);
 #pragma unroll
             for (int k = 0; k < K; k++) d1[r][k] = in[r] ? d1[r][k] - x1[r][k] : 0.f;
         }
-        if (owner) acc.f.add(fpart);
     }
 #pragma unroll
     for (int k = 0; k < K; k++) sm.dl[i * K + k] = d1[0][k];
     __syncthreads();
-    // BM: phase C was the stage's last reader
-    if (BM && i == 0 && refill_t0 != TMA_NO_REFILL) {
-        fence_proxy_async_smem();
-        tma_issue<K>(sm, s, sc.xin, sc.data, refill_t0);
-    }
 
     // phase D: dots of d_{c+2} and the store of x^{c+1}
     if (owner) {
-        float dnext[K];
 #pragma unroll
-        for (int k = 0; k < K; k++) dnext[k] = sm.dl[ri * K + k];
+        for (int k = 0; k < K; k++) {
+            const float dnext = sm.dl[ri * K + k];
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const bool pair = in[r] && (tb + r) < T - 1;
-#pragma unroll
-            for (int k = 0; k < K; k++) {
-                acc.dd += d1[r][k] * d1[r][k];
-                acc.gd += g1[r][k] * d1[r][k];
-                const float nb = r == R - 1 ? dnext[k] : d1[r < R - 1 ? r + 1 : R - 1][k];
-                const float df = pair ? nb - d1[r][k] : 0.f;
-                acc.dAd += df * df;
+            for (int r = 0; r < R; r++) {
+                acc.dd = fmaf(d1[r][k], d1[r][k], acc.dd);
+                acc.gd = fmaf(g1[r][k], d1[r][k], acc.gd);
+                const float nb = r == R - 1 ? dnext : d1[r < R - 1 ? r + 1 : R - 1][k];
+                const float df = dm[r + 1] ? nb - d1[r][k] : 0.f;  // pair (t_r, t_r + 1) inside
+                acc.dAd = fmaf(df, df, acc.dAd);
             }
         }
-        if (in[R - 1]) {
+        if (!EDGE || in[R - 1]) {
             // all four timesteps inside: 16-byte stores (tb is a multiple of 4)
             float4 *dst = reinterpret_cast<float4 *>(sc.xout + (long)tb * K);
 #pragma unroll
@@ -308,6 +315,15 @@ __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0,
     }
     // the neighbour arrays are rewritten by the next tile's phase B only after its own
     // __syncthreads-separated phase A, so no barrier is needed here
+}
+
+template <int K, int KB, int NT, bool INIT, bool BM = false>
+__device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0, const TileScalars<K> &sc,
+                                         TileAcc &acc, int refill_t0)
+{
+    constexpr int P = NT * TMA_R;
+    if (t0 >= 1 && t0 + P <= sc.T - 1) tma_tile_body<K, KB, NT, INIT, BM, false>(sm, s, t0, sc, acc, refill_t0);
+    else tma_tile_body<K, KB, NT, INIT, BM, true>(sm, s, t0, sc, acc, refill_t0);
 }
 
 }  // namespace pasc
