@@ -1,0 +1,485 @@
+// pasc_gb300.hpp -- header-only C++17 class surface over the C ABI of pasc_gb300.h, mirroring
+// the classes a PASC_inference driver builds (examples/test_signal1D/test_signal1D.cpp:188-288):
+//
+//   Decomposition(T, R, K, xdim, DDT_size)          include/general/common/decomposition.h:55
+//   Signal1DData(filename) / TSData                 include/general/data/{signal1Ddata,tsdata}.h
+//   GraphH1FEMModel(tsdata, epssqr)                 include/general/model/graphh1fem.h:75
+//   TSSolver(tsdata, annealing)                     include/general/solver/tssolver.h:80-104
+//   SPGQPSolver (TSSolver::get_gammasolver())       include/general/solver/spgqpsolver.h:118-151
+//
+// Options use the reference's console keys (spgqpsolver_maxit, tssolver_eps, ...).  Everything
+// computes on the GPU through libpasc_gb300.so; C ABI failures become pasc_gb300::Error
+// exceptions (the reference prints and continues, include/external/petscvector/algebra/
+// vector/petscvector.h:51).  Also: RAII handles Problem and Batch, PETSc binary vector I/O
+// (the format of the reference's data files) and the seeded uniform generator the Python
+// package uses for gamma0, so both front ends solve identical inputs.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../pasc_gb300.h"
+
+namespace pasc_gb300 {
+
+class Error : public std::runtime_error {
+public:
+    Error(int code, const std::string &msg)
+        : std::runtime_error("pasc_gb300 error " + std::to_string(code) + ": " + msg), code_(code) {}
+    int code() const { return code_; }
+
+private:
+    int code_;
+};
+
+inline void check(int rc)
+{
+    if (rc != PASC_OK) throw Error(rc, pasc_gb300_last_error());
+}
+
+using Options = std::map<std::string, double>;
+
+// ---------------------------------------------------------------------------------------
+// seeded uniforms: splitmix64 of (seed, stream, index), the top 53 bits scaled to [0, 1)
+// ---------------------------------------------------------------------------------------
+inline uint64_t splitmix64(uint64_t x)
+{
+    uint64_t z = x + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+inline std::vector<double> uniform(uint64_t seed, uint64_t stream, size_t n)
+{
+    const uint64_t key = splitmix64(splitmix64(seed) ^ stream);
+    std::vector<double> u(n);
+    for (size_t i = 0; i < n; i++)
+        u[i] = (double)(splitmix64((uint64_t)i * 0x9E3779B97F4A7C15ull + key) >> 11) * (1.0 / 9007199254740992.0);
+    return u;
+}
+
+// ---------------------------------------------------------------------------------------
+// PETSc binary vectors: int32 class id 1211214, int32 length, the values as big-endian FP64
+// (the files of examples/test_signal1D/data)
+// ---------------------------------------------------------------------------------------
+namespace detail {
+inline uint32_t be32(const unsigned char *p) { return (uint32_t)p[0] << 24 | (uint32_t)p[1] << 16 | (uint32_t)p[2] << 8 | p[3]; }
+inline void put_be32(unsigned char *p, uint32_t v)
+{
+    p[0] = (unsigned char)(v >> 24); p[1] = (unsigned char)(v >> 16); p[2] = (unsigned char)(v >> 8); p[3] = (unsigned char)v;
+}
+}  // namespace detail
+
+inline std::vector<double> load_vec(const std::string &path)
+{
+    std::unique_ptr<FILE, int (*)(FILE *)> f(std::fopen(path.c_str(), "rb"), &std::fclose);
+    if (!f) throw Error(PASC_ERR_ARG, "cannot open " + path);
+    unsigned char hdr[8];
+    if (std::fread(hdr, 1, 8, f.get()) != 8 || detail::be32(hdr) != 1211214u)
+        throw Error(PASC_ERR_ARG, path + ": not a PETSc binary vector");
+    const uint32_t n = detail::be32(hdr + 4);
+    std::vector<unsigned char> raw((size_t)n * 8);
+    if (std::fread(raw.data(), 1, raw.size(), f.get()) != raw.size()) throw Error(PASC_ERR_ARG, path + ": truncated");
+    std::vector<double> v(n);
+    for (uint32_t i = 0; i < n; i++) {
+        uint64_t b = 0;
+        for (int q = 0; q < 8; q++) b = b << 8 | raw[(size_t)i * 8 + q];
+        std::memcpy(&v[i], &b, 8);
+    }
+    return v;
+}
+
+inline void save_vec(const std::string &path, const std::vector<double> &v)
+{
+    std::unique_ptr<FILE, int (*)(FILE *)> f(std::fopen(path.c_str(), "wb"), &std::fclose);
+    if (!f) throw Error(PASC_ERR_ARG, "cannot write " + path);
+    std::vector<unsigned char> raw(8 + v.size() * 8);
+    detail::put_be32(raw.data(), 1211214u);
+    detail::put_be32(raw.data() + 4, (uint32_t)v.size());
+    for (size_t i = 0; i < v.size(); i++) {
+        uint64_t b;
+        std::memcpy(&b, &v[i], 8);
+        for (int q = 0; q < 8; q++) raw[8 + i * 8 + q] = (unsigned char)(b >> (56 - 8 * q));
+    }
+    if (std::fwrite(raw.data(), 1, raw.size(), f.get()) != raw.size()) throw Error(PASC_ERR_ARG, path + ": write failed");
+}
+
+// ---------------------------------------------------------------------------------------
+// RAII handles
+// ---------------------------------------------------------------------------------------
+class Problem {
+public:
+    Problem(long T, int K, double epssqr, int precision = PASC_PREC_MIXED, int xdim = 1, int device = 0)
+        : T_(T), K_(K), xdim_(xdim)
+    {
+        pasc_gb300_problem *p = nullptr;
+        check(pasc_gb300_create(&p, T, K, xdim, precision, epssqr, device));
+        h_.reset(p);
+    }
+    long T() const { return T_; }
+    int K() const { return K_; }
+    int xdim() const { return xdim_; }
+    pasc_gb300_problem *handle() const { return h_.get(); }
+
+    void set_epssqr(double e, bool scalef = true) { check(pasc_gb300_set_epssqr(h_.get(), e, scalef ? 1 : 0)); }
+    void set_data(const std::vector<double> &x) { need(x, (size_t)T_ * xdim_); check(pasc_gb300_set_data(h_.get(), x.data())); }
+    void set_gamma(const std::vector<double> &g) { need(g, (size_t)T_ * K_); check(pasc_gb300_set_gamma(h_.get(), g.data())); }
+    void set_theta(const std::vector<double> &t) { need(t, (size_t)K_ * xdim_); check(pasc_gb300_set_theta(h_.get(), t.data())); }
+    std::vector<double> get_gamma() const
+    {
+        std::vector<double> g((size_t)T_ * K_);
+        check(pasc_gb300_get_gamma(h_.get(), g.data()));
+        return g;
+    }
+    std::vector<double> get_theta() const
+    {
+        std::vector<double> t((size_t)K_ * xdim_);
+        check(pasc_gb300_get_theta(h_.get(), t.data()));
+        return t;
+    }
+    void permute_gamma() { check(pasc_gb300_permute_gamma(h_.get())); }
+    void update_theta() { check(pasc_gb300_update_theta(h_.get())); }
+    void update_b() { check(pasc_gb300_update_b(h_.get())); }
+    pasc_gb300_spgqp_stats spgqp_solve(const pasc_gb300_spgqp_opts &o)
+    {
+        pasc_gb300_spgqp_stats st;
+        check(pasc_gb300_spgqp_solve(h_.get(), &o, &st));
+        return st;
+    }
+    pasc_gb300_ts_stats ts_solve(const pasc_gb300_ts_opts &ts, const pasc_gb300_spgqp_opts &o,
+                                 const std::vector<double> *gamma_restart = nullptr)
+    {
+        pasc_gb300_ts_stats st;
+        check(pasc_gb300_ts_solve(h_.get(), &ts, &o, gamma_restart ? gamma_restart->data() : nullptr, &st));
+        return st;
+    }
+    double get_fx() const
+    {
+        double f;
+        check(pasc_gb300_get_fx(h_.get(), &f));
+        return f;
+    }
+    double abserr_reconstructed(const std::vector<double> &solution) const
+    {
+        need(solution, (size_t)T_);
+        double e;
+        check(pasc_gb300_abserr_reconstructed(h_.get(), solution.data(), &e));
+        return e;
+    }
+    std::vector<int> argmax_labels() const
+    {
+        std::vector<int> l((size_t)T_);
+        check(pasc_gb300_argmax_labels(h_.get(), l.data()));
+        return l;
+    }
+
+private:
+    struct Del {
+        void operator()(pasc_gb300_problem *p) const { pasc_gb300_destroy(p); }
+    };
+    static void need(const std::vector<double> &v, size_t n)
+    {
+        if (v.size() != n) throw Error(PASC_ERR_ARG, "expected " + std::to_string(n) + " values, got " + std::to_string(v.size()));
+    }
+    std::unique_ptr<pasc_gb300_problem, Del> h_;
+    long T_;
+    int K_, xdim_;
+};
+
+class Batch {
+public:
+    Batch(const std::vector<long> &T, const std::vector<int> &K, const std::vector<double> &epssqr, int device = 0)
+        : T_(T), K_(K)
+    {
+        if (T.size() != K.size() || T.size() != epssqr.size()) throw Error(PASC_ERR_ARG, "T, K and epssqr sizes differ");
+        pasc_gb300_batch *b = nullptr;
+        check(pasc_gb300_batch_create(&b, (int)T.size(), T.data(), K.data(), epssqr.data(), device));
+        h_.reset(b);
+    }
+    int size() const { return (int)T_.size(); }
+    void set_data(int i, const std::vector<double> &x) { check(pasc_gb300_batch_set_data(h_.get(), i, x.data())); }
+    void set_gamma(int i, const std::vector<double> &g) { check(pasc_gb300_batch_set_gamma(h_.get(), i, g.data())); }
+    void set_theta(int i, const std::vector<double> &t) { check(pasc_gb300_batch_set_theta(h_.get(), i, t.data())); }
+    std::vector<double> get_gamma(int i) const
+    {
+        std::vector<double> g((size_t)T_.at(i) * K_.at(i));
+        check(pasc_gb300_batch_get_gamma(h_.get(), i, g.data()));
+        return g;
+    }
+    std::vector<double> get_theta(int i) const
+    {
+        std::vector<double> t((size_t)K_.at(i));
+        check(pasc_gb300_batch_get_theta(h_.get(), i, t.data()));
+        return t;
+    }
+    std::vector<pasc_gb300_ts_stats> ts_solve(const pasc_gb300_ts_opts &ts, const pasc_gb300_spgqp_opts &o)
+    {
+        std::vector<pasc_gb300_ts_stats> st(T_.size());
+        check(pasc_gb300_batch_ts_solve(h_.get(), &ts, &o, st.data()));
+        return st;
+    }
+
+private:
+    struct Del {
+        void operator()(pasc_gb300_batch *b) const { pasc_gb300_batch_destroy(b); }
+    };
+    std::unique_ptr<pasc_gb300_batch, Del> h_;
+    std::vector<long> T_;
+    std::vector<int> K_;
+};
+
+// ---------------------------------------------------------------------------------------
+// options by the reference's console keys
+// ---------------------------------------------------------------------------------------
+inline pasc_gb300_spgqp_opts spgqp_opts_from(const Options &opt)
+{
+    pasc_gb300_spgqp_opts o;
+    pasc_gb300_spgqp_default_opts(&o);
+    for (const auto &kv : opt) {
+        const std::string &k = kv.first;
+        const double v = kv.second;
+        if (k == "spgqpsolver_maxit") o.maxit = (int)v;
+        else if (k == "spgqpsolver_eps") o.eps = v;
+        else if (k == "spgqpsolver_m") o.m = (int)v;
+        else if (k == "spgqpsolver_gamma") o.gamma = v;
+        else if (k == "spgqpsolver_sigma1") o.sigma1 = v;
+        else if (k == "spgqpsolver_sigma2") o.sigma2 = v;
+        else if (k == "spgqpsolver_alphainit") o.alphainit = v;
+        else if (k == "spgqpsolver_stop_difff") o.stop_difff = (int)v;
+        else if (k == "spgqpsolver_stop_normgp") o.stop_normgp = (int)v;
+        else if (k == "spgqpsolver_stop_normgp_normb") o.stop_normgp_normb = (int)v;
+        else if (k == "spgqpsolver_stop_Anormgp") o.stop_Anormgp = (int)v;
+        else if (k == "spgqpsolver_stop_Anormgp_normb") o.stop_Anormgp_normb = (int)v;
+    }
+    return o;
+}
+
+inline pasc_gb300_ts_opts ts_opts_from(const Options &opt)
+{
+    pasc_gb300_ts_opts o;
+    pasc_gb300_ts_default_opts(&o);
+    for (const auto &kv : opt) {
+        if (kv.first == "tssolver_maxit") o.maxit = (int)kv.second;
+        else if (kv.first == "tssolver_eps") o.eps = kv.second;
+        else if (kv.first == "tssolver_init_permute") o.init_permute = (int)kv.second;
+    }
+    return o;
+}
+
+// ---------------------------------------------------------------------------------------
+// the reference's classes on the path
+// ---------------------------------------------------------------------------------------
+class Decomposition {
+public:
+    // Decomposition<VectorBase>(T, R, K, xdim, DDT_size): one GPU, R = 1
+    Decomposition(long T, int R, int K, int xdim = 1, int DDT_size = 1) : T_(T), K_(K), xdim_(xdim)
+    {
+        if (R != 1) throw Error(PASC_ERR_NOTSUPP, "spatial graphs (R > 1) are not supported");
+        if (DDT_size != 1) throw Error(PASC_ERR_NOTSUPP, "one GPU per problem: DDT_size must be 1");
+    }
+    long get_T() const { return T_; }
+    int get_R() const { return 1; }
+    int get_K() const { return K_; }
+    int get_xdim() const { return xdim_; }
+
+private:
+    long T_;
+    int K_, xdim_;
+};
+
+class GraphH1FEMModel;
+
+class TSData {
+public:
+    TSData() = default;
+    explicit TSData(const std::vector<double> &data) : data_(data) {}
+    void set_decomposition(const Decomposition &d) { decomposition_ = std::make_shared<Decomposition>(d); }
+    const Decomposition &get_decomposition() const
+    {
+        if (!decomposition_) throw Error(PASC_ERR_STATE, "TSData: no decomposition set");
+        return *decomposition_;
+    }
+    long get_T() const { return get_decomposition().get_T(); }
+    int get_K() const { return get_decomposition().get_K(); }
+    int get_xdim() const { return get_decomposition().get_xdim(); }
+    const std::vector<double> &get_datavector() const { return data_; }
+    inline std::vector<double> get_gammavector() const;
+    inline std::vector<double> get_thetavector() const;
+    double get_aic() const { return aic_; }
+    void set_aic(double a) { aic_ = a; }
+    void set_model(GraphH1FEMModel *m) { model_ = m; }
+    GraphH1FEMModel *get_model() const { return model_; }
+    // TSData::load_gammavector: gamma0 in the blocked layout the reference writes, permuted
+    inline void load_gammavector(const std::vector<double> &gamma0);
+    // hard assignment gamma_tk = [k = argmax] (true argmax; the reference's cutgamma seeds its
+    // running maximum with the wrong entry, src/petscvector/data/tsdata.cpp:212)
+    inline void cutgamma();
+
+protected:
+    std::vector<double> data_;
+    std::shared_ptr<Decomposition> decomposition_;
+    GraphH1FEMModel *model_ = nullptr;
+    double aic_ = std::numeric_limits<double>::max();
+};
+
+class Signal1DData : public TSData {
+public:
+    explicit Signal1DData(const std::string &filename) : TSData(load_vec(filename)) {}
+    explicit Signal1DData(const std::vector<double> &data) : TSData(data) {}
+    long get_Tpreliminary() const { return (long)data_.size(); }
+    inline double compute_abserr_reconstructed(const std::vector<double> &solution) const;
+    // saveSignal1D: <prefix>_gamma.bin (blocked layout) and <prefix>_recovered.bin
+    inline void saveSignal1D(const std::string &prefix) const;
+};
+
+class GraphH1FEMModel {
+public:
+    // GraphH1FEMModel<VectorBase>(tsdata, epssqr): creates the GPU problem with gamma0 =
+    // uniform [0, 1) values (seed, stream 0) in the blocked layout, as set_random leaves it
+    GraphH1FEMModel(TSData &tsdata, double epssqr, int precision = PASC_PREC_MIXED, uint64_t seed = 13,
+                    int device = 0)
+        : tsdata_(tsdata), epssqr_(epssqr),
+          problem_(tsdata.get_T(), tsdata.get_K(), epssqr, precision, tsdata.get_xdim(), device)
+    {
+        const long T = tsdata.get_T();
+        const int K = tsdata.get_K();
+        problem_.set_data(tsdata.get_datavector());
+        problem_.set_gamma(uniform(seed, 0, (size_t)T * K));
+        problem_.set_theta(std::vector<double>((size_t)K * tsdata.get_xdim(), 0.0));
+        tsdata.set_model(this);
+    }
+    void set_epssqr(double e)
+    {
+        epssqr_ = e;
+        problem_.set_epssqr(e);
+    }
+    double get_epssqr() const { return epssqr_; }
+    double get_aic(double L) const { return 2.0 * std::log(L) + tsdata_.get_K(); }
+    std::string get_name() const { return "Graph-H1-FEM Time-Series Model"; }
+    Problem &problem() { return problem_; }
+    const Problem &problem() const { return problem_; }
+
+private:
+    TSData &tsdata_;
+    double epssqr_;
+    Problem problem_;
+};
+
+inline std::vector<double> TSData::get_gammavector() const
+{
+    if (!model_) throw Error(PASC_ERR_STATE, "TSData: no model");
+    return model_->problem().get_gamma();
+}
+inline std::vector<double> TSData::get_thetavector() const
+{
+    if (!model_) throw Error(PASC_ERR_STATE, "TSData: no model");
+    return model_->problem().get_theta();
+}
+inline void TSData::load_gammavector(const std::vector<double> &gamma0)
+{
+    if (!model_) throw Error(PASC_ERR_STATE, "TSData: no model");
+    model_->problem().set_gamma(gamma0);
+    model_->problem().permute_gamma();
+}
+inline void TSData::cutgamma()
+{
+    if (!model_) throw Error(PASC_ERR_STATE, "TSData: no model");
+    const std::vector<int> lab = model_->problem().argmax_labels();
+    const long T = get_T();
+    const int K = get_K();
+    std::vector<double> g((size_t)T * K, 0.0);
+    for (long t = 0; t < T; t++) g[(size_t)t * K + lab[t]] = 1.0;
+    model_->problem().set_gamma(g);
+}
+inline double Signal1DData::compute_abserr_reconstructed(const std::vector<double> &solution) const
+{
+    if (!model_) throw Error(PASC_ERR_STATE, "Signal1DData: no model");
+    return model_->problem().abserr_reconstructed(solution);
+}
+inline void Signal1DData::saveSignal1D(const std::string &prefix) const
+{
+    const long T = get_T();
+    const int K = get_K();
+    const std::vector<double> g = get_gammavector(), th = get_thetavector();
+    std::vector<double> blocked((size_t)T * K), rec((size_t)T, 0.0);
+    for (long t = 0; t < T; t++)
+        for (int k = 0; k < K; k++) {
+            blocked[(size_t)k * T + t] = g[(size_t)t * K + k];
+            rec[t] += g[(size_t)t * K + k] * th[k];
+        }
+    save_vec(prefix + "_gamma.bin", blocked);
+    save_vec(prefix + "_recovered.bin", rec);
+}
+
+class SPGQPSolver {
+public:
+    SPGQPSolver(GraphH1FEMModel &model, const Options &opt = {}) : model_(model), o_(spgqp_opts_from(opt)) {}
+    void solve()
+    {
+        last_ = model_.problem().spgqp_solve(o_);
+        it_sum_ += last_.it;
+        hessmult_sum_ += last_.hessmult;
+    }
+    double get_fx() const { return model_.problem().get_fx(); }
+    int get_it() const { return it_sum_; }
+    int get_hessmult() const { return hessmult_sum_; }
+    const pasc_gb300_spgqp_opts &opts() const { return o_; }
+    void add_it(int n) { it_sum_ += n; }
+
+private:
+    GraphH1FEMModel &model_;
+    pasc_gb300_spgqp_opts o_;
+    pasc_gb300_spgqp_stats last_{};
+    int it_sum_ = 0, hessmult_sum_ = 0;
+};
+
+class TSSolver {
+public:
+    TSSolver(TSData &tsdata, int annealing = 1, const Options &opt = {})
+        : tsdata_(tsdata), annealing_(annealing), opt_(opt), gammasolver_(model(tsdata), opt) {}
+    void set_solution_theta(const std::vector<double> &theta)
+    {
+        model(tsdata_).problem().set_theta(theta);
+        thetasolved_ = true;
+    }
+    void set_annealing(int a) { annealing_ = a; }
+    pasc_gb300_ts_stats solve(const std::vector<double> *gamma_restart = nullptr)
+    {
+        pasc_gb300_ts_opts ts = ts_opts_from(opt_);
+        ts.annealing = annealing_;
+        ts.thetasolved = thetasolved_ ? 1 : 0;
+        stats_ = model(tsdata_).problem().ts_solve(ts, gammasolver_.opts(), gamma_restart);
+        L_ = stats_.L;
+        gammasolver_.add_it(stats_.spg_it_sum);
+        tsdata_.set_aic(stats_.aic);
+        return stats_;
+    }
+    double get_L() const { return L_; }
+    SPGQPSolver &get_gammasolver() { return gammasolver_; }
+    const pasc_gb300_ts_stats &stats() const { return stats_; }
+
+private:
+    static GraphH1FEMModel &model(TSData &d)
+    {
+        if (!d.get_model()) throw Error(PASC_ERR_STATE, "TSSolver: the data has no model");
+        return *d.get_model();
+    }
+    TSData &tsdata_;
+    int annealing_;
+    Options opt_;
+    SPGQPSolver gammasolver_;
+    bool thetasolved_ = false;
+    double L_ = std::numeric_limits<double>::max();
+    pasc_gb300_ts_stats stats_{};
+};
+
+}  // namespace pasc_gb300

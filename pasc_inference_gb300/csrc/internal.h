@@ -106,6 +106,7 @@ struct McArgs {
     double *partials;               // theta-update partial sums
     float bscale;
     int *err;                       // set by a bounded wait that gave up
+    int theta_tma_grid;             // blocks of the bulk-copy theta kernel (0: not used)
 };
 cudaError_t launch_mc_convert(const double *x64, unsigned short *xbf, float *xnorm, long T, int n, cudaStream_t s);
 int mc_tc_supported(int n);
@@ -117,6 +118,7 @@ cudaError_t launch_mc_residual_simt(int K, int grid, const McArgs &a, cudaStream
 // gamma == null: only the preparation of the current theta64 (split, FP32 copy, norms)
 cudaError_t launch_mc_theta(int K, int grid, const McArgs &a, const float *gamma, cudaStream_t s);
 size_t mc_partials_size(int K, int n, int grid, long T);
+int mc_theta_tma_blocks_per_sm(int K, int n);  // 0: the bulk-copy theta kernel does not apply
 
 int batch_tile_width();
 int batch_segment_timesteps();

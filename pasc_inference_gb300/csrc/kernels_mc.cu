@@ -507,6 +507,222 @@ __global__ void __launch_bounds__(MC_THETA_VNT, K >= 7 ? 1 : 2) mc_theta_partial
     for (int i = tid; i < K * n + K; i += MC_THETA_VNT) P[i] = s_sum[i];
 }
 
+// Bulk-copy form (n in {8, ..., 256} as above): a block takes chunks of MC_TC_ROWS consecutive
+// rows; one thread copies each chunk's X rows (n BF16 per row, contiguous) and gamma rows
+// (K FP32 per row, contiguous; the gamma buffer's zero pads make every copy whole) into a
+// 3-stage shared-memory ring with cp.async.bulk, so the loads in flight live in shared
+// memory rather than registers.  A thread owns 4 channels of one row per step (8-byte shared
+// loads, conflict-free across a row) and sums in FP32 in two levels (per chunk, then over its
+// chunks); rows beyond T carry gamma = 0 from the pad and are skipped like any zero weight.
+// Every wait on a copy is bounded: a timeout sets the error word, the block waits once more
+// for its copies in flight and leaves without writing its partial.
+constexpr int MC_TC_ROWS = 64;
+constexpr int MC_TC_STAGES = 3;
+
+template <int K, int TPR>
+__host__ __device__ constexpr size_t mc_theta_tma_smem()
+{
+    return (size_t)MC_TC_STAGES * (MC_TC_ROWS * TPR * 4 * 2 + MC_TC_ROWS * K * 4) + (size_t)(TPR * 4 * K + K) * 8 +
+           MC_TC_STAGES * 8 + 128;
+}
+
+template <int K, int TPR>
+__global__ void __launch_bounds__(MC_THETA_VNT) mc_theta_tma_kernel(McArgs a, const float *gamma)
+{
+    constexpr int n = TPR * 4;                 // channels
+    constexpr int RPS = MC_THETA_VNT / TPR;    // rows per step
+    constexpr int NW = MC_THETA_VNT / 32;
+    constexpr int XB = MC_TC_ROWS * n * 2;     // bytes of a chunk's X rows
+    constexpr int GB = MC_TC_ROWS * K * 4;     // bytes of a chunk's gamma rows
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char *xs = smem_raw;
+    float *gs = reinterpret_cast<float *>(smem_raw + MC_TC_STAGES * XB);
+    double *s_sum = reinterpret_cast<double *>(smem_raw + MC_TC_STAGES * (XB + GB));
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(s_sum + n * K + K);
+
+    const int tid = threadIdx.x, c = tid % TPR, r0 = tid / TPR;
+    const long nchunks = (a.T + MC_TC_ROWS - 1) / MC_TC_ROWS;
+    if (tid == 0) {
+        for (int s = 0; s < MC_TC_STAGES; s++) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int s, long chunk) {
+        const long t0 = chunk * MC_TC_ROWS;
+        const long rows = a.T - t0 < MC_TC_ROWS ? a.T - t0 : MC_TC_ROWS;
+        const unsigned int xbytes = (unsigned int)(rows * n * 2);
+        mbar_expect_tx(&bar[s], xbytes + GB);
+        bulk_g2s(xs + s * XB, a.xbf + t0 * n, xbytes, &bar[s]);
+        bulk_g2s(gs + s * (GB / 4), gamma + t0 * K, GB, &bar[s]);
+    };
+    unsigned int inflight = 0u;
+    if (tid == 0) {
+        for (int s = 0; s < MC_TC_STAGES; s++) {
+            const long ch = blockIdx.x + (long)s * gridDim.x;
+            if (ch < nchunks) {
+                issue(s, ch);
+                inflight |= 1u << s;
+            }
+        }
+    }
+    float tot[4][K], dtot[K];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int k = 0; k < K; k++) tot[q][k] = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; k++) dtot[k] = 0.f;
+    unsigned int parity = 0u;
+    bool failed = false;
+    int j = 0;
+    for (long ch = blockIdx.x; ch < nchunks; ch += gridDim.x, j++) {
+        const int s = j % MC_TC_STAGES;
+        const bool ok = mbar_wait(&bar[s], (parity >> s) & 1u);
+        if (!__syncthreads_and(ok)) {
+            failed = true;
+            break;
+        }
+        parity ^= 1u << s;
+        if (tid == 0) inflight &= ~(1u << s);
+        const unsigned char *xc = xs + s * XB;
+        const float *gc = gs + s * (GB / 4);
+        float acc[4][K], den[K];
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int k = 0; k < K; k++) acc[q][k] = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; k++) den[k] = 0.f;
+#pragma unroll 4
+        for (int r = r0; r < MC_TC_ROWS; r += RPS) {
+            const uint2 xv = *reinterpret_cast<const uint2 *>(xc + (r * n + c * 4) * 2);
+            const float x[4] = {__uint_as_float(xv.x << 16), __uint_as_float(xv.x & 0xFFFF0000u),
+                                __uint_as_float(xv.y << 16), __uint_as_float(xv.y & 0xFFFF0000u)};
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float g = gc[r * K + k];
+                den[k] += g;
+                if (g != 0.f) {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) acc[q][k] = fmaf(g, x[q], acc[q][k]);
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int k = 0; k < K; k++) tot[q][k] += acc[q][k];
+#pragma unroll
+        for (int k = 0; k < K; k++) dtot[k] += den[k];
+        __syncthreads();  // every thread is done with stage s
+        if (tid == 0) {
+            const long nx = ch + (long)MC_TC_STAGES * gridDim.x;
+            if (nx < nchunks) {
+                fence_proxy_async_smem();
+                issue(s, nx);
+                inflight |= 1u << s;
+            }
+        }
+    }
+    if (failed) {
+        if (tid == 0) {
+            atomicExch(a.err, 3);
+            for (int s = 0; s < MC_TC_STAGES; s++)
+                if (inflight & (1u << s)) mbar_wait(&bar[s], (parity >> s) & 1u);
+        }
+        return;
+    }
+    // rows of a warp that share channel chunk c, then warps in a fixed order (FP64)
+#pragma unroll
+    for (int off = TPR; off < 32; off <<= 1) {
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int k = 0; k < K; k++) tot[q][k] += __shfl_xor_sync(0xffffffffu, tot[q][k], off);
+#pragma unroll
+        for (int k = 0; k < K; k++) dtot[k] += __shfl_xor_sync(0xffffffffu, dtot[k], off);
+    }
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int w = 0; w < NW; w++) {
+        if (warp == w && lane < TPR) {
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    double &dst = s_sum[k * n + c * 4 + q];
+                    dst = (w == 0 ? 0.0 : dst) + (double)tot[q][k];
+                }
+            if (c == 0)
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    double &dst = s_sum[K * n + k];
+                    dst = (w == 0 ? 0.0 : dst) + (double)dtot[k];
+                }
+        }
+        __syncthreads();
+    }
+    double *P = a.partials + (long)blockIdx.x * (K * n + K);
+    for (int i = tid; i < K * n + K; i += MC_THETA_VNT) P[i] = s_sum[i];
+}
+
+#define PASC_MC_TPR_SWITCH_R(r, n, FN, ...)                      \
+    switch ((n) / 4) {                                           \
+        case 2: r = FN<2>(__VA_ARGS__); break;                   \
+        case 4: r = FN<4>(__VA_ARGS__); break;                   \
+        case 8: r = FN<8>(__VA_ARGS__); break;                   \
+        case 16: r = FN<16>(__VA_ARGS__); break;                 \
+        case 32: r = FN<32>(__VA_ARGS__); break;                 \
+        case 64: r = FN<64>(__VA_ARGS__); break;                 \
+        default: r = -1; break;                                  \
+    }
+
+#define PASC_MC_TPR_SWITCH(n, FN, ...)                           \
+    switch ((n) / 4) {                                           \
+        case 2: return FN<2>(__VA_ARGS__);                       \
+        case 4: return FN<4>(__VA_ARGS__);                       \
+        case 8: return FN<8>(__VA_ARGS__);                       \
+        case 16: return FN<16>(__VA_ARGS__);                     \
+        case 32: return FN<32>(__VA_ARGS__);                     \
+        case 64: return FN<64>(__VA_ARGS__);                     \
+        default: return -1;                                      \
+    }
+
+template <int K>
+struct ThetaTma {
+    template <int TPR>
+    static int blocks()
+    {
+        const size_t smem = mc_theta_tma_smem<K, TPR>();
+        if (cudaFuncSetAttribute(mc_theta_tma_kernel<K, TPR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return -1;
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mc_theta_tma_kernel<K, TPR>, MC_THETA_VNT, smem);
+        return nb;
+    }
+    template <int TPR>
+    static int launch(int grid, const McArgs &a, const float *gamma, cudaStream_t s)
+    {
+        mc_theta_tma_kernel<K, TPR><<<grid, MC_THETA_VNT, mc_theta_tma_smem<K, TPR>(), s>>>(a, gamma);
+        return 0;
+    }
+};
+
+// blocks per SM of the bulk-copy theta kernel (sets its shared-memory limit); 0: not available
+int mc_theta_tma_blocks_per_sm(int K, int n)
+{
+    int r = -1;
+    switch (K) {
+#define PASC_CASE(KK) \
+    case KK: r = [&]() -> int { PASC_MC_TPR_SWITCH(n, ThetaTma<KK>::template blocks) }(); break;
+        PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
+        PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
+#undef PASC_CASE
+        default: break;
+    }
+    return r > 0 ? r : 0;
+}
+
 int mc_theta_vec_supported(int n) { return n == 8 || n == 16 || n == 32 || n == 64 || n == 128 || n == 256; }
 int mc_theta_vec_grid(long T) { return (int)((T + MC_THETA_ROWS - 1) / MC_THETA_ROWS); }
 
@@ -558,7 +774,12 @@ template <int NKA, int K>
 static cudaError_t launch_theta_t(int grid, const McArgs &a, const float *gamma, cudaStream_t s)
 {
     const int nb = ((a.n + 31) / 32) * 32;
-    if (gamma && mc_theta_vec_supported(a.n)) {
+    if (gamma && a.theta_tma_grid > 0) {
+        int r = -1;
+        PASC_MC_TPR_SWITCH_R(r, a.n, ThetaTma<K>::template launch, a.theta_tma_grid, a, gamma, s)
+        if (r < 0) return cudaErrorInvalidValue;
+        mc_theta_prepare_kernel<K><<<K, nb, 0, s>>>(a, a.theta_tma_grid, 1);
+    } else if (gamma && mc_theta_vec_supported(a.n)) {
         const int g = mc_theta_vec_grid(a.T);
         switch (a.n / 8) {
             case 1: mc_theta_partial_vec_kernel<K, 1><<<g, MC_THETA_VNT, 0, s>>>(a, gamma); break;
@@ -589,7 +810,7 @@ cudaError_t launch_mc_theta(int K, int grid, const McArgs &a, const float *gamma
 size_t mc_partials_size(int K, int n, int grid, long T)
 {
     const long g = mc_theta_vec_supported(n) && mc_theta_vec_grid(T) > grid ? mc_theta_vec_grid(T) : grid;
-    return (size_t)g * (K * n + K);
+    return (size_t)g * (K * n + K);  // the bulk-copy kernel runs at most `grid` blocks
 }
 
 }  // namespace pasc

@@ -241,6 +241,12 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
             long gm = (long)p->sms * 4, tb64 = (T + 63) / 64;
             p->mc_grid_theta = (int)(gm < tb64 ? gm : tb64);
             if (p->mc_grid_theta < 1) p->mc_grid_theta = 1;
+            const int tb_sm = mc_theta_tma_blocks_per_sm(K, xdim);
+            if (tb_sm > 0) {
+                const long gt = (long)p->sms * tb_sm;
+                p->mc_grid_theta_tma = (int)(gt < tb64 ? gt : tb64);
+                if (p->mc_grid_theta_tma > p->mc_grid_theta) p->mc_grid_theta_tma = p->mc_grid_theta;
+            }
             long nt = (T + 127) / 128;
             p->mc_grid_res = (int)((long)p->sms < nt ? p->sms : nt);
             if ((rc = dalloc(&p->xbf, (size_t)T * xdim)) || (rc = dalloc(&p->xnorm, T)) ||
@@ -306,6 +312,7 @@ static McArgs mc_args(pasc_gb300_problem *p)
     a.partials = p->mc_partials;
     a.bscale = (float)p->coeffB;
     a.err = p->mc_err;
+    a.theta_tma_grid = p->mc_grid_theta_tma;
     return a;
 }
 

@@ -75,6 +75,7 @@ struct pasc_gb300_problem {
     double *mc_partials = nullptr;
     int *mc_err = nullptr;
     int mc_grid_theta = 0, mc_grid_res = 0;
+    int mc_grid_theta_tma = 0;             // blocks of the bulk-copy theta kernel (0: not used)
     int mc_engine = 0;                     // residual: 0 tensor cores (when xdim allows), 1 CUDA cores
     CUtensorMap mc_tmap;
 
