@@ -216,6 +216,17 @@ int pasc_gb300_time_model_kernels(pasc_gb300_problem *p, int which, int reps, do
  * formula evaluated in FP64 from the stored data and theta. */
 int pasc_gb300_get_b(pasc_gb300_problem *p, double *b);
 
+/* FEM temporal coarsening: GraphH1FEMModel(tsdata, epssqr, fem) with fem = Fem(fem_reduce)
+ * (fem_type 0, FEM-SUM, src/petscvector/common/fem.cpp) or FemHat(fem_reduce) (fem_type 1,
+ * FEM-HAT, src/petscvector/common/femhat.cpp); graphh1fem.cpp:48-59, 116-160, 237-303.  With
+ * fem_reduce < 1 the gamma QP is solved on T2 = ceil(T*fem_reduce) timesteps: update_b reduces
+ * the residual (scaled by -1/T2) and the current gamma onto the coarse grid, spgqp_solve solves
+ * there and prolongates the solution to the full gamma; theta, data, gamma and the TSSolver
+ * loop stay on the full grid.  fem_reduce = 1 removes the reduction.  A reduced problem solves
+ * with spgqp_solve / ts_solve (not spgqp_start / spgqp_iterate) and has no adjoint. */
+int pasc_gb300_set_fem(pasc_gb300_problem *p, double fem_reduce, int fem_type);
+int pasc_gb300_get_fem(pasc_gb300_problem *p, double *fem_reduce, int *fem_type, long *T_reduced);
+
 /* Residual kernel of multichannel data (xdim > 1): 0 = tensor cores (tcgen05, BF16 X and a
  * three-part BF16 theta, FP32 accumulation; xdim in {64, 128, 256}; the default there),
  * 1 = CUDA cores (FP32; any xdim, the default otherwise).  No reference counterpart: the
@@ -303,6 +314,16 @@ int pasc_gb300_fem_h1_matmult_f64(const double *x_dev, double *y_dev, long T, in
                                   double coeff, void *stream);
 int pasc_gb300_fem_h1_matmult_f32(const float *x_dev, float *y_dev, long T, int K,
                                   float coeff, void *stream);
+
+/* Fem::reduce_gamma / prolongate_gamma (src/petscvector/common/fem.cpp:32-190,
+ * femhat.cpp:27-215) on device buffers: g1 T1*K fine values, g2 T2*K coarse values
+ * (interleaved t*K + k), fem_type 0 FEM-SUM or 1 FEM-HAT (T2 >= 2).  The reference's CUDA
+ * versions of these two operations do not link (their kernels are declared under other names,
+ * fem.cu:8-9 vs :41,55); these follow its sequential code. */
+int pasc_gb300_fem_reduce_f64(const double *g1_dev, double *g2_dev, long T1, long T2, int K, int fem_type,
+                              void *stream);
+int pasc_gb300_fem_prolongate_f64(const double *g2_dev, double *g1_dev, long T1, long T2, int K, int fem_type,
+                                  void *stream);
 
 /* Theta update for callers that cannot allocate device memory when they need it: code
  * running while a stream is captured into a CUDA graph, hosts whose device memory belongs

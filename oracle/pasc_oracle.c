@@ -733,3 +733,148 @@ int pasc_oracle_adjoint(const double *gamma, const double *data, const double *t
     free(fr); free(lam); free(r); free(p); free(q);
     return status == 4 ? 1 : 0;
 }
+
+/* ------------------------------------------------------------------------------------
+ * FEM temporal coarsening (see the header)
+ * ---------------------------------------------------------------------------------- */
+
+/* src/petscvector/common/fem.cpp:196-215 (compute_decomposition_reduced) */
+long pasc_oracle_fem_T_reduced(long T, double fem_reduce)
+{
+    if (fem_reduce < 1.0) return (long)ceil((double)T * fem_reduce);
+    return T;
+}
+
+static double fem_diff(long T1, long T2, int type)
+{
+    if (type == 0) return (double)T1 / (double)T2;                 /* fem.cpp:15 */
+    return (double)(T1 - 1) / (double)(T2 - 1);                     /* femhat.cpp:17 */
+}
+
+void pasc_oracle_fem_reduce(const double *g1, double *g2, long T1, long T2, int K, int type)
+{
+    const double diff = fem_diff(T1, T2, type);
+    if (type == 0) {
+        /* fem.cpp:64-70 */
+        for (int k = 0; k < K; k++)
+            for (long t2 = 0; t2 < T2; t2++) {
+                double mysum = 0.0;
+                for (long i = (long)round(t2 * diff); i < (long)round((t2 + 1) * diff); i++)
+                    mysum += g1[i * (long)K + k];
+                g2[t2 * (long)K + k] = mysum;
+            }
+        return;
+    }
+    /* femhat.cpp:64-100 with left_t1_idx = 0 and right_t1_idx = floor(diff*(T2-1))
+     * (femhat.h:170-180 on one rank) */
+    const long right_t1_idx = (long)floor(diff * (double)(T2 - 1));
+    for (int k = 0; k < K; k++)
+        for (long t2 = 0; t2 < T2; t2++) {
+            const double center_t1 = t2 * diff;
+            const double left_t1 = (t2 - 1) * diff;
+            const double right_t1 = (t2 + 1) * diff;
+            long id_counter = (long)floor(left_t1);
+            long t1 = (long)floor(left_t1);
+            double mysum = 0.0;
+            while (t1 <= center_t1) {
+                const double phi = (t1 - left_t1) / (center_t1 - left_t1);
+                if (id_counter >= 0) mysum += phi * g1[id_counter * (long)K + k];
+                t1 += 1;
+                id_counter += 1;
+            }
+            while (t1 < right_t1) {
+                const double phi = (t1 - right_t1) / (center_t1 - right_t1);
+                if (id_counter < right_t1_idx) mysum += phi * g1[id_counter * (long)K + k];
+                t1 += 1;
+                id_counter += 1;
+            }
+            g2[t2 * (long)K + k] = mysum;
+        }
+}
+
+void pasc_oracle_fem_prolongate(const double *g2, double *g1, long T1, long T2, int K, int type)
+{
+    const double diff = fem_diff(T1, T2, type);
+    if (type == 0) {
+        /* fem.cpp:142-147 */
+        for (int k = 0; k < K; k++)
+            for (long t2 = 0; t2 < T2; t2++)
+                for (long i = (long)round(t2 * diff); i < (long)round((t2 + 1) * diff); i++)
+                    g1[i * (long)K + k] = g2[t2 * (long)K + k];
+        return;
+    }
+    /* femhat.cpp:150-171 with Tbegin1 = left_t2_idx = 0 */
+    for (int k = 0; k < K; k++)
+        for (long t1 = 0; t1 < T1; t1++) {
+            const long l = (long)floor(t1 / diff), r = l + 1;
+            const double t1_left = l * diff, t1_right = r * diff;
+            const double phi_l = (t1 - t1_left) / (t1_right - t1_left);
+            const double phi_r = (t1 - t1_right) / (t1_left - t1_right);
+            const double gr = r < T2 ? g2[r * (long)K + k] : 0.0;
+            const double gl = l < T2 ? g2[l * (long)K + k] : 0.0;
+            double v = 0.0;
+            v += phi_l * gr;
+            v += phi_r * gl;
+            g1[t1 * (long)K + k] = v;
+        }
+}
+
+int pasc_oracle_tssolver_solve_fem(const double *data, double *gamma, double *theta, long T, int K,
+                                   double epssqr, int scalef, double fem_reduce, int fem_type,
+                                   const pasc_oracle_ts_opts *ts, const pasc_oracle_spg_opts *spg,
+                                   pasc_oracle_ts_result *r, int nthreads)
+{
+    const int nth = eff_threads(nthreads);
+    const long T2 = pasc_oracle_fem_T_reduced(T, fem_reduce);
+    const long n = T * (long)K, n2 = T2 * (long)K;
+    double *res = (double *)malloc(sizeof(double) * (size_t)n);
+    double *perm = (double *)malloc(sizeof(double) * (size_t)n);
+    double *b2 = (double *)malloc(sizeof(double) * (size_t)n2);
+    double *x2 = (double *)malloc(sizeof(double) * (size_t)n2);
+    if (!res || !perm || !b2 || !x2) {
+        free(res); free(perm); free(b2); free(x2);
+        return -1;
+    }
+    /* graphh1fem.cpp:145-151 (A, with the original T) and :280-283 (b, with T2) */
+    double coeffA = epssqr;
+    if (scalef) coeffA *= (1.0 / ((double)T));
+    else coeffA *= ((double)T2 / ((double)T));
+    double coeffB = -1.0;
+    if (scalef) coeffB *= (1.0 / ((double)T2));
+
+    if (ts->init_permute) {
+        pasc_oracle_permute_blocked_to_interleaved(gamma, perm, T, K);
+        memcpy(gamma, perm, sizeof(double) * (size_t)n);
+    }
+    double L = DBL_MAX, L_old, deltaL = DBL_MAX;
+    int it, spg_it_sum = 0, spg_hm_sum = 0, increased = 0;
+    for (it = 0; it < ts->maxit; it++) {
+        if (!ts->thetasolved) pasc_oracle_theta_update(gamma, data, theta, T, K, 1, nth);
+        pasc_oracle_residual_b(data, theta, res, T, K, 1, 1.0, nth);      /* graphh1fem.cpp:258-267 */
+        pasc_oracle_fem_reduce(res, b2, T, T2, K, fem_type);               /* :275 */
+        pasc_oracle_fem_reduce(gamma, x2, T, T2, K, fem_type);             /* :276 */
+        for (long i = 0; i < n2; i++) b2[i] *= coeffB;                     /* :280-286 */
+        pasc_oracle_spg_result sr;
+        pasc_oracle_spgqp_solve(b2, x2, T2, K, coeffA, spg, &sr, NULL, nth);
+        pasc_oracle_fem_prolongate(x2, gamma, T, T2, K, fem_type);         /* :296-298 */
+        spg_it_sum += sr.it;
+        spg_hm_sum += sr.hessmult;
+        L_old = L;
+        L = sr.fx;
+        deltaL = fabs(L - L_old);
+        if (L - L_old > 0) increased++;
+        if (ts->relative ? (deltaL < ts->eps * fabs(L)) : (deltaL < ts->eps)) break;
+    }
+    if (r) {
+        r->it_last = it;
+        r->it_sum = it;
+        r->spg_it_sum = spg_it_sum;
+        r->spg_hessmult_sum = spg_hm_sum;
+        r->L = L;
+        r->deltaL = deltaL;
+        r->aic = 2 * log(L) + K;
+        r->L_increased = increased;
+    }
+    free(res); free(perm); free(b2); free(x2);
+    return 0;
+}

@@ -155,6 +155,29 @@ int pasc_oracle_adjoint(const double *gamma, const double *data, const double *t
                         double *dloss_depssqr, double *dloss_ddata, double *dloss_dtheta,
                         pasc_oracle_adj_result *r);
 
+/* ------------------------------------------------------------------------------------
+ * FEM temporal coarsening (GraphH1FEMModel with fem_reduce < 1): the gamma QP lives on
+ * T2 = ceil(T*fem_reduce) timesteps.  One rank (Tbegin = 0, the whole range local).
+ *   type 0, FEM-SUM (src/petscvector/common/fem.cpp:32-115, 124-210): diff = T1/T2; coarse
+ *     t2 sums fine t in [round(t2*diff), round((t2+1)*diff)); prolongation copies it back.
+ *   type 1, FEM-HAT (src/petscvector/common/femhat.cpp:27-215, include/general/common/
+ *     femhat.h:154-195): diff = (T1-1)/(T2-1); reduction weights by hat functions centred at
+ *     t2*diff, prolongation interpolates linearly between the two coarse neighbours (a
+ *     neighbour past the last coarse point counts as 0).
+ * ---------------------------------------------------------------------------------- */
+long pasc_oracle_fem_T_reduced(long T, double fem_reduce);
+void pasc_oracle_fem_reduce(const double *g1, double *g2, long T1, long T2, int K, int type);
+void pasc_oracle_fem_prolongate(const double *g2, double *g1, long T1, long T2, int K, int type);
+/* pasc_oracle_tssolver_solve with the model's gamma step on the reduced problem
+ * (src/petscvector/model/graphh1fem.cpp:116-160, 237-303): b = coeffB2 * reduce((x_t -
+ * theta_k)^2) with coeffB2 = -1/T2 (scalef), x = reduce(gamma) before each gamma solve,
+ * A = epssqr/T * A_hat(T2) (scalef; epssqr*T2/T otherwise), gamma = prolongate(x) after it.
+ * xdim == 1. */
+int pasc_oracle_tssolver_solve_fem(const double *data, double *gamma, double *theta, long T, int K,
+                                   double epssqr, int scalef, double fem_reduce, int fem_type,
+                                   const pasc_oracle_ts_opts *ts, const pasc_oracle_spg_opts *spg,
+                                   pasc_oracle_ts_result *r, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,6 +103,13 @@ def lib():
         L.pasc_oracle_abserr_reconstructed.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int]
         L.pasc_oracle_abserr_reconstructed.restype = C.c_double
         L.pasc_oracle_argmax_labels.argtypes = [_dp, _ip, C.c_long, C.c_int]
+        L.pasc_oracle_fem_T_reduced.argtypes = [C.c_long, C.c_double]
+        L.pasc_oracle_fem_T_reduced.restype = C.c_long
+        L.pasc_oracle_fem_reduce.argtypes = [_dp, _dp, C.c_long, C.c_long, C.c_int, C.c_int]
+        L.pasc_oracle_fem_prolongate.argtypes = [_dp, _dp, C.c_long, C.c_long, C.c_int, C.c_int]
+        L.pasc_oracle_tssolver_solve_fem.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
+                                                     C.c_double, C.c_int, C.POINTER(TsOpts), C.POINTER(SpgOpts),
+                                                     C.POINTER(TsResult), C.c_int]
         L.pasc_oracle_recon_mse.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_void_p, C.c_void_p]
         L.pasc_oracle_recon_mse.restype = C.c_double
         L.pasc_oracle_adjoint.argtypes = [_dp, _dp, _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_double,
@@ -213,6 +220,35 @@ def argmax_labels(gamma, T, K):
     lab = np.empty(T, dtype=np.int32)
     lib().pasc_oracle_argmax_labels(_f64(gamma), lab, T, K)
     return lab
+
+
+def fem_T_reduced(T, fem_reduce):
+    return lib().pasc_oracle_fem_T_reduced(T, fem_reduce)
+
+
+def fem_reduce(g1, T1, T2, K, fem_type=0):
+    g2 = np.empty(T2 * K)
+    lib().pasc_oracle_fem_reduce(_f64(g1), g2, T1, T2, K, fem_type)
+    return g2
+
+
+def fem_prolongate(g2, T1, T2, K, fem_type=0):
+    g1 = np.empty(T1 * K)
+    lib().pasc_oracle_fem_prolongate(_f64(g2), g1, T1, T2, K, fem_type)
+    return g1
+
+
+def tssolver_solve_fem(data, gamma_raw, theta0, T, K, epssqr, fem_reduce, fem_type=0, scalef=1,
+                       ts: TsOpts | None = None, spg: SpgOpts | None = None, nthreads=1):
+    """Returns (gamma, theta, TsResult)."""
+    ts = ts or ts_opts()
+    spg = spg or spg_opts()
+    g = _f64(gamma_raw).copy()
+    th = _f64(theta0).copy()
+    r = TsResult()
+    lib().pasc_oracle_tssolver_solve_fem(_f64(data), g, th, T, K, epssqr, scalef, fem_reduce, fem_type,
+                                         C.byref(ts), C.byref(spg), C.byref(r), nthreads)
+    return g, th, r
 
 
 def recon_mse(gamma, theta, clean, T, K):

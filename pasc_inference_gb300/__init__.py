@@ -21,7 +21,7 @@ from . import capi
 from .capi import (PASC_PREC_FP64, PASC_PREC_MIXED, PascError, SpgqpOpts, SpgqpStats, TsOpts,
                    TsStats, check, load)
 
-__all__ = ["Problem", "Batch", "Decomposition", "Signal1DData", "TSData", "GraphH1FEMModel", "TSSolver",
+__all__ = ["Problem", "Batch", "Fem", "FemHat", "Decomposition", "Signal1DData", "TSData", "GraphH1FEMModel", "TSSolver",
            "SPGQPSolver", "PascError", "PASC_PREC_FP64", "PASC_PREC_MIXED", "capi"]
 
 _SPG_KEYS = {"spgqpsolver_maxit": "maxit", "spgqpsolver_eps": "eps", "spgqpsolver_m": "m",
@@ -148,6 +148,16 @@ class Problem:
         v = C.c_double()
         check(load().pasc_gb300_time_model_kernels(self._h, int(which), int(reps), C.byref(v)))
         return v.value
+
+    def set_fem(self, fem_reduce: float, fem_type: int = 0):
+        """FEM temporal coarsening of the gamma step: 0 FEM-SUM, 1 FEM-HAT; fem_reduce = 1: none."""
+        check(load().pasc_gb300_set_fem(self._h, float(fem_reduce), int(fem_type)))
+
+    def get_fem(self):
+        """(fem_reduce, fem_type, T of the gamma QP)."""
+        r, t, T2 = C.c_double(), C.c_int(), C.c_long()
+        check(load().pasc_gb300_get_fem(self._h, C.byref(r), C.byref(t), C.byref(T2)))
+        return r.value, t.value, T2.value
 
     def get_b(self) -> np.ndarray:
         out = np.empty(self.T * self.K)
@@ -388,6 +398,29 @@ class Signal1DData(TSData):
         save_vec(prefix + "_recovered.bin", g @ th)
 
 
+class Fem:
+    """Fem<VectorBase>(fem_reduce): FEM-SUM temporal coarsening of the gamma step
+    (include/general/common/fem.h); fem_reduce = 1 is no reduction."""
+    fem_type = 0
+
+    def __init__(self, fem_reduce: float = 1.0):
+        self.fem_reduce = float(fem_reduce)
+
+    def is_reduced(self) -> bool:
+        return self.fem_reduce < 1.0
+
+    def get_name(self):
+        return "FEM-SUM"
+
+
+class FemHat(Fem):
+    """FemHat<VectorBase>(fem_reduce): hat-function coarsening (include/general/common/femhat.h)."""
+    fem_type = 1
+
+    def get_name(self):
+        return "FEM-HAT"
+
+
 class GraphH1FEMModel:
     """GraphH1FEMModel<VectorBase>(tsdata, epssqr, fem=None, usethetainpenalty=False).
     Creates the GPU problem; the initial gamma is tsdata's gamma0 (or uniform [0,1) values of
@@ -395,14 +428,15 @@ class GraphH1FEMModel:
 
     def __init__(self, tsdata: TSData, epssqr: float, fem=None, usethetainpenalty: bool = False,
                  precision: int = PASC_PREC_MIXED, gamma0=None, seed: int = 13, device: int = 0):
-        if fem is not None and getattr(fem, "fem_reduce", 1.0) != 1.0:
-            raise PascError(capi.PASC_ERR_NOTSUPP, "FEM reduction (fem_reduce < 1) is not supported")
         if usethetainpenalty:
             raise PascError(capi.PASC_ERR_NOTSUPP, "usethetainpenalty is not supported")
         self.tsdata = tsdata
         self.epssqr = float(epssqr)
         T, K = tsdata.get_T(), tsdata.get_K()
         self.problem = Problem(T, K, epssqr, precision=precision, xdim=tsdata.get_xdim(), device=device)
+        self.fem = fem if fem is not None else Fem(1.0)
+        if self.fem.is_reduced():
+            self.problem.set_fem(self.fem.fem_reduce, self.fem.fem_type)
         self.problem.set_data(tsdata.get_datavector())
         if gamma0 is None:
             from .datagen import uniform

@@ -120,6 +120,15 @@ cudaError_t launch_mc_theta(int K, int grid, const McArgs &a, const float *gamma
 size_t mc_partials_size(int K, int n, int grid, long T);
 int mc_theta_tma_blocks_per_sm(int K, int n);  // 0: the bulk-copy theta kernel does not apply
 
+// FEM temporal coarsening (fem.cu).  launch_fem_reduce: g1 == null reduces the residual
+// (data_t - theta_k)^2 instead of a stored field; the result is multiplied by scale.
+long fem_T_reduced(long T, double fem_reduce);
+template <typename TIn, typename TOut>
+cudaError_t launch_fem_reduce(const TIn *g1, const double *data, const double *theta, TOut *g2, long T1, long T2,
+                              int K, int type, double scale, cudaStream_t s);
+template <typename TIn, typename TOut>
+cudaError_t launch_fem_prolongate(const TIn *g2, TOut *g1, long T1, long T2, int K, int type, cudaStream_t s);
+
 int batch_tile_width();
 int batch_segment_timesteps();
 int batch_max_tile();

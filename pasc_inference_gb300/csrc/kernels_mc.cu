@@ -572,6 +572,7 @@ __global__ void __launch_bounds__(MC_THETA_VNT) mc_theta_tma_kernel(McArgs a, co
         for (int k = 0; k < K; k++) tot[q][k] = 0.f;
 #pragma unroll
     for (int k = 0; k < K; k++) dtot[k] = 0.f;
+    for (int i = tid; i < n * K + K; i += MC_THETA_VNT) s_sum[i] = 0.0;  // a row may span warps
     unsigned int parity = 0u;
     bool failed = false;
     int j = 0;
@@ -648,16 +649,10 @@ __global__ void __launch_bounds__(MC_THETA_VNT) mc_theta_tma_kernel(McArgs a, co
 #pragma unroll
             for (int q = 0; q < 4; q++)
 #pragma unroll
-                for (int k = 0; k < K; k++) {
-                    double &dst = s_sum[k * n + c * 4 + q];
-                    dst = (w == 0 ? 0.0 : dst) + (double)tot[q][k];
-                }
+                for (int k = 0; k < K; k++) s_sum[k * n + c * 4 + q] += (double)tot[q][k];
             if (c == 0)
 #pragma unroll
-                for (int k = 0; k < K; k++) {
-                    double &dst = s_sum[K * n + k];
-                    dst = (w == 0 ? 0.0 : dst) + (double)dtot[k];
-                }
+                for (int k = 0; k < K; k++) s_sum[K * n + k] += (double)dtot[k];
         }
         __syncthreads();
     }

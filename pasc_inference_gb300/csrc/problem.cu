@@ -58,6 +58,7 @@ static void free_all(pasc_gb300_problem *p)
     if (!p) return;
     cudaSetDevice(p->device);
     if (p->adj) adjoint_free(p->adj);
+    if (p->fem_inner) free_all(p->fem_inner);
     if (p->chunk_graph) cudaGraphExecDestroy(p->chunk_graph);
     void *dev[] = {p->data64, p->theta64, p->stage64, p->red, p->red_out, p->labels_d, p->x, p->g,
                    p->d, p->Ad, p->b, p->data32_raw, p->theta32, p->xb_raw[0], p->xb_raw[1], p->st,
@@ -82,6 +83,9 @@ static int dalloc(T **ptr, size_t count)
                     cudaGetErrorString(e));
     return PASC_OK;
 }
+
+static void fem_set_inner_coeffs(pasc_gb300_problem *p);
+static int fem_update_b_async(pasc_gb300_problem *p, int *launches);
 
 static void set_coeffs(pasc_gb300_problem *p)
 {
@@ -292,10 +296,25 @@ int pasc_gb300_set_epssqr(pasc_gb300_problem *p, double epssqr, int scalef)
     p->epssqr = epssqr;
     p->scalef = scalef ? 1 : 0;
     set_coeffs(p);
+    if (p->fem_inner) fem_set_inner_coeffs(p);
     return PASC_OK;
 }
 
 }  // extern "C"
+
+// Coefficients of the reduced QP (graphh1fem.cpp:145-151 and :280-283): A keeps the original
+// T (A = epssqr/T A_hat on the coarse grid; epssqr*T2/T without scalef), b the reduced one
+// (b = -1/T2 * reduced residual; -1 without scalef).
+static void fem_set_inner_coeffs(pasc_gb300_problem *p)
+{
+    pasc_gb300_problem *q = p->fem_inner;
+    const double T = (double)p->T, T2 = (double)q->T;
+    q->epssqr = p->epssqr;
+    q->scalef = p->scalef;
+    q->coeffA = p->scalef ? p->epssqr * (1.0 / T) : p->epssqr * (T2 / T);
+    q->coeffB = p->scalef ? -1.0 * (1.0 / T2) : -1.0;
+    q->run.started = false;
+}
 
 static McArgs mc_args(pasc_gb300_problem *p)
 {
@@ -336,6 +355,37 @@ static int mc_check_error(pasc_gb300_problem *p)
         cudaMemsetAsync(p->mc_err, 0, sizeof(int), p->stream);
         return fail(PASC_ERR_TIMEOUT, "residual kernel: a bounded wait for a tile copy or the tensor cores gave up (%d)", e);
     }
+    return PASC_OK;
+}
+
+// GraphH1FEMModel::updatebeforesolve_gammasolver with a reduction (graphh1fem.cpp:237-289): the
+// residual (x_t - theta_k)^2 on the full grid, reduced and scaled into the inner b, and the
+// current gamma reduced into the inner x (the warm start, projected when the solve starts).
+static int fem_update_b_async(pasc_gb300_problem *p, int *launches)
+{
+    pasc_gb300_problem *q = p->fem_inner;
+    const long T = p->T, T2 = q->T;
+    const int K = p->K, type = p->fem_type;
+    cudaStream_t s = p->stream;
+    if (p->precision == PASC_PREC_FP64) {
+        CU((launch_fem_reduce<double, double>(nullptr, p->data64, p->theta64, q->b, T, T2, K, type, q->coeffB, s)));
+        CU((launch_fem_reduce<double, double>(p->x, nullptr, nullptr, q->x, T, T2, K, type, 1.0, s)));
+    } else {
+        if (p->xdim > 1) {
+            // the full b = bscale ||X_t - theta_k||^2 (FP32), then its reduction rescaled
+            CHK(mc_residual_async(p, launches));
+            CU((launch_fem_reduce<float, float>(p->bmat, nullptr, nullptr, q->bmat, T, T2, K, type,
+                                               q->coeffB / p->coeffB, s)));
+        } else {
+            CU((launch_fem_reduce<float, float>(nullptr, p->data64, p->theta64, q->bmat, T, T2, K, type, q->coeffB, s)));
+        }
+        CU((launch_fem_reduce<float, float>(p->xb[p->cur], nullptr, nullptr, q->xb[q->cur], T, T2, K, type, 1.0, s)));
+    }
+    if (launches) *launches += 2;
+    // the inner handle works on its own stream: its solve must see the reduced b and x
+    CU(cudaStreamSynchronize(s));
+    q->run.started = false;
+    q->have_fx = false;
     return PASC_OK;
 }
 
@@ -488,6 +538,8 @@ int pasc_gb300_update_theta(pasc_gb300_problem *p)
 
 static int update_b_async(pasc_gb300_problem *p, int *launches)
 {
+    if (p->fem_inner) return fem_update_b_async(p, launches);
+    if (p->b_external) return PASC_OK;  // written by the owner of this (inner) handle
     if (p->xdim > 1) return mc_residual_async(p, launches);
     if (p->precision == PASC_PREC_FP64) {
         CU(launch_residual_f64(p->data64, p->theta64, p->b, p->T, p->K, p->coeffB, p->stream));
@@ -647,7 +699,7 @@ static int fp64_iterate(pasc_gb300_problem *p, long n)
 // ---------------------------------------------------------------------------------------
 static int sweep_args(pasc_gb300_problem *p, SweepArgs *a)
 {
-    a->bmat = p->xdim > 1 ? p->bmat : nullptr;
+    a->bmat = p->bmat;  // set for multichannel data and for the inner handle of a reduced problem
     a->data = p->data32;
     a->theta = p->theta32;
     a->xb0 = p->xb[0];
@@ -880,6 +932,7 @@ static int spgqp_iterate(pasc_gb300_problem *p, long n, int poll)
 int pasc_gb300_spgqp_start(pasc_gb300_problem *p, const pasc_gb300_spgqp_opts *o)
 {
     if (!p) return fail(PASC_ERR_ARG, "spgqp_start: NULL problem");
+    if (p->fem_inner) return fail(PASC_ERR_NOTSUPP, "spgqp_start: a reduced (fem_reduce < 1) problem solves with spgqp_solve");
     CHK(check_opts(o));
     CU(cudaSetDevice(p->device));
     return spgqp_start(p, o);
@@ -887,6 +940,7 @@ int pasc_gb300_spgqp_start(pasc_gb300_problem *p, const pasc_gb300_spgqp_opts *o
 
 int pasc_gb300_spgqp_iterate(pasc_gb300_problem *p, long n, int poll, pasc_gb300_spgqp_stats *st)
 {
+    if (p && p->fem_inner) return fail(PASC_ERR_NOTSUPP, "spgqp_iterate: a reduced (fem_reduce < 1) problem solves with spgqp_solve");
     if (!p) return fail(PASC_ERR_ARG, "spgqp_iterate: NULL problem");
     if (!p->run.started) return fail(PASC_ERR_STATE, "spgqp_iterate: call pasc_gb300_spgqp_start first");
     if (n < 0) return fail(PASC_ERR_ARG, "spgqp_iterate: n must be >= 0");
@@ -909,6 +963,24 @@ int pasc_gb300_spgqp_solve(pasc_gb300_problem *p, const pasc_gb300_spgqp_opts *o
     if (!p) return fail(PASC_ERR_ARG, "spgqp_solve: NULL problem");
     CHK(check_opts(o));
     CU(cudaSetDevice(p->device));
+    if (p->fem_inner) {
+        // the reduced QP (b and the warm start written by update_b), then the prolongation of
+        // its solution to the full gamma (graphh1fem.cpp:292-303)
+        pasc_gb300_problem *q = p->fem_inner;
+        pasc_gb300_spgqp_stats ist;
+        CHK(pasc_gb300_spgqp_solve(q, o, &ist));
+        if (p->precision == PASC_PREC_FP64)
+            CU((launch_fem_prolongate<double, double>(q->x, p->x, p->T, q->T, p->K, p->fem_type, p->stream)));
+        else
+            CU((launch_fem_prolongate<float, float>(q->xb[q->cur], p->xb[p->cur], p->T, q->T, p->K, p->fem_type,
+                                                   p->stream)));
+        CU(cudaStreamSynchronize(p->stream));
+        p->fx_last = q->fx_last;
+        p->have_fx = q->have_fx;
+        ist.kernel_launches += 1;
+        if (st) *st = ist;
+        return PASC_OK;
+    }
     CHK(spgqp_start(p, o));
     CHK(spgqp_iterate(p, o->maxit, 1));
     if (p->run.status == PASC_SPG_RUNNING) p->run.status = PASC_SPG_MAXIT;
@@ -1080,6 +1152,58 @@ int pasc_gb300_set_sweep_variant(pasc_gb300_problem *p, int variant)
     if (variant == 1 && !sweep_tma_supported(p->K)) return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: K not supported");
     p->variant = variant;
     p->run.started = false;
+    return PASC_OK;
+}
+
+int pasc_gb300_set_fem(pasc_gb300_problem *p, double fem_reduce, int fem_type)
+{
+    if (!p) return fail(PASC_ERR_ARG, "set_fem: NULL problem");
+    if (!(fem_reduce > 0.0) || fem_reduce > 1.0) return fail(PASC_ERR_ARG, "set_fem: fem_reduce must be in (0, 1]");
+    if (fem_type != 0 && fem_type != 1) return fail(PASC_ERR_ARG, "set_fem: fem_type 0 (FEM-SUM) or 1 (FEM-HAT)");
+    CU(cudaSetDevice(p->device));
+    CU(cudaStreamSynchronize(p->stream));
+    if (p->fem_inner) {
+        free_all(p->fem_inner);
+        p->fem_inner = nullptr;
+    }
+    p->fem_reduce = fem_reduce;
+    p->fem_type = fem_type;
+    p->run.started = false;
+    p->have_fx = false;
+    if (!(fem_reduce < 1.0)) return PASC_OK;  // not reduced (Fem::is_reduced, fem.h:236-246)
+    const long T2 = fem_T_reduced(p->T, fem_reduce);
+    if (fem_type == 1 && (T2 < 2 || p->T < 2)) return fail(PASC_ERR_ARG, "set_fem: FEM-HAT needs T and T2 >= 2");
+    pasc_gb300_problem *q = nullptr;
+    CHK(pasc_gb300_create(&q, T2, p->K, 1, p->precision, p->epssqr, p->device));
+    q->b_external = true;
+    if (p->precision == PASC_PREC_MIXED) {
+        // the reduced b is materialised (the sweeps read it instead of forming it from data)
+        const size_t nx = (size_t)(T2 + PAD_FRONT + PAD_BACK) * p->K;
+        int rc = dalloc(&q->bmat_raw, nx);
+        if (rc) {
+            free_all(q);
+            return rc;
+        }
+        cudaMemset(q->bmat_raw, 0, sizeof(float) * nx);
+        q->bmat = q->bmat_raw + (size_t)PAD_FRONT * p->K;
+        const long nt_tma = (T2 + sweep_tma_tile_width() - 1) / sweep_tma_tile_width();
+        long g = (long)sweep_tma_blocks_per_sm(p->K, false, true) * q->sms;
+        q->grid_sweep[1] = (int)(g < nt_tma ? (g < 1 ? 1 : g) : nt_tma);
+        g = (long)sweep_tma_blocks_per_sm(p->K, true, true) * q->sms;
+        q->grid_sweep_init[1] = (int)(g < nt_tma ? (g < 1 ? 1 : g) : nt_tma);
+    }
+    p->fem_inner = q;
+    fem_set_inner_coeffs(p);
+    if (cudaDeviceSynchronize() != cudaSuccess) return fail(PASC_ERR_CUDA, "set_fem: initialisation failed");
+    return PASC_OK;
+}
+
+int pasc_gb300_get_fem(pasc_gb300_problem *p, double *fem_reduce, int *fem_type, long *T_reduced)
+{
+    if (!p) return fail(PASC_ERR_ARG, "get_fem: NULL problem");
+    if (fem_reduce) *fem_reduce = p->fem_reduce;
+    if (fem_type) *fem_type = p->fem_type;
+    if (T_reduced) *T_reduced = p->fem_inner ? p->fem_inner->T : p->T;
     return PASC_OK;
 }
 

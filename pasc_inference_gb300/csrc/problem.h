@@ -79,6 +79,13 @@ struct pasc_gb300_problem {
     int mc_engine = 0;                     // residual: 0 tensor cores (when xdim allows), 1 CUDA cores
     CUtensorMap mc_tmap;
 
+    // FEM temporal coarsening (pasc_gb300_set_fem): with fem_reduce < 1 the gamma QP runs on the
+    // inner handle (T2 timesteps, b written here); this handle keeps the full data, gamma, theta
+    double fem_reduce = 1.0;
+    int fem_type = 0;
+    pasc_gb300_problem *fem_inner = nullptr;
+    bool b_external = false;               // inner handle: b is written by the owner
+
     pasc::SpgRun run;
     pasc::AdjointWork *adj = nullptr;  // allocated by the first adjoint call
     double fx_last = 0.0;
