@@ -147,6 +147,7 @@ public:
         return t;
     }
     void permute_gamma() { check(pasc_gb300_permute_gamma(h_.get())); }
+    void set_fem(double fem_reduce, int fem_type) { check(pasc_gb300_set_fem(h_.get(), fem_reduce, fem_type)); }
     void update_theta() { check(pasc_gb300_update_theta(h_.get())); }
     void update_b() { check(pasc_gb300_update_b(h_.get())); }
     pasc_gb300_spgqp_stats spgqp_solve(const pasc_gb300_spgqp_opts &o)
@@ -296,6 +297,28 @@ private:
     int K_, xdim_;
 };
 
+// Fem<VectorBase>(fem_reduce) (FEM-SUM, include/general/common/fem.h) and FemHat (FEM-HAT,
+// include/general/common/femhat.h): temporal coarsening of the gamma step, fem_reduce < 1
+class Fem {
+public:
+    explicit Fem(double fem_reduce = 1.0) : fem_reduce_(fem_reduce) {}
+    virtual ~Fem() = default;
+    double get_fem_reduce() const { return fem_reduce_; }
+    bool is_reduced() const { return fem_reduce_ < 1.0; }
+    virtual int type() const { return 0; }
+    virtual std::string get_name() const { return "FEM-SUM"; }
+
+private:
+    double fem_reduce_;
+};
+
+class FemHat : public Fem {
+public:
+    explicit FemHat(double fem_reduce = 1.0) : Fem(fem_reduce) {}
+    int type() const override { return 1; }
+    std::string get_name() const override { return "FEM-HAT"; }
+};
+
 class GraphH1FEMModel;
 
 class TSData {
@@ -345,13 +368,14 @@ class GraphH1FEMModel {
 public:
     // GraphH1FEMModel<VectorBase>(tsdata, epssqr): creates the GPU problem with gamma0 =
     // uniform [0, 1) values (seed, stream 0) in the blocked layout, as set_random leaves it
-    GraphH1FEMModel(TSData &tsdata, double epssqr, int precision = PASC_PREC_MIXED, uint64_t seed = 13,
-                    int device = 0)
+    GraphH1FEMModel(TSData &tsdata, double epssqr, const Fem *fem = nullptr, int precision = PASC_PREC_MIXED,
+                    uint64_t seed = 13, int device = 0)
         : tsdata_(tsdata), epssqr_(epssqr),
           problem_(tsdata.get_T(), tsdata.get_K(), epssqr, precision, tsdata.get_xdim(), device)
     {
         const long T = tsdata.get_T();
         const int K = tsdata.get_K();
+        if (fem && fem->is_reduced()) problem_.set_fem(fem->get_fem_reduce(), fem->type());
         problem_.set_data(tsdata.get_datavector());
         problem_.set_gamma(uniform(seed, 0, (size_t)T * K));
         problem_.set_theta(std::vector<double>((size_t)K * tsdata.get_xdim(), 0.0));
