@@ -3,7 +3,7 @@
 //
 //   Decomposition(T, R, K, xdim, DDT_size)          include/general/common/decomposition.h:55
 //   Signal1DData(filename) / TSData                 include/general/data/{signal1Ddata,tsdata}.h
-//   GraphH1FEMModel(tsdata, epssqr)                 include/general/model/graphh1fem.h:75
+//   GraphH1FEMModel(tsdata, epssqr, fem, usethetainpenalty)   include/general/model/graphh1fem.h:75
 //   TSSolver(tsdata, annealing)                     include/general/solver/tssolver.h:80-104
 //   SPGQPSolver (TSSolver::get_gammasolver())       include/general/solver/spgqpsolver.h:118-151
 //
@@ -148,6 +148,13 @@ public:
     }
     void permute_gamma() { check(pasc_gb300_permute_gamma(h_.get())); }
     void set_fem(double fem_reduce, int fem_type) { check(pasc_gb300_set_fem(h_.get(), fem_reduce, fem_type)); }
+    void set_usethetainpenalty(bool on) { check(pasc_gb300_set_usethetainpenalty(h_.get(), on ? 1 : 0)); }
+    bool get_usethetainpenalty() const
+    {
+        int on = 0;
+        check(pasc_gb300_get_usethetainpenalty(h_.get(), &on));
+        return on != 0;
+    }
     void update_theta() { check(pasc_gb300_update_theta(h_.get())); }
     void update_b() { check(pasc_gb300_update_b(h_.get())); }
     pasc_gb300_spgqp_stats spgqp_solve(const pasc_gb300_spgqp_opts &o)
@@ -366,16 +373,18 @@ public:
 
 class GraphH1FEMModel {
 public:
-    // GraphH1FEMModel<VectorBase>(tsdata, epssqr): creates the GPU problem with gamma0 =
-    // uniform [0, 1) values (seed, stream 0) in the blocked layout, as set_random leaves it
-    GraphH1FEMModel(TSData &tsdata, double epssqr, const Fem *fem = nullptr, int precision = PASC_PREC_MIXED,
-                    uint64_t seed = 13, int device = 0)
-        : tsdata_(tsdata), epssqr_(epssqr),
+    // GraphH1FEMModel<VectorBase>(tsdata, epssqr, fem, usethetainpenalty): creates the GPU
+    // problem with gamma0 = uniform [0, 1) values (seed, stream 0) in the blocked layout, as
+    // set_random leaves it
+    GraphH1FEMModel(TSData &tsdata, double epssqr, const Fem *fem = nullptr, bool usethetainpenalty = false,
+                    int precision = PASC_PREC_MIXED, uint64_t seed = 13, int device = 0)
+        : tsdata_(tsdata), epssqr_(epssqr), usethetainpenalty_(usethetainpenalty),
           problem_(tsdata.get_T(), tsdata.get_K(), epssqr, precision, tsdata.get_xdim(), device)
     {
         const long T = tsdata.get_T();
         const int K = tsdata.get_K();
         if (fem && fem->is_reduced()) problem_.set_fem(fem->get_fem_reduce(), fem->type());
+        if (usethetainpenalty) problem_.set_usethetainpenalty(true);
         problem_.set_data(tsdata.get_datavector());
         problem_.set_gamma(uniform(seed, 0, (size_t)T * K));
         problem_.set_theta(std::vector<double>((size_t)K * tsdata.get_xdim(), 0.0));
@@ -388,6 +397,7 @@ public:
     }
     double get_epssqr() const { return epssqr_; }
     double get_aic(double L) const { return 2.0 * std::log(L) + tsdata_.get_K(); }
+    bool get_usethetainpenalty() const { return usethetainpenalty_; }
     std::string get_name() const { return "Graph-H1-FEM Time-Series Model"; }
     Problem &problem() { return problem_; }
     const Problem &problem() const { return problem_; }
@@ -395,6 +405,7 @@ public:
 private:
     TSData &tsdata_;
     double epssqr_;
+    bool usethetainpenalty_;
     Problem problem_;
 };
 

@@ -227,6 +227,16 @@ int pasc_gb300_get_b(pasc_gb300_problem *p, double *b);
 int pasc_gb300_set_fem(pasc_gb300_problem *p, double fem_reduce, int fem_type);
 int pasc_gb300_get_fem(pasc_gb300_problem *p, double *fem_reduce, int *fem_type, long *T_reduced);
 
+/* Theta in the penalty: GraphH1FEMModel(tsdata, epssqr, fem, usethetainpenalty = true)
+ * (graphh1fem.cpp:8-19, 154-160; include/general/model/graphh1fem.h:61, 75).  Block k of the
+ * gamma QP's A is alpha*theta_k*theta_k*A_hat (BlockGraphSparseMatrix with coefficients,
+ * blockgraphsparse.cpp:161-185; alpha = epssqr/T), and the theta step is
+ * theta_k = gamma_k'x / (sum gamma_k + gamma_k'(alpha A_hat)gamma_k / 2)
+ * (updatebeforesolve_thetasolver, graphh1fem.cpp:306-380).  xdim == 1 and fem_reduce == 1 only
+ * (PASC_ERR_NOTSUPP otherwise); no adjoint. */
+int pasc_gb300_set_usethetainpenalty(pasc_gb300_problem *p, int on);
+int pasc_gb300_get_usethetainpenalty(pasc_gb300_problem *p, int *on);
+
 /* Residual kernel of multichannel data (xdim > 1): 0 = tensor cores (tcgen05, BF16 X and a
  * three-part BF16 theta, FP32 accumulation; xdim in {64, 128, 256}; the default there),
  * 1 = CUDA cores (FP32; any xdim, the default otherwise).  No reference counterpart: the

@@ -207,7 +207,22 @@ void pasc_oracle_project(double *x, long T, int K, int nthreads)
 /* Product: MatMult row by row over columns in ascending order starting from 0.0, then    */
 /* VecScale by the coefficient (spgqpsolver.cpp:122-123,164-165).                          */
 /* ------------------------------------------------------------------------------------- */
+/* y = A x with A = coeff * A_hat, or with kc != NULL the block k scaled by kc[k] instead of coeff
+ * (BlockGraphSparseMatrix with coefficients, blockgraphsparse.cpp:161-185: VecScale of the
+ * MatMult's block k by alpha*theta_k*theta_k) */
+static void matmult_kc(const double *x, double *y, long T, int K, double coeff, const double *kc, int nthreads);
+
 void pasc_oracle_fem_h1_matmult(const double *x, double *y, long T, int K, double coeff, int nthreads)
+{
+    matmult_kc(x, y, T, K, coeff, NULL, nthreads);
+}
+
+void pasc_oracle_fem_h1_matmult_kc(const double *x, double *y, long T, int K, const double *kc, int nthreads)
+{
+    matmult_kc(x, y, T, K, 0.0, kc, nthreads);
+}
+
+static void matmult_kc(const double *x, double *y, long T, int K, double coeff, const double *kc, int nthreads)
 {
     int nth = eff_threads(nthreads);
     long N = T * (long)K;
@@ -227,7 +242,11 @@ void pasc_oracle_fem_h1_matmult(const double *x, double *y, long T, int K, doubl
         }
         y[i] = sum;
     }
-    vscale(y, coeff, N, nth);
+    if (!kc) {
+        vscale(y, coeff, N, nth);
+        return;
+    }
+    for (long i = 0; i < N; i++) y[i] = kc[i % K] * y[i];
 }
 
 double pasc_oracle_A_coeff(double epssqr, long T, int scalef)
@@ -342,9 +361,24 @@ static double get_fx(const double *g, const double *b, const double *x, double *
     return 0.5 * tempt;
 }
 
+static int spgqp_impl(const double *b, double *x, long T, int K, double coeff, const double *kc,
+                      const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, double *trace, int nthreads);
+
 int pasc_oracle_spgqp_solve(const double *b, double *x, long T, int K, double coeff,
                             const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r,
                             double *trace, int nthreads)
+{
+    return spgqp_impl(b, x, T, K, coeff, NULL, o, r, trace, nthreads);
+}
+
+int pasc_oracle_spgqp_solve_kc(const double *b, double *x, long T, int K, const double *kc,
+                               const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, int nthreads)
+{
+    return spgqp_impl(b, x, T, K, 0.0, kc, o, r, NULL, nthreads);
+}
+
+static int spgqp_impl(const double *b, double *x, long T, int K, double coeff, const double *kc,
+                      const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, double *trace, int nthreads)
 {
     int nth = eff_threads(nthreads);
     long n = T * (long)K;
@@ -369,7 +403,7 @@ int pasc_oracle_spgqp_solve(const double *b, double *x, long T, int K, double co
 
     pasc_oracle_project(x, T, K, nth); /* :116 */
 
-    pasc_oracle_fem_h1_matmult(x, g, T, K, coeff, nth); /* MatMult + VecScale :122-123 */
+    matmult_kc(x, g, T, K, coeff, kc, nth); /* MatMult + VecScale :122-123 */
     hessmult += 1;
     vaxpy(g, -1.0, b, n, nth); /* :128 */
 
@@ -389,7 +423,7 @@ int pasc_oracle_spgqp_solve(const double *b, double *x, long T, int K, double co
         pasc_oracle_project(d, T, K, nth); /* :153 */
         vaxpy(d, -1.0, x, n, nth);        /* :158 */
 
-        pasc_oracle_fem_h1_matmult(d, Ad, T, K, coeff, nth); /* :164-165 */
+        matmult_kc(d, Ad, T, K, coeff, kc, nth); /* :164-165 */
         hessmult += 1;
 
         dd = vdot(d, d, n, nth);  /* :357 */
@@ -819,10 +853,46 @@ void pasc_oracle_fem_prolongate(const double *g2, double *g1, long T1, long T2, 
         }
 }
 
+/* GraphH1FEMModel::updatebeforesolve_thetasolver with usethetainpenalty
+ * (src/petscvector/model/graphh1fem.cpp:306-380): theta is set to 1, Agamma = A gamma with
+ * that theta (block k scaled by alpha*1*1), and theta_k = (c gamma_k'x) / (c sum gamma_k +
+ * gamma_k'Agamma_k / 2) with c = 1 (0 when the denominator is 0). */
+void pasc_oracle_theta_update_penalty(const double *gamma, const double *data, double *theta, long T, int K,
+                                      double alpha)
+{
+    const long N = T * (long)K;
+    double *kc = (double *)malloc(sizeof(double) * (size_t)K);
+    double *Ag = (double *)malloc(sizeof(double) * (size_t)N);
+    if (!kc || !Ag) {
+        free(kc); free(Ag);
+        return;
+    }
+    for (int k = 0; k < K; k++) kc[k] = alpha * 1.0 * 1.0;
+    matmult_kc(gamma, Ag, T, K, 0.0, kc, 1);
+    for (int k = 0; k < K; k++) {
+        double gAg = 0.0, gx = 0.0, gs = 0.0;
+        for (long t = 0; t < T; t++) gAg += gamma[t * (long)K + k] * Ag[t * (long)K + k];
+        for (long t = 0; t < T; t++) gx += data[t] * gamma[t * (long)K + k];
+        for (long t = 0; t < T; t++) gs += gamma[t * (long)K + k];
+        const double c = 1.0;
+        theta[k] = (c * gs + 0.5 * gAg != 0) ? (c * gx) / (c * gs + 0.5 * gAg) : 0.0;
+    }
+    free(kc); free(Ag);
+}
+
 int pasc_oracle_tssolver_solve_fem(const double *data, double *gamma, double *theta, long T, int K,
                                    double epssqr, int scalef, double fem_reduce, int fem_type,
                                    const pasc_oracle_ts_opts *ts, const pasc_oracle_spg_opts *spg,
                                    pasc_oracle_ts_result *r, int nthreads)
+{
+    return pasc_oracle_tssolver_solve_model(data, gamma, theta, T, K, epssqr, scalef, fem_reduce, fem_type, 0, ts,
+                                            spg, r, nthreads);
+}
+
+int pasc_oracle_tssolver_solve_model(const double *data, double *gamma, double *theta, long T, int K,
+                                     double epssqr, int scalef, double fem_reduce, int fem_type,
+                                     int usethetainpenalty, const pasc_oracle_ts_opts *ts,
+                                     const pasc_oracle_spg_opts *spg, pasc_oracle_ts_result *r, int nthreads)
 {
     const int nth = eff_threads(nthreads);
     const long T2 = pasc_oracle_fem_T_reduced(T, fem_reduce);
@@ -848,14 +918,25 @@ int pasc_oracle_tssolver_solve_fem(const double *data, double *gamma, double *th
     }
     double L = DBL_MAX, L_old, deltaL = DBL_MAX;
     int it, spg_it_sum = 0, spg_hm_sum = 0, increased = 0;
+    double kc[64];
+    if (usethetainpenalty && (K > 64 || fem_reduce < 1.0)) {
+        free(res); free(perm); free(b2); free(x2);
+        return -1; /* the reference's theta step multiplies the reduced A with the full gamma */
+    }
     for (it = 0; it < ts->maxit; it++) {
-        if (!ts->thetasolved) pasc_oracle_theta_update(gamma, data, theta, T, K, 1, nth);
+        if (!ts->thetasolved) {
+            if (usethetainpenalty) pasc_oracle_theta_update_penalty(gamma, data, theta, T, K, coeffA);
+            else pasc_oracle_theta_update(gamma, data, theta, T, K, 1, nth);
+        }
+        if (usethetainpenalty)
+            for (int k = 0; k < K; k++) kc[k] = coeffA * theta[k] * theta[k]; /* blockgraphsparse.cpp:177 */
         pasc_oracle_residual_b(data, theta, res, T, K, 1, 1.0, nth);      /* graphh1fem.cpp:258-267 */
         pasc_oracle_fem_reduce(res, b2, T, T2, K, fem_type);               /* :275 */
         pasc_oracle_fem_reduce(gamma, x2, T, T2, K, fem_type);             /* :276 */
         for (long i = 0; i < n2; i++) b2[i] *= coeffB;                     /* :280-286 */
         pasc_oracle_spg_result sr;
-        pasc_oracle_spgqp_solve(b2, x2, T2, K, coeffA, spg, &sr, NULL, nth);
+        if (usethetainpenalty) pasc_oracle_spgqp_solve_kc(b2, x2, T2, K, kc, spg, &sr, nth);
+        else pasc_oracle_spgqp_solve(b2, x2, T2, K, coeffA, spg, &sr, NULL, nth);
         pasc_oracle_fem_prolongate(x2, gamma, T, T2, K, fem_type);         /* :296-298 */
         spg_it_sum += sr.it;
         spg_hm_sum += sr.hessmult;

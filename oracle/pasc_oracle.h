@@ -173,6 +173,20 @@ void pasc_oracle_fem_prolongate(const double *g2, double *g1, long T1, long T2, 
  * theta_k)^2) with coeffB2 = -1/T2 (scalef), x = reduce(gamma) before each gamma solve,
  * A = epssqr/T * A_hat(T2) (scalef; epssqr*T2/T otherwise), gamma = prolongate(x) after it.
  * xdim == 1. */
+/* usethetainpenalty (graphh1fem.cpp:154-160, 306-380, blockgraphsparse.cpp:161-185): the
+ * gamma QP's block k is scaled by kc[k] = coeff*theta_k*theta_k (spgqp_solve_kc), and theta is
+ * updated with the penalty term (theta_update_penalty, alpha = the QP coefficient). */
+void pasc_oracle_fem_h1_matmult_kc(const double *x, double *y, long T, int K, const double *kc, int nthreads);
+int pasc_oracle_spgqp_solve_kc(const double *b, double *x, long T, int K, const double *kc,
+                               const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, int nthreads);
+void pasc_oracle_theta_update_penalty(const double *gamma, const double *data, double *theta, long T, int K,
+                                      double alpha);
+/* the general model: FEM coarsening and/or usethetainpenalty (not both: the reference's theta
+ * step multiplies the reduced operator with the full gamma) */
+int pasc_oracle_tssolver_solve_model(const double *data, double *gamma, double *theta, long T, int K,
+                                     double epssqr, int scalef, double fem_reduce, int fem_type,
+                                     int usethetainpenalty, const pasc_oracle_ts_opts *ts,
+                                     const pasc_oracle_spg_opts *spg, pasc_oracle_ts_result *r, int nthreads);
 int pasc_oracle_tssolver_solve_fem(const double *data, double *gamma, double *theta, long T, int K,
                                    double epssqr, int scalef, double fem_reduce, int fem_type,
                                    const pasc_oracle_ts_opts *ts, const pasc_oracle_spg_opts *spg,

@@ -110,6 +110,13 @@ def lib():
         L.pasc_oracle_tssolver_solve_fem.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
                                                      C.c_double, C.c_int, C.POINTER(TsOpts), C.POINTER(SpgOpts),
                                                      C.POINTER(TsResult), C.c_int]
+        L.pasc_oracle_fem_h1_matmult_kc.argtypes = [_dp, _dp, C.c_long, C.c_int, _dp, C.c_int]
+        L.pasc_oracle_spgqp_solve_kc.argtypes = [_dp, _dp, C.c_long, C.c_int, _dp, C.POINTER(SpgOpts),
+                                                 C.POINTER(SpgResult), C.c_int]
+        L.pasc_oracle_theta_update_penalty.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_double]
+        L.pasc_oracle_tssolver_solve_model.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
+                                                       C.c_double, C.c_int, C.c_int, C.POINTER(TsOpts),
+                                                       C.POINTER(SpgOpts), C.POINTER(TsResult), C.c_int]
         L.pasc_oracle_recon_mse.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_void_p, C.c_void_p]
         L.pasc_oracle_recon_mse.restype = C.c_double
         L.pasc_oracle_adjoint.argtypes = [_dp, _dp, _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_double,
@@ -248,6 +255,43 @@ def tssolver_solve_fem(data, gamma_raw, theta0, T, K, epssqr, fem_reduce, fem_ty
     r = TsResult()
     lib().pasc_oracle_tssolver_solve_fem(_f64(data), g, th, T, K, epssqr, scalef, fem_reduce, fem_type,
                                          C.byref(ts), C.byref(spg), C.byref(r), nthreads)
+    return g, th, r
+
+
+def theta_update_penalty(gamma, data, T, K, alpha):
+    th = np.empty(K)
+    lib().pasc_oracle_theta_update_penalty(_f64(gamma), _f64(data), th, T, K, alpha)
+    return th
+
+
+def fem_h1_matmult_kc(x, T, K, kc):
+    y = np.empty(T * K)
+    lib().pasc_oracle_fem_h1_matmult_kc(_f64(x), y, T, K, _f64(kc), 1)
+    return y
+
+
+def spgqp_solve_kc(b, x0, T, K, kc, opts: SpgOpts | None = None):
+    opts = opts or spg_opts()
+    x = _f64(x0).copy()
+    r = SpgResult()
+    lib().pasc_oracle_spgqp_solve_kc(_f64(b), x, T, K, _f64(kc), C.byref(opts), C.byref(r), 1)
+    return x, r
+
+
+def tssolver_solve_model(data, gamma_raw, theta0, T, K, epssqr, fem_reduce=1.0, fem_type=0,
+                         usethetainpenalty=False, scalef=1, ts: TsOpts | None = None,
+                         spg: SpgOpts | None = None, nthreads=1):
+    """Returns (gamma, theta, TsResult)."""
+    ts = ts or ts_opts()
+    spg = spg or spg_opts()
+    g = _f64(gamma_raw).copy()
+    th = _f64(theta0).copy()
+    r = TsResult()
+    rc = lib().pasc_oracle_tssolver_solve_model(_f64(data), g, th, T, K, epssqr, scalef, fem_reduce, fem_type,
+                                                1 if usethetainpenalty else 0, C.byref(ts), C.byref(spg),
+                                                C.byref(r), nthreads)
+    if rc != 0:
+        raise ValueError("tssolver_solve_model: unsupported combination")
     return g, th, r
 
 

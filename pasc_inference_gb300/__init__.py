@@ -159,6 +159,16 @@ class Problem:
         check(load().pasc_gb300_get_fem(self._h, C.byref(r), C.byref(t), C.byref(T2)))
         return r.value, t.value, T2.value
 
+    def set_usethetainpenalty(self, on: bool = True):
+        """Theta in the penalty: block k of A scaled by alpha*theta_k^2, theta step with the
+        penalty term (xdim 1, no FEM reduction)."""
+        check(load().pasc_gb300_set_usethetainpenalty(self._h, 1 if on else 0))
+
+    def get_usethetainpenalty(self) -> bool:
+        v = C.c_int()
+        check(load().pasc_gb300_get_usethetainpenalty(self._h, C.byref(v)))
+        return bool(v.value)
+
     def get_b(self) -> np.ndarray:
         out = np.empty(self.T * self.K)
         check(load().pasc_gb300_get_b(self._h, out))
@@ -428,8 +438,6 @@ class GraphH1FEMModel:
 
     def __init__(self, tsdata: TSData, epssqr: float, fem=None, usethetainpenalty: bool = False,
                  precision: int = PASC_PREC_MIXED, gamma0=None, seed: int = 13, device: int = 0):
-        if usethetainpenalty:
-            raise PascError(capi.PASC_ERR_NOTSUPP, "usethetainpenalty is not supported")
         self.tsdata = tsdata
         self.epssqr = float(epssqr)
         T, K = tsdata.get_T(), tsdata.get_K()
@@ -437,6 +445,9 @@ class GraphH1FEMModel:
         self.fem = fem if fem is not None else Fem(1.0)
         if self.fem.is_reduced():
             self.problem.set_fem(self.fem.fem_reduce, self.fem.fem_type)
+        self.usethetainpenalty = bool(usethetainpenalty)
+        if self.usethetainpenalty:
+            self.problem.set_usethetainpenalty(True)
         self.problem.set_data(tsdata.get_datavector())
         if gamma0 is None:
             from .datagen import uniform
@@ -451,6 +462,9 @@ class GraphH1FEMModel:
 
     def get_aic(self, L: float) -> float:
         return 2 * np.log(L) + self.tsdata.get_K()
+
+    def get_usethetainpenalty(self) -> bool:
+        return self.usethetainpenalty
 
     def get_name(self):
         return "Graph-H1-FEM Time-Series Model"

@@ -100,6 +100,8 @@ PROTOTYPES = {
     "pasc_gb300_fem_reduce_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_long, C.c_int, C.c_int, C.c_void_p]),
     "pasc_gb300_fem_prolongate_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_long, C.c_int, C.c_int,
                                                 C.c_void_p]),
+    "pasc_gb300_set_usethetainpenalty": (C.c_int, [_h, C.c_int]),
+    "pasc_gb300_get_usethetainpenalty": (C.c_int, [_h, C.POINTER(C.c_int)]),
     "pasc_gb300_time_model_kernels": (C.c_int, [_h, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "pasc_gb300_set_residual_engine": (C.c_int, [_h, C.c_int]),
     "pasc_gb300_get_residual_engine": (C.c_int, [_h, C.POINTER(C.c_int)]),

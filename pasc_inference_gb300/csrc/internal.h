@@ -52,6 +52,9 @@ struct SweepArgs {
     double *partials;   // gridDim.x * 4
     SpgDevState *st;
     long T;
+    // theta in the penalty (GraphH1FEMModel with usethetainpenalty): block k of A is
+    // coeff * kw[k] * A_hat with kw[k] = theta_k^2; null: every block is coeff * A_hat
+    const float *kw = nullptr;
 };
 
 struct ThetaArgs {
@@ -63,6 +66,9 @@ struct ThetaArgs {
     SpgDevState *st;          // counter2 is the last-block ticket
     long T;
     int cur;                  // buffer holding gamma
+    // theta in the penalty: theta_k = g'x / (sum g + g'(pen_alpha A_hat)g / 2) when tp
+    double pen_alpha = 0.0;
+    int tp = 0;
 };
 
 // One signal of a batch (device copy).
@@ -142,13 +148,14 @@ void record_error(const char *msg);
 // Launchers (kernels_fused.cu).  Return a cudaError_t.
 int sweep_block_threads();
 int sweep_tile_width();
-int sweep_blocks_per_sm(int K, bool init);
+int sweep_blocks_per_sm(int K, bool init, bool tp = false);  // tp: the theta-in-penalty form
 cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);  // a.bmat selects the b source
 // Bulk-copy (TMA) form of the sweep: 4 timesteps per thread, double-buffered tiles.
 bool sweep_tma_supported(int K);
 int sweep_tma_tile_width();
 int sweep_tma_max_tile();
-int sweep_tma_blocks_per_sm(int K, bool init, bool bmat = false);  // bmat: the materialised-b form
+// bmat: the materialised-b form; tp: the theta-in-penalty form (SweepArgs::kw set)
+int sweep_tma_blocks_per_sm(int K, bool init, bool bmat = false, bool tp = false);
 cudaError_t launch_sweep_tma(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);
 cudaError_t launch_theta_f32(int K, int grid, const ThetaArgs &a, cudaStream_t s);
 cudaError_t launch_project_f32(float *x, long T, int K, cudaStream_t s);
@@ -158,7 +165,9 @@ cudaError_t launch_f32_to_f64(const float *src, double *dst, long n, cudaStream_
 
 // Plain FP64 kernels (kernels_plain.cu).
 cudaError_t launch_project_f64(double *x, long T, int K, cudaStream_t s);
-cudaError_t launch_matmult_f64(const double *x, double *y, long T, int K, double coeff, cudaStream_t s);
+// kc != null: block k scaled by kc[k] (device memory) instead of coeff
+cudaError_t launch_matmult_f64(const double *x, double *y, long T, int K, double coeff, cudaStream_t s,
+                               const double *kc = nullptr);
 cudaError_t launch_axpy_f64(double *y, double a, const double *x, long n, cudaStream_t s);
 cudaError_t launch_xmay_f64(double *d, const double *x, double a, const double *g, long n, cudaStream_t s);
 cudaError_t launch_residual_f64(const double *data, const double *theta, double *b, long T, int K,
@@ -173,8 +182,12 @@ cudaError_t launch_dots_f64(int nq, const double *a0, const double *b0, const do
                             double *scratch, double *out, cudaStream_t s);
 cudaError_t launch_fx_f64(const double *x, const double *g, const double *b, long n,
                           double *scratch, double *out, cudaStream_t s);
+// tp: theta in the penalty, theta_k = g'x / (sum g + g'(pen_alpha A_hat)g / 2)
 cudaError_t launch_theta_f64(const double *gamma, const double *data, double *theta, long T, int K,
-                             double *scratch, cudaStream_t s);
+                             double *scratch, cudaStream_t s, bool tp = false, double pen_alpha = 0.0);
+// block coefficients of theta in the penalty from theta64: ck64[k] = (coeff theta_k) theta_k,
+// kw32[k] = theta_k^2 in FP32
+cudaError_t launch_tp_coeffs(const double *theta64, double coeff, int K, double *ck64, float *kw32, cudaStream_t s);
 cudaError_t launch_recon_abserr(const double *gamma, const double *theta, const double *sol,
                                 long T, int K, double *scratch, double *out, cudaStream_t s);
 cudaError_t launch_argmax(const double *gamma, int *labels, long T, int K, cudaStream_t s);

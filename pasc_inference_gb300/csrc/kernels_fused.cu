@@ -79,7 +79,8 @@ constexpr int SWEEP_W = SWEEP_NT - SWEEP_HL - SWEEP_HR;  // owned timesteps per 
 int sweep_block_threads() { return SWEEP_NT; }
 int sweep_tile_width() { return SWEEP_W; }
 
-template <int K, bool INIT, bool BMAT>
+// TP: theta in the penalty, block k of A is coeff * a.kw[k] * A_hat (usethetainpenalty)
+template <int K, bool INIT, bool BMAT, bool TP = false>
 __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_sweep_kernel(SweepArgs a)
 {
     __shared__ float s_x[SWEEP_NT * K];  // x^c (zero outside 0 <= t < T)
@@ -100,9 +101,13 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
     const float bscale = (float)st->bscale;
     const int T = (int)a.T;  // K*T < 2^31 (checked at creation)
 
-    float theta[K];
+    float theta[K], ck[K], kw[K];
 #pragma unroll
-    for (int k = 0; k < K; k++) theta[k] = BMAT ? 0.f : a.theta[k];
+    for (int k = 0; k < K; k++) {
+        theta[k] = BMAT ? 0.f : a.theta[k];
+        kw[k] = TP ? a.kw[k] : 1.f;
+        ck[k] = TP ? coeff * kw[k] : coeff;
+    }
 
     KahanF acc_f;  // the objective keeps a compensated sum; the dots need less
     float acc_dd = 0.f, acc_dAd = 0.f, acc_gd = 0.f;
@@ -185,7 +190,7 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
 #pragma unroll
             for (int k = 0; k < K; k++) {
                 const float S = ml * (xc[k] - s_x[il + k]) + mr * (xc[k] - s_x[ir + k]);
-                const float g = coeff * S - bk[k];
+                const float g = ck[k] * S - bk[k];
                 z[k] = xc[k] - a0 * g;
             }
             project_reg<K>(z);
@@ -205,7 +210,7 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
 #pragma unroll
             for (int k = 0; k < K; k++) {
                 const float S = ml * (x1[k] - s_y[il + k]) + mr * (x1[k] - s_y[ir + k]);
-                g1[k] = coeff * S - bk[k];
+                g1[k] = ck[k] * S - bk[k];
                 fpart += (g1[k] - bk[k]) * x1[k];
                 d1[k] = x1[k] - a1 * g1[k];
             }
@@ -227,7 +232,7 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
                 acc_dd += d1[k] * d1[k];
                 acc_gd += g1[k] * d1[k];
                 const float df = right ? s_d[ir + k] - d1[k] : 0.f;
-                acc_dAd += df * df;
+                acc_dAd += TP ? kw[k] * df * df : df * df;
             }
             store_row<K>(xout + t * K, x1);
         }
@@ -254,17 +259,18 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
 }
 
 template <int K, bool INIT>
-static int blocks_per_sm_t()
+static int blocks_per_sm_t(bool tp)
 {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_kernel<K, INIT, false>, SWEEP_NT, 0);
+    if (tp) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_kernel<K, INIT, false, true>, SWEEP_NT, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_kernel<K, INIT, false>, SWEEP_NT, 0);
     return nb > 0 ? nb : 1;
 }
 
-int sweep_blocks_per_sm(int K, bool init)
+int sweep_blocks_per_sm(int K, bool init, bool tp)
 {
     switch (K) {
-#define PASC_CASE(KK) case KK: return init ? blocks_per_sm_t<KK, true>() : blocks_per_sm_t<KK, false>();
+#define PASC_CASE(KK) case KK: return init ? blocks_per_sm_t<KK, true>(tp) : blocks_per_sm_t<KK, false>(tp);
         PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
         PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
 #undef PASC_CASE
@@ -280,6 +286,9 @@ cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStr
         if (a.bmat) {                                                                   \
             if (init) spg_sweep_kernel<KK, true, true><<<grid, SWEEP_NT, 0, s>>>(a);    \
             else spg_sweep_kernel<KK, false, true><<<grid, SWEEP_NT, 0, s>>>(a);        \
+        } else if (a.kw) {                                                              \
+            if (init) spg_sweep_kernel<KK, true, false, true><<<grid, SWEEP_NT, 0, s>>>(a); \
+            else spg_sweep_kernel<KK, false, false, true><<<grid, SWEEP_NT, 0, s>>>(a); \
         } else {                                                                        \
             if (init) spg_sweep_kernel<KK, true, false><<<grid, SWEEP_NT, 0, s>>>(a);   \
             else spg_sweep_kernel<KK, false, false><<<grid, SWEEP_NT, 0, s>>>(a);       \
@@ -297,47 +306,66 @@ cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStr
 // theta update (graphh1fem.cpp:347-380): theta_k = sum_t gamma_tk x_t / sum_t gamma_tk.
 // FP32 gamma/data, compensated FP32 per thread, FP64 per block and grid; the last block
 // writes theta in FP64 and FP32.
+// TP (usethetainpenalty, graphh1fem.cpp:318-372): theta_k = g'x / (sum g + g'(alpha A_hat)g / 2)
+// with gamma_k'A_hat gamma_k taken in the difference form 2 sum_t (g_{t+1} - g_t)^2.
 // ---------------------------------------------------------------------------------------
 constexpr int THETA_NT = 256;
 
-template <int K>
+template <int K, bool TP = false>
 __global__ void __launch_bounds__(THETA_NT) theta_kernel(ThetaArgs a)
 {
-    __shared__ double s_red[2 * K * (THETA_NT / 32)];
+    constexpr int NQ = TP ? 3 * K : 2 * K;
+    __shared__ double s_red[NQ * (THETA_NT / 32)];
     const float *gam = a.cur ? a.xb1 : a.xb0;
-    KahanF sx[K], sg[K];
+    KahanF sx[K], sg[K], sa[TP ? K : 1];
     const long stride = (long)gridDim.x * THETA_NT;
     for (long t = (long)blockIdx.x * THETA_NT + threadIdx.x; t < a.T; t += stride) {
         const float x = __ldg(a.data + t);
+        const bool right = TP && t + 1 < a.T;
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const float gk = __ldcs(gam + t * K + k);
             sg[k].add(gk);
             sx[k].add(__fmul_rn(x, gk));
+            if (TP && right) {
+                const float df = __ldg(gam + (t + 1) * K + k) - gk;
+                sa[TP ? k : 0].add(df * df);
+            }
         }
     }
-    double v[2 * K];
+    double v[NQ];
 #pragma unroll
-    for (int k = 0; k < K; k++) { v[k] = sx[k].value(); v[K + k] = sg[k].value(); }
-    block_sum<2 * K>(v, s_red);
+    for (int k = 0; k < K; k++) {
+        v[k] = sx[k].value();
+        v[K + k] = sg[k].value();
+        if (TP) v[(TP ? 2 * K : 0) + k] = sa[TP ? k : 0].value();
+    }
+    block_sum<NQ>(v, s_red);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int q = 0; q < 2 * K; q++) a.partials[blockIdx.x * 2 * K + q] = v[q];
+        for (int q = 0; q < NQ; q++) a.partials[blockIdx.x * NQ + q] = v[q];
     }
     if (!last_block_done(&a.st->counter2)) return;
-    double w[2 * K];
+    double w[NQ];
 #pragma unroll
-    for (int q = 0; q < 2 * K; q++) w[q] = 0.0;
+    for (int q = 0; q < NQ; q++) w[q] = 0.0;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += THETA_NT) {
 #pragma unroll
-        for (int q = 0; q < 2 * K; q++) w[q] += __ldcg(a.partials + b * 2 * K + q);
+        for (int q = 0; q < NQ; q++) w[q] += __ldcg(a.partials + b * NQ + q);
     }
-    block_sum<2 * K>(w, s_red);
+    block_sum<NQ>(w, s_red);
     if (threadIdx.x == 0) {
         a.st->counter2 = 0;
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const double th = (w[K + k] != 0.0) ? w[k] / w[K + k] : 0.0;
+            double th;
+            if (TP) {
+                const double gAg = a.pen_alpha * (2.0 * w[(TP ? 2 * K : 0) + k]);
+                const double den = 1.0 * w[K + k] + 0.5 * gAg;
+                th = den != 0.0 ? (1.0 * w[k]) / den : 0.0;
+            } else {
+                th = (w[K + k] != 0.0) ? w[k] / w[K + k] : 0.0;
+            }
             a.theta64[k] = th;
             a.theta32[k] = (float)th;
         }
@@ -347,7 +375,11 @@ __global__ void __launch_bounds__(THETA_NT) theta_kernel(ThetaArgs a)
 cudaError_t launch_theta_f32(int K, int grid, const ThetaArgs &a, cudaStream_t s)
 {
     switch (K) {
-#define PASC_CASE(KK) case KK: theta_kernel<KK><<<grid, THETA_NT, 0, s>>>(a); break;
+#define PASC_CASE(KK)                                                          \
+    case KK:                                                                   \
+        if (a.tp) theta_kernel<KK, true><<<grid, THETA_NT, 0, s>>>(a);         \
+        else theta_kernel<KK><<<grid, THETA_NT, 0, s>>>(a);                    \
+        break;
         PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
         PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
 #undef PASC_CASE

@@ -60,29 +60,55 @@ cudaError_t launch_project_f64(double *x, long T, int K, cudaStream_t s)
 // FEM-H1 operator: assembled row (blockgraphsparse.cpp:51-109, R = 1) summed over ascending
 // columns from 0.0 like MatMult, then VecScale by coeff (spgqpsolver.cpp:122-123).
 // ---------------------------------------------------------------------------------------
-__global__ void matmult_f64_kernel(const double *x, double *y, long T, int K, double coeff)
+// the assembled row t of A_hat applied to column k of x (x points at element (t, k))
+__device__ __forceinline__ double ahat_row_f64(const double *x, long t, long T, int K)
+{
+    double sum = 0.0;
+    if (T == 1) {
+        sum = __dadd_rn(sum, __dmul_rn(0.0, x[0]));
+    } else {
+        const double w = (t == 0 || t == T - 1) ? 2.0 : 4.0;
+        if (t > 0) sum = __dadd_rn(sum, __dmul_rn(-2.0, x[-K]));
+        sum = __dadd_rn(sum, __dmul_rn(w, x[0]));
+        if (t < T - 1) sum = __dadd_rn(sum, __dmul_rn(-2.0, x[K]));
+    }
+    return sum;
+}
+
+// kc != null: block k scaled by kc[k] (BlockGraphSparseMatrix with coefficients,
+// blockgraphsparse.cpp:161-185: VecScale of block k by alpha*theta_k*theta_k)
+__global__ void matmult_f64_kernel(const double *x, double *y, long T, int K, double coeff, const double *kc)
 {
     const long n = T * K;
     const long stride = (long)gridDim.x * blockDim.x;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const long t = i / K;
-        double sum = 0.0;
-        if (T == 1) {
-            sum = __dadd_rn(sum, __dmul_rn(0.0, x[i]));
-        } else {
-            const double w = (t == 0 || t == T - 1) ? 2.0 : 4.0;
-            if (t > 0) sum = __dadd_rn(sum, __dmul_rn(-2.0, x[i - K]));
-            sum = __dadd_rn(sum, __dmul_rn(w, x[i]));
-            if (t < T - 1) sum = __dadd_rn(sum, __dmul_rn(-2.0, x[i + K]));
-        }
-        y[i] = __dmul_rn(coeff, sum);
+        const double sum = ahat_row_f64(x + i, t, T, K);
+        y[i] = __dmul_rn(kc ? kc[i - t * K] : coeff, sum);
     }
 }
 
-cudaError_t launch_matmult_f64(const double *x, double *y, long T, int K, double coeff, cudaStream_t s)
+cudaError_t launch_matmult_f64(const double *x, double *y, long T, int K, double coeff, cudaStream_t s,
+                               const double *kc)
 {
     if (T <= 0) return cudaSuccess;
-    matmult_f64_kernel<<<grid_elems(T * K), PLAIN_NT, 0, s>>>(x, y, T, K, coeff);
+    matmult_f64_kernel<<<grid_elems(T * K), PLAIN_NT, 0, s>>>(x, y, T, K, coeff, kc);
+    return cudaGetLastError();
+}
+
+// ck64[k] = (coeff * theta_k) * theta_k (the order of blockgraphsparse.cpp:177), kw32[k] = theta_k^2
+__global__ void tp_coeffs_kernel(const double *theta, double coeff, int K, double *ck64, float *kw32)
+{
+    const int k = threadIdx.x;
+    if (k >= K) return;
+    const double th = theta[k];
+    ck64[k] = __dmul_rn(__dmul_rn(coeff, th), th);
+    if (kw32) kw32[k] = (float)__dmul_rn(th, th);
+}
+
+cudaError_t launch_tp_coeffs(const double *theta64, double coeff, int K, double *ck64, float *kw32, cudaStream_t s)
+{
+    tp_coeffs_kernel<<<1, 32 * ((K + 31) / 32), 0, s>>>(theta64, coeff, K, ck64, kw32);
     return cudaGetLastError();
 }
 
@@ -234,16 +260,19 @@ cudaError_t launch_fx_f64(const double *x, const double *g, const double *b, lon
     return cudaGetLastError();
 }
 
-// theta_k = sum_t gamma_tk x_t / sum_t gamma_tk (graphh1fem.cpp:347-380), K <= 32 per pass.
-template <int KB>
+// theta_k = sum_t gamma_tk x_t / sum_t gamma_tk (graphh1fem.cpp:347-380), KB clusters per pass.
+// TP (usethetainpenalty, graphh1fem.cpp:318-372): theta is set to 1, Agamma = A gamma with that
+// theta (block k scaled by alpha), and theta_k = g'x / (sum g + gamma_k'Agamma_k / 2).
+template <int KB, bool TP>
 __global__ void __launch_bounds__(PLAIN_NT) theta_f64_kernel(const double *gamma, const double *data,
                                                              double *theta, long T, int K, int k0,
-                                                             double *scratch)
+                                                             double *scratch, double alpha)
 {
-    __shared__ double s_red[2 * KB * (PLAIN_NT / 32)];
-    double v[2 * KB];
+    constexpr int NQ = (TP ? 3 : 2) * KB;
+    __shared__ double s_red[NQ * (PLAIN_NT / 32)];
+    double v[NQ];
 #pragma unroll
-    for (int q = 0; q < 2 * KB; q++) v[q] = 0.0;
+    for (int q = 0; q < NQ; q++) v[q] = 0.0;
     const int nk = min(KB, K - k0);
     const long stride = (long)gridDim.x * PLAIN_NT;
     for (long t = (long)blockIdx.x * PLAIN_NT + threadIdx.x; t < T; t += stride) {
@@ -254,37 +283,49 @@ __global__ void __launch_bounds__(PLAIN_NT) theta_f64_kernel(const double *gamma
                 const double gk = gamma[t * K + k0 + q];
                 v[q] = __dadd_rn(v[q], __dmul_rn(x, gk));
                 v[KB + q] = __dadd_rn(v[KB + q], gk);
+                if (TP) {
+                    const double agk = __dmul_rn(alpha, ahat_row_f64(gamma + t * K + k0 + q, t, T, K));
+                    v[(TP ? 2 * KB : 0) + q] = __dadd_rn(v[(TP ? 2 * KB : 0) + q], __dmul_rn(gk, agk));
+                }
             }
         }
     }
-    block_sum<2 * KB>(v, s_red);
+    block_sum<NQ>(v, s_red);
     unsigned int *counter = reinterpret_cast<unsigned int *>(scratch + 4096 * 4);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int q = 0; q < 2 * KB; q++) scratch[blockIdx.x * 2 * KB + q] = v[q];
+        for (int q = 0; q < NQ; q++) scratch[blockIdx.x * NQ + q] = v[q];
     }
     if (!last_block_done(counter)) return;
-    double w[2 * KB];
+    double w[NQ];
 #pragma unroll
-    for (int q = 0; q < 2 * KB; q++) w[q] = 0.0;
+    for (int q = 0; q < NQ; q++) w[q] = 0.0;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += PLAIN_NT) {
 #pragma unroll
-        for (int q = 0; q < 2 * KB; q++) w[q] = __dadd_rn(w[q], __ldcg(scratch + b * 2 * KB + q));
+        for (int q = 0; q < NQ; q++) w[q] = __dadd_rn(w[q], __ldcg(scratch + b * NQ + q));
     }
-    block_sum<2 * KB>(w, s_red);
+    block_sum<NQ>(w, s_red);
     if (threadIdx.x == 0) {
         *counter = 0;
-        for (int q = 0; q < nk; q++) theta[k0 + q] = (w[KB + q] != 0.0) ? w[q] / w[KB + q] : 0.0;
+        for (int q = 0; q < nk; q++) {
+            if (TP) {
+                const double den = 1.0 * w[KB + q] + 0.5 * w[(TP ? 2 * KB : 0) + q];
+                theta[k0 + q] = den != 0.0 ? (1.0 * w[q]) / den : 0.0;
+            } else {
+                theta[k0 + q] = (w[KB + q] != 0.0) ? w[q] / w[KB + q] : 0.0;
+            }
+        }
     }
 }
 
 cudaError_t launch_theta_f64(const double *gamma, const double *data, double *theta, long T, int K,
-                             double *scratch, cudaStream_t s)
+                             double *scratch, cudaStream_t s, bool tp, double pen_alpha)
 {
-    // 4096*4 doubles of partials: grid * 2*KB must fit
-    const int g = min(grid_reduce(), 4096 * 4 / (2 * 8));
+    // 4096*4 doubles of partials: grid * 3*KB must fit
+    const int g = min(grid_reduce(), 4096 * 4 / (3 * 8));
     for (int k0 = 0; k0 < K; k0 += 8) {
-        theta_f64_kernel<8><<<g, PLAIN_NT, 0, s>>>(gamma, data, theta, T, K, k0, scratch);
+        if (tp) theta_f64_kernel<8, true><<<g, PLAIN_NT, 0, s>>>(gamma, data, theta, T, K, k0, scratch, pen_alpha);
+        else theta_f64_kernel<8, false><<<g, PLAIN_NT, 0, s>>>(gamma, data, theta, T, K, k0, scratch, 0.0);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

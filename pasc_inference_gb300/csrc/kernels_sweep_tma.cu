@@ -14,6 +14,9 @@
 //   - each thread reads its 4*K values with 16-byte shared loads (conflict-free), keeps them in
 //     registers, and exchanges only its first and last timestep with its neighbours;
 //   - x^{c+1} goes from registers straight to HBM with 16-byte stores.
+// MODE 0: b formed from data and theta; 1: b read from a materialised T*K array (multichannel
+// data, reduced FEM problems); 2: as 0 with theta in the penalty (block k of A weighted by
+// theta_k^2, GraphH1FEMModel with usethetainpenalty, blockgraphsparse.cpp:161-185).
 // Every wait on an mbarrier is bounded: a wait that gives up sets the error word of the
 // device state (the host then reports PASC_ERR_TIMEOUT), the block waits once more, bounded,
 // for the copies it has in flight, and leaves its tile loop.
@@ -22,9 +25,10 @@
 
 namespace pasc {
 
-template <int K, int NT, bool INIT, bool BM>
+template <int K, int NT, bool INIT, int MODE>
 __global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
 {
+    constexpr bool BM = MODE == 1, TP = MODE == 2;
     constexpr int P = NT * TMA_R;
     constexpr int W = P - 2 * TMA_HALO;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -45,7 +49,10 @@ __global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
     sc.bscale = (float)st->bscale;
     sc.T = (int)a.T;
 #pragma unroll
-    for (int k = 0; k < K; k++) sc.theta[k] = a.theta[k];
+    for (int k = 0; k < K; k++) {
+        sc.theta[k] = a.theta[k];
+        sc.kw[k] = TP ? a.kw[k] : 1.f;
+    }
     const int ntiles = (sc.T + W - 1) / W;
     const int i = threadIdx.x;
 
@@ -79,8 +86,8 @@ __global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
         }
         parity ^= 1u << s;
         const int next2 = tile + 2 * (int)gridDim.x;
-        tma_tile<K, K, NT, INIT, BM>(sm, s, tile * W - TMA_HALO, sc, acc,
-                                 next2 < ntiles ? next2 * W - TMA_HALO : TMA_NO_REFILL);
+        tma_tile<K, K, NT, INIT, BM, TP>(sm, s, tile * W - TMA_HALO, sc, acc,
+                                         next2 < ntiles ? next2 * W - TMA_HALO : TMA_NO_REFILL);
     }
 
     // block and grid reductions
@@ -107,30 +114,32 @@ static cudaError_t launch_tma_t(int grid, const SweepArgs &a, cudaStream_t s)
 {
     // the dynamic shared memory limit was raised by tma_blocks_per_sm_t at problem creation
     // (no attribute call here: launches may be inside a stream capture)
-    if (a.bmat) spg_sweep_tma_kernel<K, NT, INIT, true><<<grid, NT, sizeof(TmaSmem<K, NT, true>), s>>>(a);
-    else spg_sweep_tma_kernel<K, NT, INIT, false><<<grid, NT, sizeof(TmaSmem<K, NT, false>), s>>>(a);
+    if (a.bmat) spg_sweep_tma_kernel<K, NT, INIT, 1><<<grid, NT, sizeof(TmaSmem<K, NT, true>), s>>>(a);
+    else if (a.kw) spg_sweep_tma_kernel<K, NT, INIT, 2><<<grid, NT, sizeof(TmaSmem<K, NT, false>), s>>>(a);
+    else spg_sweep_tma_kernel<K, NT, INIT, 0><<<grid, NT, sizeof(TmaSmem<K, NT, false>), s>>>(a);
     return cudaGetLastError();
 }
 
-template <int K, int NT, bool INIT, bool BM>
-static int tma_blocks_per_sm_bm()
+template <int K, int NT, bool INIT, int MODE>
+static int tma_blocks_per_sm_mode()
 {
-    const size_t smem = sizeof(TmaSmem<K, NT, BM>);
-    cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const size_t smem = sizeof(TmaSmem<K, NT, MODE == 1>);
+    cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_tma_kernel<K, NT, INIT, BM>, NT, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_tma_kernel<K, NT, INIT, MODE>, NT, smem);
     return nb > 0 ? nb : 1;
 }
 
-// sets the shared-memory limit of both forms (data / materialised b); returns the occupancy
-// of the form `bm` selects
+// sets the shared-memory limit of the three forms; returns the occupancy of the form that
+// `bm` / `tp` select
 template <int K, int NT, bool INIT>
-static int tma_blocks_per_sm_t(bool bm)
+static int tma_blocks_per_sm_t(bool bm, bool tp)
 {
-    const int n0 = tma_blocks_per_sm_bm<K, NT, INIT, false>();
-    const int n1 = tma_blocks_per_sm_bm<K, NT, INIT, true>();
-    return bm ? n1 : n0;
+    const int n0 = tma_blocks_per_sm_mode<K, NT, INIT, 0>();
+    const int n1 = tma_blocks_per_sm_mode<K, NT, INIT, 1>();
+    const int n2 = tma_blocks_per_sm_mode<K, NT, INIT, 2>();
+    return bm ? n1 : (tp ? n2 : n0);
 }
 
 constexpr int TMA_NT = 128;
@@ -140,11 +149,13 @@ int sweep_tma_max_tile() { return TMA_NT * TMA_R; }
 
 bool sweep_tma_supported(int K) { return K >= 1 && K <= 8; }
 
-int sweep_tma_blocks_per_sm(int K, bool init, bool bmat)
+int sweep_tma_blocks_per_sm(int K, bool init, bool bmat, bool tp)
 {
     switch (K) {
-#define PASC_CASE(KK) \
-    case KK: return init ? tma_blocks_per_sm_t<KK, TMA_NT, true>(bmat) : tma_blocks_per_sm_t<KK, TMA_NT, false>(bmat);
+#define PASC_CASE(KK)                                                       \
+    case KK:                                                                \
+        return init ? tma_blocks_per_sm_t<KK, TMA_NT, true>(bmat, tp)       \
+                    : tma_blocks_per_sm_t<KK, TMA_NT, false>(bmat, tp);
         PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
         PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
 #undef PASC_CASE

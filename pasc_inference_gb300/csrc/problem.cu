@@ -63,7 +63,7 @@ static void free_all(pasc_gb300_problem *p)
     void *dev[] = {p->data64, p->theta64, p->stage64, p->red, p->red_out, p->labels_d, p->x, p->g,
                    p->d, p->Ad, p->b, p->data32_raw, p->theta32, p->xb_raw[0], p->xb_raw[1], p->st,
                    p->partials, p->xbf, p->xnorm, p->bmat_raw, p->theta_split, p->theta_f32, p->tnorm,
-                   p->mc_partials, p->mc_err};
+                   p->mc_partials, p->mc_err, p->tp_ck64, p->tp_kw32};
     for (void *q : dev)
         if (q) cudaFree(q);
     if (p->st_h) cudaFreeHost(p->st_h);
@@ -239,7 +239,8 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
             np = np > p->grid_sweep[v] ? np : p->grid_sweep[v];
             np = np > p->grid_sweep_init[v] ? np : p->grid_sweep_init[v];
         }
-        np = np * 4 > (long)p->grid_theta * 2 * K ? np * 4 : (long)p->grid_theta * 2 * K;
+        // (the theta kernel with theta in the penalty keeps 3K partials per block)
+        np = np * 4 > (long)p->grid_theta * 3 * K ? np * 4 : (long)p->grid_theta * 3 * K;
         if ((rc = dalloc(&p->partials, np))) return bail(rc);
         if (xdim > 1) {
             long gm = (long)p->sms * 4, tb64 = (T + 63) / 64;
@@ -297,6 +298,11 @@ int pasc_gb300_set_epssqr(pasc_gb300_problem *p, double epssqr, int scalef)
     p->scalef = scalef ? 1 : 0;
     set_coeffs(p);
     if (p->fem_inner) fem_set_inner_coeffs(p);
+    if (p->tp) {
+        CU(cudaSetDevice(p->device));
+        CU(launch_tp_coeffs(p->theta64, p->coeffA, p->K, p->tp_ck64, p->tp_kw32, p->stream));
+        CU(cudaStreamSynchronize(p->stream));
+    }
     return PASC_OK;
 }
 
@@ -462,6 +468,7 @@ int pasc_gb300_set_theta(pasc_gb300_problem *p, const double *theta)
     } else if (p->precision == PASC_PREC_MIXED) {
         CU(launch_f64_to_f32(p->theta64, p->theta32, p->K, p->stream));
     }
+    if (p->tp) CU(launch_tp_coeffs(p->theta64, p->coeffA, p->K, p->tp_ck64, p->tp_kw32, p->stream));
     CU(cudaStreamSynchronize(p->stream));
     CHK(mc_check_error(p));
     return PASC_OK;
@@ -507,7 +514,8 @@ static int update_theta_async(pasc_gb300_problem *p, int *launches)
         return PASC_OK;
     }
     if (p->precision == PASC_PREC_FP64) {
-        CU(launch_theta_f64(p->x, p->data64, p->theta64, p->T, p->K, p->red, p->stream));
+        // theta in the penalty: Agamma with theta = 1, i.e. A = coeffA * A_hat (graphh1fem.cpp:314-325)
+        CU(launch_theta_f64(p->x, p->data64, p->theta64, p->T, p->K, p->red, p->stream, p->tp, p->coeffA));
         if (launches) *launches += (p->K + 7) / 8;
     } else {
         ThetaArgs a;
@@ -520,7 +528,13 @@ static int update_theta_async(pasc_gb300_problem *p, int *launches)
         a.st = p->st;
         a.T = p->T;
         a.cur = p->cur;
+        a.tp = p->tp ? 1 : 0;
+        a.pen_alpha = p->coeffA;
         CU(launch_theta_f32(p->K, p->grid_theta, a, p->stream));
+        if (launches) *launches += 1;
+    }
+    if (p->tp) {
+        CU(launch_tp_coeffs(p->theta64, p->coeffA, p->K, p->tp_ck64, p->tp_kw32, p->stream));
         if (launches) *launches += 1;
     }
     return PASC_OK;
@@ -600,7 +614,7 @@ static int fp64_start(pasc_gb300_problem *p)
     r.normb = sqrt(v[0]);             // :104
     r.alpha = r.o.alphainit;          // :108
     CU(launch_project_f64(p->x, T, K, s));                   // :116
-    CU(launch_matmult_f64(p->x, p->g, T, K, p->coeffA, s));  // :122-123
+    CU(launch_matmult_f64(p->x, p->g, T, K, p->coeffA, s, p->tp ? p->tp_ck64 : nullptr));  // :122-123
     CU(launch_axpy_f64(p->g, -1.0, p->b, N, s));             // :128
     CU(launch_fx_f64(p->x, p->g, p->b, N, p->red, p->red_out, s));  // :133
     r.launches += 4;
@@ -636,7 +650,7 @@ static int fp64_iterate(pasc_gb300_problem *p, long n)
         CU(launch_xmay_f64(p->d, p->x, r.alpha, p->g, N, s));    // :146-147
         CU(launch_project_f64(p->d, T, K, s));                    // :153
         CU(launch_axpy_f64(p->d, -1.0, p->x, N, s));              // :158
-        CU(launch_matmult_f64(p->d, p->Ad, T, K, p->coeffA, s));  // :164-165
+        CU(launch_matmult_f64(p->d, p->Ad, T, K, p->coeffA, s, p->tp ? p->tp_ck64 : nullptr));  // :164-165
         r.hessmult += 1;
         CU(launch_dots_f64(3, p->d, p->d, p->d, p->Ad, p->d, p->g, N, p->red, p->red_out, s));  // :357-363
         r.launches += 5;
@@ -707,6 +721,7 @@ static int sweep_args(pasc_gb300_problem *p, SweepArgs *a)
     a->partials = p->partials;
     a->st = p->st;
     a->T = p->T;
+    a->kw = p->tp ? p->tp_kw32 : nullptr;
     return PASC_OK;
 }
 
@@ -714,12 +729,16 @@ static constexpr int GRAPH_CHUNK = 16;
 
 static cudaError_t launch_variant(pasc_gb300_problem *p, int v, bool init, const SweepArgs &a)
 {
-    if (v == 1) return launch_sweep_tma(p->K, init, init ? p->grid_sweep_init[1] : p->grid_sweep[1], a, p->stream);
-    return launch_sweep(p->K, init, init ? p->grid_sweep_init[0] : p->grid_sweep[0], a, p->stream);
+    const int *gs = a.kw ? p->grid_sweep_tp : p->grid_sweep;
+    const int *gi = a.kw ? p->grid_sweep_init_tp : p->grid_sweep_init;
+    if (v == 1) return launch_sweep_tma(p->K, init, init ? gi[1] : gs[1], a, p->stream);
+    return launch_sweep(p->K, init, init ? gi[0] : gs[0], a, p->stream);
 }
 
 static int ensure_chunk_graph(pasc_gb300_problem *p)
 {
+    // (the captured kernel depends on the theta-in-penalty flag too: set_usethetainpenalty
+    // destroys the graph)
     if (p->chunk_graph && p->chunk_graph_variant == p->variant) return PASC_OK;
     if (p->chunk_graph) {
         cudaGraphExecDestroy(p->chunk_graph);
@@ -1160,6 +1179,8 @@ int pasc_gb300_set_fem(pasc_gb300_problem *p, double fem_reduce, int fem_type)
     if (!p) return fail(PASC_ERR_ARG, "set_fem: NULL problem");
     if (!(fem_reduce > 0.0) || fem_reduce > 1.0) return fail(PASC_ERR_ARG, "set_fem: fem_reduce must be in (0, 1]");
     if (fem_type != 0 && fem_type != 1) return fail(PASC_ERR_ARG, "set_fem: fem_type 0 (FEM-SUM) or 1 (FEM-HAT)");
+    if (p->tp && fem_reduce < 1.0)
+        return fail(PASC_ERR_NOTSUPP, "set_fem: theta in the penalty with a reduced (fem_reduce < 1) problem");
     CU(cudaSetDevice(p->device));
     CU(cudaStreamSynchronize(p->stream));
     if (p->fem_inner) {
@@ -1275,6 +1296,64 @@ int pasc_gb300_get_sweep_variant(pasc_gb300_problem *p, int *variant)
 {
     if (!p || !variant) return fail(PASC_ERR_ARG, "get_sweep_variant: NULL argument");
     *variant = p->variant;
+    return PASC_OK;
+}
+
+// GraphH1FEMModel(..., usethetainpenalty) (graphh1fem.cpp:8-19, 154-160): block k of the gamma
+// QP's A is scaled by alpha*theta_k*theta_k, and the theta step includes the penalty term.
+// One-dimensional data without FEM reduction only: the reference's theta step multiplies the
+// reduced operator with the full gamma (PETSc refuses the sizes), and its multichannel form
+// has no penalty term.
+int pasc_gb300_set_usethetainpenalty(pasc_gb300_problem *p, int on)
+{
+    if (!p) return fail(PASC_ERR_ARG, "set_usethetainpenalty: NULL problem");
+    if (on && p->xdim != 1)
+        return fail(PASC_ERR_NOTSUPP, "set_usethetainpenalty: one-dimensional data (xdim == 1) only");
+    if (on && p->fem_inner)
+        return fail(PASC_ERR_NOTSUPP, "set_usethetainpenalty: not with a reduced (fem_reduce < 1) problem");
+    CU(cudaSetDevice(p->device));
+    CU(cudaStreamSynchronize(p->stream));
+    p->run.started = false;
+    p->have_fx = false;
+    if (p->chunk_graph) {
+        cudaGraphExecDestroy(p->chunk_graph);
+        p->chunk_graph = nullptr;
+    }
+    p->tp = on != 0;
+    if (!p->tp) return PASC_OK;
+    if (!p->tp_ck64) {
+        int rc;
+        if ((rc = dalloc(&p->tp_ck64, p->K))) return rc;
+        if ((rc = dalloc(&p->tp_kw32, p->K))) return rc;
+    }
+    if (p->precision == PASC_PREC_MIXED) {
+        // the theta-in-penalty sweeps may hold fewer blocks per SM; never more than the
+        // partials buffer was sized for
+        const long nt_thread = (p->T + sweep_tile_width() - 1) / sweep_tile_width();
+        const long nt_tma = (p->T + sweep_tma_tile_width() - 1) / sweep_tma_tile_width();
+        auto grid = [&](long per_sm, long ntiles, int cap) {
+            long g = per_sm * p->sms;
+            g = g < ntiles ? g : ntiles;
+            g = g < cap ? g : cap;
+            return (int)(g < 1 ? 1 : g);
+        };
+        p->grid_sweep_tp[0] = grid(sweep_blocks_per_sm(p->K, false, true), nt_thread, p->grid_sweep[0]);
+        p->grid_sweep_init_tp[0] = grid(sweep_blocks_per_sm(p->K, true, true), nt_thread, p->grid_sweep_init[0]);
+        if (sweep_tma_supported(p->K)) {
+            p->grid_sweep_tp[1] = grid(sweep_tma_blocks_per_sm(p->K, false, false, true), nt_tma, p->grid_sweep[1]);
+            p->grid_sweep_init_tp[1] =
+                grid(sweep_tma_blocks_per_sm(p->K, true, false, true), nt_tma, p->grid_sweep_init[1]);
+        }
+    }
+    CU(launch_tp_coeffs(p->theta64, p->coeffA, p->K, p->tp_ck64, p->tp_kw32, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_get_usethetainpenalty(pasc_gb300_problem *p, int *on)
+{
+    if (!p || !on) return fail(PASC_ERR_ARG, "get_usethetainpenalty: NULL argument");
+    *on = p->tp ? 1 : 0;
     return PASC_OK;
 }
 

@@ -86,6 +86,13 @@ struct pasc_gb300_problem {
     pasc_gb300_problem *fem_inner = nullptr;
     bool b_external = false;               // inner handle: b is written by the owner
 
+    // theta in the penalty (pasc_gb300_set_usethetainpenalty): block k of A is
+    // coeffA * theta_k^2 * A_hat; ck64[k] = (coeffA theta_k) theta_k, kw32[k] = theta_k^2
+    bool tp = false;
+    double *tp_ck64 = nullptr;
+    float *tp_kw32 = nullptr;
+    int grid_sweep_tp[2] = {0, 0}, grid_sweep_init_tp[2] = {0, 0};
+
     pasc::SpgRun run;
     pasc::AdjointWork *adj = nullptr;  // allocated by the first adjoint call
     double fx_last = 0.0;

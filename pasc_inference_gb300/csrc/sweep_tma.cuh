@@ -94,6 +94,7 @@ template <int K>
 struct TileScalars {
     float a0, beta, a1, coeff, bscale;
     float theta[K];
+    float kw[K];  // TP: block weights theta_k^2 (block k of A is coeff * kw[k] * A_hat)
     int T;
     const float *xin;
     float *xout;
@@ -126,8 +127,9 @@ __device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM> &sm, int s, const 
 // (A_hat x)_r = 2 (D_r - D_{r+1}), which is bit for bit the difference form
 // 2[t>0](x_t - x_{t-1}) + 2[t<T-1](x_t - x_{t+1}) and needs one subtraction per neighbour
 // pair.  EDGE: the tile touches t <= 0 or t >= T-1 and needs the range masks; interior tiles
-// (all but the first and last of a signal) run without them.
-template <int K, int KB, int NT, bool INIT, bool BM, bool EDGE>
+// (all but the first and last of a signal) run without them.  TP: theta in the penalty, the
+// operator of cluster k is scaled by sc.kw[k] (and so is its share of d'Ad).
+template <int K, int KB, int NT, bool INIT, bool BM, bool EDGE, bool TP = false>
 __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM> &sm, int s, int t0, const TileScalars<K> &sc,
                                               TileAcc &acc, int refill_t0)
 {
@@ -222,7 +224,7 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM> &sm, int s, in
             for (int j = 0; j <= R; j++) D[j] = dm[j] ? D[j] : 0.f;
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                const float g = fmaf(c2, D[r] - D[r + 1], -bk[r][k]);
+                const float g = fmaf(TP ? c2 * sc.kw[k] : c2, D[r] - D[r + 1], -bk[r][k]);
                 x1[r][k] = fmaf(-sc.a0, g, xc[r][k]);  // z before the projection
             }
         }
@@ -264,7 +266,7 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM> &sm, int s, in
             for (int j = 0; j <= R; j++) E[j] = dm[j] ? E[j] : 0.f;
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                g1[r][k] = fmaf(c2, E[r] - E[r + 1], -bk[r][k]);
+                g1[r][k] = fmaf(TP ? c2 * sc.kw[k] : c2, E[r] - E[r + 1], -bk[r][k]);
                 const float fk = (g1[r][k] - bk[r][k]) * x1[r][k];
                 fpart += in[r] ? fk : 0.f;
                 d1[r][k] = fmaf(-sc.a1, g1[r][k], x1[r][k]);
@@ -293,7 +295,7 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM> &sm, int s, in
                 acc.gd = fmaf(g1[r][k], d1[r][k], acc.gd);
                 const float nb = r == R - 1 ? dnext : d1[r < R - 1 ? r + 1 : R - 1][k];
                 const float df = dm[r + 1] ? nb - d1[r][k] : 0.f;  // pair (t_r, t_r + 1) inside
-                acc.dAd = fmaf(df, df, acc.dAd);
+                acc.dAd = fmaf(TP ? df * sc.kw[k] : df, df, acc.dAd);
             }
         }
         if (!EDGE || in[R - 1]) {
@@ -317,13 +319,13 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM> &sm, int s, in
     // __syncthreads-separated phase A, so no barrier is needed here
 }
 
-template <int K, int KB, int NT, bool INIT, bool BM = false>
+template <int K, int KB, int NT, bool INIT, bool BM = false, bool TP = false>
 __device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0, const TileScalars<K> &sc,
                                          TileAcc &acc, int refill_t0)
 {
     constexpr int P = NT * TMA_R;
-    if (t0 >= 1 && t0 + P <= sc.T - 1) tma_tile_body<K, KB, NT, INIT, BM, false>(sm, s, t0, sc, acc, refill_t0);
-    else tma_tile_body<K, KB, NT, INIT, BM, true>(sm, s, t0, sc, acc, refill_t0);
+    if (t0 >= 1 && t0 + P <= sc.T - 1) tma_tile_body<K, KB, NT, INIT, BM, false, TP>(sm, s, t0, sc, acc, refill_t0);
+    else tma_tile_body<K, KB, NT, INIT, BM, true, TP>(sm, s, t0, sc, acc, refill_t0);
 }
 
 }  // namespace pasc
