@@ -15,6 +15,7 @@
 // package uses for gamma0, so both front ends solve identical inputs.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -125,6 +126,19 @@ public:
         check(pasc_gb300_create(&p, T, K, xdim, precision, epssqr, device));
         h_.reset(p);
     }
+    // graph / image mode: T timesteps on a graph of R = nbr_ptr.size() - 1 nodes (CSR lists,
+    // sorted, symmetric); the problem holds T*R blocks of K
+    Problem(long T, const std::vector<int> &nbr_ptr, const std::vector<int> &nbr_idx, int K, double epssqr,
+            int precision = PASC_PREC_MIXED, int device = 0)
+        : T_(T * (long)(nbr_ptr.size() - 1)), K_(K), xdim_(1)
+    {
+        if (nbr_ptr.size() < 2) throw Error(PASC_ERR_ARG, "graph problem: nbr_ptr needs R + 1 >= 2 entries");
+        const int one = 0;
+        pasc_gb300_problem *p = nullptr;
+        check(pasc_gb300_create_graph(&p, T, (long)nbr_ptr.size() - 1, K, precision, epssqr, device, nbr_ptr.data(),
+                                      nbr_idx.empty() ? &one : nbr_idx.data()));
+        h_.reset(p);
+    }
     long T() const { return T_; }
     int K() const { return K_; }
     int xdim() const { return xdim_; }
@@ -148,6 +162,14 @@ public:
     }
     void permute_gamma() { check(pasc_gb300_permute_gamma(h_.get())); }
     void set_fem(double fem_reduce, int fem_type) { check(pasc_gb300_set_fem(h_.get(), fem_reduce, fem_type)); }
+    // -1: chosen by timing at the first solve; 0: one timestep per thread; 1: bulk-copy tiles
+    void set_sweep_variant(int v) { check(pasc_gb300_set_sweep_variant(h_.get(), v)); }
+    int get_sweep_variant() const
+    {
+        int v = -1;
+        check(pasc_gb300_get_sweep_variant(h_.get(), &v));
+        return v;
+    }
     void set_usethetainpenalty(bool on) { check(pasc_gb300_set_usethetainpenalty(h_.get(), on ? 1 : 0)); }
     bool get_usethetainpenalty() const
     {
@@ -286,22 +308,158 @@ inline pasc_gb300_ts_opts ts_opts_from(const Options &opt)
 // ---------------------------------------------------------------------------------------
 // the reference's classes on the path
 // ---------------------------------------------------------------------------------------
+// BGMGraph<VectorBase> (include/general/algebra/graph/bgmgraph.h): n nodes with coordinates
+// (dim values per node, stored dimension by dimension) joined when closer than a threshold
+// (process, src/petscvector/algebra/graph/bgmgraph.cpp:73-152); neighbour lists as CSR
+// arrays sorted ascending.  BGMGraphGrid1D / BGMGraphGrid2D: the chain and the 4-neighbour
+// pixel grid (process_grid).
+class BGMGraph {
+public:
+    BGMGraph() = default;
+    BGMGraph(const std::vector<double> &coordinates, int n, int dim) : coords_(coordinates), n_(n), dim_(dim) {}
+    BGMGraph(const std::string &filename, int dim = 2) : coords_(load_vec(filename)), dim_(dim)
+    {
+        n_ = (int)(coords_.size() / (size_t)dim);
+    }
+    virtual ~BGMGraph() = default;
+    void process(double threshold)
+    {
+        ptr_.assign((size_t)n_ + 1, 0);
+        long nnz = 0;
+        check(pasc_gb300_graph_threshold(coords_.data(), n_, dim_, threshold, ptr_.data(), nullptr, 0, &nnz));
+        idx_.assign((size_t)nnz, 0);
+        check(pasc_gb300_graph_threshold(coords_.data(), n_, dim_, threshold, ptr_.data(), idx_.data(), nnz, &nnz));
+        threshold_ = threshold;
+        processed_ = true;
+    }
+    int get_n() const { return n_; }
+    int get_m() const { return processed_ ? ptr_.back() / 2 : 0; }
+    int get_m_max() const
+    {
+        int m = 0;
+        for (int i = 0; i < n_ && processed_; i++) m = std::max(m, ptr_[i + 1] - ptr_[i]);
+        return m;
+    }
+    int get_dim() const { return dim_; }
+    double get_threshold() const { return threshold_; }
+    bool is_processed() const { return processed_; }
+    const std::vector<int> &nbr_ptr() const { return ptr_; }
+    const std::vector<int> &nbr_idx() const { return idx_; }
+    virtual std::string get_name() const { return "BGMGraph"; }
+
+protected:
+    std::vector<double> coords_;
+    int n_ = 0, dim_ = 1;
+    double threshold_ = -1.0;
+    bool processed_ = false;
+    std::vector<int> ptr_, idx_;
+};
+
+class BGMGraphGrid1D : public BGMGraph {
+public:
+    explicit BGMGraphGrid1D(int width) : width_(width)
+    {
+        n_ = width;
+        dim_ = 1;
+    }
+    void process_grid()
+    {
+        ptr_.assign((size_t)width_ + 1, 0);
+        idx_.assign((size_t)std::max(2 * (width_ - 1), 1), 0);
+        check(pasc_gb300_graph_grid1d(width_, ptr_.data(), idx_.data()));
+        idx_.resize((size_t)ptr_.back());
+        threshold_ = 1.1;
+        processed_ = true;
+    }
+    std::string get_name() const override { return "BGMGraphGrid1D"; }
+
+private:
+    int width_;
+};
+
+class BGMGraphGrid2D : public BGMGraph {
+public:
+    BGMGraphGrid2D(int width, int height) : width_(width), height_(height)
+    {
+        n_ = width * height;
+        dim_ = 2;
+    }
+    void process_grid()
+    {
+        ptr_.assign((size_t)n_ + 1, 0);
+        idx_.assign((size_t)std::max(2 * (height_ * (width_ - 1) + width_ * (height_ - 1)), 1), 0);
+        check(pasc_gb300_graph_grid2d(width_, height_, ptr_.data(), idx_.data()));
+        idx_.resize((size_t)ptr_.back());
+        threshold_ = 1.1;
+        processed_ = true;
+    }
+    int get_width() const { return width_; }
+    int get_height() const { return height_; }
+    std::string get_name() const override { return "BGMGraphGrid2D"; }
+
+private:
+    int width_, height_;
+};
+
 class Decomposition {
 public:
-    // Decomposition<VectorBase>(T, R, K, xdim, DDT_size): one GPU, R = 1
-    Decomposition(long T, int R, int K, int xdim = 1, int DDT_size = 1) : T_(T), K_(K), xdim_(xdim)
+    // Decomposition<VectorBase>(T, R, K, xdim, DDT_size): one GPU; R > 1 nodes without a graph
+    // are disjoint (the graph GraphH1FEMModel builds when none is given, graphh1fem.cpp:30-45)
+    Decomposition(long T, int R, int K, int xdim = 1, int DDT_size = 1) : T_(T), R_(R), K_(K), xdim_(xdim)
     {
-        if (R != 1) throw Error(PASC_ERR_NOTSUPP, "spatial graphs (R > 1) are not supported");
         if (DDT_size != 1) throw Error(PASC_ERR_NOTSUPP, "one GPU per problem: DDT_size must be 1");
+        if (R < 1) throw Error(PASC_ERR_ARG, "R must be >= 1");
+        if (R > 1) {
+            std::vector<double> c((size_t)R);
+            for (int r = 0; r < R; r++) c[r] = r;
+            auto g = std::make_shared<BGMGraph>(c, R, 1);
+            g->process(0.0);
+            graph_ = g;
+            if (xdim != 1) throw Error(PASC_ERR_NOTSUPP, "graph problems take scalar data (xdim 1)");
+        }
+    }
+    // Decomposition<VectorBase>(T, graph, K, xdim, DDR_size)
+    Decomposition(long T, const BGMGraph &graph, int K, int xdim = 1, int DDR_size = 1)
+        : T_(T), R_(graph.get_n()), K_(K), xdim_(xdim), graph_(std::make_shared<BGMGraph>(graph))
+    {
+        if (DDR_size != 1) throw Error(PASC_ERR_NOTSUPP, "one GPU per problem: DDR_size must be 1");
+        if (!graph.is_processed()) throw Error(PASC_ERR_STATE, "the graph is not processed");
+        if (xdim != 1) throw Error(PASC_ERR_NOTSUPP, "graph problems take scalar data (xdim 1)");
     }
     long get_T() const { return T_; }
-    int get_R() const { return 1; }
+    int get_R() const { return R_; }
     int get_K() const { return K_; }
     int get_xdim() const { return xdim_; }
+    const BGMGraph *get_graph() const { return graph_.get(); }
+    // permute_TRK: blocked k*R*T + r*T + t <-> interleaved (t*R + r)*K + k
+    std::vector<double> permute_TRK(const std::vector<double> &v, bool invert = false) const
+    {
+        std::vector<double> out(v.size());
+        for (int k = 0; k < K_; k++)
+            for (long r = 0; r < R_; r++)
+                for (long t = 0; t < T_; t++) {
+                    const size_t b = (size_t)k * R_ * T_ + (size_t)r * T_ + t, i = ((size_t)t * R_ + r) * K_ + k;
+                    if (invert) out[b] = v[i];
+                    else out[i] = v[b];
+                }
+        return out;
+    }
+    // permute_TRxdim: data r*T + t (file order) <-> t*R + r
+    std::vector<double> permute_TRxdim(const std::vector<double> &v, bool invert = false) const
+    {
+        std::vector<double> out(v.size());
+        for (long r = 0; r < R_; r++)
+            for (long t = 0; t < T_; t++) {
+                if (invert) out[(size_t)r * T_ + t] = v[(size_t)t * R_ + r];
+                else out[(size_t)t * R_ + r] = v[(size_t)r * T_ + t];
+            }
+        return out;
+    }
 
 private:
     long T_;
-    int K_, xdim_;
+    int R_, K_, xdim_;
+    std::shared_ptr<BGMGraph> graph_;
 };
 
 // Fem<VectorBase>(fem_reduce) (FEM-SUM, include/general/common/fem.h) and FemHat (FEM-HAT,
@@ -339,6 +497,7 @@ public:
         return *decomposition_;
     }
     long get_T() const { return get_decomposition().get_T(); }
+    int get_R() const { return get_decomposition().get_R(); }
     int get_K() const { return get_decomposition().get_K(); }
     int get_xdim() const { return get_decomposition().get_xdim(); }
     const std::vector<double> &get_datavector() const { return data_; }
@@ -371,6 +530,32 @@ public:
     inline void saveSignal1D(const std::string &prefix) const;
 };
 
+// ImageData<VectorBase>(decomposition, filename, width, height) (src/petscvector/data/
+// imagedata.cpp:7-38): pixels node-major in the file (r*T + t), interleaved here (t*R + r)
+class ImageData : public TSData {
+public:
+    ImageData(const Decomposition &dec, const std::string &filename, int width, int height)
+        : ImageData(dec, load_vec(filename), width, height)
+    {
+    }
+    ImageData(const Decomposition &dec, const std::vector<double> &raw, int width, int height)
+        : width_(width), height_(height)
+    {
+        if ((long)raw.size() != dec.get_T() * dec.get_R())
+            throw Error(PASC_ERR_ARG, "ImageData: the data does not have T*width*height values");
+        set_decomposition(dec);
+        data_ = dec.permute_TRxdim(raw);
+    }
+    int get_width() const { return width_; }
+    int get_height() const { return height_; }
+    // saveImage (imagedata.cpp:40-103): <prefix>_original.bin, _gamma.bin (blocked),
+    // _recovered.bin (sum_k theta_k gamma_k), node-major
+    inline void saveImage(const std::string &prefix, bool save_original = true) const;
+
+private:
+    int width_, height_;
+};
+
 class GraphH1FEMModel {
 public:
     // GraphH1FEMModel<VectorBase>(tsdata, epssqr, fem, usethetainpenalty): creates the GPU
@@ -379,9 +564,9 @@ public:
     GraphH1FEMModel(TSData &tsdata, double epssqr, const Fem *fem = nullptr, bool usethetainpenalty = false,
                     int precision = PASC_PREC_MIXED, uint64_t seed = 13, int device = 0)
         : tsdata_(tsdata), epssqr_(epssqr), usethetainpenalty_(usethetainpenalty),
-          problem_(tsdata.get_T(), tsdata.get_K(), epssqr, precision, tsdata.get_xdim(), device)
+          problem_(make_problem(tsdata, epssqr, precision, device))
     {
-        const long T = tsdata.get_T();
+        const long T = tsdata.get_T() * tsdata.get_R();  // blocks of K
         const int K = tsdata.get_K();
         if (fem && fem->is_reduced()) problem_.set_fem(fem->get_fem_reduce(), fem->type());
         if (usethetainpenalty) problem_.set_usethetainpenalty(true);
@@ -403,6 +588,12 @@ public:
     const Problem &problem() const { return problem_; }
 
 private:
+    static Problem make_problem(const TSData &d, double epssqr, int precision, int device)
+    {
+        const BGMGraph *g = d.get_decomposition().get_graph();
+        if (g) return Problem(d.get_T(), g->nbr_ptr(), g->nbr_idx(), d.get_K(), epssqr, precision, device);
+        return Problem(d.get_T(), d.get_K(), epssqr, precision, d.get_xdim(), device);
+    }
     TSData &tsdata_;
     double epssqr_;
     bool usethetainpenalty_;
@@ -429,7 +620,7 @@ inline void TSData::cutgamma()
 {
     if (!model_) throw Error(PASC_ERR_STATE, "TSData: no model");
     const std::vector<int> lab = model_->problem().argmax_labels();
-    const long T = get_T();
+    const long T = get_T() * get_R();  // blocks of K
     const int K = get_K();
     std::vector<double> g((size_t)T * K, 0.0);
     for (long t = 0; t < T; t++) g[(size_t)t * K + lab[t]] = 1.0;
@@ -453,6 +644,19 @@ inline void Signal1DData::saveSignal1D(const std::string &prefix) const
         }
     save_vec(prefix + "_gamma.bin", blocked);
     save_vec(prefix + "_recovered.bin", rec);
+}
+
+inline void ImageData::saveImage(const std::string &prefix, bool save_original) const
+{
+    const Decomposition &dec = get_decomposition();
+    if (save_original) save_vec(prefix + "_original.bin", dec.permute_TRxdim(data_, true));
+    const std::vector<double> g = get_gammavector(), th = get_thetavector();
+    const int K = get_K();
+    std::vector<double> rec(data_.size(), 0.0);
+    for (size_t s = 0; s < rec.size(); s++)
+        for (int k = 0; k < K; k++) rec[s] += g[s * K + k] * th[k];
+    save_vec(prefix + "_gamma.bin", dec.permute_TRK(g, true));
+    save_vec(prefix + "_recovered.bin", dec.permute_TRxdim(rec, true));
 }
 
 class SPGQPSolver {

@@ -227,6 +227,39 @@ int pasc_gb300_get_b(pasc_gb300_problem *p, double *b);
 int pasc_gb300_set_fem(pasc_gb300_problem *p, double fem_reduce, int fem_type);
 int pasc_gb300_get_fem(pasc_gb300_problem *p, double *fem_reduce, int *fem_type, long *T_reduced);
 
+/* Graph (R > 1) and image mode: GraphH1FEMModel on Decomposition(T, graph, K, 1, 1)
+ * (include/general/common/decomposition.h; graphh1fem.cpp:8-65) with the operator
+ * BlockGraphSparseMatrix on a graph of R nodes (blockgraphsparse.cpp:7-103): row (t, r, k)
+ * has -2 at (t+-1, r), -1 at (t, r') and (t+-1, r') for every neighbour r' of r, and the
+ * diagonal that makes the row sum to zero.  The problem has T*R blocks of K: gamma index
+ * (t*R + r)*K + k, data index t*R + r (T*R values), theta K values; A = epssqr/T * A_graph and
+ * b = -(x - theta_k)^2 / T keep the number of timesteps T.  pasc_gb300_permute_gamma maps the
+ * blocked layout k*R*T + r*T + t (Decomposition::permute_TRK, decomposition.cpp:257-340).
+ * The graph: CSR neighbour lists of the R nodes (nbr_ptr: R+1 offsets, nbr_idx: nbr_ptr[R]
+ * indices), each list sorted ascending, no duplicates, no self-loops, symmetric (checked;
+ * PASC_ERR_ARG otherwise).  Image data (test_image): T = 1, R = width*height, the grid graph.
+ * Not with FEM reduction, theta in the penalty, multichannel data or the adjoint
+ * (PASC_ERR_NOTSUPP).  The mixed path runs two kernels per SPG iteration. */
+int pasc_gb300_create_graph(pasc_gb300_problem **out, long T, long R, int K, int precision, double epssqr,
+                            int device, const int *nbr_ptr, const int *nbr_idx);
+/* T = timesteps, R = nodes (1 and 0 edges for a 1-D problem) */
+int pasc_gb300_get_graph(pasc_gb300_problem *p, long *T, long *R, long *nnz);
+
+/* Graphs the reference builds, as CSR neighbour lists sorted ascending (host functions):
+ * BGMGraphGrid1D::process_grid (bgmgraphgrid1D.h:76-115; nbr_ptr: width+1, nbr_idx:
+ * 2*(width-1)), BGMGraphGrid2D::process_grid (bgmgraphgrid2D.h:88-142; node i*width + j,
+ * nbr_idx: 2*(height*(width-1) + width*(height-1))), and BGMGraph::process(threshold)
+ * (bgmgraph.cpp:73-152): nodes i, j are neighbours when sum_d (c[i+d*n] - c[j+d*n])^2 <
+ * threshold^2.  graph_threshold with nbr_idx == NULL computes nbr_ptr and *nnz only. */
+int pasc_gb300_graph_grid1d(int width, int *nbr_ptr, int *nbr_idx);
+int pasc_gb300_graph_grid2d(int width, int height, int *nbr_ptr, int *nbr_idx);
+int pasc_gb300_graph_threshold(const double *coords, int n, int dim, double threshold, int *nbr_ptr, int *nbr_idx,
+                               long idx_capacity, long *nnz);
+/* y = coeff * A_graph x on device buffers (T*R*K values; nbr_* in device memory), FP64 in the
+ * assembled matrix's sorted column order (MatMult of blockgraphsparse.cpp:152-160). */
+int pasc_gb300_graph_matmult_f64(const double *x_dev, double *y_dev, long T, long R, int K, double coeff,
+                                 const int *nbr_ptr_dev, const int *nbr_idx_dev, void *stream);
+
 /* Theta in the penalty: GraphH1FEMModel(tsdata, epssqr, fem, usethetainpenalty = true)
  * (graphh1fem.cpp:8-19, 154-160; include/general/model/graphh1fem.h:61, 75).  Block k of the
  * gamma QP's A is alpha*theta_k*theta_k*A_hat (BlockGraphSparseMatrix with coefficients,

@@ -210,7 +210,12 @@ void pasc_oracle_project(double *x, long T, int K, int nthreads)
 /* y = A x with A = coeff * A_hat, or with kc != NULL the block k scaled by kc[k] instead of coeff
  * (BlockGraphSparseMatrix with coefficients, blockgraphsparse.cpp:161-185: VecScale of the
  * MatMult's block k by alpha*theta_k*theta_k) */
-static void matmult_kc(const double *x, double *y, long T, int K, double coeff, const double *kc, int nthreads);
+static void matmult_g(const double *x, double *y, long T, int K, double coeff, const double *kc,
+                      const pasc_oracle_graph *G, int nthreads);
+static void matmult_kc(const double *x, double *y, long T, int K, double coeff, const double *kc, int nthreads)
+{
+    matmult_g(x, y, T, K, coeff, kc, NULL, nthreads);
+}
 
 void pasc_oracle_fem_h1_matmult(const double *x, double *y, long T, int K, double coeff, int nthreads)
 {
@@ -222,10 +227,61 @@ void pasc_oracle_fem_h1_matmult_kc(const double *x, double *y, long T, int K, co
     matmult_kc(x, y, T, K, 0.0, kc, nthreads);
 }
 
-static void matmult_kc(const double *x, double *y, long T, int K, double coeff, const double *kc, int nthreads)
+/* Row (t, r, k) of the assembled BlockGraphSparseMatrix with a graph of R nodes
+ * (blockgraphsparse.cpp:48-103): diagonal Wsum = 3m+4 inside, 2m+2 at t = 0 or T-1, m when
+ * T = 1 (m = number of neighbours of r); -2 at (t+-1, r); -1 at (t, r') and (t+-1, r') for
+ * every neighbour r'.  PETSc keeps the columns of a row sorted, and MatMult sums them in that
+ * order from 0: here t' = t-1, t, t+1 and, inside each, r' ascending (neighbour lists are
+ * sorted, r itself merged in).  Without neighbours (R = 1) this is the 1-D row below. */
+static void graph_rows(const double *x, double *y, long T, int K, const pasc_oracle_graph *G, int nth)
+{
+    const long R = G->R;
+    const long N = T * R * (long)K;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
+#endif
+    for (long i = 0; i < N; i++) {
+        const long s = i / K;
+        const int k = (int)(i - s * K);
+        const long t = s / R, r = s - t * R;
+        const int q0 = G->ptr[r], q1 = G->ptr[r + 1], m = q1 - q0;
+        double wsum;
+        if (t == 0 || t == T - 1) wsum = T > 1 ? (double)(2 * m + 2) : (double)m;
+        else wsum = (double)(3 * m + 4);
+        double sum = 0.0;
+        for (long tt = t - 1; tt <= t + 1; tt++) {
+            if (tt < 0 || tt >= T) continue;
+            int q = q0, self = 0;
+            while (q < q1 || !self) {
+                long rn;
+                double v;
+                if (!self && (q >= q1 || G->idx[q] > r)) {
+                    rn = r;
+                    v = tt == t ? wsum : -2.0;
+                    self = 1;
+                } else {
+                    rn = G->idx[q++];
+                    v = -1.0;
+                }
+                sum += v * x[(tt * R + rn) * K + k];
+            }
+        }
+        y[i] = sum;
+    }
+}
+
+static void matmult_g(const double *x, double *y, long T, int K, double coeff, const double *kc,
+                      const pasc_oracle_graph *G, int nthreads)
 {
     int nth = eff_threads(nthreads);
-    long N = T * (long)K;
+    long N = T * (long)K * (G ? G->R : 1);
+    if (G) {
+        graph_rows(x, y, T, K, G, nth);
+        if (!kc) vscale(y, coeff, N, nth);
+        else
+            for (long i = 0; i < N; i++) y[i] = kc[i % K] * y[i];
+        return;
+    }
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static) num_threads(nth) if (nth > 1)
 #endif
@@ -362,26 +418,42 @@ static double get_fx(const double *g, const double *b, const double *x, double *
 }
 
 static int spgqp_impl(const double *b, double *x, long T, int K, double coeff, const double *kc,
-                      const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, double *trace, int nthreads);
+                      const pasc_oracle_graph *G, const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r,
+                      double *trace, int nthreads);
+
+int pasc_oracle_spgqp_solve_graph(const double *b, double *x, long T, int K, double coeff, const pasc_oracle_graph *G,
+                                  const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, int nthreads)
+{
+    return spgqp_impl(b, x, T, K, coeff, NULL, G, o, r, NULL, nthreads);
+}
+
+void pasc_oracle_graph_matmult(const double *x, double *y, long T, int K, double coeff, const pasc_oracle_graph *G,
+                               int nthreads)
+{
+    matmult_g(x, y, T, K, coeff, NULL, G, nthreads);
+}
 
 int pasc_oracle_spgqp_solve(const double *b, double *x, long T, int K, double coeff,
                             const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r,
                             double *trace, int nthreads)
 {
-    return spgqp_impl(b, x, T, K, coeff, NULL, o, r, trace, nthreads);
+    return spgqp_impl(b, x, T, K, coeff, NULL, NULL, o, r, trace, nthreads);
 }
 
 int pasc_oracle_spgqp_solve_kc(const double *b, double *x, long T, int K, const double *kc,
                                const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, int nthreads)
 {
-    return spgqp_impl(b, x, T, K, 0.0, kc, o, r, NULL, nthreads);
+    return spgqp_impl(b, x, T, K, 0.0, kc, NULL, o, r, NULL, nthreads);
 }
 
+/* T: timesteps; with a graph the QP has T*R blocks of K (index (t*R + r)*K + k) */
 static int spgqp_impl(const double *b, double *x, long T, int K, double coeff, const double *kc,
-                      const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, double *trace, int nthreads)
+                      const pasc_oracle_graph *G, const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r,
+                      double *trace, int nthreads)
 {
     int nth = eff_threads(nthreads);
-    long n = T * (long)K;
+    const long nb = T * (G ? G->R : 1); /* blocks of K */
+    long n = nb * (long)K;
     double *g = (double *)malloc(sizeof(double) * (size_t)n);
     double *d = (double *)malloc(sizeof(double) * (size_t)n);
     double *Ad = (double *)malloc(sizeof(double) * (size_t)n);
@@ -401,9 +473,9 @@ static int spgqp_impl(const double *b, double *x, long T, int K, double coeff, c
     double normb = sqrt(vdot(b, b, n, nth)); /* VecNorm(b, NORM_2)  :104 */
     alpha_bb = o->alphainit;                 /* :108 */
 
-    pasc_oracle_project(x, T, K, nth); /* :116 */
+    pasc_oracle_project(x, nb, K, nth); /* :116 */
 
-    matmult_kc(x, g, T, K, coeff, kc, nth); /* MatMult + VecScale :122-123 */
+    matmult_g(x, g, T, K, coeff, kc, G, nth); /* MatMult + VecScale :122-123 */
     hessmult += 1;
     vaxpy(g, -1.0, b, n, nth); /* :128 */
 
@@ -420,10 +492,10 @@ static int spgqp_impl(const double *b, double *x, long T, int K, double coeff, c
 
         vcopy(d, x, n, nth);              /* :146 */
         vaxpy(d, -alpha_bb, g, n, nth);   /* :147 */
-        pasc_oracle_project(d, T, K, nth); /* :153 */
+        pasc_oracle_project(d, nb, K, nth); /* :153 */
         vaxpy(d, -1.0, x, n, nth);        /* :158 */
 
-        matmult_kc(d, Ad, T, K, coeff, kc, nth); /* :164-165 */
+        matmult_g(d, Ad, T, K, coeff, kc, G, nth); /* :164-165 */
         hessmult += 1;
 
         dd = vdot(d, d, n, nth);  /* :357 */
@@ -957,5 +1029,146 @@ int pasc_oracle_tssolver_solve_model(const double *data, double *gamma, double *
         r->L_increased = increased;
     }
     free(res); free(perm); free(b2); free(x2);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------------- */
+/* Graph (R > 1) and image mode: BGMGraph / BGMGraphGrid1D / BGMGraphGrid2D neighbour      */
+/* lists, Decomposition::permute_TRK, and the TSSolver of GraphH1FEMModel over T*R blocks. */
+/* ------------------------------------------------------------------------------------- */
+
+/* Decomposition<PetscVector>::permute_TRblocksize (decomposition.cpp:260-340) on one rank:
+ * the blocked layout k*R*T + r*T + t becomes (t*R + r)*K + k. */
+void pasc_oracle_permute_TRK(const double *orig, double *out, long T, long R, int K)
+{
+    for (int k = 0; k < K; k++)
+        for (long r = 0; r < R; r++)
+            for (long t = 0; t < T; t++) out[(t * R + r) * K + k] = orig[(long)k * R * T + r * T + t];
+}
+
+/* BGMGraphGrid1D::process_grid (include/general/algebra/graph/bgmgraphgrid1D.h:76-115):
+ * node i has i-1 and i+1.  Lists sorted ascending (ptr: width+1, idx: 2*(width-1)). */
+void pasc_oracle_graph_grid1d(int width, int *ptr, int *idx)
+{
+    int q = 0;
+    for (int i = 0; i < width; i++) {
+        ptr[i] = q;
+        if (i > 0) idx[q++] = i - 1;
+        if (i < width - 1) idx[q++] = i + 1;
+    }
+    ptr[width] = q;
+}
+
+/* BGMGraphGrid2D::process_grid (include/general/algebra/graph/bgmgraphgrid2D.h:88-142):
+ * node idx = i*width + j has left (j > 0), right, down (i > 0, idx - width) and up; the
+ * lists are stored sorted ascending: idx-width, idx-1, idx+1, idx+width. */
+void pasc_oracle_graph_grid2d(int width, int height, int *ptr, int *idx)
+{
+    int q = 0;
+    for (int id = 0; id < width * height; id++) {
+        const int i = id / width, j = id - i * width;
+        ptr[id] = q;
+        if (i > 0) idx[q++] = id - width;
+        if (j > 0) idx[q++] = id - 1;
+        if (j < width - 1) idx[q++] = id + 1;
+        if (i < height - 1) idx[q++] = id + width;
+    }
+    ptr[width * height] = q;
+}
+
+/* BGMGraph::process(threshold) (src/petscvector/algebra/graph/bgmgraph.cpp:73-152): i and j
+ * are neighbours when sum_d (c_i,d - c_j,d)^2 < threshold^2, coordinates stored dimension by
+ * dimension (c_i,d = coords[i + d*n], bgmgraph.h:164-171).  The pair loop (i < j) appends j
+ * to i's list and i to j's, so every list comes out ascending.  idx == NULL: only ptr. */
+long pasc_oracle_graph_threshold(const double *coords, int n, int dim, double threshold, int *ptr, int *idx)
+{
+    int *cnt = (int *)calloc((size_t)n + 1, sizeof(int));
+    if (!cnt) return -1;
+    const double thr2 = threshold * threshold;
+    for (int i = 0; i < n; i++)
+        for (int j = i + 1; j < n; j++) {
+            double s = 0.0;
+            for (int d = 0; d < dim; d++) {
+                const double df = coords[i + (long)d * n] - coords[j + (long)d * n];
+                s += df * df;
+            }
+            if (s < thr2) {
+                cnt[i]++;
+                cnt[j]++;
+            }
+        }
+    long q = 0;
+    for (int i = 0; i < n; i++) {
+        ptr[i] = (int)q;
+        q += cnt[i];
+    }
+    ptr[n] = (int)q;
+    if (idx) {
+        for (int i = 0; i < n; i++) cnt[i] = ptr[i];
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++) {
+                double s = 0.0;
+                for (int d = 0; d < dim; d++) {
+                    const double df = coords[i + (long)d * n] - coords[j + (long)d * n];
+                    s += df * df;
+                }
+                if (s < thr2) {
+                    idx[cnt[i]++] = j;
+                    idx[cnt[j]++] = i;
+                }
+            }
+    }
+    free(cnt);
+    return q;
+}
+
+/* TSSolver::solve with GraphH1FEMModel on a graph of R nodes (fem not reduced): gamma has
+ * T*R blocks of K, data T*R values (index t*R + r), theta K; A = epssqr/T * A_graph and
+ * b = -(x - theta_k)^2 / T keep the number of timesteps T (graphh1fem.cpp:146-151, 280-283). */
+int pasc_oracle_tssolver_solve_graph(const double *data, double *gamma, double *theta, long T, int K,
+                                     double epssqr, int scalef, const pasc_oracle_graph *G,
+                                     const pasc_oracle_ts_opts *ts, const pasc_oracle_spg_opts *spg,
+                                     pasc_oracle_ts_result *r, int nthreads)
+{
+    const int nth = eff_threads(nthreads);
+    const long R = G->R, nb = T * R, n = nb * (long)K;
+    double *b = (double *)malloc(sizeof(double) * (size_t)n);
+    double *perm = (double *)malloc(sizeof(double) * (size_t)n);
+    if (!b || !perm) {
+        free(b); free(perm);
+        return -1;
+    }
+    const double coeffA = pasc_oracle_A_coeff(epssqr, T, scalef);
+    const double coeffB = pasc_oracle_b_coeff(T, scalef);
+    if (ts->init_permute) {
+        pasc_oracle_permute_TRK(gamma, perm, T, R, K);
+        memcpy(gamma, perm, sizeof(double) * (size_t)n);
+    }
+    double L = DBL_MAX, L_old, deltaL = DBL_MAX;
+    int it, spg_it_sum = 0, spg_hm_sum = 0, increased = 0;
+    for (it = 0; it < ts->maxit; it++) {
+        if (!ts->thetasolved) pasc_oracle_theta_update(gamma, data, theta, nb, K, 1, nth);
+        pasc_oracle_residual_b(data, theta, b, nb, K, 1, coeffB, nth);
+        pasc_oracle_spg_result sr;
+        spgqp_impl(b, gamma, T, K, coeffA, NULL, G, spg, &sr, NULL, nth);
+        spg_it_sum += sr.it;
+        spg_hm_sum += sr.hessmult;
+        L_old = L;
+        L = sr.fx;
+        deltaL = fabs(L - L_old);
+        if (L - L_old > 0) increased++;
+        if (ts->relative ? (deltaL < ts->eps * fabs(L)) : (deltaL < ts->eps)) break;
+    }
+    if (r) {
+        r->it_last = it;
+        r->it_sum = it;
+        r->spg_it_sum = spg_it_sum;
+        r->spg_hessmult_sum = spg_hm_sum;
+        r->L = L;
+        r->deltaL = deltaL;
+        r->aic = 2 * log(L) + K;
+        r->L_increased = increased;
+    }
+    free(b); free(perm);
     return 0;
 }

@@ -173,6 +173,25 @@ void pasc_oracle_fem_prolongate(const double *g2, double *g1, long T1, long T2, 
  * theta_k)^2) with coeffB2 = -1/T2 (scalef), x = reduce(gamma) before each gamma solve,
  * A = epssqr/T * A_hat(T2) (scalef; epssqr*T2/T otherwise), gamma = prolongate(x) after it.
  * xdim == 1. */
+/* A graph of R nodes for BlockGraphSparseMatrix (BGMGraph neighbour lists, src/petscvector/
+ * algebra/graph/bgmgraph.cpp:73-152): node r's neighbours are idx[ptr[r] .. ptr[r+1]-1],
+ * sorted ascending, no duplicates, no r itself. */
+typedef struct {
+    long R;
+    const int *ptr;
+    const int *idx;
+} pasc_oracle_graph;
+
+/* y = coeff * A_graph x over T timesteps and R nodes (x, y: T*R*K, index (t*R + r)*K + k) */
+void pasc_oracle_graph_matmult(const double *x, double *y, long T, int K, double coeff, const pasc_oracle_graph *G,
+                               int nthreads);
+int pasc_oracle_spgqp_solve_graph(const double *b, double *x, long T, int K, double coeff, const pasc_oracle_graph *G,
+                                  const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, int nthreads);
+void pasc_oracle_permute_TRK(const double *orig, double *out, long T, long R, int K);
+void pasc_oracle_graph_grid1d(int width, int *ptr, int *idx);
+void pasc_oracle_graph_grid2d(int width, int height, int *ptr, int *idx);
+long pasc_oracle_graph_threshold(const double *coords, int n, int dim, double threshold, int *ptr, int *idx);
+
 /* usethetainpenalty (graphh1fem.cpp:154-160, 306-380, blockgraphsparse.cpp:161-185): the
  * gamma QP's block k is scaled by kc[k] = coeff*theta_k*theta_k (spgqp_solve_kc), and theta is
  * updated with the penalty term (theta_update_penalty, alpha = the QP coefficient). */
@@ -187,6 +206,10 @@ int pasc_oracle_tssolver_solve_model(const double *data, double *gamma, double *
                                      double epssqr, int scalef, double fem_reduce, int fem_type,
                                      int usethetainpenalty, const pasc_oracle_ts_opts *ts,
                                      const pasc_oracle_spg_opts *spg, pasc_oracle_ts_result *r, int nthreads);
+int pasc_oracle_tssolver_solve_graph(const double *data, double *gamma, double *theta, long T, int K,
+                                     double epssqr, int scalef, const pasc_oracle_graph *G,
+                                     const pasc_oracle_ts_opts *ts, const pasc_oracle_spg_opts *spg,
+                                     pasc_oracle_ts_result *r, int nthreads);
 int pasc_oracle_tssolver_solve_fem(const double *data, double *gamma, double *theta, long T, int K,
                                    double epssqr, int scalef, double fem_reduce, int fem_type,
                                    const pasc_oracle_ts_opts *ts, const pasc_oracle_spg_opts *spg,

@@ -110,6 +110,17 @@ def lib():
         L.pasc_oracle_tssolver_solve_fem.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
                                                      C.c_double, C.c_int, C.POINTER(TsOpts), C.POINTER(SpgOpts),
                                                      C.POINTER(TsResult), C.c_int]
+        L.pasc_oracle_graph_matmult.argtypes = [_dp, _dp, C.c_long, C.c_int, C.c_double, C.POINTER(Graph), C.c_int]
+        L.pasc_oracle_spgqp_solve_graph.argtypes = [_dp, _dp, C.c_long, C.c_int, C.c_double, C.POINTER(Graph),
+                                                    C.POINTER(SpgOpts), C.POINTER(SpgResult), C.c_int]
+        L.pasc_oracle_permute_TRK.argtypes = [_dp, _dp, C.c_long, C.c_long, C.c_int]
+        L.pasc_oracle_graph_grid1d.argtypes = [C.c_int, _ip, _ip]
+        L.pasc_oracle_graph_grid2d.argtypes = [C.c_int, C.c_int, _ip, _ip]
+        L.pasc_oracle_graph_threshold.argtypes = [_dp, C.c_int, C.c_int, C.c_double, _ip, C.c_void_p]
+        L.pasc_oracle_graph_threshold.restype = C.c_long
+        L.pasc_oracle_tssolver_solve_graph.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
+                                                       C.POINTER(Graph), C.POINTER(TsOpts), C.POINTER(SpgOpts),
+                                                       C.POINTER(TsResult), C.c_int]
         L.pasc_oracle_fem_h1_matmult_kc.argtypes = [_dp, _dp, C.c_long, C.c_int, _dp, C.c_int]
         L.pasc_oracle_spgqp_solve_kc.argtypes = [_dp, _dp, C.c_long, C.c_int, _dp, C.POINTER(SpgOpts),
                                                  C.POINTER(SpgResult), C.c_int]
@@ -292,6 +303,84 @@ def tssolver_solve_model(data, gamma_raw, theta0, T, K, epssqr, fem_reduce=1.0, 
                                                 C.byref(r), nthreads)
     if rc != 0:
         raise ValueError("tssolver_solve_model: unsupported combination")
+    return g, th, r
+
+
+class Graph(C.Structure):
+    """pasc_oracle_graph: CSR neighbour lists of R nodes (sorted, no self, no duplicates)."""
+
+    _fields_ = [("R", C.c_long), ("ptr", C.POINTER(C.c_int)), ("idx", C.POINTER(C.c_int))]
+
+
+def make_graph(ptr, idx):
+    """(Graph structure, the arrays it points into) -- keep both alive together."""
+    ptr = np.ascontiguousarray(ptr, dtype=np.int32)
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    if idx.size == 0:
+        idx = np.zeros(1, dtype=np.int32)
+    g = Graph(len(ptr) - 1, ptr.ctypes.data_as(C.POINTER(C.c_int)), idx.ctypes.data_as(C.POINTER(C.c_int)))
+    return g, (ptr, idx)
+
+
+def graph_grid1d(width):
+    ptr = np.empty(width + 1, dtype=np.int32)
+    idx = np.empty(max(2 * (width - 1), 1), dtype=np.int32)
+    lib().pasc_oracle_graph_grid1d(width, ptr, idx)
+    return ptr, idx[: ptr[-1]].copy()
+
+
+def graph_grid2d(width, height):
+    ptr = np.empty(width * height + 1, dtype=np.int32)
+    idx = np.empty(max(2 * (height * (width - 1) + width * (height - 1)), 1), dtype=np.int32)
+    lib().pasc_oracle_graph_grid2d(width, height, ptr, idx)
+    return ptr, idx[: ptr[-1]].copy()
+
+
+def graph_threshold(coords, n, dim, threshold):
+    """coords: dim*n values, dimension by dimension (c[i + d*n])."""
+    c = _f64(coords)
+    ptr = np.empty(n + 1, dtype=np.int32)
+    nnz = lib().pasc_oracle_graph_threshold(c, n, dim, threshold, ptr, None)
+    idx = np.empty(max(nnz, 1), dtype=np.int32)
+    lib().pasc_oracle_graph_threshold(c, n, dim, threshold, ptr, idx.ctypes.data)
+    return ptr, idx[:nnz].copy()
+
+
+def graph_matmult(x, T, K, coeff, ptr, idx):
+    g, keep = make_graph(ptr, idx)
+    y = np.empty(T * g.R * K)
+    lib().pasc_oracle_graph_matmult(_f64(x), y, T, K, coeff, C.byref(g), 1)
+    return y
+
+
+def spgqp_solve_graph(b, x0, T, K, coeff, ptr, idx, opts: SpgOpts | None = None):
+    opts = opts or spg_opts()
+    g, keep = make_graph(ptr, idx)
+    x = _f64(x0).copy()
+    r = SpgResult()
+    lib().pasc_oracle_spgqp_solve_graph(_f64(b), x, T, K, coeff, C.byref(g), C.byref(opts), C.byref(r), 1)
+    return x, r
+
+
+def permute_TRK(v, T, R, K):
+    out = np.empty(T * R * K)
+    lib().pasc_oracle_permute_TRK(_f64(v), out, T, R, K)
+    return out
+
+
+def tssolver_solve_graph(data, gamma_raw, theta0, T, K, epssqr, ptr, idx, scalef=1, ts: TsOpts | None = None,
+                         spg: SpgOpts | None = None, nthreads=1):
+    """Returns (gamma, theta, TsResult); data T*R, gamma T*R*K (blocked when ts.init_permute)."""
+    ts = ts or ts_opts()
+    spg = spg or spg_opts()
+    gr, keep = make_graph(ptr, idx)
+    g = _f64(gamma_raw).copy()
+    th = _f64(theta0).copy()
+    r = TsResult()
+    rc = lib().pasc_oracle_tssolver_solve_graph(_f64(data), g, th, T, K, epssqr, scalef, C.byref(gr), C.byref(ts),
+                                                C.byref(spg), C.byref(r), nthreads)
+    if rc != 0:
+        raise MemoryError("tssolver_solve_graph")
     return g, th, r
 
 

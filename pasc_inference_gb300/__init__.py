@@ -2,7 +2,9 @@
 class surface over the C ABI of include/pasc_gb300.h.
 
 Class names, constructor arguments and option names follow PASC_inference:
-  Decomposition(T, R, K, xdim, DDT_size)        include/general/common/decomposition.h:55
+  Decomposition(T, R | graph, K, xdim, DD_size)  include/general/common/decomposition.h:55
+  BGMGraph, BGMGraphGrid1D, BGMGraphGrid2D       include/general/algebra/graph/
+  ImageData(decomposition, filename, width, height)   include/general/data/imagedata.h
   Signal1DData(filename | array)                 include/general/data/signal1Ddata.h
   GraphH1FEMModel(tsdata, epssqr, fem=None, usethetainpenalty=False)
                                                  include/general/model/graphh1fem.h:75
@@ -22,7 +24,8 @@ from .capi import (PASC_PREC_FP64, PASC_PREC_MIXED, PascError, SpgqpOpts, SpgqpS
                    TsStats, check, load)
 
 __all__ = ["Problem", "Batch", "Fem", "FemHat", "Decomposition", "Signal1DData", "TSData", "GraphH1FEMModel", "TSSolver",
-           "SPGQPSolver", "PascError", "PASC_PREC_FP64", "PASC_PREC_MIXED", "capi"]
+           "SPGQPSolver", "BGMGraph", "BGMGraphGrid1D", "BGMGraphGrid2D", "ImageData", "PascError",
+           "PASC_PREC_FP64", "PASC_PREC_MIXED", "capi"]
 
 _SPG_KEYS = {"spgqpsolver_maxit": "maxit", "spgqpsolver_eps": "eps", "spgqpsolver_m": "m",
              "spgqpsolver_gamma": "gamma", "spgqpsolver_sigma1": "sigma1",
@@ -55,13 +58,29 @@ class Problem:
     """One FEM-H1 problem on one GPU (a pasc_gb300_problem handle)."""
 
     def __init__(self, T: int, K: int, epssqr: float = 1.0, precision: int = PASC_PREC_MIXED,
-                 xdim: int = 1, device: int = 0):
+                 xdim: int = 1, device: int = 0, graph=None):
+        """graph: (nbr_ptr, nbr_idx) CSR neighbour lists of R nodes (or a BGMGraph) for the
+        graph / image mode; T then counts timesteps and the problem has T*R blocks of K."""
         L = load()
         h = C.c_void_p()
-        check(L.pasc_gb300_create(C.byref(h), int(T), int(K), int(xdim), int(precision),
-                                  float(epssqr), int(device)))
+        self.Ttime, self.R = int(T), 1
+        if graph is not None:
+            ptr, idx = graph.csr() if hasattr(graph, "csr") else graph
+            ptr = np.ascontiguousarray(ptr, dtype=np.int32)
+            idx = np.ascontiguousarray(idx, dtype=np.int32)
+            if idx.size == 0:
+                idx = np.zeros(1, dtype=np.int32)
+            if xdim != 1:
+                raise PascError(capi.PASC_ERR_NOTSUPP, "graph problems take scalar data (xdim 1)")
+            self.R = len(ptr) - 1
+            check(L.pasc_gb300_create_graph(C.byref(h), int(T), self.R, int(K), int(precision), float(epssqr),
+                                            int(device), ptr, idx))
+        else:
+            check(L.pasc_gb300_create(C.byref(h), int(T), int(K), int(xdim), int(precision),
+                                      float(epssqr), int(device)))
         self._h = h
-        self.T, self.K, self.xdim, self.precision = int(T), int(K), int(xdim), int(precision)
+        # T counts the blocks of K (timesteps x nodes), as the handle does
+        self.T, self.K, self.xdim, self.precision = int(T) * self.R, int(K), int(xdim), int(precision)
         self.epssqr = float(epssqr)
 
     def close(self):
@@ -158,6 +177,12 @@ class Problem:
         r, t, T2 = C.c_double(), C.c_int(), C.c_long()
         check(load().pasc_gb300_get_fem(self._h, C.byref(r), C.byref(t), C.byref(T2)))
         return r.value, t.value, T2.value
+
+    def get_graph(self):
+        """(timesteps, nodes, neighbour entries); (T, 1, 0) for a 1-D problem."""
+        T, R, nnz = C.c_long(), C.c_long(), C.c_long()
+        check(load().pasc_gb300_get_graph(self._h, C.byref(T), C.byref(R), C.byref(nnz)))
+        return T.value, R.value, nnz.value
 
     def set_usethetainpenalty(self, on: bool = True):
         """Theta in the penalty: block k of A scaled by alpha*theta_k^2, theta step with the
@@ -295,15 +320,136 @@ class Batch:
 # ------------------------------------------------------------------------------------------
 # mirror of the reference classes on the path
 # ------------------------------------------------------------------------------------------
-class Decomposition:
-    """Decomposition<VectorBase>(T, R, K, xdim, DDT_size): layouts of one GPU (R = 1)."""
+class BGMGraph:
+    """BGMGraph<VectorBase>: a graph of n nodes given by coordinates (dim values per node,
+    stored dimension by dimension, or a PETSc binary file of them), with edges between nodes
+    closer than a threshold (process, src/petscvector/algebra/graph/bgmgraph.cpp:73-152).
+    Neighbour lists are kept as CSR arrays sorted ascending."""
 
-    def __init__(self, T: int, R: int, K: int, xdim: int = 1, DDT_size: int = 1):
-        if R != 1:
-            raise PascError(capi.PASC_ERR_NOTSUPP, "spatial graphs (R > 1) are not supported")
-        if DDT_size != 1:
-            raise PascError(capi.PASC_ERR_NOTSUPP, "one GPU per problem: DDT_size must be 1")
-        self.T, self.R, self.K, self.xdim = int(T), 1, int(K), int(xdim)
+    def __init__(self, coordinates=None, n: int | None = None, dim: int = 2, filename: str | None = None):
+        if filename is not None or isinstance(coordinates, str):
+            from .petscio import load_vec
+            coordinates = load_vec(filename or coordinates)
+        self.coordinates = None if coordinates is None else np.ascontiguousarray(coordinates, dtype=np.float64)
+        self.dim = int(dim)
+        self.n = int(n) if n is not None else (0 if coordinates is None else self.coordinates.size // self.dim)
+        self.threshold = -1.0
+        self.processed = False
+        self.ptr = None
+        self.idx = None
+
+    def process(self, threshold: float):
+        L = load()
+        ptr = np.empty(self.n + 1, dtype=np.int32)
+        nnz = C.c_long()
+        check(L.pasc_gb300_graph_threshold(self.coordinates, self.n, self.dim, float(threshold), ptr, None, 0,
+                                           C.byref(nnz)))
+        idx = np.empty(max(nnz.value, 1), dtype=np.int32)
+        check(L.pasc_gb300_graph_threshold(self.coordinates, self.n, self.dim, float(threshold), ptr,
+                                           idx.ctypes.data, idx.size, C.byref(nnz)))
+        self._set(ptr, idx[: nnz.value], threshold)
+
+    def _set(self, ptr, idx, threshold):
+        self.ptr, self.idx = ptr, np.ascontiguousarray(idx, dtype=np.int32)
+        self.threshold = float(threshold)
+        self.processed = True
+
+    def csr(self):
+        if not self.processed:
+            raise PascError(capi.PASC_ERR_STATE, "graph not processed")
+        return self.ptr, self.idx
+
+    def get_n(self):
+        return self.n
+
+    def get_m(self):
+        return int(self.ptr[-1]) // 2
+
+    def get_m_max(self):
+        return int(np.max(np.diff(self.ptr))) if self.n > 0 else 0
+
+    def get_dim(self):
+        return self.dim
+
+    def get_threshold(self):
+        return self.threshold
+
+    def get_neighbor_nmbs(self):
+        return np.diff(self.ptr)
+
+    def get_neighbor_ids(self):
+        return [self.idx[self.ptr[r]:self.ptr[r + 1]] for r in range(self.n)]
+
+    def get_coordinates(self):
+        return self.coordinates
+
+    def get_name(self):
+        return "BGMGraph"
+
+
+class BGMGraphGrid1D(BGMGraph):
+    """BGMGraphGrid1D<VectorBase>(width): a chain of width nodes (bgmgraphgrid1D.h)."""
+
+    def __init__(self, width: int):
+        super().__init__(np.arange(width, dtype=np.float64), width, 1)
+        self.width = int(width)
+
+    def process_grid(self):
+        ptr = np.empty(self.width + 1, dtype=np.int32)
+        idx = np.empty(max(2 * (self.width - 1), 1), dtype=np.int32)
+        check(load().pasc_gb300_graph_grid1d(self.width, ptr, idx))
+        self._set(ptr, idx[: ptr[-1]], 1.1)
+
+    def get_name(self):
+        return "BGMGraphGrid1D"
+
+
+class BGMGraphGrid2D(BGMGraph):
+    """BGMGraphGrid2D<VectorBase>(width, height): the 4-neighbour pixel grid of an image,
+    node i*width + j (bgmgraphgrid2D.h:88-142)."""
+
+    def __init__(self, width: int, height: int):
+        self.width, self.height = int(width), int(height)
+        jj, ii = np.meshgrid(np.arange(width, dtype=np.float64), np.arange(height, dtype=np.float64))
+        super().__init__(np.concatenate([jj.ravel(), ii.ravel()]), width * height, 2)
+
+    def process_grid(self):
+        n = self.width * self.height
+        ptr = np.empty(n + 1, dtype=np.int32)
+        idx = np.empty(max(2 * (self.height * (self.width - 1) + self.width * (self.height - 1)), 1), dtype=np.int32)
+        check(load().pasc_gb300_graph_grid2d(self.width, self.height, ptr, idx))
+        self._set(ptr, idx[: ptr[-1]], 1.1)
+
+    def get_width(self):
+        return self.width
+
+    def get_height(self):
+        return self.height
+
+    def get_name(self):
+        return "BGMGraphGrid2D"
+
+
+class Decomposition:
+    """Decomposition<VectorBase>(T, R, K, xdim, DDT_size) or (T, graph, K, xdim, DDR_size):
+    layouts of one GPU.  With R > 1 nodes and no graph the nodes are disjoint (the graph the
+    model builds when none is given, graphh1fem.cpp:30-45)."""
+
+    def __init__(self, T: int, R, K: int, xdim: int = 1, DD_size: int = 1):
+        if DD_size != 1:
+            raise PascError(capi.PASC_ERR_NOTSUPP, "one GPU per problem: DDT_size / DDR_size must be 1")
+        if isinstance(R, BGMGraph):
+            self.graph = R
+            R = R.get_n()
+        else:
+            self.graph = None
+            if int(R) > 1:
+                g = BGMGraph(np.arange(int(R), dtype=np.float64), int(R), 1)
+                g.process(0.0)
+                self.graph = g
+        self.T, self.R, self.K, self.xdim = int(T), int(R), int(K), int(xdim)
+        if self.R > 1 and self.xdim != 1:
+            raise PascError(capi.PASC_ERR_NOTSUPP, "graph problems take scalar data (xdim 1)")
 
     def get_T(self):
         return self.T
@@ -316,6 +462,25 @@ class Decomposition:
 
     def get_xdim(self):
         return self.xdim
+
+    def get_graph(self):
+        return self.graph
+
+    def permute_TRK(self, v, invert: bool = False):
+        """blocked k*R*T + r*T + t <-> interleaved (t*R + r)*K + k (decomposition.cpp:257-340)."""
+        T, R, K = self.T, self.R, self.K
+        v = np.asarray(v, dtype=np.float64)
+        if not invert:
+            return v.reshape(K, R, T).transpose(2, 1, 0).ravel().copy()
+        return v.reshape(T, R, K).transpose(2, 1, 0).ravel().copy()
+
+    def permute_TRxdim(self, v, invert: bool = False):
+        """data: r*T + t (file order) <-> t*R + r."""
+        T, R = self.T, self.R
+        v = np.asarray(v, dtype=np.float64)
+        if not invert:
+            return v.reshape(R, T).T.ravel().copy()
+        return v.reshape(T, R).T.ravel().copy()
 
 
 class TSData:
@@ -338,6 +503,9 @@ class TSData:
     def get_T(self):
         return self.decomposition.get_T()
 
+    def get_R(self):
+        return self.decomposition.get_R()
+
     def get_K(self):
         return self.decomposition.get_K()
 
@@ -346,6 +514,42 @@ class TSData:
 
     def get_datavector(self):
         return self.datavector
+
+    # data preprocessing (src/petscvector/data/tsdata.cpp:384-560); the model's copy is refreshed
+    def _data_changed(self):
+        if self.model is not None:
+            self.model.problem.set_data(self.datavector)
+
+    def cutdata(self, a: float, b: float):
+        """Clamps the data to [a, b] (tsdata.cpp:461-478)."""
+        self.datavector = np.minimum(np.maximum(self.datavector, a), b)
+        self._data_changed()
+
+    def shiftdata(self, a: float):
+        self.datavector = self.datavector + a
+        self._data_changed()
+
+    def scaledata(self, a: float, b: float, scale_min: float | None = None, scale_max: float | None = None):
+        """Maps [scale_min, scale_max] (default: the data's range) linearly onto [a, b], theta
+        with it (tsdata.cpp:384-422, 511-548)."""
+        if scale_min is None:
+            scale_min, scale_max = float(np.min(self.datavector)), float(np.max(self.datavector))
+        self.scale_min, self.scale_max = scale_min, scale_max
+        k = (b - a) / (scale_max - scale_min)
+        q = a - k * scale_min
+        self.datavector = self.datavector * k + q
+        self._data_changed()
+        if self.model is not None:
+            self.model.problem.set_theta(k * self.model.problem.get_theta() + q)
+
+    def unscaledata(self, a: float, b: float):
+        """Inverse of scaledata (tsdata.cpp:424-459)."""
+        k = (b - a) / (self.scale_max - self.scale_min)
+        q = a - k * self.scale_min
+        self.datavector = (self.datavector - q) * (1.0 / k)
+        self._data_changed()
+        if self.model is not None:
+            self.model.problem.set_theta((self.model.problem.get_theta() - q) / k)
 
     def get_gammavector(self):
         if self.model is not None:
@@ -375,8 +579,9 @@ class TSData:
     def cutgamma(self):
         """Hard assignment: gamma_tk = 1 for the argmax k (true argmax, see the C ABI note)."""
         lab = self.model.problem.argmax_labels()
-        g = np.zeros((self.get_T(), self.get_K()))
-        g[np.arange(self.get_T()), lab] = 1.0
+        nb = self.get_T() * self.get_R()
+        g = np.zeros((nb, self.get_K()))
+        g[np.arange(nb), lab] = 1.0
         self.model.problem.set_gamma(g.ravel())
 
 
@@ -406,6 +611,43 @@ class Signal1DData(TSData):
         th = self.get_thetavector()
         save_vec(prefix + "_gamma.bin", g.T.ravel())
         save_vec(prefix + "_recovered.bin", g @ th)
+
+
+class ImageData(TSData):
+    """ImageData<VectorBase>(decomposition, filename, width, height): one image (T = 1) or a
+    sequence, R = width*height pixels on the decomposition's graph (src/petscvector/data/
+    imagedata.cpp:7-38); the file (PETSc binary) or array holds the pixels node-major
+    (r*T + t), permuted to the interleaved layout t*R + r."""
+
+    def __init__(self, decomposition: Decomposition, filename_or_data, width: int, height: int):
+        if isinstance(filename_or_data, str):
+            from .petscio import load_vec
+            raw = load_vec(filename_or_data)
+        else:
+            raw = np.ascontiguousarray(filename_or_data, dtype=np.float64)
+        if raw.size != decomposition.get_T() * decomposition.get_R():
+            raise PascError(capi.PASC_ERR_ARG, "ImageData: the data does not have T*width*height values")
+        self.width, self.height = int(width), int(height)
+        super().__init__(decomposition, decomposition.permute_TRxdim(raw))
+
+    def get_width(self):
+        return self.width
+
+    def get_height(self):
+        return self.height
+
+    def save_image(self, prefix: str, save_original: bool = True):
+        """saveImage (imagedata.cpp:40-103): <prefix>_original.bin (the data), _gamma.bin
+        (blocked layout) and _recovered.bin (sum_k theta_k gamma_k), pixels node-major."""
+        from .petscio import save_vec
+        dec = self.decomposition
+        if save_original:
+            save_vec(prefix + "_original.bin", dec.permute_TRxdim(self.datavector, invert=True))
+        g = self.get_gammavector()
+        th = self.get_thetavector()
+        save_vec(prefix + "_gamma.bin", dec.permute_TRK(g, invert=True))
+        rec = g.reshape(-1, self.get_K()) @ th
+        save_vec(prefix + "_recovered.bin", dec.permute_TRxdim(rec, invert=True))
 
 
 class Fem:
@@ -441,7 +683,9 @@ class GraphH1FEMModel:
         self.tsdata = tsdata
         self.epssqr = float(epssqr)
         T, K = tsdata.get_T(), tsdata.get_K()
-        self.problem = Problem(T, K, epssqr, precision=precision, xdim=tsdata.get_xdim(), device=device)
+        graph = tsdata.decomposition.get_graph() if hasattr(tsdata.decomposition, "get_graph") else None
+        self.problem = Problem(T, K, epssqr, precision=precision, xdim=tsdata.get_xdim(), device=device, graph=graph)
+        T = T * self.problem.R  # blocks of K
         self.fem = fem if fem is not None else Fem(1.0)
         if self.fem.is_reduced():
             self.problem.set_fem(self.fem.fem_reduce, self.fem.fem_type)

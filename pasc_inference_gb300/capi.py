@@ -100,6 +100,15 @@ PROTOTYPES = {
     "pasc_gb300_fem_reduce_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_long, C.c_int, C.c_int, C.c_void_p]),
     "pasc_gb300_fem_prolongate_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_long, C.c_int, C.c_int,
                                                 C.c_void_p]),
+    "pasc_gb300_create_graph": (C.c_int, [C.POINTER(_h), C.c_long, C.c_long, C.c_int, C.c_int, C.c_double, C.c_int,
+                                          _ip, _ip]),
+    "pasc_gb300_get_graph": (C.c_int, [_h, C.POINTER(C.c_long), C.POINTER(C.c_long), C.POINTER(C.c_long)]),
+    "pasc_gb300_graph_grid1d": (C.c_int, [C.c_int, _ip, _ip]),
+    "pasc_gb300_graph_grid2d": (C.c_int, [C.c_int, C.c_int, _ip, _ip]),
+    "pasc_gb300_graph_threshold": (C.c_int, [_dp, C.c_int, C.c_int, C.c_double, _ip, C.c_void_p, C.c_long,
+                                             C.POINTER(C.c_long)]),
+    "pasc_gb300_graph_matmult_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_long, C.c_int, C.c_double,
+                                               C.c_void_p, C.c_void_p, C.c_void_p]),
     "pasc_gb300_set_usethetainpenalty": (C.c_int, [_h, C.c_int]),
     "pasc_gb300_get_usethetainpenalty": (C.c_int, [_h, C.POINTER(C.c_int)]),
     "pasc_gb300_time_model_kernels": (C.c_int, [_h, C.c_int, C.c_int, C.POINTER(C.c_double)]),

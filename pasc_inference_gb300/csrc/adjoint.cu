@@ -396,6 +396,7 @@ static int ensure_work(pasc_gb300_problem *p)
     if (p->xdim > 1) return afail(PASC_ERR_NOTSUPP, "adjoint: 1-D signals only");
     if (p->fem_inner) return afail(PASC_ERR_NOTSUPP, "adjoint: reduced (fem_reduce < 1) problems are not supported");
     if (p->tp) return afail(PASC_ERR_NOTSUPP, "adjoint: theta in the penalty is not supported");
+    if (p->graph) return afail(PASC_ERR_NOTSUPP, "adjoint: graph (R > 1) problems are not supported");
     AdjointWork *w = new AdjointWork();
     w->K = p->K;
     w->T = p->T;

@@ -57,6 +57,18 @@ struct SweepArgs {
     const float *kw = nullptr;
 };
 
+// Graph (R > 1) mode, mixed path (graph.cu): x and d ping-pong, buffer st->cur current.
+struct GraphSweepArgs {
+    const float *data;        // T*R
+    const float *theta;       // K
+    float *xb0, *xb1;         // gamma
+    float *db0, *db1;         // direction d of the current gamma
+    double *partials;         // gridDim.x * 4
+    SpgDevState *st;
+    const int *ptr, *idx;     // neighbour lists (CSR over R nodes, sorted, symmetric)
+    long T, R;
+};
+
 struct ThetaArgs {
     const float *data;
     const float *xb0, *xb1;  // gamma lives in buffer st->cur
@@ -135,6 +147,14 @@ cudaError_t launch_fem_reduce(const TIn *g1, const double *data, const double *t
 template <typename TIn, typename TOut>
 cudaError_t launch_fem_prolongate(const TIn *g2, TOut *g1, long T1, long T2, int K, int type, cudaStream_t s);
 
+// Graph (R > 1) and image mode (graph.cu).
+const char *graph_check(long R, const int *ptr, const int *idx);  // null: valid
+int graph_sweep_threads();
+int graph_sweep_grid(long nblocks);
+cudaError_t launch_graph_sweep(int K, bool init, int grid, const GraphSweepArgs &a, cudaStream_t s);
+cudaError_t launch_graph_matmult_f64(const double *x, double *y, long T, long R, int K, double coeff,
+                                     const int *ptr, const int *idx, cudaStream_t s, const double *kc = nullptr);
+
 int batch_tile_width();
 int batch_segment_timesteps();
 int batch_max_tile();
@@ -172,8 +192,9 @@ cudaError_t launch_axpy_f64(double *y, double a, const double *x, long n, cudaSt
 cudaError_t launch_xmay_f64(double *d, const double *x, double a, const double *g, long n, cudaStream_t s);
 cudaError_t launch_residual_f64(const double *data, const double *theta, double *b, long T, int K,
                                 double bscale, cudaStream_t s);
-cudaError_t launch_permute_f64(const double *src, double *dst, long T, int K, cudaStream_t s);
-cudaError_t launch_permute_f32(const float *src, float *dst, long T, int K, cudaStream_t s);
+// blocked k*R*Tt + r*Tt + t -> interleaved (t*R + r)*K + k over T = Tt*R blocks (R = 1: k*T + t)
+cudaError_t launch_permute_f64(const double *src, double *dst, long T, int K, cudaStream_t s, long R = 1);
+cudaError_t launch_permute_f32(const float *src, float *dst, long T, int K, cudaStream_t s, long R = 1);
 // Deterministic dot products: out[q] = sum_i a_q[i] * b_q[i] for q < nq (nq <= 3); a scratch
 // of dot_partials_size() doubles.  fxmode: out[0] = sum_i x_i * (g_i - b_i) (get_fx).
 size_t dot_partials_size();

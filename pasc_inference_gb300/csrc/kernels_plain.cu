@@ -165,29 +165,33 @@ cudaError_t launch_residual_f64(const double *data, const double *theta, double 
 }
 
 // blocked k*T+t -> interleaved t*K+k  (decomposition.cpp:266-356, R = 1)
+// T blocks = Tt timesteps x R nodes; block s = t*R + r comes from k*R*Tt + r*Tt + t
+// (with R > 1, Decomposition::permute_TRblocksize, decomposition.cpp:260-340)
 template <typename F>
-__global__ void permute_kernel(const F *src, F *dst, long T, int K)
+__global__ void permute_kernel(const F *src, F *dst, long T, int K, long R)
 {
     const long n = T * K;
+    const long Tt = T / R;
     const long stride = (long)gridDim.x * blockDim.x;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const long t = i / K;
-        const int k = (int)(i - t * K);
-        dst[i] = src[(long)k * T + t];
+        const long s = i / K;
+        const int k = (int)(i - s * K);
+        const long t = s / R, r = s - t * R;
+        dst[i] = src[(long)k * T + r * Tt + t];
     }
 }
 
-cudaError_t launch_permute_f64(const double *src, double *dst, long T, int K, cudaStream_t s)
+cudaError_t launch_permute_f64(const double *src, double *dst, long T, int K, cudaStream_t s, long R)
 {
     if (T <= 0) return cudaSuccess;
-    permute_kernel<double><<<grid_elems(T * K), PLAIN_NT, 0, s>>>(src, dst, T, K);
+    permute_kernel<double><<<grid_elems(T * K), PLAIN_NT, 0, s>>>(src, dst, T, K, R);
     return cudaGetLastError();
 }
 
-cudaError_t launch_permute_f32(const float *src, float *dst, long T, int K, cudaStream_t s)
+cudaError_t launch_permute_f32(const float *src, float *dst, long T, int K, cudaStream_t s, long R)
 {
     if (T <= 0) return cudaSuccess;
-    permute_kernel<float><<<grid_elems(T * K), PLAIN_NT, 0, s>>>(src, dst, T, K);
+    permute_kernel<float><<<grid_elems(T * K), PLAIN_NT, 0, s>>>(src, dst, T, K, R);
     return cudaGetLastError();
 }
 

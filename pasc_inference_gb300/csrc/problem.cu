@@ -63,7 +63,8 @@ static void free_all(pasc_gb300_problem *p)
     void *dev[] = {p->data64, p->theta64, p->stage64, p->red, p->red_out, p->labels_d, p->x, p->g,
                    p->d, p->Ad, p->b, p->data32_raw, p->theta32, p->xb_raw[0], p->xb_raw[1], p->st,
                    p->partials, p->xbf, p->xnorm, p->bmat_raw, p->theta_split, p->theta_f32, p->tnorm,
-                   p->mc_partials, p->mc_err, p->tp_ck64, p->tp_kw32};
+                   p->mc_partials, p->mc_err, p->tp_ck64, p->tp_kw32, p->gptr, p->gidx, p->db_raw[0],
+                   p->db_raw[1], p->gpartials};
     for (void *q : dev)
         if (q) cudaFree(q);
     if (p->st_h) cudaFreeHost(p->st_h);
@@ -89,14 +90,24 @@ static int fem_update_b_async(pasc_gb300_problem *p, int *launches);
 
 static void set_coeffs(pasc_gb300_problem *p)
 {
-    // graphh1fem.cpp:146-151 and :280-283 (not reduced: T_reduced == T)
+    // graphh1fem.cpp:146-151 and :280-283 (not reduced: T_reduced == T); T counts timesteps,
+    // not the T*R blocks of a graph problem
+    const long T = p->graph ? p->graph_T : p->T;
     double c = p->epssqr;
-    if (p->scalef) c *= (1.0 / ((double)p->T));
-    else c *= ((double)p->T / ((double)p->T));
+    if (p->scalef) c *= (1.0 / ((double)T));
+    else c *= ((double)T / ((double)T));
     p->coeffA = c;
     double cb = -1.0;
-    if (p->scalef) cb *= (1.0 / ((double)p->T));
+    if (p->scalef) cb *= (1.0 / ((double)T));
     p->coeffB = cb;
+}
+
+// A x in FP64 (MatMult + VecScale): the 1-D chain, or the graph operator
+static cudaError_t apply_A_f64(pasc_gb300_problem *p, const double *x, double *y, cudaStream_t s)
+{
+    const double *kc = p->tp ? p->tp_ck64 : nullptr;
+    if (p->graph) return launch_graph_matmult_f64(x, y, p->graph_T, p->graph_R, p->K, p->coeffA, p->gptr, p->gidx, s, kc);
+    return launch_matmult_f64(x, y, p->T, p->K, p->coeffA, s, kc);
 }
 
 extern "C" {
@@ -486,11 +497,11 @@ int pasc_gb300_get_theta(pasc_gb300_problem *p, double *theta)
 static int permute_gamma_async(pasc_gb300_problem *p)
 {
     if (p->precision == PASC_PREC_FP64) {
-        CU(launch_permute_f64(p->x, p->stage64, p->T, p->K, p->stream));
+        CU(launch_permute_f64(p->x, p->stage64, p->T, p->K, p->stream, p->graph_R));
         CU(cudaMemcpyAsync(p->x, p->stage64, sizeof(double) * p->N, cudaMemcpyDeviceToDevice, p->stream));
     } else {
         float *src = p->xb[p->cur], *dst = p->xb[p->cur ^ 1];
-        CU(launch_permute_f32(src, dst, p->T, p->K, p->stream));
+        CU(launch_permute_f32(src, dst, p->T, p->K, p->stream, p->graph_R));
         p->cur ^= 1;
     }
     return PASC_OK;
@@ -614,7 +625,7 @@ static int fp64_start(pasc_gb300_problem *p)
     r.normb = sqrt(v[0]);             // :104
     r.alpha = r.o.alphainit;          // :108
     CU(launch_project_f64(p->x, T, K, s));                   // :116
-    CU(launch_matmult_f64(p->x, p->g, T, K, p->coeffA, s, p->tp ? p->tp_ck64 : nullptr));  // :122-123
+    CU(apply_A_f64(p, p->x, p->g, s));                       // :122-123
     CU(launch_axpy_f64(p->g, -1.0, p->b, N, s));             // :128
     CU(launch_fx_f64(p->x, p->g, p->b, N, p->red, p->red_out, s));  // :133
     r.launches += 4;
@@ -650,7 +661,7 @@ static int fp64_iterate(pasc_gb300_problem *p, long n)
         CU(launch_xmay_f64(p->d, p->x, r.alpha, p->g, N, s));    // :146-147
         CU(launch_project_f64(p->d, T, K, s));                    // :153
         CU(launch_axpy_f64(p->d, -1.0, p->x, N, s));              // :158
-        CU(launch_matmult_f64(p->d, p->Ad, T, K, p->coeffA, s, p->tp ? p->tp_ck64 : nullptr));  // :164-165
+        CU(apply_A_f64(p, p->d, p->Ad, s));                       // :164-165
         r.hessmult += 1;
         CU(launch_dots_f64(3, p->d, p->d, p->d, p->Ad, p->d, p->g, N, p->red, p->red_out, s));  // :357-363
         r.launches += 5;
@@ -729,6 +740,22 @@ static constexpr int GRAPH_CHUNK = 16;
 
 static cudaError_t launch_variant(pasc_gb300_problem *p, int v, bool init, const SweepArgs &a)
 {
+    if (p->graph) {
+        GraphSweepArgs g;
+        g.data = p->data32;
+        g.theta = p->theta32;
+        g.xb0 = p->xb[0];
+        g.xb1 = p->xb[1];
+        g.db0 = p->db_raw[0];
+        g.db1 = p->db_raw[1];
+        g.partials = p->gpartials;
+        g.st = p->st;
+        g.ptr = p->gptr;
+        g.idx = p->gidx;
+        g.T = p->graph_T;
+        g.R = p->graph_R;
+        return launch_graph_sweep(p->K, init, p->grid_graph, g, p->stream);
+    }
     const int *gs = a.kw ? p->grid_sweep_tp : p->grid_sweep;
     const int *gi = a.kw ? p->grid_sweep_init_tp : p->grid_sweep_init;
     if (v == 1) return launch_sweep_tma(p->K, init, init ? gi[1] : gs[1], a, p->stream);
@@ -816,6 +843,7 @@ static void fill_device_state(pasc_gb300_problem *p, SpgDevState *h)
 // without changing the solve; the faster kernel is kept for the problem's lifetime.
 static int autotune_variant(pasc_gb300_problem *p)
 {
+    if (p->graph) p->variant = 0;  // one graph sweep
     if (p->variant >= 0) return PASC_OK;
     if (!sweep_tma_supported(p->K)) {
         p->variant = 0;
@@ -872,7 +900,7 @@ static int mixed_start(pasc_gb300_problem *p)
     CU(cudaStreamSynchronize(s));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, p->ev0, p->ev1);
-    p->run.launches += 1;
+    p->run.launches += p->graph ? 2 : 1;
     p->run.time_s += ms * 1e-3;
     CHK(check_device_error(p));
     sync_run_from_device(p);
@@ -906,7 +934,7 @@ static int mixed_iterate(pasc_gb300_problem *p, long n, int poll)
             for (long q = 0; q < want; q++) CU(launch_variant(p, p->variant, false, a));
         }
         done += want;
-        p->run.launches += (int)want;
+        p->run.launches += (int)want * (p->graph ? 2 : 1);
         if (poll) {
             CU(cudaMemcpyAsync(h, p->st, sizeof(SpgDevState), cudaMemcpyDeviceToHost, s));
             CU(cudaStreamSynchronize(s));
@@ -1169,6 +1197,7 @@ int pasc_gb300_set_sweep_variant(pasc_gb300_problem *p, int variant)
     if (variant < -1 || variant > 1) return fail(PASC_ERR_ARG, "set_sweep_variant: variant must be -1, 0 or 1");
     if (p->precision != PASC_PREC_MIXED) return fail(PASC_ERR_STATE, "set_sweep_variant: mixed precision only");
     if (variant == 1 && !sweep_tma_supported(p->K)) return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: K not supported");
+    if (variant == 1 && p->graph) return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: a graph problem has one sweep");
     p->variant = variant;
     p->run.started = false;
     return PASC_OK;
@@ -1181,6 +1210,8 @@ int pasc_gb300_set_fem(pasc_gb300_problem *p, double fem_reduce, int fem_type)
     if (fem_type != 0 && fem_type != 1) return fail(PASC_ERR_ARG, "set_fem: fem_type 0 (FEM-SUM) or 1 (FEM-HAT)");
     if (p->tp && fem_reduce < 1.0)
         return fail(PASC_ERR_NOTSUPP, "set_fem: theta in the penalty with a reduced (fem_reduce < 1) problem");
+    if (p->graph && fem_reduce < 1.0)
+        return fail(PASC_ERR_NOTSUPP, "set_fem: FEM reduction of a graph (R > 1) problem");
     CU(cudaSetDevice(p->device));
     CU(cudaStreamSynchronize(p->stream));
     if (p->fem_inner) {
@@ -1311,6 +1342,7 @@ int pasc_gb300_set_usethetainpenalty(pasc_gb300_problem *p, int on)
         return fail(PASC_ERR_NOTSUPP, "set_usethetainpenalty: one-dimensional data (xdim == 1) only");
     if (on && p->fem_inner)
         return fail(PASC_ERR_NOTSUPP, "set_usethetainpenalty: not with a reduced (fem_reduce < 1) problem");
+    if (on && p->graph) return fail(PASC_ERR_NOTSUPP, "set_usethetainpenalty: not with a graph (R > 1) problem");
     CU(cudaSetDevice(p->device));
     CU(cudaStreamSynchronize(p->stream));
     p->run.started = false;
@@ -1347,6 +1379,55 @@ int pasc_gb300_set_usethetainpenalty(pasc_gb300_problem *p, int on)
     }
     CU(launch_tp_coeffs(p->theta64, p->coeffA, p->K, p->tp_ck64, p->tp_kw32, p->stream));
     CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+// GraphH1FEMModel on a Decomposition(T, graph, K, 1, 1) (graphh1fem.cpp:8-65 with a BGMGraph,
+// blockgraphsparse.cpp:7-103): a problem of T*R blocks of K with the graph operator.
+int pasc_gb300_create_graph(pasc_gb300_problem **out, long T, long R, int K, int precision, double epssqr, int device,
+                            const int *nbr_ptr, const int *nbr_idx)
+{
+    if (!out) return fail(PASC_ERR_ARG, "create_graph: out is NULL");
+    *out = nullptr;
+    if (T < 1) return fail(PASC_ERR_ARG, "create_graph: T must be >= 1 (got %ld)", T);
+    if (R < 1 || (double)T * (double)R > 2.0e9) return fail(PASC_ERR_ARG, "create_graph: R must be >= 1 and T*R < 2e9");
+    if (const char *why = graph_check(R, nbr_ptr, nbr_idx)) return fail(PASC_ERR_ARG, "create_graph: %s", why);
+    pasc_gb300_problem *p = nullptr;
+    CHK(pasc_gb300_create(&p, T * R, K, 1, precision, epssqr, device));
+    p->graph = true;
+    p->graph_T = T;
+    p->graph_R = R;
+    p->graph_nnz = nbr_ptr[R];
+    p->variant = 0;
+    set_coeffs(p);
+    int rc;
+    auto bail = [&](int code) { free_all(p); return code; };
+    if ((rc = dalloc(&p->gptr, (size_t)R + 1)) || (rc = dalloc(&p->gidx, (size_t)(p->graph_nnz > 0 ? p->graph_nnz : 1))))
+        return bail(rc);
+    if (cudaMemcpy(p->gptr, nbr_ptr, sizeof(int) * (R + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        (p->graph_nnz > 0 &&
+         cudaMemcpy(p->gidx, nbr_idx, sizeof(int) * p->graph_nnz, cudaMemcpyHostToDevice) != cudaSuccess))
+        return bail(fail(PASC_ERR_CUDA, "create_graph: upload failed"));
+    if (precision == PASC_PREC_MIXED) {
+        const long N = p->N;
+        p->grid_graph = graph_sweep_grid(T * R);
+        if ((rc = dalloc(&p->db_raw[0], N)) || (rc = dalloc(&p->db_raw[1], N)) ||
+            (rc = dalloc(&p->gpartials, (size_t)p->grid_graph * 4)))
+            return bail(rc);
+        cudaMemset(p->db_raw[0], 0, sizeof(float) * N);
+        cudaMemset(p->db_raw[1], 0, sizeof(float) * N);
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) return bail(fail(PASC_ERR_CUDA, "create_graph: initialisation failed"));
+    *out = p;
+    return PASC_OK;
+}
+
+int pasc_gb300_get_graph(pasc_gb300_problem *p, long *T, long *R, long *nnz)
+{
+    if (!p) return fail(PASC_ERR_ARG, "get_graph: NULL problem");
+    if (T) *T = p->graph ? p->graph_T : p->T;
+    if (R) *R = p->graph ? p->graph_R : 1;
+    if (nnz) *nnz = p->graph ? p->graph_nnz : 0;
     return PASC_OK;
 }
 

@@ -86,6 +86,15 @@ struct pasc_gb300_problem {
     pasc_gb300_problem *fem_inner = nullptr;
     bool b_external = false;               // inner handle: b is written by the owner
 
+    // graph (R > 1) / image mode (pasc_gb300_create_graph): T above counts the T*R blocks of K;
+    // graph_T is the number of timesteps (it scales A and b), graph_R the number of nodes
+    bool graph = false;
+    long graph_T = 0, graph_R = 1, graph_nnz = 0;
+    int *gptr = nullptr, *gidx = nullptr;  // device CSR
+    float *db_raw[2] = {nullptr, nullptr}; // mixed path: direction ping-pong
+    double *gpartials = nullptr;
+    int grid_graph = 0;
+
     // theta in the penalty (pasc_gb300_set_usethetainpenalty): block k of A is
     // coeffA * theta_k^2 * A_hat; ck64[k] = (coeffA theta_k) theta_k, kw32[k] = theta_k^2
     bool tp = false;

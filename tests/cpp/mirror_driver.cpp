@@ -4,6 +4,9 @@
 //
 //   mirror_driver --host-checks <dir>              checks that need no GPU
 //   mirror_driver <data.bin> <K> <epssqr> <prefix>  solve on GPU 0, print L, theta, iterations
+//   mirror_driver --image <data.bin> <width> <height> <K> <epssqr> <prefix>
+//                                                   the test_image sequence (examples/test_image/
+//                                                   test_image.cpp:156-221): grid graph, T = 1
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -28,13 +31,21 @@ static int host_checks(const std::string &dir)
     std::printf("uniform");
     for (double x : u) std::printf(" %.17g", x);
     std::printf("\n");
+    // R > 1 nodes without a graph: disjoint nodes; a grid graph's edges
+    {
+        Decomposition d(100, 2, 3, 1, 1);
+        BGMGraphGrid2D grid(4, 3);
+        grid.process_grid();
+        std::printf("R=2 nodes %d edges %d grid %d %d\n", d.get_graph()->get_n(), d.get_graph()->get_m(), grid.get_m(),
+                    grid.get_m_max());
+    }
     // errors become exceptions
     try {
-        Decomposition d(100, 2, 3, 1, 1);
-        std::printf("R=2 accepted FAILED\n");
+        Decomposition d(100, 2, 3, 2, 1);
+        std::printf("xdim=2 graph accepted FAILED\n");
         return 1;
     } catch (const Error &e) {
-        std::printf("R=2 code %d\n", e.code());
+        std::printf("xdim=2 code %d\n", e.code());
     }
     try {
         Problem p(0, 3, 1.0);
@@ -50,6 +61,22 @@ int main(int argc, char **argv)
 {
     try {
         if (argc == 3 && std::string(argv[1]) == "--host-checks") return host_checks(argv[2]);
+        if (argc == 8 && std::string(argv[1]) == "--image") {
+            const int width = std::atoi(argv[3]), height = std::atoi(argv[4]), K = std::atoi(argv[5]);
+            BGMGraphGrid2D graph(width, height);
+            graph.process_grid();
+            Decomposition decomposition(1, graph, K, 1, 1);
+            ImageData mydata(decomposition, argv[2], width, height);
+            GraphH1FEMModel mymodel(mydata, std::atof(argv[6]));
+            TSSolver mysolver(mydata, 1, {{"spgqpsolver_m", 10}, {"spgqpsolver_eps", 1e-10}});
+            mysolver.solve();
+            std::printf("L %.17g\n", mysolver.get_L());
+            std::printf("theta");
+            for (double t : mydata.get_thetavector()) std::printf(" %.17g", t);
+            std::printf("\n");
+            mydata.saveImage(argv[7]);
+            return 0;
+        }
         if (argc != 5) {
             std::fprintf(stderr, "usage: %s <data.bin> <K> <epssqr> <prefix> | --host-checks <dir>\n", argv[0]);
             return 2;
@@ -59,6 +86,9 @@ int main(int argc, char **argv)
         Signal1DData mydata(argv[1]);
         mydata.set_decomposition(Decomposition(mydata.get_Tpreliminary(), 1, K, 1, 1));
         GraphH1FEMModel mymodel(mydata, epssqr);
+        // the sweep kernel is otherwise chosen by timing, per process; pinned so that this run
+        // and the Python one make the same FP32 roundings
+        mymodel.problem().set_sweep_variant(1);
         TSSolver mysolver(mydata, 1, {{"spgqpsolver_m", 10}, {"spgqpsolver_eps", 1e-6}});
         mysolver.solve();
         std::printf("L %.17g\n", mysolver.get_L());

@@ -33,7 +33,8 @@ def test_host_side_pieces(driver, tmp_path):
     assert lines["roundtrip"] == "ok"
     u = np.array([float(v) for v in lines["uniform"].split()])
     assert np.array_equal(u, datagen.uniform(13, 0, 5))  # bit for bit
-    assert int(lines["R=2"].split()[-1]) == capi.PASC_ERR_NOTSUPP
+    assert lines["R=2"].split() == ["nodes", "2", "edges", "0", "grid", "17", "4"]
+    assert int(lines["xdim=2"].split()[-1]) == capi.PASC_ERR_NOTSUPP
     assert int(lines["T=0"].split()[-1]) == capi.PASC_ERR_ARG
     # the file written by the C++ side is read back by the Python reader
     assert np.array_equal(petscio.load_vec(str(tmp_path / "roundtrip.bin")),
@@ -52,7 +53,8 @@ def test_driver_matches_python_mirror(driver, tmp_path):
 
     data = Signal1DData(path)
     data.set_decomposition(Decomposition(data.get_Tpreliminary(), 1, 2, 1, 1))
-    GraphH1FEMModel(data, 10.0)
+    model = GraphH1FEMModel(data, 10.0)
+    model.problem.set_sweep_variant(1)  # as the driver does (the timed choice is per process)
     solver = TSSolver(data, options={"spgqpsolver_m": 10, "spgqpsolver_eps": 1e-6})
     solver.solve()
     assert L_cpp == solver.get_L()
@@ -62,3 +64,30 @@ def test_driver_matches_python_mirror(driver, tmp_path):
     rec = petscio.load_vec(str(tmp_path / "cpp_recovered.bin"))
     assert g.size == 2 * sig.T and rec.size == sig.T
     assert np.allclose(rec, g.reshape(2, -1).T @ th_cpp)
+
+
+@pytest.mark.gpu
+def test_image_driver_matches_python_mirror(driver, tmp_path):
+    from pasc_inference_gb300 import BGMGraphGrid2D, ImageData
+    w, h, K = 40, 30, 2
+    rng = np.random.default_rng(4)
+    yy, xx = np.mgrid[0:h, 0:w]
+    truth = (((xx - w / 3) ** 2 + (yy - h / 2) ** 2) < (h / 4) ** 2).astype(float).ravel()
+    img = truth + 0.4 * rng.standard_normal(w * h)
+    path = str(tmp_path / "image.bin")
+    petscio.save_vec(path, img)
+    r = subprocess.run([driver, "--image", path, str(w), str(h), str(K), "2.0", str(tmp_path / "cpp")],
+                       capture_output=True, text=True, check=True)
+    lines = dict(l.split(" ", 1) for l in r.stdout.strip().splitlines())
+    graph = BGMGraphGrid2D(w, h)
+    graph.process_grid()
+    data = ImageData(Decomposition(1, graph, K, 1, 1), path, w, h)
+    GraphH1FEMModel(data, 2.0)
+    solver = TSSolver(data, options={"spgqpsolver_m": 10, "spgqpsolver_eps": 1e-10})
+    solver.solve()
+    # one graph sweep kernel, same inputs: the two mirrors make the same calls
+    assert float(lines["L"]) == solver.get_L()
+    assert np.array_equal(np.array([float(v) for v in lines["theta"].split()]), data.get_thetavector())
+    rec = petscio.load_vec(str(tmp_path / "cpp_recovered.bin"))
+    g = petscio.load_vec(str(tmp_path / "cpp_gamma.bin"))
+    assert rec.size == w * h and g.size == K * w * h

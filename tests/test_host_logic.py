@@ -65,8 +65,11 @@ def test_reference_option_names():
 def test_decomposition_limits():
     d = Decomposition(100, 1, 3, 1, 1)
     assert (d.get_T(), d.get_K(), d.get_R()) == (100, 3, 1)
+    # R > 1 nodes without a graph: disjoint nodes (graph mode); multichannel graph data refused
+    d4 = Decomposition(100, 4, 3, 1, 1)
+    assert d4.get_R() == 4 and d4.get_graph().get_m() == 0
     with pytest.raises(PascError):
-        Decomposition(100, 4, 3, 1, 1)
+        Decomposition(100, 4, 3, 2, 1)
     with pytest.raises(PascError):
         Decomposition(100, 1, 3, 1, 2)
 
