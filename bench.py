@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-multichannel", action="store_true")
+    ap.add_argument("--no-image", action="store_true")
     ap.add_argument("--variant", type=int, default=-1, choices=[-1, 0, 1],
                     help="sweep kernel: -1 chosen by timing (default), 0 one timestep per thread, "
                          "1 bulk-copy tiles (pin it when profiling: a profiler distorts the timing)")
@@ -320,6 +321,8 @@ def main():
         result["multichannel"] = measure_multichannel(dev, peak)
     if info.rank == 0 and not args.no_adjoint:
         result["adjoint"] = measure_adjoint(dev, peak)
+    if info.rank == 0 and not args.no_image:
+        result["image"] = measure_image(dev, peak)
     if info.rank == 0 and not args.no_cpu:
         rate, dt = oracle_iter_rate(sig, theta, args.eps2, T, 5, 0)
         result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
@@ -456,6 +459,74 @@ def measure_multichannel(dev, peak):
     t_th = time.perf_counter() - t0
     res["cpu_oracle"] = {"residual_s": t_res, "residual_cores": cpu_cores(), "theta_update_s": t_th,
                          "theta_update_cores": 1}
+    return res
+
+
+def _image_data(w, h, seed=7, sigma=0.4):
+    """Background 0, a disc 1, a bar 2, Gaussian noise (a test_image-style input)."""
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:h, 0:w]
+    lab = (((xx - w / 3) ** 2 + (yy - h / 2) ** 2) < (min(w, h) / 4) ** 2).astype(np.int8)
+    lab[(xx > 0.65 * w) & (xx < 0.9 * w) & (yy > 0.2 * h) & (yy < 0.8 * h)] = 2
+    return lab.ravel().astype(np.float64) + sigma * rng.standard_normal(w * h)
+
+
+def measure_image(dev, peak):
+    """Image mode (T = 1, 4-neighbour grid graph): the mixed graph SPG iteration (two kernels)
+    on a 4096x4096 image with K = 3, the TSSolver on a 1024x1024 image, and the FP64 oracle's SPG
+    iteration on the large image."""
+    from pasc_inference_gb300 import PASC_PREC_MIXED, BGMGraphGrid2D, Problem, capi, datagen
+    sys.path.insert(0, ROOT)
+    from oracle import pasc_oracle as orc
+    K, eps2 = 3, 2.0
+    w = h = 4096
+    R = w * h
+    data = _image_data(w, h)
+    g = BGMGraphGrid2D(w, h)
+    g.process_grid()
+    theta = np.array([0.0, 1.0, 2.0])
+    B_it = (20.0 * K + 4.0) * R  # read x, d, data; write x, d; read d (FP32)
+    res = {"workload": f"image {w}x{h} (T=1, 4-neighbour grid graph), K={K}, epssqr={eps2}, disc and bar on 0, "
+                       "noise 0.4", "R": R, "K": K,
+           "bytes_per_iteration": B_it,
+           "bytes_note": "the two-kernel graph iteration moves 20K+4 bytes per pixel; a fused single pass "
+                         "would need 8K+4 (halo recomputation over a general graph is not bounded)"}
+    with Problem(1, K, eps2, precision=PASC_PREC_MIXED, device=dev, graph=g) as p:
+        p.set_data(data)
+        p.set_gamma(datagen.uniform(13, 0, R * K))
+        p.set_theta(theta)
+        p.update_b()
+        p.spgqp_start(capi.spgqp_opts(m=10, maxit=100000, stop_difff=0))
+        p.spgqp_iterate(20, poll=False)
+        p.spgqp_iterate(300, poll=False)
+        ms, nl = p.spgqp_last_iterate()
+        it_ms = ms / 300
+        ach = B_it / (it_ms * 1e-3) / 1e9
+        res["spg_iteration"] = {"it_per_s": 1e3 / it_ms, "us_per_it": it_ms * 1e3, "gpu_launches_per_it": nl / 300,
+                                "achieved": ach, "unit": "GB/s", "frac": ach / peak,
+                                "kernels": "graph_sweep_a_kernel<3,false> + graph_sweep_b_kernel<3,false>"}
+        x = p.get_gamma()
+    # the FP64 oracle's SPG iteration on the same image (all cores)
+    b = orc.residual_b(data, theta, R, K, bscale=orc.b_coeff(1))
+    t0 = time.perf_counter()
+    orc.spgqp_solve_graph(b, x, 1, K, orc.A_coeff(eps2, 1), g.ptr, g.idx, orc.spg_opts(maxit=3, eps=0.0, m=10))
+    dt = time.perf_counter() - t0
+    res["cpu_oracle"] = {"it_per_s": 3 / dt, "sample": "3 SPG iterations of the FP64 oracle (one core)",
+                         "cores": 1}
+    # TSSolver on a 1024x1024 image with the reference's default stopping rules
+    w2 = 1024
+    d2 = _image_data(w2, w2, seed=8)
+    g2 = BGMGraphGrid2D(w2, w2)
+    g2.process_grid()
+    with Problem(1, K, eps2, precision=PASC_PREC_MIXED, device=dev, graph=g2) as p:
+        p.set_data(d2)
+        p.set_gamma(datagen.uniform(13, 0, w2 * w2 * K))
+        p.set_theta(np.zeros(K))
+        t0 = time.perf_counter()
+        st = p.ts_solve(capi.ts_opts(), capi.spgqp_opts(m=10))
+        res["tssolver_1024"] = {"wall_s": time.perf_counter() - t0, "L": st.L, "outer_it": st.it_last,
+                                "spg_it": st.spg_it_sum, "theta": p.get_theta().tolist()}
+    res["peak"] = peak
     return res
 
 

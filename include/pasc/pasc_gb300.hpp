@@ -170,6 +170,8 @@ public:
         check(pasc_gb300_get_sweep_variant(h_.get(), &v));
         return v;
     }
+    // 0 automatic (SPGQPSolver), 1 SPGQPSolver, 2 SPGQPSolverC
+    void set_gamma_solver_type(int t) { check(pasc_gb300_set_gamma_solver_type(h_.get(), t)); }
     void set_usethetainpenalty(bool on) { check(pasc_gb300_set_usethetainpenalty(h_.get(), on ? 1 : 0)); }
     bool get_usethetainpenalty() const
     {

@@ -260,6 +260,15 @@ int pasc_gb300_graph_threshold(const double *coords, int n, int dim, double thre
 int pasc_gb300_graph_matmult_f64(const double *x_dev, double *y_dev, long T, long R, int K, double coeff,
                                  const int *nbr_ptr_dev, const int *nbr_idx_dev, void *stream);
 
+/* The gamma solver GraphH1FEMModel builds (gammasolvertype, include/general/model/
+ * graphh1fem.h:42-48; console option graphh1femmodel_gammasolvertype): 0 = automatic (1),
+ * 1 = SPGQPSolver, 2 = SPGQPSolverC (include/general/solver/spgqpsolver_coeff.h:611-835: the
+ * coefficient eps of A = eps*A1 is factored out: d'Ad and the BB step use A1, the first step is
+ * alphainit/eps, the A-condition takes 2*eps*xi and the sigma1 clamp acts on the unscaled
+ * beta).  3 (PERMON) and 4 (TAO) give PASC_ERR_NOTSUPP, as does 2 with theta in the penalty. */
+int pasc_gb300_set_gamma_solver_type(pasc_gb300_problem *p, int type);
+int pasc_gb300_get_gamma_solver_type(pasc_gb300_problem *p, int *type);
+
 /* Theta in the penalty: GraphH1FEMModel(tsdata, epssqr, fem, usethetainpenalty = true)
  * (graphh1fem.cpp:8-19, 154-160; include/general/model/graphh1fem.h:61, 75).  Block k of the
  * gamma QP's A is alpha*theta_k*theta_k*A_hat (BlockGraphSparseMatrix with coefficients,

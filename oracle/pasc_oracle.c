@@ -1172,3 +1172,140 @@ int pasc_oracle_tssolver_solve_graph(const double *data, double *gamma, double *
     free(b); free(perm);
     return 0;
 }
+
+/* ------------------------------------------------------------------------------------- */
+/* SPGQPSolverC: the SPG-QP with the operator's coefficient factored out                  */
+/* (include/general/solver/spgqpsolver_coeff.h:611-835; GraphH1FEMModel with               */
+/* graphh1femmodel_gammasolvertype = 2, src/petscvector/model/graphh1fem.cpp:185-191).     */
+/* A = coeff * A1 is applied as A1 (coefficient set to 1) and the coefficient enters the   */
+/* gradient, the step and the A-condition explicitly.                                       */
+/* ------------------------------------------------------------------------------------- */
+static int spgqp_c_impl(const double *b, double *x, long T, int K, double coeff, const pasc_oracle_graph *G,
+                        const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, int nthreads)
+{
+    int nth = eff_threads(nthreads);
+    const long nb = T * (G ? G->R : 1);
+    const long n = nb * (long)K;
+    double *g = (double *)malloc(sizeof(double) * (size_t)n);
+    double *d = (double *)malloc(sizeof(double) * (size_t)n);
+    double *Ad = (double *)malloc(sizeof(double) * (size_t)n);
+    double *temp = (double *)malloc(sizeof(double) * (size_t)n);
+    spg_fs fs;
+    fs.m = o->m;
+    fs.last_idx = 0;
+    fs.fs = (double *)malloc(sizeof(double) * (size_t)(o->m > 0 ? o->m : 1));
+    if (!g || !d || !Ad || !temp || !fs.fs) {
+        free(g); free(d); free(Ad); free(temp); free(fs.fs);
+        return -1;
+    }
+    const double epssqr = coeff;                            /* :615 */
+    const double epssqrinv = epssqr == 0 ? 1.0 : 1.0 / epssqr; /* :616-621 */
+    int it = 0, hessmult = 0;
+    double fx, fx_old, fx_max, xi, beta_bar, beta_hat, beta, dd = 0.0, gd = 0.0, dAd = 0.0, alpha_bb;
+    const double normb = sqrt(vdot(b, b, n, nth));
+    alpha_bb = o->alphainit;
+
+    pasc_oracle_project(x, nb, K, nth);          /* :663 */
+    matmult_g(x, g, T, K, 1.0, NULL, G, nth);    /* g = A*x with coefficient 1 :667 */
+    vscale(g, epssqr, n, nth);                   /* g *= epssqr :668 */
+    hessmult += 1;
+    vaxpy(g, -1.0, b, n, nth);                   /* :671 */
+    fx = get_fx(g, b, x, temp, n, nth);          /* :676 */
+    fx_old = DBL_MAX;
+    fs_init(&fs, fx);
+
+    while (it < o->maxit) {
+        it += 1;
+        vcopy(d, x, n, nth);                      /* d = x - epssqrinv*alpha_bb*g :694 */
+        vaxpy(d, -(epssqrinv * alpha_bb), g, n, nth);
+        pasc_oracle_project(d, nb, K, nth);       /* :699 */
+        vaxpy(d, -1.0, x, n, nth);                /* :704 */
+        matmult_g(d, Ad, T, K, 1.0, NULL, G, nth); /* Ad = A*d, coefficient 1 :709 */
+        hessmult += 1;
+        dd = vdot(d, d, n, nth);
+        dAd = vdot(d, Ad, n, nth);
+        gd = vdot(d, g, n, nth);
+        fx_max = fs_get_max(&fs);
+        xi = (fx_max - fx) / dAd;                 /* :730-745 */
+        beta_bar = -gd / dAd;
+        beta_hat = o->gamma * beta_bar + sqrt(o->gamma * o->gamma * beta_bar * beta_bar + 2 * epssqr * xi);
+        if (epssqrinv * beta_hat < o->sigma1) beta_hat = o->sigma1;
+        if (epssqrinv * beta_hat < o->sigma2) beta = epssqrinv * beta_hat;
+        else beta = o->sigma2;
+        vaxpy(x, beta, d, n, nth);                /* :751 */
+        vaxpy(g, epssqr * beta, Ad, n, nth);      /* :752 */
+        fx_old = fx;
+        fx = get_fx(g, b, x, temp, n, nth);       /* :760 */
+        fs_update(&fs, fx);
+        alpha_bb = dd / dAd;                      /* :768 */
+        if (o->stop_difff && fabs(fx - fx_old) < o->eps) break; /* :800-814 */
+        if (o->stop_normgp && dd < o->eps) break;
+        if (o->stop_normgp_normb && dd < o->eps * normb) break;
+        if (o->stop_Anormgp && dAd < o->eps) break;
+        if (o->stop_Anormgp_normb && dAd < o->eps * normb) break;
+    }
+    if (r) {
+        r->it = it;
+        r->hessmult = hessmult;
+        r->fx = fx;
+        r->gP = dd;
+        r->dAd = dAd;
+        r->normb = normb;
+    }
+    free(g); free(d); free(Ad); free(temp); free(fs.fs);
+    return 0;
+}
+
+int pasc_oracle_spgqp_solve_coeff(const double *b, double *x, long T, int K, double coeff, const pasc_oracle_graph *G,
+                                  const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, int nthreads)
+{
+    return spgqp_c_impl(b, x, T, K, coeff, G, o, r, nthreads);
+}
+
+/* TSSolver with SPGQPSolverC as the gamma solver (1-D or graph problems, fem not reduced) */
+int pasc_oracle_tssolver_solve_coeff(const double *data, double *gamma, double *theta, long T, int K, double epssqr,
+                                     int scalef, const pasc_oracle_graph *G, const pasc_oracle_ts_opts *ts,
+                                     const pasc_oracle_spg_opts *spg, pasc_oracle_ts_result *r, int nthreads)
+{
+    const int nth = eff_threads(nthreads);
+    const long R = G ? G->R : 1, nb = T * R, n = nb * (long)K;
+    double *b = (double *)malloc(sizeof(double) * (size_t)n);
+    double *perm = (double *)malloc(sizeof(double) * (size_t)n);
+    if (!b || !perm) {
+        free(b); free(perm);
+        return -1;
+    }
+    const double coeffA = pasc_oracle_A_coeff(epssqr, T, scalef);
+    const double coeffB = pasc_oracle_b_coeff(T, scalef);
+    if (ts->init_permute) {
+        pasc_oracle_permute_TRK(gamma, perm, T, R, K);
+        memcpy(gamma, perm, sizeof(double) * (size_t)n);
+    }
+    double L = DBL_MAX, L_old, deltaL = DBL_MAX;
+    int it, spg_it_sum = 0, spg_hm_sum = 0, increased = 0;
+    for (it = 0; it < ts->maxit; it++) {
+        if (!ts->thetasolved) pasc_oracle_theta_update(gamma, data, theta, nb, K, 1, nth);
+        pasc_oracle_residual_b(data, theta, b, nb, K, 1, coeffB, nth);
+        pasc_oracle_spg_result sr;
+        spgqp_c_impl(b, gamma, T, K, coeffA, G, spg, &sr, nth);
+        spg_it_sum += sr.it;
+        spg_hm_sum += sr.hessmult;
+        L_old = L;
+        L = sr.fx;
+        deltaL = fabs(L - L_old);
+        if (L - L_old > 0) increased++;
+        if (ts->relative ? (deltaL < ts->eps * fabs(L)) : (deltaL < ts->eps)) break;
+    }
+    if (r) {
+        r->it_last = it;
+        r->it_sum = it;
+        r->spg_it_sum = spg_it_sum;
+        r->spg_hessmult_sum = spg_hm_sum;
+        r->L = L;
+        r->deltaL = deltaL;
+        r->aic = 2 * log(L) + K;
+        r->L_increased = increased;
+    }
+    free(b); free(perm);
+    return 0;
+}

@@ -206,6 +206,13 @@ int pasc_oracle_tssolver_solve_model(const double *data, double *gamma, double *
                                      double epssqr, int scalef, double fem_reduce, int fem_type,
                                      int usethetainpenalty, const pasc_oracle_ts_opts *ts,
                                      const pasc_oracle_spg_opts *spg, pasc_oracle_ts_result *r, int nthreads);
+/* SPGQPSolverC (include/general/solver/spgqpsolver_coeff.h:611-835): the coefficient of
+ * A = coeff * A1 factored out of the iteration; G may be NULL (1-D).  TSSolver with it. */
+int pasc_oracle_spgqp_solve_coeff(const double *b, double *x, long T, int K, double coeff, const pasc_oracle_graph *G,
+                                  const pasc_oracle_spg_opts *o, pasc_oracle_spg_result *r, int nthreads);
+int pasc_oracle_tssolver_solve_coeff(const double *data, double *gamma, double *theta, long T, int K, double epssqr,
+                                     int scalef, const pasc_oracle_graph *G, const pasc_oracle_ts_opts *ts,
+                                     const pasc_oracle_spg_opts *spg, pasc_oracle_ts_result *r, int nthreads);
 int pasc_oracle_tssolver_solve_graph(const double *data, double *gamma, double *theta, long T, int K,
                                      double epssqr, int scalef, const pasc_oracle_graph *G,
                                      const pasc_oracle_ts_opts *ts, const pasc_oracle_spg_opts *spg,

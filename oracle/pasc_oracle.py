@@ -121,6 +121,11 @@ def lib():
         L.pasc_oracle_tssolver_solve_graph.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
                                                        C.POINTER(Graph), C.POINTER(TsOpts), C.POINTER(SpgOpts),
                                                        C.POINTER(TsResult), C.c_int]
+        L.pasc_oracle_spgqp_solve_coeff.argtypes = [_dp, _dp, C.c_long, C.c_int, C.c_double, C.c_void_p,
+                                                    C.POINTER(SpgOpts), C.POINTER(SpgResult), C.c_int]
+        L.pasc_oracle_tssolver_solve_coeff.argtypes = [_dp, _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
+                                                       C.c_void_p, C.POINTER(TsOpts), C.POINTER(SpgOpts),
+                                                       C.POINTER(TsResult), C.c_int]
         L.pasc_oracle_fem_h1_matmult_kc.argtypes = [_dp, _dp, C.c_long, C.c_int, _dp, C.c_int]
         L.pasc_oracle_spgqp_solve_kc.argtypes = [_dp, _dp, C.c_long, C.c_int, _dp, C.POINTER(SpgOpts),
                                                  C.POINTER(SpgResult), C.c_int]
@@ -381,6 +386,39 @@ def tssolver_solve_graph(data, gamma_raw, theta0, T, K, epssqr, ptr, idx, scalef
                                                 C.byref(spg), C.byref(r), nthreads)
     if rc != 0:
         raise MemoryError("tssolver_solve_graph")
+    return g, th, r
+
+
+def spgqp_solve_coeff(b, x0, T, K, coeff, opts: SpgOpts | None = None, ptr=None, idx=None):
+    """SPGQPSolverC; with ptr/idx on the graph of those neighbour lists."""
+    opts = opts or spg_opts()
+    x = _f64(x0).copy()
+    r = SpgResult()
+    if ptr is not None:
+        g, keep = make_graph(ptr, idx)
+        gp = C.cast(C.pointer(g), C.c_void_p)
+    else:
+        gp = None
+    lib().pasc_oracle_spgqp_solve_coeff(_f64(b), x, T, K, coeff, gp, C.byref(opts), C.byref(r), 1)
+    return x, r
+
+
+def tssolver_solve_coeff(data, gamma_raw, theta0, T, K, epssqr, ptr=None, idx=None, scalef=1,
+                         ts: TsOpts | None = None, spg: SpgOpts | None = None, nthreads=1):
+    ts = ts or ts_opts()
+    spg = spg or spg_opts()
+    if ptr is not None:
+        gr, keep = make_graph(ptr, idx)
+        gp = C.cast(C.pointer(gr), C.c_void_p)
+    else:
+        gp = None
+    g = _f64(gamma_raw).copy()
+    th = _f64(theta0).copy()
+    r = TsResult()
+    rc = lib().pasc_oracle_tssolver_solve_coeff(_f64(data), g, th, T, K, epssqr, scalef, gp, C.byref(ts),
+                                                C.byref(spg), C.byref(r), nthreads)
+    if rc != 0:
+        raise MemoryError("tssolver_solve_coeff")
     return g, th, r
 
 

@@ -178,6 +178,15 @@ class Problem:
         check(load().pasc_gb300_get_fem(self._h, C.byref(r), C.byref(t), C.byref(T2)))
         return r.value, t.value, T2.value
 
+    def set_gamma_solver_type(self, t: int):
+        """0 automatic (SPGQPSolver), 1 SPGQPSolver, 2 SPGQPSolverC."""
+        check(load().pasc_gb300_set_gamma_solver_type(self._h, int(t)))
+
+    def get_gamma_solver_type(self) -> int:
+        v = C.c_int()
+        check(load().pasc_gb300_get_gamma_solver_type(self._h, C.byref(v)))
+        return v.value
+
     def get_graph(self):
         """(timesteps, nodes, neighbour entries); (T, 1, 0) for a 1-D problem."""
         T, R, nnz = C.c_long(), C.c_long(), C.c_long()
@@ -679,7 +688,8 @@ class GraphH1FEMModel:
     the given seed, the reference's set_random) in the blocked layout."""
 
     def __init__(self, tsdata: TSData, epssqr: float, fem=None, usethetainpenalty: bool = False,
-                 precision: int = PASC_PREC_MIXED, gamma0=None, seed: int = 13, device: int = 0):
+                 precision: int = PASC_PREC_MIXED, gamma0=None, seed: int = 13, device: int = 0,
+                 gammasolvertype: int = 0):
         self.tsdata = tsdata
         self.epssqr = float(epssqr)
         T, K = tsdata.get_T(), tsdata.get_K()
@@ -687,6 +697,7 @@ class GraphH1FEMModel:
         self.problem = Problem(T, K, epssqr, precision=precision, xdim=tsdata.get_xdim(), device=device, graph=graph)
         T = T * self.problem.R  # blocks of K
         self.fem = fem if fem is not None else Fem(1.0)
+        self.problem.set_gamma_solver_type(gammasolvertype)  # graphh1femmodel_gammasolvertype
         if self.fem.is_reduced():
             self.problem.set_fem(self.fem.fem_reduce, self.fem.fem_type)
         self.usethetainpenalty = bool(usethetainpenalty)

@@ -109,6 +109,8 @@ PROTOTYPES = {
                                              C.POINTER(C.c_long)]),
     "pasc_gb300_graph_matmult_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_long, C.c_int, C.c_double,
                                                C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pasc_gb300_set_gamma_solver_type": (C.c_int, [_h, C.c_int]),
+    "pasc_gb300_get_gamma_solver_type": (C.c_int, [_h, C.POINTER(C.c_int)]),
     "pasc_gb300_set_usethetainpenalty": (C.c_int, [_h, C.c_int]),
     "pasc_gb300_get_usethetainpenalty": (C.c_int, [_h, C.POINTER(C.c_int)]),
     "pasc_gb300_time_model_kernels": (C.c_int, [_h, C.c_int, C.c_int, C.POINTER(C.c_double)]),

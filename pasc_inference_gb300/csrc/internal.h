@@ -27,6 +27,7 @@ struct SpgDevState {
     // problem and settings (copied in by the host before every solve)
     double coeff;       // A = coeff * A_hat
     double bscale;      // b = bscale * residual
+    int coeffmode;      // SPGQPSolverC: coefficient factored out of the step rules (dAd, dd/dAd unscaled)
     double eps, gamma, sigma1, sigma2;
     int maxit, m;
     int stop_difff, stop_normgp, stop_normgp_normb, stop_Anormgp, stop_Anormgp_normb;

@@ -102,12 +102,12 @@ static void set_coeffs(pasc_gb300_problem *p)
     p->coeffB = cb;
 }
 
-// A x in FP64 (MatMult + VecScale): the 1-D chain, or the graph operator
-static cudaError_t apply_A_f64(pasc_gb300_problem *p, const double *x, double *y, cudaStream_t s)
+// coeff * A_hat x in FP64 (MatMult + VecScale): the 1-D chain, or the graph operator
+static cudaError_t apply_A_f64(pasc_gb300_problem *p, const double *x, double *y, cudaStream_t s, double coeff)
 {
     const double *kc = p->tp ? p->tp_ck64 : nullptr;
-    if (p->graph) return launch_graph_matmult_f64(x, y, p->graph_T, p->graph_R, p->K, p->coeffA, p->gptr, p->gidx, s, kc);
-    return launch_matmult_f64(x, y, p->T, p->K, p->coeffA, s, kc);
+    if (p->graph) return launch_graph_matmult_f64(x, y, p->graph_T, p->graph_R, p->K, coeff, p->gptr, p->gidx, s, kc);
+    return launch_matmult_f64(x, y, p->T, p->K, coeff, s, kc);
 }
 
 extern "C" {
@@ -625,7 +625,9 @@ static int fp64_start(pasc_gb300_problem *p)
     r.normb = sqrt(v[0]);             // :104
     r.alpha = r.o.alphainit;          // :108
     CU(launch_project_f64(p->x, T, K, s));                   // :116
-    CU(apply_A_f64(p, p->x, p->g, s));                       // :122-123
+    // :122-123; SPGQPSolverC (spgqpsolver_coeff.h:667-668) multiplies with coefficient 1 and
+    // scales by eps afterwards: 1.0 * sum is exact, so eps * sum is the same value
+    CU(apply_A_f64(p, p->x, p->g, s, p->coeffA));
     CU(launch_axpy_f64(p->g, -1.0, p->b, N, s));             // :128
     CU(launch_fx_f64(p->x, p->g, p->b, N, p->red, p->red_out, s));  // :133
     r.launches += 4;
@@ -654,14 +656,18 @@ static int fp64_iterate(pasc_gb300_problem *p, long n)
     const int K = p->K;
     cudaStream_t s = p->stream;
     double v[3];
+    // SPGQPSolverC (spgqpsolver_coeff.h:611-835): d'Ad, the BB step and the A-condition without
+    // the coefficient, which enters the step scalars instead
+    const bool cm = p->solver_type == 2;
+    const double eps = p->coeffA, einv = eps == 0 ? 1.0 : 1.0 / eps;
     CU(cudaEventRecord(p->ev0, s));
     for (long q = 0; q < n && r.status == PASC_SPG_RUNNING; q++) {
         if (r.it >= o->maxit) { r.status = PASC_SPG_MAXIT; break; }
         r.it += 1;
-        CU(launch_xmay_f64(p->d, p->x, r.alpha, p->g, N, s));    // :146-147
+        CU(launch_xmay_f64(p->d, p->x, cm ? einv * r.alpha : r.alpha, p->g, N, s));  // :146-147
         CU(launch_project_f64(p->d, T, K, s));                    // :153
         CU(launch_axpy_f64(p->d, -1.0, p->x, N, s));              // :158
-        CU(apply_A_f64(p, p->d, p->Ad, s));                       // :164-165
+        CU(apply_A_f64(p, p->d, p->Ad, s, cm ? 1.0 : p->coeffA));  // :164-165
         r.hessmult += 1;
         CU(launch_dots_f64(3, p->d, p->d, p->d, p->Ad, p->d, p->g, N, p->red, p->red_out, s));  // :357-363
         r.launches += 5;
@@ -675,9 +681,15 @@ static int fp64_iterate(pasc_gb300_problem *p, long n)
             for (int i = 0; i < o->m; i++) fx_max = r.fs[i] > fx_max ? r.fs[i] : fx_max;  // :176
             const double xi = (fx_max - r.fx) / dAd;  // :182-195
             const double beta_bar = -gd / dAd;
-            double beta_hat = o->gamma * beta_bar + sqrt(o->gamma * o->gamma * beta_bar * beta_bar + 2 * xi);
-            if (beta_hat < o->sigma1) beta_hat = o->sigma1;
-            beta = beta_hat < o->sigma2 ? beta_hat : o->sigma2;
+            if (cm) {
+                double beta_hat = o->gamma * beta_bar + sqrt(o->gamma * o->gamma * beta_bar * beta_bar + 2 * eps * xi);
+                if (einv * beta_hat < o->sigma1) beta_hat = o->sigma1;
+                beta = einv * beta_hat < o->sigma2 ? einv * beta_hat : o->sigma2;
+            } else {
+                double beta_hat = o->gamma * beta_bar + sqrt(o->gamma * o->gamma * beta_bar * beta_bar + 2 * xi);
+                if (beta_hat < o->sigma1) beta_hat = o->sigma1;
+                beta = beta_hat < o->sigma2 ? beta_hat : o->sigma2;
+            }
             alpha_next = dd / dAd;  // :216
         } else if (gd < 0.0) {
             // linear along d (A_hat d = 0): the reference's division by zero falls through to
@@ -690,7 +702,7 @@ static int fp64_iterate(pasc_gb300_problem *p, long n)
             break;
         }
         CU(launch_axpy_f64(p->x, beta, p->d, N, s));   // :200
-        CU(launch_axpy_f64(p->g, beta, p->Ad, N, s));  // :201
+        CU(launch_axpy_f64(p->g, cm ? eps * beta : beta, p->Ad, N, s));  // :201
         CU(launch_fx_f64(p->x, p->g, p->b, N, p->red, p->red_out, s));  // :209
         r.launches += 3;
         CHK(read_red(p, 1, v));
@@ -821,8 +833,11 @@ static void fill_device_state(pasc_gb300_problem *p, SpgDevState *h)
 {
     const pasc_gb300_spgqp_opts *o = &p->run.o;
     memset(h, 0, sizeof(SpgDevState));
-    h->alpha_prev = o->alphainit;
-    h->alpha_cur = o->alphainit;  // alpha of the first direction (:108)
+    // alpha of the first direction (:108); SPGQPSolverC steps by alphainit / eps
+    const double a0 = p->solver_type == 2 ? (p->coeffA == 0 ? 1.0 : 1.0 / p->coeffA) * o->alphainit : o->alphainit;
+    h->alpha_prev = a0;
+    h->alpha_cur = a0;
+    h->coeffmode = p->solver_type == 2 ? 1 : 0;
     h->coeff = p->coeffA;
     h->bscale = p->coeffB;
     h->eps = o->eps;
@@ -948,7 +963,7 @@ static int mixed_iterate(pasc_gb300_problem *p, long n, int poll)
     cudaEventElapsedTime(&ms, p->ev0, p->ev1);
     p->run.time_s += ms * 1e-3;
     p->run.last_iterate_ms = ms;
-    p->run.last_iterate_launches = (int)done;
+    p->run.last_iterate_launches = (int)done * (p->graph ? 2 : 1);
     CHK(check_device_error(p));
     sync_run_from_device(p);
     if (p->run.status == PASC_SPG_RUNNING && p->run.it >= p->run.o.maxit) p->run.status = PASC_SPG_MAXIT;
@@ -1244,6 +1259,7 @@ int pasc_gb300_set_fem(pasc_gb300_problem *p, double fem_reduce, int fem_type)
         g = (long)sweep_tma_blocks_per_sm(p->K, true, true) * q->sms;
         q->grid_sweep_init[1] = (int)(g < nt_tma ? (g < 1 ? 1 : g) : nt_tma);
     }
+    q->solver_type = p->solver_type;
     p->fem_inner = q;
     fem_set_inner_coeffs(p);
     if (cudaDeviceSynchronize() != cudaSuccess) return fail(PASC_ERR_CUDA, "set_fem: initialisation failed");
@@ -1343,6 +1359,7 @@ int pasc_gb300_set_usethetainpenalty(pasc_gb300_problem *p, int on)
     if (on && p->fem_inner)
         return fail(PASC_ERR_NOTSUPP, "set_usethetainpenalty: not with a reduced (fem_reduce < 1) problem");
     if (on && p->graph) return fail(PASC_ERR_NOTSUPP, "set_usethetainpenalty: not with a graph (R > 1) problem");
+    if (on && p->solver_type == 2) return fail(PASC_ERR_NOTSUPP, "set_usethetainpenalty: not with SPGQPSolverC");
     CU(cudaSetDevice(p->device));
     CU(cudaStreamSynchronize(p->stream));
     p->run.started = false;
@@ -1428,6 +1445,29 @@ int pasc_gb300_get_graph(pasc_gb300_problem *p, long *T, long *R, long *nnz)
     if (T) *T = p->graph ? p->graph_T : p->T;
     if (R) *R = p->graph ? p->graph_R : 1;
     if (nnz) *nnz = p->graph ? p->graph_nnz : 0;
+    return PASC_OK;
+}
+
+// GraphH1FEMModel's gammasolvertype (include/general/model/graphh1fem.h:42-48, option
+// graphh1femmodel_gammasolvertype, graphh1fem.cpp:12-16, 171-191): 0 auto (= 1), 1 SPGQPSolver,
+// 2 SPGQPSolverC.  PERMON (3) and TAO (4) need libraries the reference links optionally.
+int pasc_gb300_set_gamma_solver_type(pasc_gb300_problem *p, int type)
+{
+    if (!p) return fail(PASC_ERR_ARG, "set_gamma_solver_type: NULL problem");
+    if (type < 0 || type > 4) return fail(PASC_ERR_ARG, "set_gamma_solver_type: type 0..4");
+    if (type >= 3) return fail(PASC_ERR_NOTSUPP, "set_gamma_solver_type: PERMON / TAO solvers are not provided");
+    if (type == 2 && p->tp)
+        return fail(PASC_ERR_NOTSUPP, "set_gamma_solver_type: SPGQPSolverC with theta in the penalty");
+    p->solver_type = type == 0 ? 1 : type;
+    p->run.started = false;
+    if (p->fem_inner) p->fem_inner->solver_type = p->solver_type;
+    return PASC_OK;
+}
+
+int pasc_gb300_get_gamma_solver_type(pasc_gb300_problem *p, int *type)
+{
+    if (!p || !type) return fail(PASC_ERR_ARG, "get_gamma_solver_type: NULL argument");
+    *type = p->solver_type;
     return PASC_OK;
 }
 

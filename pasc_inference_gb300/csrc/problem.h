@@ -95,6 +95,9 @@ struct pasc_gb300_problem {
     double *gpartials = nullptr;
     int grid_graph = 0;
 
+    // gamma solver: 1 = SPGQPSolver, 2 = SPGQPSolverC (coefficient factored out)
+    int solver_type = 1;
+
     // theta in the penalty (pasc_gb300_set_usethetainpenalty): block k of A is
     // coeffA * theta_k^2 * A_hat; ck64[k] = (coeffA theta_k) theta_k, kw32[k] = theta_k^2
     bool tp = false;

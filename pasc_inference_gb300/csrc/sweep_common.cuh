@@ -2,7 +2,10 @@
 // block of the grid turns the reduced sums (w[0] = sum (g-b)'x, w[1] = d'd, w[2] = sum of
 // squared neighbour differences of d, w[3] = g'd) into the reference's step-length, GLL and
 // stopping decisions (src/petscvector/solver/spgqpsolver.cpp:131-274, src/general/solver/
-// spg_fs.cpp), in FP64, and writes the scalars of the next sweep.
+// spg_fs.cpp), in FP64, and writes the scalars of the next sweep.  With st->coeffmode the rules
+// are SPGQPSolverC's (include/general/solver/spgqpsolver_coeff.h:611-835): d'Ad without the
+// coefficient eps, BB step einv*dd/dAd, A-condition with 2*eps*xi and the sigma1 clamp applied
+// to beta_hat itself; the sweeps take alpha and beta in the usual units either way.
 #pragma once
 
 #include "common.cuh"
@@ -17,7 +20,9 @@ __device__ __forceinline__ void spg_finish_sweep(SpgDevState *st, int cur, const
     st->sweeps += 1;
     const double fnew = 0.5 * w[0];
     const double dd = w[1];
-    const double dAd = 2.0 * st->coeff * w[2];
+    const bool cm = st->coeffmode != 0;
+    const double eps = st->coeff, einv = eps == 0.0 ? 1.0 : 1.0 / eps;
+    const double dAd = cm ? 2.0 * w[2] : 2.0 * st->coeff * w[2];  // the solver's own d'Ad
     const double gd = w[3];
 
     if (INIT) {
@@ -49,7 +54,8 @@ __device__ __forceinline__ void spg_finish_sweep(SpgDevState *st, int cur, const
         // two objectives summed from FP32 terms (their difference is resolved only to ~1e-7
         // of f, far above the usual eps, so the explicit form would stop on rounding noise)
         const double ddo = st->dd, dAdo = st->dAd;
-        const double dfx = st->beta * st->gd + 0.5 * st->beta * st->beta * dAdo;
+        const double dAdtrue = cm ? eps * dAdo : dAdo;
+        const double dfx = st->beta * st->gd + 0.5 * st->beta * st->beta * dAdtrue;
         if ((st->stop_difff && fabs(dfx) < st->eps) ||
             (st->stop_normgp && ddo < st->eps) ||
             (st->stop_normgp_normb && ddo < st->eps * st->normb) ||
@@ -70,10 +76,17 @@ __device__ __forceinline__ void spg_finish_sweep(SpgDevState *st, int cur, const
         for (int q = 0; q < st->m; q++) fx_max = st->fs[q] > fx_max ? st->fs[q] : fx_max;
         const double xi = (fx_max - st->fx) / dAd;
         const double beta_bar = -gd / dAd;
-        double beta_hat = st->gamma * beta_bar + sqrt(st->gamma * st->gamma * beta_bar * beta_bar + 2 * xi);
-        if (beta_hat < st->sigma1) beta_hat = st->sigma1;
-        nbeta = beta_hat < st->sigma2 ? beta_hat : st->sigma2;
-        nalpha = dd / dAd;
+        if (cm) {
+            double beta_hat = st->gamma * beta_bar + sqrt(st->gamma * st->gamma * beta_bar * beta_bar + 2 * eps * xi);
+            if (einv * beta_hat < st->sigma1) beta_hat = st->sigma1;
+            nbeta = einv * beta_hat < st->sigma2 ? einv * beta_hat : st->sigma2;
+            nalpha = einv * (dd / dAd);
+        } else {
+            double beta_hat = st->gamma * beta_bar + sqrt(st->gamma * st->gamma * beta_bar * beta_bar + 2 * xi);
+            if (beta_hat < st->sigma1) beta_hat = st->sigma1;
+            nbeta = beta_hat < st->sigma2 ? beta_hat : st->sigma2;
+            nalpha = dd / dAd;
+        }
     } else if (gd < 0.0) {
         // d'Ad = 0 with d != 0: the objective is linear along d (A_hat d = 0, e.g. T == 1).
         // The reference divides by zero here; its comparisons then fall through to

@@ -222,3 +222,32 @@ def test_image_tssolver_recovers_regions(oracle):
     labb = np.argmax(g0b.reshape(R, K), axis=1)
     accb = max(np.mean(labb == truth), np.mean(labb == 1 - truth))
     assert acc > accb
+
+
+def test_spgqp_coeff_variant(oracle):
+    """SPGQPSolverC: with the coefficient factored out the iteration differs from SPGQPSolver
+    only in the first step (alphainit / coeff instead of alphainit), the sigma1 clamp and the
+    unscaled d'Ad of the stopping tests; both reach the same minimiser."""
+    T, K = 800, 3
+    sig = datagen.signal1d(T, K, [0.0, 1.0, 2.0], 50, 200, 0.5, 9)
+    theta = np.array([0.0, 1.0, 2.0])
+    b = oracle.residual_b(sig.data, theta, T, K)
+    x0 = datagen.normalised_gamma(sig.gamma0, T, K)
+    coeff = oracle.A_coeff(30.0, T)
+    o = oracle.spg_opts(maxit=20000, eps=1e-14, m=10)
+    xa, ra, _ = oracle.spgqp_solve(b, x0, T, K, coeff, o)
+    xc, rc = oracle.spgqp_solve_coeff(b, x0, T, K, coeff, o)
+    assert rc.fx == pytest.approx(ra.fx, rel=1e-9)
+    assert np.max(np.abs(xa - xc)) < 1e-4
+    # coeff = 1: the two loops are the same loop (the first step is alphainit in both)
+    xa1, ra1, _ = oracle.spgqp_solve(b, x0, T, K, 1.0, oracle.spg_opts(maxit=50, eps=0.0, m=10))
+    xc1, rc1 = oracle.spgqp_solve_coeff(b, x0, T, K, 1.0, oracle.spg_opts(maxit=50, eps=0.0, m=10))
+    assert np.array_equal(xa1, xc1) and ra1.fx == rc1.fx
+    # on a graph
+    ptr, idx = oracle.graph_grid2d(20, 15)
+    R = 300
+    bg = -np.random.default_rng(2).random(R * K)
+    x0g = oracle.project(np.random.default_rng(3).random(R * K), R, K)
+    xg, rg = oracle.spgqp_solve_graph(bg, x0g, 1, K, 0.7, ptr, idx, oracle.spg_opts(maxit=20000, eps=1e-14, m=10))
+    xgc, rgc = oracle.spgqp_solve_coeff(bg, x0g, 1, K, 0.7, oracle.spg_opts(maxit=20000, eps=1e-14, m=10), ptr, idx)
+    assert rgc.fx == pytest.approx(rg.fx, rel=1e-9)
