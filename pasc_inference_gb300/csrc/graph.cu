@@ -286,6 +286,30 @@ const char *graph_check(long R, const int *ptr, const int *idx)
     return nullptr;
 }
 
+// true when the lists are those of BGMGraphGrid2D(W, H) with H >= 2 (node i*W + j)
+bool graph_is_grid2d(long R, const int *ptr, const int *idx, int *W, int *H)
+{
+    if (R < 4 || ptr[1] - ptr[0] < 1 || idx[ptr[0]] != 1) return false;
+    long w;
+    if (ptr[1] - ptr[0] == 2 && idx[ptr[0] + 1] >= 2) w = idx[ptr[0] + 1];
+    else return false;
+    if (R % w != 0 || R / w < 2) return false;
+    const long h = R / w;
+    long q = 0;
+    for (long id = 0; id < R; id++) {
+        const long i = id / w, j = id - i * w;
+        if (ptr[id] != q) return false;
+        if (i > 0 && idx[q++] != id - w) return false;
+        if (j > 0 && idx[q++] != id - 1) return false;
+        if (j < w - 1 && idx[q++] != id + 1) return false;
+        if (i < h - 1 && idx[q++] != id + w) return false;
+    }
+    if (ptr[R] != q || w > 2000000000L || h > 2000000000L) return false;
+    *W = (int)w;
+    *H = (int)h;
+    return true;
+}
+
 }  // namespace pasc
 
 using namespace pasc;

@@ -70,6 +70,16 @@ struct GraphSweepArgs {
     long T, R;
 };
 
+// Image mode (T = 1 on the W x H pixel grid), mixed path: the fused tile sweep (image.cu).
+struct ImageSweepArgs {
+    const float *data;        // W*H, row-major
+    const float *theta;       // K
+    float *xb0, *xb1;         // gamma, ping-pong (buffer st->cur current)
+    double *partials;         // gridDim.x * 4
+    SpgDevState *st;
+    int W, H;
+};
+
 struct ThetaArgs {
     const float *data;
     const float *xb0, *xb1;  // gamma lives in buffer st->cur
@@ -155,6 +165,12 @@ int graph_sweep_grid(long nblocks);
 cudaError_t launch_graph_sweep(int K, bool init, int grid, const GraphSweepArgs &a, cudaStream_t s);
 cudaError_t launch_graph_matmult_f64(const double *x, double *y, long T, long R, int K, double coeff,
                                      const int *ptr, const int *idx, cudaStream_t s, const double *kc = nullptr);
+
+bool graph_is_grid2d(long R, const int *ptr, const int *idx, int *W, int *H);  // host check
+size_t image_sweep_smem(int K);
+int image_sweep_blocks_per_sm(int K);  // also sets the kernels' shared-memory limit
+int image_sweep_tiles(int W, int H);
+cudaError_t launch_image_sweep(int K, bool init, int grid, const ImageSweepArgs &a, cudaStream_t s);
 
 int batch_tile_width();
 int batch_segment_timesteps();

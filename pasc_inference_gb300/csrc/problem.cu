@@ -3,6 +3,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <string.h>
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <new>
@@ -752,6 +753,18 @@ static constexpr int GRAPH_CHUNK = 16;
 
 static cudaError_t launch_variant(pasc_gb300_problem *p, int v, bool init, const SweepArgs &a)
 {
+    if (p->graph && v == 1) {
+        ImageSweepArgs g;
+        g.data = p->data32;
+        g.theta = p->theta32;
+        g.xb0 = p->xb[0];
+        g.xb1 = p->xb[1];
+        g.partials = p->gpartials;
+        g.st = p->st;
+        g.W = p->img_W;
+        g.H = p->img_H;
+        return launch_image_sweep(p->K, init, p->grid_image, g, p->stream);
+    }
     if (p->graph) {
         GraphSweepArgs g;
         g.data = p->data32;
@@ -858,7 +871,7 @@ static void fill_device_state(pasc_gb300_problem *p, SpgDevState *h)
 // without changing the solve; the faster kernel is kept for the problem's lifetime.
 static int autotune_variant(pasc_gb300_problem *p)
 {
-    if (p->graph) p->variant = 0;  // one graph sweep
+    if (p->graph && p->variant < 0) p->variant = p->img_W > 0 ? 1 : 0;  // the fused image sweep where it applies
     if (p->variant >= 0) return PASC_OK;
     if (!sweep_tma_supported(p->K)) {
         p->variant = 0;
@@ -915,7 +928,7 @@ static int mixed_start(pasc_gb300_problem *p)
     CU(cudaStreamSynchronize(s));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, p->ev0, p->ev1);
-    p->run.launches += p->graph ? 2 : 1;
+    p->run.launches += p->graph && p->variant == 0 ? 2 : 1;
     p->run.time_s += ms * 1e-3;
     CHK(check_device_error(p));
     sync_run_from_device(p);
@@ -949,7 +962,7 @@ static int mixed_iterate(pasc_gb300_problem *p, long n, int poll)
             for (long q = 0; q < want; q++) CU(launch_variant(p, p->variant, false, a));
         }
         done += want;
-        p->run.launches += (int)want * (p->graph ? 2 : 1);
+        p->run.launches += (int)want * (p->graph && p->variant == 0 ? 2 : 1);
         if (poll) {
             CU(cudaMemcpyAsync(h, p->st, sizeof(SpgDevState), cudaMemcpyDeviceToHost, s));
             CU(cudaStreamSynchronize(s));
@@ -963,7 +976,7 @@ static int mixed_iterate(pasc_gb300_problem *p, long n, int poll)
     cudaEventElapsedTime(&ms, p->ev0, p->ev1);
     p->run.time_s += ms * 1e-3;
     p->run.last_iterate_ms = ms;
-    p->run.last_iterate_launches = (int)done * (p->graph ? 2 : 1);
+    p->run.last_iterate_launches = (int)done * (p->graph && p->variant == 0 ? 2 : 1);
     CHK(check_device_error(p));
     sync_run_from_device(p);
     if (p->run.status == PASC_SPG_RUNNING && p->run.it >= p->run.o.maxit) p->run.status = PASC_SPG_MAXIT;
@@ -1212,7 +1225,8 @@ int pasc_gb300_set_sweep_variant(pasc_gb300_problem *p, int variant)
     if (variant < -1 || variant > 1) return fail(PASC_ERR_ARG, "set_sweep_variant: variant must be -1, 0 or 1");
     if (p->precision != PASC_PREC_MIXED) return fail(PASC_ERR_STATE, "set_sweep_variant: mixed precision only");
     if (variant == 1 && !sweep_tma_supported(p->K)) return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: K not supported");
-    if (variant == 1 && p->graph) return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: a graph problem has one sweep");
+    if (variant == 1 && p->graph && p->img_W == 0)
+        return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: the fused image sweep needs T = 1 on a pixel grid (H >= 2)");
     p->variant = variant;
     p->run.started = false;
     return PASC_OK;
@@ -1415,7 +1429,7 @@ int pasc_gb300_create_graph(pasc_gb300_problem **out, long T, long R, int K, int
     p->graph_T = T;
     p->graph_R = R;
     p->graph_nnz = nbr_ptr[R];
-    p->variant = 0;
+    p->variant = -1;  // the fused image sweep where it applies, else the general graph sweep
     set_coeffs(p);
     int rc;
     auto bail = [&](int code) { free_all(p); return code; };
@@ -1428,8 +1442,17 @@ int pasc_gb300_create_graph(pasc_gb300_problem **out, long T, long R, int K, int
     if (precision == PASC_PREC_MIXED) {
         const long N = p->N;
         p->grid_graph = graph_sweep_grid(T * R);
+        int W = 0, H = 0;
+        if (T == 1 && graph_is_grid2d(R, nbr_ptr, nbr_idx, &W, &H)) {
+            const int per_sm = image_sweep_blocks_per_sm(K);
+            const int tiles = image_sweep_tiles(W, H);
+            p->img_W = W;
+            p->img_H = H;
+            p->grid_image = std::max(1, std::min(tiles, per_sm * p->sms));
+        }
+        const int gp = std::max(p->grid_graph, p->grid_image);
         if ((rc = dalloc(&p->db_raw[0], N)) || (rc = dalloc(&p->db_raw[1], N)) ||
-            (rc = dalloc(&p->gpartials, (size_t)p->grid_graph * 4)))
+            (rc = dalloc(&p->gpartials, (size_t)gp * 4)))
             return bail(rc);
         cudaMemset(p->db_raw[0], 0, sizeof(float) * N);
         cudaMemset(p->db_raw[1], 0, sizeof(float) * N);

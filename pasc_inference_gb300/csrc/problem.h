@@ -94,6 +94,7 @@ struct pasc_gb300_problem {
     float *db_raw[2] = {nullptr, nullptr}; // mixed path: direction ping-pong
     double *gpartials = nullptr;
     int grid_graph = 0;
+    int img_W = 0, img_H = 0, grid_image = 0;  // T = 1 on a pixel grid: the fused image sweep
 
     // gamma solver: 1 = SPGQPSolver, 2 = SPGQPSolverC (coefficient factored out)
     int solver_type = 1;

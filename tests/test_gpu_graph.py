@@ -158,10 +158,11 @@ def _compare_ts(st, th, gam, r_o, th_o, g_o, nb, K, prec, tol_th_mixed=1e-5):
 # curvature ~3 (pi/40)^2 ~ 0.02, so the FP32 gradient noise (~1e-6: differences of FP32 gamma
 # times the coefficient) leaves the mixed fixed point ~5e-5 away along them; its theta bound is
 # 5e-5 of the scale (measured 1.8e-5), the others keep 1e-5.
-@pytest.mark.parametrize("prec", [PASC_PREC_FP64, PASC_PREC_MIXED])
+@pytest.mark.parametrize("prec,variant", [(PASC_PREC_FP64, None), (PASC_PREC_MIXED, 0), (PASC_PREC_MIXED, 1)])
 @pytest.mark.parametrize("w,h,K,eps2,tol_th_mixed", [(64, 48, 2, 1.0, 1e-5), (40, 40, 3, 1.0, 1e-5),
-                                                     (40, 40, 3, 3.0, 5e-5)])
-def test_image_tssolver_vs_oracle(gpulib, oracle, prec, w, h, K, eps2, tol_th_mixed):
+                                                     (40, 40, 3, 3.0, 5e-5), (37, 23, 2, 1.0, 1e-5)])
+def test_image_tssolver_vs_oracle(gpulib, oracle, prec, variant, w, h, K, eps2, tol_th_mixed):
+    """variant 0: the general graph sweep (two kernels); 1: the fused image tile sweep."""
     data, truth = _image(w, h, K)
     g = _grid(w, h)
     R = w * h
@@ -171,10 +172,16 @@ def test_image_tssolver_vs_oracle(gpulib, oracle, prec, w, h, K, eps2, tol_th_mi
     g_o, th_o, r_o = oracle.tssolver_solve_graph(data, g0, np.zeros(K), 1, K, eps2, g.ptr, g.idx,
                                                  ts=oracle.ts_opts(**ts_kw), spg=oracle.spg_opts(**spg_kw))
     with Problem(1, K, eps2, precision=prec, graph=g) as p:
+        if variant is not None:
+            p.set_sweep_variant(variant)
         p.set_data(data)
         p.set_gamma(g0)
         p.set_theta(np.zeros(K))
         st = p.ts_solve(capi.ts_opts(**ts_kw), capi.spgqp_opts(**spg_kw))
+        if variant is not None:
+            assert p.get_sweep_variant() == variant
+            # one launch per SPG iteration for the fused sweep, two for the general one
+            assert st.kernel_launches >= st.spg_it_sum * (1 if variant == 1 else 2)
         _compare_ts(st, p.get_theta(), p.get_gamma(), r_o, th_o, g_o, R, K, prec, tol_th_mixed)
 
 
@@ -202,9 +209,39 @@ def test_graph_series_tssolver_vs_oracle(gpulib, oracle, prec):
         _compare_ts(st, p.get_theta(), p.get_gamma(), r_o, th_o, g_o, T * R, K, prec)
 
 
+@pytest.mark.parametrize("w,h,K", [(2, 2, 1), (5, 3, 2), (33, 17, 3), (64, 48, 8), (100, 7, 5)])
+def test_image_sweep_follows_general_sweep(gpulib, w, h, K):
+    """The fused image sweep and the general graph sweep make the same iteration: a
+    fixed-length run (30 iterations) from the same start gives objectives within 1e-5 and
+    gammas within 1e-4 (FP32 sums in another order); a tiny image may stop early at an exact
+    fixed point."""
+    rng = np.random.default_rng(w * h + K)
+    g = _grid(w, h)
+    data = rng.standard_normal(w * h)
+    theta = np.linspace(-1.0, 1.0, K)
+    x0 = datagen.normalised_gamma(datagen.uniform(9, 0, w * h * K), w * h, K)
+    res = []
+    for v in (0, 1):
+        with Problem(1, K, 0.7, graph=g) as p:
+            p.set_sweep_variant(v)
+            p.set_data(data)
+            p.set_gamma(x0)
+            p.set_theta(theta)
+            p.update_b()
+            st = p.spgqp_solve(capi.spgqp_opts(maxit=30, eps=0.0, m=10))
+            res.append((st.fx, st.it, p.get_gamma(), st.status))
+    # a tiny image may reach an exact fixed point (projected step zero) a few iterations early,
+    # at an iteration that depends on rounding
+    if res[0][3] == res[1][3] == capi.PASC_SPG_MAXIT:
+        assert res[0][1] == res[1][1]
+    assert abs(res[0][0] - res[1][0]) <= 1e-5 * abs(res[0][0]) + 1e-7
+    assert np.max(np.abs(res[0][2] - res[1][2])) <= 1e-4
+
+
 def test_refusals(gpulib):
     g = _grid(4, 4)
     with Problem(2, 3, 1.0, graph=g) as p:
+        # (T = 2: the fused image sweep does not apply)
         for call in (lambda: p.set_fem(0.5, 0), lambda: p.set_usethetainpenalty(True),
                      lambda: p.set_sweep_variant(1)):
             with pytest.raises(PascError) as e:
