@@ -485,27 +485,30 @@ def measure_image(dev, peak):
     g = BGMGraphGrid2D(w, h)
     g.process_grid()
     theta = np.array([0.0, 1.0, 2.0])
-    B_it = (20.0 * K + 4.0) * R  # read x, d, data; write x, d; read d (FP32)
+    B_fused = (8.0 * K + 4.0) * R   # read x, data; write x (FP32): the fused image sweep
+    B_graph = (20.0 * K + 4.0) * R  # read x, d, data; write x, d; read d: the general graph sweep
     res = {"workload": f"image {w}x{h} (T=1, 4-neighbour grid graph), K={K}, epssqr={eps2}, disc and bar on 0, "
-                       "noise 0.4", "R": R, "K": K,
-           "bytes_per_iteration": B_it,
-           "bytes_note": "the two-kernel graph iteration moves 20K+4 bytes per pixel; a fused single pass "
-                         "would need 8K+4 (halo recomputation over a general graph is not bounded)"}
-    with Problem(1, K, eps2, precision=PASC_PREC_MIXED, device=dev, graph=g) as p:
-        p.set_data(data)
-        p.set_gamma(datagen.uniform(13, 0, R * K))
-        p.set_theta(theta)
-        p.update_b()
-        p.spgqp_start(capi.spgqp_opts(m=10, maxit=100000, stop_difff=0))
-        p.spgqp_iterate(20, poll=False)
-        p.spgqp_iterate(300, poll=False)
-        ms, nl = p.spgqp_last_iterate()
-        it_ms = ms / 300
-        ach = B_it / (it_ms * 1e-3) / 1e9
-        res["spg_iteration"] = {"it_per_s": 1e3 / it_ms, "us_per_it": it_ms * 1e3, "gpu_launches_per_it": nl / 300,
-                                "achieved": ach, "unit": "GB/s", "frac": ach / peak,
-                                "kernels": "graph_sweep_a_kernel<3,false> + graph_sweep_b_kernel<3,false>"}
-        x = p.get_gamma()
+                       "noise 0.4", "R": R, "K": K}
+    for v, name, B_it, kern in ((1, "spg_iteration", B_fused, "image_sweep_kernel<3,false>"),
+                                (0, "spg_iteration_general_graph_sweep", B_graph,
+                                 "graph_sweep_a_kernel<3,false> + graph_sweep_b_kernel<3,false>")):
+        with Problem(1, K, eps2, precision=PASC_PREC_MIXED, device=dev, graph=g) as p:
+            p.set_sweep_variant(v)
+            p.set_data(data)
+            p.set_gamma(datagen.uniform(13, 0, R * K))
+            p.set_theta(theta)
+            p.update_b()
+            p.spgqp_start(capi.spgqp_opts(m=10, maxit=100000, stop_difff=0))
+            p.spgqp_iterate(20, poll=False)
+            p.spgqp_iterate(300, poll=False)
+            ms, nl = p.spgqp_last_iterate()
+            it_ms = ms / 300
+            ach = B_it / (it_ms * 1e-3) / 1e9
+            res[name] = {"it_per_s": 1e3 / it_ms, "us_per_it": it_ms * 1e3, "gpu_launches_per_it": nl / 300,
+                         "bytes_per_iteration": B_it, "achieved": ach, "unit": "GB/s", "frac": ach / peak,
+                         "kernels": kern}
+            if v == 1:
+                x = p.get_gamma()
     # the FP64 oracle's SPG iteration on the same image (all cores)
     b = orc.residual_b(data, theta, R, K, bscale=orc.b_coeff(1))
     t0 = time.perf_counter()
