@@ -116,6 +116,13 @@ class Problem:
         check(load().pasc_gb300_get_gamma(self._h, out))
         return out
 
+    def get_gamma_into(self, out: np.ndarray) -> np.ndarray:
+        """get_gamma into a caller's array (e.g. page-locked host memory)."""
+        if out.dtype != np.float64 or out.size != self.T * self.K or not out.flags.c_contiguous:
+            raise ValueError("get_gamma_into: a contiguous float64 array of T*K values is needed")
+        check(load().pasc_gb300_get_gamma(self._h, out))
+        return out
+
     def set_theta(self, theta):
         check(load().pasc_gb300_set_theta(self._h, np.ascontiguousarray(theta, dtype=np.float64)))
 
