@@ -25,14 +25,24 @@
 
 namespace pasc {
 
+// Timesteps per thread and threads per block of the tile: 4 x 128, or for K >= 6 (whose
+// per-thread arrays of 4 timesteps need ~165 registers, 3 blocks per SM) 2 x 256; the tile is
+// 512 timesteps either way.
+template <int K>
+struct TmaShape {
+    static constexpr int R = K >= 6 ? 2 : 4;
+    static constexpr int NT = 512 / R;
+};
+
 template <int K, int NT, bool INIT, int MODE>
 __global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
 {
     constexpr bool BM = MODE == 1, TP = MODE == 2;
-    constexpr int P = NT * TMA_R;
+    constexpr int R = TmaShape<K>::R;
+    constexpr int P = NT * R;
     constexpr int W = P - 2 * TMA_HALO;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    TmaSmem<K, NT, BM> &sm = *reinterpret_cast<TmaSmem<K, NT, BM> *>(smem_raw);
+    TmaSmem<K, NT, BM, R> &sm = *reinterpret_cast<TmaSmem<K, NT, BM, R> *>(smem_raw);
 
     SpgDevState *st = a.st;
     if (st->status != PASC_SPG_RUNNING) return;  // uniform across the grid
@@ -86,8 +96,8 @@ __global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
         }
         parity ^= 1u << s;
         const int next2 = tile + 2 * (int)gridDim.x;
-        tma_tile<K, K, NT, INIT, BM, TP>(sm, s, tile * W - TMA_HALO, sc, acc,
-                                         next2 < ntiles ? next2 * W - TMA_HALO : TMA_NO_REFILL);
+        tma_tile<K, K, NT, INIT, BM, TP, R>(sm, s, tile * W - TMA_HALO, sc, acc,
+                                            next2 < ntiles ? next2 * W - TMA_HALO : TMA_NO_REFILL);
     }
 
     // block and grid reductions
@@ -114,16 +124,17 @@ static cudaError_t launch_tma_t(int grid, const SweepArgs &a, cudaStream_t s)
 {
     // the dynamic shared memory limit was raised by tma_blocks_per_sm_t at problem creation
     // (no attribute call here: launches may be inside a stream capture)
-    if (a.bmat) spg_sweep_tma_kernel<K, NT, INIT, 1><<<grid, NT, sizeof(TmaSmem<K, NT, true>), s>>>(a);
-    else if (a.kw) spg_sweep_tma_kernel<K, NT, INIT, 2><<<grid, NT, sizeof(TmaSmem<K, NT, false>), s>>>(a);
-    else spg_sweep_tma_kernel<K, NT, INIT, 0><<<grid, NT, sizeof(TmaSmem<K, NT, false>), s>>>(a);
+    constexpr int R = TmaShape<K>::R;
+    if (a.bmat) spg_sweep_tma_kernel<K, NT, INIT, 1><<<grid, NT, sizeof(TmaSmem<K, NT, true, R>), s>>>(a);
+    else if (a.kw) spg_sweep_tma_kernel<K, NT, INIT, 2><<<grid, NT, sizeof(TmaSmem<K, NT, false, R>), s>>>(a);
+    else spg_sweep_tma_kernel<K, NT, INIT, 0><<<grid, NT, sizeof(TmaSmem<K, NT, false, R>), s>>>(a);
     return cudaGetLastError();
 }
 
 template <int K, int NT, bool INIT, int MODE>
 static int tma_blocks_per_sm_mode()
 {
-    const size_t smem = sizeof(TmaSmem<K, NT, MODE == 1>);
+    const size_t smem = sizeof(TmaSmem<K, NT, MODE == 1, TmaShape<K>::R>);
     cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     int nb = 0;
@@ -142,10 +153,10 @@ static int tma_blocks_per_sm_t(bool bm, bool tp)
     return bm ? n1 : (tp ? n2 : n0);
 }
 
-constexpr int TMA_NT = 128;
+constexpr int TMA_P = 512;  // timesteps per tile, for every K (TmaShape)
 
-int sweep_tma_tile_width() { return TMA_NT * TMA_R - 2 * TMA_HALO; }
-int sweep_tma_max_tile() { return TMA_NT * TMA_R; }
+int sweep_tma_tile_width() { return TMA_P - 2 * TMA_HALO; }
+int sweep_tma_max_tile() { return TMA_P; }
 
 bool sweep_tma_supported(int K) { return K >= 1 && K <= 8; }
 
@@ -154,8 +165,8 @@ int sweep_tma_blocks_per_sm(int K, bool init, bool bmat, bool tp)
     switch (K) {
 #define PASC_CASE(KK)                                                       \
     case KK:                                                                \
-        return init ? tma_blocks_per_sm_t<KK, TMA_NT, true>(bmat, tp)       \
-                    : tma_blocks_per_sm_t<KK, TMA_NT, false>(bmat, tp);
+        return init ? tma_blocks_per_sm_t<KK, TmaShape<KK>::NT, true>(bmat, tp)       \
+                    : tma_blocks_per_sm_t<KK, TmaShape<KK>::NT, false>(bmat, tp);
         PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
         PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
 #undef PASC_CASE
@@ -168,7 +179,8 @@ cudaError_t launch_sweep_tma(int K, bool init, int grid, const SweepArgs &a, cud
     switch (K) {
 #define PASC_CASE(KK)                                                                    \
     case KK:                                                                             \
-        return init ? launch_tma_t<KK, TMA_NT, true>(grid, a, s) : launch_tma_t<KK, TMA_NT, false>(grid, a, s);
+        return init ? launch_tma_t<KK, TmaShape<KK>::NT, true>(grid, a, s)                 \
+                    : launch_tma_t<KK, TmaShape<KK>::NT, false>(grid, a, s);
         PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
         PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
 #undef PASC_CASE

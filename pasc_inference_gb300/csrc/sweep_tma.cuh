@@ -76,10 +76,11 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned int 
 }
 
 // Shared memory of a block, sized for up to KB clusters.  BM: the stages carry the tile's b
-// (P*K values, materialised for multichannel data) instead of its data values.
-template <int KB, int NT, bool BM = false>
+// (P*K values, materialised for multichannel data) instead of its data values.  R: timesteps
+// per thread (4, or 2 for large K, whose per-thread arrays would not fit the registers).
+template <int KB, int NT, bool BM = false, int R = TMA_R>
 struct TmaSmem {
-    static constexpr int P = NT * TMA_R;
+    static constexpr int P = NT * R;
     alignas(16) float x[2][P * KB];  // gamma tile, two stages (stride K for K <= KB)
     alignas(16) float dat[2][BM ? P * KB : P];  // data tile (BM: b tile), two stages
     float yl[NT * KB], yr[NT * KB];  // x^{c+1} of each thread's first / last timestep
@@ -107,10 +108,11 @@ struct TileAcc {
 };
 
 // Thread 0: bring the tile starting at timestep t0 into stage s.
-template <int K, int KB, int NT, bool BM>
-__device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM> &sm, int s, const float *xin, const float *data, int t0)
+template <int K, int KB, int NT, bool BM, int R>
+__device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM, R> &sm, int s, const float *xin, const float *data,
+                                          int t0)
 {
-    constexpr int P = NT * TMA_R;
+    constexpr int P = NT * R;
     const unsigned int bytes_x = P * K * sizeof(float), bytes_d = (BM ? P * K : P) * sizeof(float);
     mbar_expect_tx(&sm.bar[s], bytes_x + bytes_d);
     bulk_g2s(sm.x[s], xin + (long)t0 * K, bytes_x, &sm.bar[s]);
@@ -129,14 +131,14 @@ __device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM> &sm, int s, const 
 // pair.  EDGE: the tile touches t <= 0 or t >= T-1 and needs the range masks; interior tiles
 // (all but the first and last of a signal) run without them.  TP: theta in the penalty, the
 // operator of cluster k is scaled by sc.kw[k] (and so is its share of d'Ad).
-template <int K, int KB, int NT, bool INIT, bool BM, bool EDGE, bool TP = false>
-__device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM> &sm, int s, int t0, const TileScalars<K> &sc,
+template <int K, int KB, int NT, bool INIT, bool BM, bool EDGE, bool TP = false, int R = TMA_R>
+__device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s, int t0, const TileScalars<K> &sc,
                                               TileAcc &acc, int refill_t0)
 {
-    constexpr int R = TMA_R;
+    constexpr int HT = TMA_HALO / R;  // halo threads at each end of the tile
     const int i = threadIdx.x;
     const int li = i > 0 ? i - 1 : i, ri = i < NT - 1 ? i + 1 : i;  // clamped neighbours
-    const bool owner = i >= 1 && i <= NT - 2;                        // owns its 4 timesteps
+    const bool owner = i >= HT && i <= NT - 1 - HT;                  // owns its R timesteps
     const int T = sc.T;
     const int tb = t0 + i * R;  // first timestep of this thread
     const float c2 = 2.f * sc.coeff;
@@ -154,18 +156,34 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM> &sm, int s, in
         const float *bt = &sm.dat[s][i * R * K];  // BM: this thread's R*K values of b
         float dv[R];
         if (!BM) {
-            const float4 d4 = *reinterpret_cast<const float4 *>(&sm.dat[s][i * R]);
-            dv[0] = d4.x; dv[1] = d4.y; dv[2] = d4.z; dv[3] = d4.w;
+            if constexpr (R == 4) {
+                const float4 d4 = *reinterpret_cast<const float4 *>(&sm.dat[s][i * R]);
+                dv[0] = d4.x; dv[1] = d4.y; dv[2] = d4.z; dv[3] = d4.w;
+            } else {
+                const float2 d2 = *reinterpret_cast<const float2 *>(&sm.dat[s][i * R]);
+                dv[0] = d2.x; dv[1] = d2.y;
+            }
         }
-        const float4 *src = reinterpret_cast<const float4 *>(&sm.x[s][i * R * K]);
+        if constexpr ((R * K) % 4 == 0) {
+            const float4 *src = reinterpret_cast<const float4 *>(&sm.x[s][i * R * K]);
 #pragma unroll
-        for (int q = 0; q < K; q++) {
-            const float4 v = src[q];
-            const int e = 4 * q;
-            xc[(e + 0) / K][(e + 0) % K] = v.x;
-            xc[(e + 1) / K][(e + 1) % K] = v.y;
-            xc[(e + 2) / K][(e + 2) % K] = v.z;
-            xc[(e + 3) / K][(e + 3) % K] = v.w;
+            for (int q = 0; q < R * K / 4; q++) {
+                const float4 v = src[q];
+                const int e = 4 * q;
+                xc[(e + 0) / K][(e + 0) % K] = v.x;
+                xc[(e + 1) / K][(e + 1) % K] = v.y;
+                xc[(e + 2) / K][(e + 2) % K] = v.z;
+                xc[(e + 3) / K][(e + 3) % K] = v.w;
+            }
+        } else {
+            const float2 *src = reinterpret_cast<const float2 *>(&sm.x[s][i * R * K]);
+#pragma unroll
+            for (int q = 0; q < R * K / 2; q++) {
+                const float2 v = src[q];
+                const int e = 2 * q;
+                xc[(e + 0) / K][(e + 0) % K] = v.x;
+                xc[(e + 1) / K][(e + 1) % K] = v.y;
+            }
         }
 #pragma unroll
         for (int k = 0; k < K; k++) {
@@ -299,13 +317,23 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM> &sm, int s, in
             }
         }
         if (!EDGE || in[R - 1]) {
-            // all four timesteps inside: 16-byte stores (tb is a multiple of 4)
-            float4 *dst = reinterpret_cast<float4 *>(sc.xout + (long)tb * K);
+            // all R timesteps inside: 16-byte stores when R*K is a multiple of 4 (tb*K*4 bytes is
+            // then a multiple of 16: tb is a multiple of R), 8-byte stores otherwise
+            if constexpr ((R * K) % 4 == 0) {
+                float4 *dst = reinterpret_cast<float4 *>(sc.xout + (long)tb * K);
 #pragma unroll
-            for (int q = 0; q < K; q++) {
-                const int e = 4 * q;
-                dst[q] = make_float4(x1[(e + 0) / K][(e + 0) % K], x1[(e + 1) / K][(e + 1) % K],
-                                     x1[(e + 2) / K][(e + 2) % K], x1[(e + 3) / K][(e + 3) % K]);
+                for (int q = 0; q < R * K / 4; q++) {
+                    const int e = 4 * q;
+                    dst[q] = make_float4(x1[(e + 0) / K][(e + 0) % K], x1[(e + 1) / K][(e + 1) % K],
+                                         x1[(e + 2) / K][(e + 2) % K], x1[(e + 3) / K][(e + 3) % K]);
+                }
+            } else {
+                float2 *dst = reinterpret_cast<float2 *>(sc.xout + (long)tb * K);
+#pragma unroll
+                for (int q = 0; q < R * K / 2; q++) {
+                    const int e = 2 * q;
+                    dst[q] = make_float2(x1[(e + 0) / K][(e + 0) % K], x1[(e + 1) / K][(e + 1) % K]);
+                }
             }
         } else {
 #pragma unroll
@@ -319,13 +347,13 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM> &sm, int s, in
     // __syncthreads-separated phase A, so no barrier is needed here
 }
 
-template <int K, int KB, int NT, bool INIT, bool BM = false, bool TP = false>
-__device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM> &sm, int s, int t0, const TileScalars<K> &sc,
+template <int K, int KB, int NT, bool INIT, bool BM = false, bool TP = false, int R = TMA_R>
+__device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM, R> &sm, int s, int t0, const TileScalars<K> &sc,
                                          TileAcc &acc, int refill_t0)
 {
-    constexpr int P = NT * TMA_R;
-    if (t0 >= 1 && t0 + P <= sc.T - 1) tma_tile_body<K, KB, NT, INIT, BM, false, TP>(sm, s, t0, sc, acc, refill_t0);
-    else tma_tile_body<K, KB, NT, INIT, BM, true, TP>(sm, s, t0, sc, acc, refill_t0);
+    constexpr int P = NT * R;
+    if (t0 >= 1 && t0 + P <= sc.T - 1) tma_tile_body<K, KB, NT, INIT, BM, false, TP, R>(sm, s, t0, sc, acc, refill_t0);
+    else tma_tile_body<K, KB, NT, INIT, BM, true, TP, R>(sm, s, t0, sc, acc, refill_t0);
 }
 
 }  // namespace pasc
