@@ -153,7 +153,6 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
     // phase A: this thread's 4 timesteps of x^c and b, plus the neighbours' edge values
     float xc[R][K], bk[R][K], xlft[K], xrgt[K];
     {
-        const float *bt = &sm.dat[s][i * R * K];  // BM: this thread's R*K values of b
         float dv[R];
         if (!BM) {
             if constexpr (R == 4) {
@@ -190,13 +189,36 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
             xlft[k] = sm.x[s][(li * R + R - 1) * K + k];
             xrgt[k] = sm.x[s][(ri * R) * K + k];
         }
+        if (BM) {
+            // this thread's R*K values of b, in vector loads as x (scalar loads at a stride of
+            // R*K floats would hit the same banks from most lanes of a warp)
+            if constexpr ((R * K) % 4 == 0) {
+                const float4 *b4 = reinterpret_cast<const float4 *>(&sm.dat[s][i * R * K]);
+#pragma unroll
+                for (int q = 0; q < R * K / 4; q++) {
+                    const float4 v = b4[q];
+                    const int e = 4 * q;
+                    bk[(e + 0) / K][(e + 0) % K] = v.x;
+                    bk[(e + 1) / K][(e + 1) % K] = v.y;
+                    bk[(e + 2) / K][(e + 2) % K] = v.z;
+                    bk[(e + 3) / K][(e + 3) % K] = v.w;
+                }
+            } else {
+                const float2 *b2 = reinterpret_cast<const float2 *>(&sm.dat[s][i * R * K]);
+#pragma unroll
+                for (int q = 0; q < R * K / 2; q++) {
+                    const float2 v = b2[q];
+                    const int e = 2 * q;
+                    bk[(e + 0) / K][(e + 0) % K] = v.x;
+                    bk[(e + 1) / K][(e + 1) % K] = v.y;
+                }
+            }
+        }
 #pragma unroll
         for (int r = 0; r < R; r++)
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                if (BM) {
-                    bk[r][k] = bt[r * K + k];
-                } else {
+                if (!BM) {
                     const float rr = dv[r] - sc.theta[k];
                     bk[r][k] = sc.bscale * (rr * rr);
                 }
