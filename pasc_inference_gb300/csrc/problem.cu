@@ -80,9 +80,11 @@ template <typename T>
 static int dalloc(T **ptr, size_t count)
 {
     cudaError_t e = cudaMalloc((void **)ptr, sizeof(T) * (count > 0 ? count : 1));
-    if (e != cudaSuccess)
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
         return fail(PASC_ERR_ALLOC, "cudaMalloc of %zu bytes failed: %s", sizeof(T) * count,
                     cudaGetErrorString(e));
+    }
     return PASC_OK;
 }
 
@@ -1382,13 +1384,16 @@ int pasc_gb300_set_usethetainpenalty(pasc_gb300_problem *p, int on)
         cudaGraphExecDestroy(p->chunk_graph);
         p->chunk_graph = nullptr;
     }
-    p->tp = on != 0;
-    if (!p->tp) return PASC_OK;
-    if (!p->tp_ck64) {
-        int rc;
-        if ((rc = dalloc(&p->tp_ck64, p->K))) return rc;
-        if ((rc = dalloc(&p->tp_kw32, p->K))) return rc;
+    if (!on) {
+        p->tp = false;
+        return PASC_OK;
     }
+    if (!p->tp_ck64 || !p->tp_kw32) {
+        int rc;
+        if (!p->tp_ck64 && (rc = dalloc(&p->tp_ck64, p->K))) return rc;
+        if (!p->tp_kw32 && (rc = dalloc(&p->tp_kw32, p->K))) return rc;
+    }
+    p->tp = true;
     if (p->precision == PASC_PREC_MIXED) {
         // the theta-in-penalty sweeps may hold fewer blocks per SM; never more than the
         // partials buffer was sized for
