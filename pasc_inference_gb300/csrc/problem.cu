@@ -5,6 +5,9 @@
 #include <string.h>
 #include <algorithm>
 #include <chrono>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cstdio>
 #include <new>
 #include <string>
@@ -868,9 +871,30 @@ static void fill_device_state(pasc_gb300_problem *p, SpgDevState *h)
     h->cur = p->cur;
 }
 
+// Choices of the sweep kernel made by timing, shared by the problems of the process: one per
+// device, K, sweep form (data / materialised b / theta in the penalty) and power-of-two bucket
+// of T, so that a problem of a shape already timed starts without the timing runs.
+struct VariantKey {
+    int device, K, form, tbucket;
+    bool operator<(const VariantKey &o) const
+    {
+        return std::tie(device, K, form, tbucket) < std::tie(o.device, o.K, o.form, o.tbucket);
+    }
+};
+static std::mutex variant_cache_mutex;
+static std::map<VariantKey, int> variant_cache;
+
+static VariantKey variant_key(const pasc_gb300_problem *p)
+{
+    int tb = 0;
+    for (long t = p->T; t > 1; t >>= 1) tb++;
+    return VariantKey{p->device, p->K, p->bmat ? 1 : (p->tp ? 2 : 0), tb};
+}
+
 // Chooses the sweep kernel by timing.  The INIT sweep reads only buffer `cur` and the data
 // and writes the other buffer and the state, so it can be repeated with either kernel
-// without changing the solve; the faster kernel is kept for the problem's lifetime.
+// without changing the solve; the faster kernel is kept for the problem's lifetime (and for
+// later problems of the same shape).
 static int autotune_variant(pasc_gb300_problem *p)
 {
     if (p->graph && p->variant < 0) p->variant = p->img_W > 0 ? 1 : 0;  // the fused image sweep where it applies
@@ -878,6 +902,15 @@ static int autotune_variant(pasc_gb300_problem *p)
     if (!sweep_tma_supported(p->K)) {
         p->variant = 0;
         return PASC_OK;
+    }
+    const VariantKey key = variant_key(p);
+    {
+        std::lock_guard<std::mutex> g(variant_cache_mutex);
+        auto it = variant_cache.find(key);
+        if (it != variant_cache.end()) {
+            p->variant = it->second;
+            return PASC_OK;
+        }
     }
     cudaStream_t s = p->stream;
     SweepArgs a;
@@ -906,6 +939,8 @@ static int autotune_variant(pasc_gb300_problem *p)
         }
     }
     p->variant = bestv;
+    std::lock_guard<std::mutex> g(variant_cache_mutex);
+    variant_cache[key] = bestv;
     return PASC_OK;
 }
 
