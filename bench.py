@@ -576,7 +576,10 @@ def measure_adjoint(dev, peak, eps0=300.0):
         deps, dX, dth, a = p.adjoint()
         t2 = time.perf_counter()
     N = T * K
-    B_cg = 80.0 * N + 4.0 * T  # per CG iteration: apply (r, p read; p, q written; mask) + update
+    # per FP32 CG iteration of the mixed path's refinement: apply (r, p read; p, q written; mask)
+    # 16N + 4T, update (d, p, r, q read; d, r written) 24N.  The time per iteration is the whole
+    # adjoint's device time over the iterations (setup, FP64 residuals and output included).
+    B_cg = 40.0 * N + 4.0 * T
     cg_s = a.time_s / max(a.cg_it, 1)
     res.update({"loss": loss, "dloss_depssqr": deps, "solve_s": t1 - t0, "spg_it": st.it,
                 "adjoint_s": t2 - t1, "adjoint_device_s": a.time_s, "cg_it": a.cg_it,

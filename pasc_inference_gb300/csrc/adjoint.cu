@@ -14,10 +14,14 @@
 // being mistaken for free ones.  The optimality conditions on S, P(A gamma - b) = 0, differentiated at
 // a fixed active set give  P A P gamma' = -P(A' gamma - b'),  so for a loss l(gamma)
 //     l' = -lambda'(A' gamma - b'),   lambda in S solving  P A P lambda = P dl/dgamma.
-// lambda is found by conjugate gradients on S in FP64: two kernels per CG iteration (apply
-// P A P to the search direction and reduce p'q; update lambda and r and reduce r'r), the
-// scalars kept on the device (last block of each launch), launched in CUDA-graph chunks with
-// the host polling a status word in between.  The gradients then follow in one pass:
+// lambda is found by conjugate gradients on S: two kernels per CG iteration (apply P A P to the
+// search direction and reduce p'q; update lambda and r and reduce r'r), the scalars kept on
+// the device (last block of each launch), launched in CUDA-graph chunks with the host polling
+// a status word in between.  The fp64 problem runs them in FP64.  The mixed problem runs them
+// in FP32 inside FP64 iterative refinement (this part's FP64 rate, not HBM, bounds an FP64 CG
+// iteration): the FP64 residual rhs - P A P lambda is rounded to FP32, an FP32 CG reduces it
+// by 1e-4, its correction is added to the FP64 lambda, and the loop repeats until the FP64
+// residual meets cg_tol; the solution is FP64-accurate, the iterations stream FP32.  The gradients then follow in one pass:
 //     dl/d epssqr  = -(d coeff/d epssqr) * sum_tk lambda_tk (A_hat gamma)_tk
 //     dl/d x_t     =  sum_k lambda_tk * 2 bscale (x_t - theta_k)
 //     dl/d theta_k = -sum_t lambda_tk * 2 bscale (x_t - theta_k)      (through b only)
@@ -37,13 +41,21 @@ namespace pasc {
 constexpr int ADJ_NT = 256;
 constexpr int ADJ_CHUNK = 16;  // CG iterations per captured graph
 
-enum { ADJ_RUNNING = 0, ADJ_CONVERGED = 1, ADJ_MAXIT = 2, ADJ_BREAKDOWN = 4 };
+enum { ADJ_RUNNING = 0, ADJ_CONVERGED = 1, ADJ_MAXIT = 2, ADJ_BREAKDOWN = 4, ADJ_INNER_DONE = 8 };
+
+constexpr double ADJ_INNER_TOL = 1e-4;  // residual reduction of one FP32 refinement step
+constexpr int ADJ_MAX_OUTER = 20;
 
 struct AdjDevState {
     double rr, rr0, pq, alpha, beta, tol;
     double free_dims;
     int it, maxit, status, pcur;
     unsigned int counter;
+    double rr_in0;  // FP32 refinement: r'r at the start of the current inner solve
+    int outer;
+    unsigned int fall;  // clusters free at every timestep (their cluster-constant, zero-sum
+                        // vectors are the null space of P A P on S)
+    double nullc[8];    // component of lambda along that null space, per cluster
 };
 
 struct AdjointWork {
@@ -52,6 +64,8 @@ struct AdjointWork {
     double *gam = nullptr;           // N: FP64 gamma (the mixed path converts into it)
     double *gl = nullptr;            // N: dl/dgamma
     double *lam = nullptr, *r = nullptr, *pb[2] = {nullptr, nullptr}, *q = nullptr;  // N each
+    float *r32 = nullptr, *pb32[2] = {nullptr, nullptr}, *q32 = nullptr, *d32 = nullptr;  // N each (mixed)
+    cudaGraphExec_t chunk32 = nullptr;
     unsigned int *mask = nullptr;    // T: free clusters of each timestep (bit k)
     double *clean = nullptr, *dX = nullptr;  // T each
     double *partials = nullptr;      // grid * 16
@@ -68,8 +82,9 @@ void adjoint_free(AdjointWork *w)
 {
     if (!w) return;
     if (w->chunk) cudaGraphExecDestroy(w->chunk);
+    if (w->chunk32) cudaGraphExecDestroy(w->chunk32);
     void *dev[] = {w->gam, w->gl, w->lam, w->r, w->pb[0], w->pb[1], w->q, w->mask, w->clean, w->dX,
-                   w->partials, w->out, w->st, w->ticket};
+                   w->partials, w->out, w->st, w->ticket, w->r32, w->pb32[0], w->pb32[1], w->q32, w->d32};
     for (void *p : dev)
         if (p) cudaFree(p);
     if (w->out_h) cudaFreeHost(w->out_h);
@@ -174,9 +189,11 @@ __global__ void __launch_bounds__(ADJ_NT) adj_setup_kernel(const double *gam, co
                                                            double *r, double *p0, double *p1,
                                                            double *partials, AdjDevState *st)
 {
-    __shared__ double scratch[2 * (ADJ_NT / 32)];
+    __shared__ double scratch[(2 + K) * (ADJ_NT / 32)];
     const double a = 1.0 / (8.0 * coeff + fabs(bscale));
-    double v2[2] = {0.0, 0.0};
+    double v2[2 + K];
+#pragma unroll
+    for (int j = 0; j < 2 + K; j++) v2[j] = 0.0;
     for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
         const double x = data[t];
         double z[K], zs[K];
@@ -209,12 +226,18 @@ __global__ void __launch_bounds__(ADJ_NT) adj_setup_kernel(const double *gam, co
         }
         const int nf = __popc(m);
         v2[1] += nf > 1 ? (double)(nf - 1) : 0.0;
+#pragma unroll
+        for (int k = 0; k < K; k++) v2[2 + k] += (double)((m >> k) & 1u);
     }
-    double w[2];
-    if (!grid_sum<2>(v2, partials, &st->counter, scratch, w)) return;
+    double w[2 + K];
+    if (!grid_sum<2 + K>(v2, partials, &st->counter, scratch, w)) return;
     if (threadIdx.x == 0) {
         st->rr = st->rr0 = w[0];
         st->free_dims = w[1];
+        unsigned int fall = 0u;
+#pragma unroll
+        for (int k = 0; k < K; k++) fall |= (w[2 + k] == (double)T ? 1u : 0u) << k;
+        st->fall = fall;
         st->it = 0;
         st->beta = 0.0;
         st->pcur = 0;
@@ -315,6 +338,227 @@ __global__ void __launch_bounds__(ADJ_NT) adj_update_kernel(double *lam, double 
     }
 }
 
+// ---- FP32 refinement (mixed problems) ----
+
+template <int K>
+__device__ __forceinline__ void proj_free_f(float (&v)[K], unsigned int m)
+{
+    const int nf = __popc(m);
+    if (nf <= 1) {
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = 0.f;
+        return;
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; k++) s += ((m >> k) & 1u) ? v[k] : 0.f;
+    const float mean = s / (float)nf;
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = ((m >> k) & 1u) ? v[k] - mean : 0.f;
+}
+
+// FP64 residual r = rhs - P A P lambda (lambda with its neighbours), rounded into r32; the
+// correction d32 and both FP32 search directions restart at 0.  Last block: r'r, the outer
+// convergence test, and the inner solve's start.
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_residual_kernel(const unsigned int *mask, const double *lam,
+                                                              const double *rhs, float *r32, float *p0, float *p1,
+                                                              float *d32, long T, double coeff, double *partials,
+                                                              AdjDevState *st)
+{
+    __shared__ double scratch[1 * (ADJ_NT / 32)];
+    double v[1] = {0.0};
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        double y[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const double lc = lam[t * K + k];
+            double ag = 0.0;
+            if (t > 0) ag += 2.0 * (lc - lam[(t - 1) * K + k]);
+            if (t < T - 1) ag += 2.0 * (lc - lam[(t + 1) * K + k]);
+            y[k] = coeff * ag;
+        }
+        proj_free<K>(y, mask[t]);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const long i = t * K + k;
+            const double rv = rhs[i] - y[k];
+            r32[i] = (float)rv;
+            p0[i] = 0.f;
+            p1[i] = 0.f;
+            d32[i] = 0.f;
+            v[0] += rv * rv;
+        }
+    }
+    double w[1];
+    if (!grid_sum<1>(v, partials, &st->counter, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        st->rr = w[0];
+        st->rr_in0 = w[0];
+        st->beta = 0.0;
+        st->pcur = 0;
+        if (!isfinite(w[0])) st->status = ADJ_BREAKDOWN;
+        else if (w[0] <= st->tol * st->tol * st->rr0) st->status = ADJ_CONVERGED;
+        else if (st->outer >= ADJ_MAX_OUTER || st->it >= st->maxit) st->status = ADJ_MAXIT;
+        else st->status = ADJ_RUNNING;
+        st->outer += 1;
+    }
+}
+
+// FP32 form of adj_apply_kernel (p = r + beta p_old, q = P A p, p'q summed in FP64)
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_apply32_kernel(const unsigned int *mask, const float *r,
+                                                             float *pb0, float *pb1, float *q, long T, float coeff,
+                                                             double *partials, AdjDevState *st)
+{
+    __shared__ double scratch[1 * (ADJ_NT / 32)];
+    if (st->status != ADJ_RUNNING) return;  // uniform
+    const int pc = st->pcur;
+    const float beta = (float)st->beta;
+    const float *pold = pc ? pb1 : pb0;
+    float *pnew = pc ? pb0 : pb1;
+    double v[1] = {0.0};
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        float pc_[K], y[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            pc_[k] = fmaf(beta, pold[t * K + k], r[t * K + k]);
+            y[k] = 0.f;
+        }
+        if (t > 0) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float pl = fmaf(beta, pold[(t - 1) * K + k], r[(t - 1) * K + k]);
+                y[k] += 2.f * (pc_[k] - pl);
+            }
+        }
+        if (t < T - 1) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float pr = fmaf(beta, pold[(t + 1) * K + k], r[(t + 1) * K + k]);
+                y[k] += 2.f * (pc_[k] - pr);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) y[k] *= coeff;
+        proj_free_f<K>(y, mask[t]);
+        float part = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            pnew[t * K + k] = pc_[k];
+            q[t * K + k] = y[k];
+            part = fmaf(pc_[k], y[k], part);
+        }
+        v[0] += (double)part;
+    }
+    double w[1];
+    if (!grid_sum<1>(v, partials, &st->counter, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        st->pq = w[0];
+        if (w[0] > 0.0 && isfinite(w[0])) {
+            st->alpha = st->rr / w[0];
+        } else {
+            st->alpha = 0.0;
+            st->status = ADJ_BREAKDOWN;
+        }
+    }
+}
+
+// FP32 form of adj_update_kernel on the correction d32; the inner solve ends when r'r has
+// dropped by ADJ_INNER_TOL^2
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_update32_kernel(float *d, float *r, const float *pb0, const float *pb1,
+                                                              const float *q, long T, double *partials,
+                                                              AdjDevState *st)
+{
+    __shared__ double scratch[1 * (ADJ_NT / 32)];
+    if (st->status != ADJ_RUNNING) return;
+    const float alpha = (float)st->alpha;
+    const float *p = st->pcur ? pb0 : pb1;
+    double v[1] = {0.0};
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        float part = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const long i = t * K + k;
+            d[i] = fmaf(alpha, p[i], d[i]);
+            const float rn = fmaf(-alpha, q[i], r[i]);
+            r[i] = rn;
+            part = fmaf(rn, rn, part);
+        }
+        v[0] += (double)part;
+    }
+    double w[1];
+    if (!grid_sum<1>(v, partials, &st->counter, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        const double rr = w[0];
+        st->beta = rr / st->rr;
+        st->rr = rr;
+        st->it += 1;
+        st->pcur ^= 1;
+        if (!isfinite(rr)) st->status = ADJ_BREAKDOWN;
+        else if (rr <= ADJ_INNER_TOL * ADJ_INNER_TOL * st->rr_in0 || st->it >= st->maxit) st->status = ADJ_INNER_DONE;
+    }
+}
+
+// lambda = P(lambda + d32): FP64 accumulation of the FP32 correction, projected back onto S
+// (the FP32 correction leaves S by its rounding, and a component outside S would be
+// amplified by the solve of the next step)
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_accum_kernel(double *lam, const float *d, const unsigned int *mask,
+                                                           long T)
+{
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        double v[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = lam[t * K + k] + (double)d[t * K + k];
+        proj_free<K>(v, mask[t]);
+#pragma unroll
+        for (int k = 0; k < K; k++) lam[t * K + k] = v[k];
+    }
+}
+
+// The null space of P A P on S: v_tk = c_k for all t with c supported on the clusters free at
+// every timestep and summing to 0 (A_hat annihilates constants in t).  Conjugate gradients
+// from 0 stay orthogonal to it; the FP32 steps of the refinement do not quite (the rounded
+// right-hand side has a component there), and that component moves dl/dx (not dl/depssqr).
+// lambda is returned orthogonal to the null space, the minimum-norm solution.
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_nullmean_kernel(const double *lam, long T, double *partials,
+                                                              AdjDevState *st)
+{
+    __shared__ double scratch[K * (ADJ_NT / 32)];
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = 0.0;
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] += lam[t * K + k];
+    }
+    double w[K];
+    if (!grid_sum<K>(v, partials, &st->counter, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        const unsigned int f = st->fall;
+        const int nf = __popc(f);
+        double mean = 0.0;
+        for (int k = 0; k < K; k++) mean += ((f >> k) & 1u) ? w[k] / (double)T : 0.0;
+        mean = nf > 0 ? mean / nf : 0.0;
+        for (int k = 0; k < K; k++) st->nullc[k] = (nf >= 2 && ((f >> k) & 1u)) ? w[k] / (double)T - mean : 0.0;
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_nullsub_kernel(double *lam, long T, const AdjDevState *st)
+{
+    double c[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) c[k] = st->nullc[k];
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+#pragma unroll
+        for (int k = 0; k < K; k++) lam[t * K + k] -= c[k];
+    }
+}
+
 // gradients from lambda (see the head of the file).  dX may be null.
 template <int K>
 __global__ void __launch_bounds__(ADJ_NT) adj_output_kernel(const double *lam, const double *gam,
@@ -410,7 +654,10 @@ static int ensure_work(pasc_gb300_problem *p)
               dal((void **)&w->dX, sizeof(double) * T) && dal((void **)&w->partials, sizeof(double) * 16 * w->grid) &&
               dal((void **)&w->out, sizeof(double) * 16) && dal((void **)&w->st, sizeof(AdjDevState)) &&
               dal((void **)&w->ticket, sizeof(unsigned int));
-    if (ok && p->precision == PASC_PREC_MIXED) ok = dal((void **)&w->gam, sizeof(double) * N);
+    if (ok && p->precision == PASC_PREC_MIXED)
+        ok = dal((void **)&w->gam, sizeof(double) * N) && dal((void **)&w->r32, sizeof(float) * N) &&
+             dal((void **)&w->pb32[0], sizeof(float) * N) && dal((void **)&w->pb32[1], sizeof(float) * N) &&
+             dal((void **)&w->q32, sizeof(float) * N) && dal((void **)&w->d32, sizeof(float) * N);
     if (ok) ok = cudaMallocHost((void **)&w->out_h, sizeof(double) * 16) == cudaSuccess &&
                  cudaMallocHost((void **)&w->st_h, sizeof(AdjDevState)) == cudaSuccess;
     if (!ok) {
@@ -458,6 +705,67 @@ static int ensure_adj_graph(pasc_gb300_problem *p)
     if (e != cudaSuccess) {
         w->chunk = nullptr;
         return afail(PASC_ERR_CUDA, std::string("adjoint graph: ") + cudaGetErrorString(e));
+    }
+    return PASC_OK;
+}
+
+// CUDA graph of ADJ_CHUNK FP32 CG iterations (mixed problems)
+static int ensure_adj_graph32(pasc_gb300_problem *p)
+{
+    AdjointWork *w = p->adj;
+    if (w->chunk32) return PASC_OK;
+    ACU(cudaStreamSynchronize(p->stream));
+    cudaGraph_t g;
+    ACU(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    const float coeff = (float)p->coeffA;
+    for (int i = 0; i < ADJ_CHUNK; i++) {
+        PASC_ADJ_DISPATCH(p->K, {
+            adj_apply32_kernel<KK><<<w->grid, ADJ_NT, 0, p->stream>>>(w->mask, w->r32, w->pb32[0], w->pb32[1],
+                                                                      w->q32, p->T, coeff, w->partials, w->st);
+            adj_update32_kernel<KK><<<w->grid, ADJ_NT, 0, p->stream>>>(w->d32, w->r32, w->pb32[0], w->pb32[1],
+                                                                       w->q32, p->T, w->partials, w->st);
+        });
+    }
+    cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+    if (e != cudaSuccess) return afail(PASC_ERR_CUDA, std::string("adjoint capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&w->chunk32, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        w->chunk32 = nullptr;
+        return afail(PASC_ERR_CUDA, std::string("adjoint graph: ") + cudaGetErrorString(e));
+    }
+    return PASC_OK;
+}
+
+// FP32 conjugate gradients inside FP64 iterative refinement (mixed problems): w->r holds the
+// FP64 right-hand side P dl/dgamma, lambda starts at 0
+static int adj_refine(pasc_gb300_problem *p, AdjDevState *h, int *launches)
+{
+    AdjointWork *w = p->adj;
+    cudaStream_t s = p->stream;
+    auto residual = [&]() -> int {
+        PASC_ADJ_DISPATCH(p->K, (adj_residual_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(
+                                    w->mask, w->lam, w->r, w->r32, w->pb32[0], w->pb32[1], w->d32, p->T, p->coeffA,
+                                    w->partials, w->st)));
+        ACU(cudaGetLastError());
+        *launches += 1;
+        ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
+        ACU(cudaStreamSynchronize(s));
+        return PASC_OK;
+    };
+    ACHK(residual());  // lambda = 0: r32 = the right-hand side
+    while (h->status == ADJ_RUNNING) {
+        while (h->status == ADJ_RUNNING) {
+            ACU(cudaGraphLaunch(w->chunk32, s));
+            *launches += 2 * ADJ_CHUNK;
+            ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
+            ACU(cudaStreamSynchronize(s));
+        }
+        if (h->status != ADJ_INNER_DONE) break;  // breakdown
+        PASC_ADJ_DISPATCH(p->K, (adj_accum_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(w->lam, w->d32, w->mask, p->T)));
+        ACU(cudaGetLastError());
+        *launches += 1;
+        ACHK(residual());
     }
     return PASC_OK;
 }
@@ -518,7 +826,9 @@ int pasc_gb300_adjoint(pasc_gb300_problem *p, const double *dloss_dgamma, const 
     }
     const double *g = nullptr;
     ACHK(adj_gamma(p, &g));
-    ACHK(ensure_adj_graph(p));
+    const bool mixed = p->precision == PASC_PREC_MIXED;
+    if (mixed) ACHK(ensure_adj_graph32(p));
+    else ACHK(ensure_adj_graph(p));
     ACU(cudaEventRecord(p->ev0, s));
 
     AdjDevState *h = w->st_h;
@@ -534,11 +844,24 @@ int pasc_gb300_adjoint(pasc_gb300_problem *p, const double *dloss_dgamma, const 
     ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
     ACU(cudaStreamSynchronize(s));
     if (h->status == ADJ_RUNNING && o->cg_maxit == 0) h->status = ADJ_MAXIT;
-    while (h->status == ADJ_RUNNING) {
-        ACU(cudaGraphLaunch(w->chunk, s));
-        launches += 2 * ADJ_CHUNK;
-        ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
-        ACU(cudaStreamSynchronize(s));
+    if (mixed && h->status == ADJ_RUNNING) {
+        ACHK(adj_refine(p, h, &launches));
+    } else {
+        while (h->status == ADJ_RUNNING) {
+            ACU(cudaGraphLaunch(w->chunk, s));
+            launches += 2 * ADJ_CHUNK;
+            ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
+            ACU(cudaStreamSynchronize(s));
+        }
+    }
+    if (h->status != ADJ_BREAKDOWN && __builtin_popcount(h->fall) >= 2) {
+        // lambda orthogonal to the null space of P A P (see adj_nullmean_kernel)
+        PASC_ADJ_DISPATCH(p->K, {
+            adj_nullmean_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(w->lam, p->T, w->partials, w->st);
+            adj_nullsub_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(w->lam, p->T, w->st);
+        });
+        ACU(cudaGetLastError());
+        launches += 2;
     }
     const double dcoeff = p->scalef ? 1.0 / (double)p->T : 1.0;  // d coeff / d epssqr
     PASC_ADJ_DISPATCH(p->K, (adj_output_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(
