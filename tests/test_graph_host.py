@@ -102,3 +102,31 @@ def test_decomposition_layouts(oracle):
     # R > 1 without a graph: disjoint nodes (graphh1fem.cpp:30-45)
     dec2 = Decomposition(T, 5, K)
     assert dec2.get_graph().get_m() == 0 and dec2.get_graph().get_n() == 5
+
+
+def test_imagedata_layout_and_data_ops(tmp_path):
+    """ImageData reads node-major pixels (r*T + t) into the interleaved layout t*R + r; the
+    TSData preprocessing (cutdata, scaledata / unscaledata, shiftdata; tsdata.cpp:384-560) on
+    the host copy, before a model exists."""
+    from pasc_inference_gb300 import ImageData, petscio
+    T, w, h, K = 3, 4, 2, 2
+    g = BGMGraphGrid2D(w, h)
+    g.process_grid()
+    dec = Decomposition(T, g, K)
+    raw = np.arange(T * w * h, dtype=float)
+    path = str(tmp_path / "img.bin")
+    petscio.save_vec(path, raw)
+    img = ImageData(dec, path, w, h)
+    assert np.array_equal(img.get_datavector().reshape(T, w * h), raw.reshape(w * h, T).T)
+    with pytest.raises(capi.PascError):
+        ImageData(dec, raw[:-1], w, h)
+    img.cutdata(2.0, 20.0)
+    d = img.get_datavector()
+    assert d.min() == 2.0 and d.max() == 20.0
+    img.scaledata(-1.0, 1.0)
+    d = img.get_datavector()
+    assert d.min() == pytest.approx(-1.0) and d.max() == pytest.approx(1.0)
+    img.unscaledata(-1.0, 1.0)
+    assert np.allclose(img.get_datavector().reshape(T, w * h), np.clip(raw, 2, 20).reshape(w * h, T).T)
+    img.shiftdata(0.5)
+    assert img.get_datavector().min() == pytest.approx(2.5)
