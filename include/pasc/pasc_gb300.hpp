@@ -514,12 +514,22 @@ public:
     // hard assignment gamma_tk = [k = argmax] (true argmax; the reference's cutgamma seeds its
     // running maximum with the wrong entry, src/petscvector/data/tsdata.cpp:212)
     inline void cutgamma();
+    // data preprocessing (src/petscvector/data/tsdata.cpp:384-560): clamp to [a, b], shift,
+    // map [scale_min, scale_max] (default: the data's range) linearly onto [a, b] and back
+    // (theta with it); a model's copy of the data is refreshed
+    inline void cutdata(double a, double b);
+    inline void shiftdata(double a);
+    inline void scaledata(double a, double b);
+    inline void scaledata(double a, double b, double scale_min, double scale_max);
+    inline void unscaledata(double a, double b);
 
 protected:
+    inline void data_changed();
     std::vector<double> data_;
     std::shared_ptr<Decomposition> decomposition_;
     GraphH1FEMModel *model_ = nullptr;
     double aic_ = std::numeric_limits<double>::max();
+    double scale_min_ = 0.0, scale_max_ = 1.0;
 };
 
 class Signal1DData : public TSData {
@@ -617,6 +627,50 @@ inline void TSData::load_gammavector(const std::vector<double> &gamma0)
     if (!model_) throw Error(PASC_ERR_STATE, "TSData: no model");
     model_->problem().set_gamma(gamma0);
     model_->problem().permute_gamma();
+}
+inline void TSData::data_changed()
+{
+    if (model_) model_->problem().set_data(data_);
+}
+inline void TSData::cutdata(double a, double b)
+{
+    for (double &v : data_) v = v > b ? b : (v < a ? a : v);
+    data_changed();
+}
+inline void TSData::shiftdata(double a)
+{
+    for (double &v : data_) v += a;
+    data_changed();
+}
+inline void TSData::scaledata(double a, double b)
+{
+    if (data_.empty()) return;
+    const auto mm = std::minmax_element(data_.begin(), data_.end());
+    scaledata(a, b, *mm.first, *mm.second);
+}
+inline void TSData::scaledata(double a, double b, double scale_min, double scale_max)
+{
+    scale_min_ = scale_min;
+    scale_max_ = scale_max;
+    const double k = (b - a) / (scale_max - scale_min), q = a - k * scale_min;
+    for (double &v : data_) v = v * k + q;
+    data_changed();
+    if (model_) {
+        std::vector<double> th = model_->problem().get_theta();
+        for (double &t : th) t = k * t + q;
+        model_->problem().set_theta(th);
+    }
+}
+inline void TSData::unscaledata(double a, double b)
+{
+    const double k = (b - a) / (scale_max_ - scale_min_), q = a - k * scale_min_;
+    for (double &v : data_) v = (v - q) * (1.0 / k);
+    data_changed();
+    if (model_) {
+        std::vector<double> th = model_->problem().get_theta();
+        for (double &t : th) t = (t - q) / k;
+        model_->problem().set_theta(th);
+    }
 }
 inline void TSData::cutgamma()
 {

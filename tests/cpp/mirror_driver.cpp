@@ -39,6 +39,18 @@ static int host_checks(const std::string &dir)
         std::printf("R=2 nodes %d edges %d grid %d %d\n", d.get_graph()->get_n(), d.get_graph()->get_m(), grid.get_m(),
                     grid.get_m_max());
     }
+    // data preprocessing on the host copy
+    {
+        Signal1DData sd(std::vector<double>{-3.0, 0.0, 1.0, 5.0});
+        sd.cutdata(-1.0, 2.0);
+        sd.scaledata(0.0, 1.0);
+        std::printf("scaled");
+        for (double x : sd.get_datavector()) std::printf(" %.17g", x);
+        sd.unscaledata(0.0, 1.0);
+        std::printf("\nunscaled");
+        for (double x : sd.get_datavector()) std::printf(" %.17g", x);
+        std::printf("\n");
+    }
     // errors become exceptions
     try {
         Decomposition d(100, 2, 3, 2, 1);

@@ -34,6 +34,8 @@ def test_host_side_pieces(driver, tmp_path):
     u = np.array([float(v) for v in lines["uniform"].split()])
     assert np.array_equal(u, datagen.uniform(13, 0, 5))  # bit for bit
     assert lines["R=2"].split() == ["nodes", "2", "edges", "0", "grid", "17", "4"]
+    assert np.allclose([float(v) for v in lines["scaled"].split()], [0.0, 1.0 / 3, 2.0 / 3, 1.0])
+    assert np.allclose([float(v) for v in lines["unscaled"].split()], [-1.0, 0.0, 1.0, 2.0])
     assert int(lines["xdim=2"].split()[-1]) == capi.PASC_ERR_NOTSUPP
     assert int(lines["T=0"].split()[-1]) == capi.PASC_ERR_ARG
     # the file written by the C++ side is read back by the Python reader
