@@ -83,12 +83,23 @@ struct TmaSmem {
     static constexpr int P = NT * R;
     alignas(16) float x[2][P * KB];  // gamma tile, two stages (stride K for K <= KB)
     alignas(16) float dat[2][BM ? P * KB : P];  // data tile (BM: b tile), two stages
-    float yl[NT * KB], yr[NT * KB];  // x^{c+1} of each thread's first / last timestep
-    float dl[NT * KB];               // d_{c+2} of each thread's first timestep
+    // x^{c+1} of each thread's first / last timestep and d_{c+2} of its first timestep (layout:
+    // nbr_idx)
+    float yl[NT * KB], yr[NT * KB];
+    float dl[NT * KB];
     double red[4 * (NT / 32)];
     unsigned long long bar[2];
     int job;                          // batched kernel: the work item this block took
 };
+
+// Slot of cluster k of thread i in the neighbour arrays yl, yr, dl.  Thread-major (i*K + k)
+// for odd K, whose stride meets every bank once per 32 threads; cluster-major (k*NT + i) for
+// even K >= 4, where a stride of K floats would put 2-8 lanes of a warp on one bank.
+template <int K, int NT>
+__device__ __forceinline__ int nbr_idx(int i, int k)
+{
+    return (K % 2 == 0 && K >= 4) ? k * NT + i : i * K + k;
+}
 
 // Scalars of one signal's sweep.
 template <int K>
@@ -184,10 +195,31 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
                 xc[(e + 1) / K][(e + 1) % K] = v.y;
             }
         }
+        // the neighbours' edge rows: vector loads for K = 4, 6, 8 (rows 16 or 8 bytes aligned),
+        // which also spread a warp's loads over more banks (the rows lie R*K floats apart)
+        const float *nl = &sm.x[s][(li * R + R - 1) * K], *nr = &sm.x[s][(ri * R) * K];
+        if constexpr (K % 4 == 0) {
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            xlft[k] = sm.x[s][(li * R + R - 1) * K + k];
-            xrgt[k] = sm.x[s][(ri * R) * K + k];
+            for (int q = 0; q < K / 4; q++) {
+                const float4 a = reinterpret_cast<const float4 *>(nl)[q];
+                const float4 c = reinterpret_cast<const float4 *>(nr)[q];
+                xlft[4 * q] = a.x; xlft[4 * q + 1] = a.y; xlft[4 * q + 2] = a.z; xlft[4 * q + 3] = a.w;
+                xrgt[4 * q] = c.x; xrgt[4 * q + 1] = c.y; xrgt[4 * q + 2] = c.z; xrgt[4 * q + 3] = c.w;
+            }
+        } else if constexpr (K % 2 == 0 && K >= 4) {
+#pragma unroll
+            for (int q = 0; q < K / 2; q++) {
+                const float2 a = reinterpret_cast<const float2 *>(nl)[q];
+                const float2 c = reinterpret_cast<const float2 *>(nr)[q];
+                xlft[2 * q] = a.x; xlft[2 * q + 1] = a.y;
+                xrgt[2 * q] = c.x; xrgt[2 * q + 1] = c.y;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                xlft[k] = nl[k];
+                xrgt[k] = nr[k];
+            }
         }
         if (BM) {
             // this thread's R*K values of b, in vector loads as x (scalar loads at a stride of
@@ -280,8 +312,8 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
     }
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        sm.yl[i * K + k] = x1[0][k];
-        sm.yr[i * K + k] = x1[R - 1][k];
+        sm.yl[nbr_idx<K, NT>(i, k)] = x1[0][k];
+        sm.yr[nbr_idx<K, NT>(i, k)] = x1[R - 1][k];
     }
     __syncthreads();
 
@@ -298,10 +330,10 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
 #pragma unroll
         for (int k = 0; k < K; k++) {
             float E[R + 1];
-            E[0] = x1[0][k] - sm.yr[li * K + k];
+            E[0] = x1[0][k] - sm.yr[nbr_idx<K, NT>(li, k)];
 #pragma unroll
             for (int r = 1; r < R; r++) E[r] = x1[r][k] - x1[r - 1][k];
-            E[R] = sm.yl[ri * K + k] - x1[R - 1][k];
+            E[R] = sm.yl[nbr_idx<K, NT>(ri, k)] - x1[R - 1][k];
 #pragma unroll
             for (int j = 0; j <= R; j++) E[j] = dm[j] ? E[j] : 0.f;
 #pragma unroll
@@ -321,14 +353,14 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
         }
     }
 #pragma unroll
-    for (int k = 0; k < K; k++) sm.dl[i * K + k] = d1[0][k];
+    for (int k = 0; k < K; k++) sm.dl[nbr_idx<K, NT>(i, k)] = d1[0][k];
     __syncthreads();
 
     // phase D: dots of d_{c+2} and the store of x^{c+1}
     if (owner) {
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const float dnext = sm.dl[ri * K + k];
+            const float dnext = sm.dl[nbr_idx<K, NT>(ri, k)];
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 acc.dd = fmaf(d1[r][k], d1[r][k], acc.dd);
