@@ -169,8 +169,20 @@ __global__ void __launch_bounds__(128, 1) mc_residual_tc_kernel(const __grid_con
     unsigned int ph_full = 0u, ph_mma = 0u;
     int err = 0;
     int j = 0;
+    // ||X_t||^2 of this thread's timestep is loaded one tile ahead, so that its HBM latency
+    // overlaps the current tile's MMAs and epilogue
+    float xn_next = 0.f;
+    {
+        const long t = (long)blockIdx.x * MC_TILE + tid;
+        if (blockIdx.x < ntiles && t < a.T) xn_next = a.xnorm[t];
+    }
     for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, j++) {
         const int s = j % S;
+        const float xn = xn_next;
+        {
+            const long t = (tile + gridDim.x) * MC_TILE + tid;
+            xn_next = t < a.T ? a.xnorm[t] : 0.f;
+        }
         bool ok = true;
         if (tid == 0) {
             ok = mbar_wait(&full[s], (ph_full >> s) & 1u);
@@ -212,7 +224,6 @@ __global__ void __launch_bounds__(128, 1) mc_residual_tc_kernel(const __grid_con
         tmem_load_32cols(tmem + ((unsigned int)(32 * warp) << 16), d);
         const long t = tile * MC_TILE + tid;
         if (t < a.T) {
-            const float xn = a.xnorm[t];
             float out[K];
 #pragma unroll
             for (int k = 0; k < K; k++) {
@@ -220,8 +231,15 @@ __global__ void __launch_bounds__(128, 1) mc_residual_tc_kernel(const __grid_con
                 out[k] = bscale * ((xn - 2.f * R) + tn[k]);
             }
             float *dst = a.bmat + t * K;
+            if constexpr (K % 4 == 0) {
+                // rows of K floats start 16-byte aligned
 #pragma unroll
-            for (int k = 0; k < K; k++) dst[k] = out[k];
+                for (int q = 0; q < K / 4; q++)
+                    reinterpret_cast<float4 *>(dst)[q] = make_float4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < K; k++) dst[k] = out[k];
+            }
         }
         tc_fence_before();
         __syncthreads();  // tensor memory is rewritten by the next tile's MMAs
