@@ -21,7 +21,8 @@ Besides the headline line it measures, on rank 0:
   roofline   the sweep kernel's algorithmic bytes (8*K*T + 4*T per iteration: gamma read and
              written in FP32, the data read once) over its CUDA-event time, against the
              measured HBM copy bandwidth.
-  cpu_baseline  the FP64 CPU oracle (a port of the reference's CPU path) on all host cores.
+  cpu_baseline  the FP64 CPU oracle (a port of the reference's CPU path) on all host cores, and
+             on one (`one_thread`).
   batched    the 256-signal uneven workload (T log-uniform in [1e3, 1e6], K in 2..5, epssqr
              log-uniform in [1, 1000]): every signal's TSSolver (SPG eps 1e-6, m 10; outer loop
              to 1e-6 relative change of L) solved by one batch handle (one launch per SPG
@@ -330,9 +331,12 @@ def main():
         result["image"] = measure_image(dev, peak)
     if info.rank == 0 and not args.no_cpu:
         rate, dt = oracle_iter_rate(sig, theta, args.eps2, T, 5, 0)
+        rate1, dt1 = oracle_iter_rate(sig, theta, args.eps2, T, 2, 1)
         result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
                                   "sample": f"5 SPG iterations of the FP64 oracle on the full T={T} "
-                                            f"signal ({dt:.1f} s, OpenMP)"}
+                                            f"signal ({dt:.1f} s, OpenMP)",
+                                  "one_thread": {"value": rate1, "unit": UNIT, "cores": 1,
+                                                 "sample": f"2 SPG iterations, same signal ({dt1:.1f} s)"}}
     if info.rank == 0:
         print(json.dumps(result), flush=True)
     dist.finalize(info)
