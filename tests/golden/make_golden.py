@@ -13,7 +13,7 @@ against host-array shims) and records inputs and outputs of:
              - the reference's test vectors Matlab/signal1D_scalability/tests/small_data.bin
                and small_gamma0.bin (T=1000, K=2; gamma0 used as the set_random values),
              - the first 2000 samples of examples/test_signal1D/data/samplesignal.bin,
-             - the synthetic configs[0]-style signal of pasc_inference_gb300.datagen.
+             - the synthetic T = 1e4, K = 2 signal (levels {1, 2}) of pasc_inference_gb300.datagen.
 The fixtures let the CPU tests pin the oracle to the reference without the reference tree.
 """
 from __future__ import annotations

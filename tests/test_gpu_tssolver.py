@@ -110,7 +110,8 @@ def _tight_case(oracle, name, g, eps2, prec, tol_L, tol_th, min_agree):
 
 def test_mirror_classes_cfg0(gpulib, oracle):
     """The reference-style object graph (Decomposition, Signal1DData, GraphH1FEMModel, TSSolver)
-    on the configs[0] workload, against the oracle's full TSSolver."""
+    on the plain-method workload (T = 1e4, K = 2, levels {1, 2}, noise 1.0, epssqr 10), against
+    the oracle's full TSSolver."""
     sig = datagen.signal1d_cfg0()
     T, K = sig.T, sig.K
     mydata = Signal1DData(sig.data)

@@ -9,7 +9,7 @@
 3. SPG-QP on tiny problems against the optimality conditions of the QP over a product of
    simplices and against a general-purpose solver (SLSQP);
 4. TSSolver on the golden fixtures (the reference's small_data test vector, the first 2000
-   samples of its samplesignal, a configs[0]-style signal): L never increases along the outer
+   samples of its samplesignal, a synthetic T = 1e4 signal with levels {1, 2}): L never increases along the outer
    loop, and where the signal has levels {1, 2} theta ends near them."""
 import numpy as np
 import pytest
