@@ -5,6 +5,7 @@ import ctypes as C
 import os
 import re
 import subprocess
+import sys
 
 import pytest
 
@@ -75,3 +76,43 @@ def test_no_device_is_reported_not_crashed(lib):
     rc = lib.pasc_gb300_create(C.byref(h), 100, 3, 1, 1, 1.0, 0)
     assert rc == capi.PASC_ERR_CUDA
     assert b"no CUDA device" in lib.pasc_gb300_last_error()
+
+
+NULL_SWEEP = r"""
+import ctypes as C, sys
+sys.path.insert(0, sys.argv[1])
+from pasc_inference_gb300 import capi
+L = C.CDLL(capi.LIB_PATH)
+for name, (res, args) in capi.PROTOTYPES.items():
+    creator = name in ("pasc_gb300_create", "pasc_gb300_create_graph", "pasc_gb300_batch_create")
+    if not args or (args[0] is not capi._h and not creator):
+        continue
+    fn = getattr(L, name)
+    fn.restype = C.c_int
+    conv, vals = [], []
+    for a in args:
+        if a in (C.c_int, C.c_long, C.c_double, C.c_float):
+            conv.append(a)
+            vals.append(1 if creator else 0)
+        else:
+            conv.append(C.c_void_p)
+            vals.append(None)
+    fn.argtypes = conv
+    print(name, fn(*vals), flush=True)
+"""
+
+
+def test_null_handles_and_pointers_are_refused(lib):
+    """Every entry point that takes a handle or device pointer first, called with NULL for it
+    and NULL / 0 for everything else, returns an error code (destroy: OK) instead of crashing;
+    the constructors refuse a NULL output pointer.  Run in a child process so that a crash
+    fails this test and not the session."""
+    r = subprocess.run([sys.executable, "-c", NULL_SWEEP, ROOT], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    rcs = dict(line.rsplit(" ", 1) for line in r.stdout.split("\n") if line.strip())
+    assert len(rcs) >= 50, rcs
+    for name, rc in rcs.items():
+        if name in ("pasc_gb300_destroy", "pasc_gb300_batch_destroy"):
+            assert int(rc) == capi.PASC_OK, name
+        else:
+            assert int(rc) == capi.PASC_ERR_ARG, (name, rc)
