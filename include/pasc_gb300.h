@@ -42,7 +42,7 @@ enum pasc_gb300_error {
     PASC_ERR_CUDA = 2,      /* a CUDA runtime call failed */
     PASC_ERR_ALLOC = 3,     /* device or host allocation failed */
     PASC_ERR_STATE = 4,     /* call not valid in the handle's current state */
-    PASC_ERR_NOTSUPP = 5,   /* configuration not supported by this build */
+    PASC_ERR_NOTSUPP = 5,   /* configuration not supported by the library */
     PASC_ERR_TIMEOUT = 6    /* a bounded device wait gave up */
 };
 

@@ -1,6 +1,6 @@
 """Multi-process helpers for runs launched one rank per GPU (torchrun / torch.distributed.run).
 
-The FEM-H1 SPG path does not shard in this build: N GPUs run N independent replicas of the
+The FEM-H1 SPG path does not shard in this library: N GPUs run N independent replicas of the
 workload ("replicas only").  Ranks exchange nothing on the data path; these helpers only
 synchronise the timed region (barrier) and combine timings (max over ranks) on the host with
 the gloo backend, so no GPU collective is ever issued."""
