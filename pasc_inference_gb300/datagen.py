@@ -141,10 +141,22 @@ class BatchInstance:
     gamma0: np.ndarray
 
 
-def batched(n: int = 256, seed: int = 3, tmin: int = 1000, tmax: int = 1_000_000) -> list[BatchInstance]:
+def batched_lengths(n: int = 256, seed: int = 3, tmin: int = 1000, tmax: int = 1_000_000) -> list[int]:
+    """T of each signal of `batched` with the same arguments, without generating the signals."""
+    u = uniform(seed, 100, 6 * n).reshape(n, 6)
+    return [int(round(np.exp(np.log(tmin) + u[i, 0] * (np.log(tmax) - np.log(tmin))))) for i in range(n)]
+
+
+def batched(n: int = 256, seed: int = 3, tmin: int = 1000, tmax: int = 1_000_000,
+            indices=None) -> list[BatchInstance]:
+    """The uneven batch: n signals with T log-uniform in [tmin, tmax], K uniform in 2..5,
+    epssqr log-uniform in [1, 1000], sorted levels U[0, 4], segments U[T/50, T/5], noise
+    U[0.2, 1].  `indices` selects which signals to generate (all of them, in order, by default);
+    signal i is the same whichever others are generated."""
     u = uniform(seed, 100, 6 * n).reshape(n, 6)
     out = []
-    for i in range(n):
+    for i in (range(n) if indices is None else indices):
+        i = int(i)
         T = int(round(np.exp(np.log(tmin) + u[i, 0] * (np.log(tmax) - np.log(tmin)))))
         K = 2 + min(int(u[i, 1] * 4), 3)
         eps = float(np.exp(u[i, 2] * np.log(1000.0)))
