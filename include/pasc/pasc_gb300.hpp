@@ -162,6 +162,15 @@ public:
     }
     void permute_gamma() { check(pasc_gb300_permute_gamma(h_.get())); }
     void set_fem(double fem_reduce, int fem_type) { check(pasc_gb300_set_fem(h_.get(), fem_reduce, fem_type)); }
+    // timesteps of the gamma QP (ceil(T*fem_reduce) under FEM coarsening, else T)
+    long get_T_reduced() const
+    {
+        double r;
+        int t;
+        long T2;
+        check(pasc_gb300_get_fem(h_.get(), &r, &t, &T2));
+        return T2;
+    }
     // -1: chosen by timing at the first solve; 0: one timestep per thread; 1: bulk-copy tiles
     void set_sweep_variant(int v) { check(pasc_gb300_set_sweep_variant(h_.get(), v)); }
     int get_sweep_variant() const
@@ -576,7 +585,7 @@ public:
     GraphH1FEMModel(TSData &tsdata, double epssqr, const Fem *fem = nullptr, bool usethetainpenalty = false,
                     int precision = PASC_PREC_MIXED, uint64_t seed = 13, int device = 0)
         : tsdata_(tsdata), epssqr_(epssqr), usethetainpenalty_(usethetainpenalty),
-          problem_(make_problem(tsdata, epssqr, precision, device))
+          fem_reduce_(fem ? fem->get_fem_reduce() : 1.0), problem_(make_problem(tsdata, epssqr, precision, device))
     {
         const long T = tsdata.get_T() * tsdata.get_R();  // blocks of K
         const int K = tsdata.get_K();
@@ -596,6 +605,20 @@ public:
     double get_aic(double L) const { return 2.0 * std::log(L) + tsdata_.get_K(); }
     bool get_usethetainpenalty() const { return usethetainpenalty_; }
     std::string get_name() const { return "Graph-H1-FEM Time-Series Model"; }
+    // GraphH1FEMModel::get_T / get_T_reduced / get_fem_reduce (graphh1fem.h:456-468)
+    long get_T() const { return tsdata_.get_T(); }
+    long get_T_reduced() const { return fem_reduce_ < 1.0 ? problem_.get_T_reduced() : tsdata_.get_T(); }
+    double get_fem_reduce() const { return fem_reduce_; }
+    const BGMGraph *get_graph() const { return tsdata_.get_decomposition().get_graph(); }
+    // GraphH1FEMModel::get_L: the gamma QP's objective at the current gamma and theta
+    // (graphh1fem.h:366-370)
+    double get_L() const { return problem_.get_fx(); }
+    // GraphH1FEMModel::get_linear_quadratic sets both terms to 0 (graphh1fem.h:373-377)
+    void get_linear_quadratic(double *linearL, double *quadraticL) const
+    {
+        *linearL = 0.0;
+        *quadraticL = 0.0;
+    }
     Problem &problem() { return problem_; }
     const Problem &problem() const { return problem_; }
 
@@ -609,6 +632,7 @@ private:
     TSData &tsdata_;
     double epssqr_;
     bool usethetainpenalty_;
+    double fem_reduce_;
     Problem problem_;
 };
 

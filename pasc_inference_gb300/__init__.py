@@ -731,6 +731,35 @@ class GraphH1FEMModel:
     def get_name(self):
         return "Graph-H1-FEM Time-Series Model"
 
+    def get_epssqr(self) -> float:
+        return self.epssqr
+
+    def get_T(self) -> int:
+        """Timesteps of the data (GraphH1FEMModel::get_T, graphh1fem.h:461-463)."""
+        return self.tsdata.get_T()
+
+    def get_T_reduced(self) -> int:
+        """Timesteps of the gamma QP: ceil(T*fem_reduce) under FEM coarsening, else T
+        (graphh1fem.h:456-458)."""
+        return self.problem.get_fem()[2] if self.fem.is_reduced() else self.tsdata.get_T()
+
+    def get_fem_reduce(self) -> float:
+        return self.fem.fem_reduce
+
+    def get_graph(self):
+        """The decomposition's graph (None for a 1-D signal)."""
+        d = self.tsdata.decomposition
+        return d.get_graph() if hasattr(d, "get_graph") else None
+
+    def get_L(self, gammasolver=None, thetasolver=None) -> float:
+        """The gamma QP's objective at the current gamma and theta (GraphH1FEMModel::get_L
+        returns the gamma solver's fx, graphh1fem.h:366-370)."""
+        return self.problem.get_fx()
+
+    def get_linear_quadratic(self, gammasolver=None, thetasolver=None):
+        """(0, 0), as GraphH1FEMModel::get_linear_quadratic sets both (graphh1fem.h:373-377)."""
+        return 0.0, 0.0
+
 
 class SPGQPSolver:
     """SPGQPSolver<VectorBase> on the model's QP (gamma step)."""

@@ -110,3 +110,34 @@ def test_replica_timing_two_gloo_ranks(tmp_path):
     import json
     res = [json.loads(o.strip().splitlines()[-1]) for o, _ in outs]
     assert all(r["ws"] == 2 and r["max"] == 11.0 and r["sum"] == 2.0 for r in res)
+
+
+def test_model_getters_wiring(monkeypatch):
+    """GraphH1FEMModel's reference getters (get_T, get_T_reduced, get_fem_reduce, get_L,
+    get_linear_quadratic, get_graph, get_epssqr) over a stand-in for the GPU problem."""
+    import pasc_inference_gb300 as P
+
+    class FakeProblem:
+        def __init__(self, T, K, epssqr, precision=None, xdim=1, device=0, graph=None):
+            self.T, self.K, self.R = T, K, 1
+            self.calls = []
+
+        def __getattr__(self, name):
+            return lambda *a, **k: self.calls.append(name)
+
+        def get_fem(self):
+            return 0.25, 0, 250
+
+        def get_fx(self):
+            return -1.5
+
+    monkeypatch.setattr(P, "Problem", FakeProblem)
+    data = P.Signal1DData(np.linspace(0.0, 1.0, 1000))
+    data.set_decomposition(P.Decomposition(1000, 1, 3, 1, 1))
+    m = P.GraphH1FEMModel(data, 7.0, fem=P.Fem(0.25))
+    assert (m.get_T(), m.get_T_reduced(), m.get_fem_reduce(), m.get_epssqr()) == (1000, 250, 0.25, 7.0)
+    assert m.get_L() == -1.5 and m.get_linear_quadratic() == (0.0, 0.0)
+    assert m.get_graph() is None  # a 1-D signal has no graph
+    assert "set_fem" in m.problem.calls
+    m2 = P.GraphH1FEMModel(data, 7.0)
+    assert m2.get_T_reduced() == 1000 and m2.get_fem_reduce() == 1.0
