@@ -54,6 +54,16 @@ def ts_opts_from(options: dict | None) -> TsOpts:
     return o
 
 
+def _vec(a, n: int, what: str) -> np.ndarray:
+    """a as a contiguous array of exactly n float64 values: the ABI reads n values from the
+    pointer it gets, so a shorter array is refused here (PASC_ERR_ARG) instead of being read
+    past its end."""
+    v = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+    if v.size != n:
+        raise PascError(capi.PASC_ERR_ARG, f"{what}: {n} values expected, got {v.size}")
+    return v
+
+
 class Problem:
     """One FEM-H1 problem on one GPU (a pasc_gb300_problem handle)."""
 
@@ -106,10 +116,10 @@ class Problem:
         check(load().pasc_gb300_set_epssqr(self._h, float(epssqr), 1 if scalef else 0))
 
     def set_data(self, data):
-        check(load().pasc_gb300_set_data(self._h, np.ascontiguousarray(data, dtype=np.float64)))
+        check(load().pasc_gb300_set_data(self._h, _vec(data, self.T * self.xdim, "set_data")))
 
     def set_gamma(self, gamma):
-        check(load().pasc_gb300_set_gamma(self._h, np.ascontiguousarray(gamma, dtype=np.float64)))
+        check(load().pasc_gb300_set_gamma(self._h, _vec(gamma, self.T * self.K, "set_gamma")))
 
     def get_gamma(self) -> np.ndarray:
         out = np.empty(self.T * self.K)
@@ -124,7 +134,7 @@ class Problem:
         return out
 
     def set_theta(self, theta):
-        check(load().pasc_gb300_set_theta(self._h, np.ascontiguousarray(theta, dtype=np.float64)))
+        check(load().pasc_gb300_set_theta(self._h, _vec(theta, self.K * self.xdim, "set_theta")))
 
     def get_theta(self) -> np.ndarray:
         out = np.empty(self.K * self.xdim)
@@ -234,7 +244,7 @@ class Problem:
         st = TsStats()
         gr = None
         if gamma_restart is not None:
-            gr = np.ascontiguousarray(gamma_restart, dtype=np.float64)
+            gr = _vec(gamma_restart, self.T * self.K, "ts_solve gamma_restart")
         check(load().pasc_gb300_ts_solve(self._h, C.byref(ts or capi.ts_opts()),
                                          C.byref(spg or capi.spgqp_opts()),
                                          gr.ctypes.data if gr is not None else None, C.byref(st)))
@@ -243,7 +253,7 @@ class Problem:
     def abserr_reconstructed(self, solution) -> float:
         v = C.c_double()
         check(load().pasc_gb300_abserr_reconstructed(
-            self._h, np.ascontiguousarray(solution, dtype=np.float64), C.byref(v)))
+            self._h, _vec(solution, self.T, "abserr_reconstructed"), C.byref(v)))
         return v.value
 
     def argmax_labels(self) -> np.ndarray:
@@ -254,7 +264,7 @@ class Problem:
     # derivatives through the converged gamma step
     def recon_mse(self, clean) -> float:
         v = C.c_double()
-        check(load().pasc_gb300_recon_mse(self._h, np.ascontiguousarray(clean, dtype=np.float64), C.byref(v)))
+        check(load().pasc_gb300_recon_mse(self._h, _vec(clean, self.T, "recon_mse"), C.byref(v)))
         return v.value
 
     def adjoint(self, dloss_dgamma=None, opts: capi.AdjointOpts | None = None):
@@ -263,7 +273,7 @@ class Problem:
         ddata = np.empty(self.T)
         dtheta = np.empty(self.K)
         st = capi.AdjointStats()
-        g = None if dloss_dgamma is None else np.ascontiguousarray(dloss_dgamma, dtype=np.float64)
+        g = None if dloss_dgamma is None else _vec(dloss_dgamma, self.T * self.K, "adjoint dloss_dgamma")
         check(load().pasc_gb300_adjoint(self._h, g.ctypes.data if g is not None else None,
                                         C.byref(opts or capi.adjoint_opts()), C.byref(deps),
                                         ddata.ctypes.data, dtheta.ctypes.data, C.byref(st)))
@@ -302,11 +312,20 @@ class Batch:
     def __exit__(self, *a):
         self.close()
 
+    def _vec(self, i, a, what: int, name: str):
+        """Signal i's array checked against its size (what: 1 data T_i, 2 gamma T_i*K_i, 3 theta
+        K_i); an index outside the batch is left to the ABI, which refuses it."""
+        i = int(i)
+        if not 0 <= i < self.n:
+            return np.ascontiguousarray(a, dtype=np.float64)
+        T, K = int(self.T[i]), int(self.K[i])
+        return _vec(a, {1: T, 2: T * K, 3: K}[what], name)
+
     def set_data(self, i: int, data):
-        check(load().pasc_gb300_batch_set_data(self._h, int(i), np.ascontiguousarray(data, dtype=np.float64)))
+        check(load().pasc_gb300_batch_set_data(self._h, int(i), self._vec(i, data, 1, "batch_set_data")))
 
     def set_gamma(self, i: int, gamma):
-        check(load().pasc_gb300_batch_set_gamma(self._h, int(i), np.ascontiguousarray(gamma, dtype=np.float64)))
+        check(load().pasc_gb300_batch_set_gamma(self._h, int(i), self._vec(i, gamma, 2, "batch_set_gamma")))
 
     def get_gamma(self, i: int) -> np.ndarray:
         out = np.empty(int(self.T[i]) * int(self.K[i]))
@@ -314,7 +333,7 @@ class Batch:
         return out
 
     def set_theta(self, i: int, theta):
-        check(load().pasc_gb300_batch_set_theta(self._h, int(i), np.ascontiguousarray(theta, dtype=np.float64)))
+        check(load().pasc_gb300_batch_set_theta(self._h, int(i), self._vec(i, theta, 3, "batch_set_theta")))
 
     def get_theta(self, i: int) -> np.ndarray:
         out = np.empty(int(self.K[i]))

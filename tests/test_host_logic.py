@@ -141,3 +141,34 @@ def test_model_getters_wiring(monkeypatch):
     assert "set_fem" in m.problem.calls
     m2 = P.GraphH1FEMModel(data, 7.0)
     assert m2.get_T_reduced() == 1000 and m2.get_fem_reduce() == 1.0
+
+
+def test_vector_sizes_are_checked_before_the_abi():
+    """The Python mirror refuses arrays whose size is not the one the ABI will read
+    (PASC_ERR_ARG), and hands through the caller's array without a copy when it fits
+    (page-locked buffers stay page-locked)."""
+    import pasc_inference_gb300 as P
+    from pasc_inference_gb300 import capi
+    p = object.__new__(P.Problem)
+    p._h, p.T, p.K, p.xdim = None, 10, 3, 1
+    for call, n in ((p.set_data, 10), (p.set_gamma, 30), (p.set_theta, 3), (p.recon_mse, 10),
+                    (p.abserr_reconstructed, 10)):
+        with pytest.raises(capi.PascError) as e:
+            call(np.zeros(n + 1))
+        assert e.value.code == capi.PASC_ERR_ARG and "values expected" in str(e.value)
+        with pytest.raises(capi.PascError) as e:  # right size: reaches the ABI, which refuses the NULL handle
+            call(np.zeros(n))
+        assert "values expected" not in str(e.value)
+    x = np.arange(30.0)
+    assert np.shares_memory(P._vec(x, 30, "x"), x)
+    b = object.__new__(P.Batch)
+    b._h, b.n, b.T, b.K = None, 2, np.array([5, 7]), np.array([2, 3], dtype=np.int32)
+    with pytest.raises(capi.PascError) as e:
+        b.set_gamma(1, np.zeros(14))
+    assert "values expected" in str(e.value)
+    with pytest.raises(capi.PascError) as e:
+        b.set_gamma(1, np.zeros(21))
+    assert "values expected" not in str(e.value)
+    with pytest.raises(capi.PascError) as e:  # an index outside the batch is the ABI's to refuse
+        b.set_theta(-1, np.zeros(3))
+    assert "values expected" not in str(e.value)
