@@ -55,11 +55,11 @@ def ts_opts_from(options: dict | None) -> TsOpts:
 
 
 def _vec(a, n: int, what: str) -> np.ndarray:
-    """a as a contiguous array of exactly n float64 values: the ABI reads n values from the
+    """a as a contiguous float64 array of at least n values: the ABI reads n values from the
     pointer it gets, so a shorter array is refused here (PASC_ERR_ARG) instead of being read
-    past its end."""
+    past its end (of a longer one the first n values are used)."""
     v = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
-    if v.size != n:
+    if v.size < n:
         raise PascError(capi.PASC_ERR_ARG, f"{what}: {n} values expected, got {v.size}")
     return v
 

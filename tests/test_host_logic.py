@@ -144,9 +144,9 @@ def test_model_getters_wiring(monkeypatch):
 
 
 def test_vector_sizes_are_checked_before_the_abi():
-    """The Python mirror refuses arrays whose size is not the one the ABI will read
-    (PASC_ERR_ARG), and hands through the caller's array without a copy when it fits
-    (page-locked buffers stay page-locked)."""
+    """The Python mirror refuses arrays shorter than what the ABI will read (PASC_ERR_ARG),
+    and hands through the caller's array without a copy when it fits (page-locked buffers
+    stay page-locked)."""
     import pasc_inference_gb300 as P
     from pasc_inference_gb300 import capi
     p = object.__new__(P.Problem)
@@ -154,7 +154,7 @@ def test_vector_sizes_are_checked_before_the_abi():
     for call, n in ((p.set_data, 10), (p.set_gamma, 30), (p.set_theta, 3), (p.recon_mse, 10),
                     (p.abserr_reconstructed, 10)):
         with pytest.raises(capi.PascError) as e:
-            call(np.zeros(n + 1))
+            call(np.zeros(n - 1))
         assert e.value.code == capi.PASC_ERR_ARG and "values expected" in str(e.value)
         with pytest.raises(capi.PascError) as e:  # right size: reaches the ABI, which refuses the NULL handle
             call(np.zeros(n))
@@ -164,7 +164,7 @@ def test_vector_sizes_are_checked_before_the_abi():
     b = object.__new__(P.Batch)
     b._h, b.n, b.T, b.K = None, 2, np.array([5, 7]), np.array([2, 3], dtype=np.int32)
     with pytest.raises(capi.PascError) as e:
-        b.set_gamma(1, np.zeros(14))
+        b.set_gamma(1, np.zeros(20))
     assert "values expected" in str(e.value)
     with pytest.raises(capi.PascError) as e:
         b.set_gamma(1, np.zeros(21))
