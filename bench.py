@@ -63,6 +63,66 @@ UNIT = "SPG iterations/s"
 WORKLOAD = "signal1d T=1e7 K=3 levels {0,1,2} sigma=0.5, epssqr=10, theta fixed, GLL m=10"
 
 
+# ------------------------------------------------------------------------------------------
+# replicas: one process per GPU under torchrun.  The SPG path does not shard ("replicas
+# only"): ranks exchange nothing on the data path; these helpers only synchronise the timed
+# region (barrier) and combine timings (max over ranks) on the host over gloo, so no GPU
+# collective is issued.  torch.distributed is used here only, never by the library.
+# ------------------------------------------------------------------------------------------
+class RankInfo:
+    def __init__(self, rank=0, world_size=1, local_rank=0):
+        self.rank, self.world_size, self.local_rank = rank, world_size, local_rank
+        self.initialised = False
+
+
+def dist_init(timeout_s: float = 600.0) -> RankInfo:
+    """Joins the process group when launched with WORLD_SIZE > 1 (gloo over 127.0.0.1)."""
+    info = RankInfo(int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+                    int(os.environ.get("LOCAL_RANK", "0")))
+    if info.world_size > 1:
+        import datetime
+
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        os.environ.setdefault("MASTER_PORT", "29531")
+        if not dist.is_initialized():
+            dist.init_process_group("gloo", rank=info.rank, world_size=info.world_size,
+                                    timeout=datetime.timedelta(seconds=timeout_s))
+        info.initialised = True
+    return info
+
+
+def dist_barrier(info: RankInfo) -> None:
+    if info.world_size > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _allreduce(info: RankInfo, value: float, op: str) -> float:
+    if info.world_size <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=getattr(dist.ReduceOp, op))
+    return float(t.item())
+
+
+def max_over_ranks(info: RankInfo, value: float) -> float:
+    return _allreduce(info, value, "MAX")
+
+
+def sum_over_ranks(info: RankInfo, value: float) -> float:
+    return _allreduce(info, value, "SUM")
+
+
+def dist_finalize(info: RankInfo) -> None:
+    if info.world_size > 1:
+        import torch.distributed as dist
+        if dist.is_initialized():
+            dist.destroy_process_group()
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -85,6 +145,12 @@ def parse():
                     help="sweep kernel: -1 chosen by timing (default), 0 one timestep per thread, "
                          "1 bulk-copy tiles (pin it when profiling: a profiler distorts the timing)")
     return ap.parse_args()
+
+
+def bench_config(T, K, eps2):
+    """The workload description both arms print (identical dicts for the same arguments)."""
+    return {"workload": WORKLOAD, "T": int(T), "K": int(K), "epssqr": float(eps2), "parallelism": "replicas",
+            "l2": "inputs larger than L2"}
 
 
 def measured_peaks():
@@ -224,9 +290,9 @@ def run_reference(args, info):
         "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": WORKLOAD, "T": args.T, "K": 3, "epssqr": args.eps2,
-                   "parallelism": "replicas", "l2": "inputs larger than L2"},
+        "config": bench_config(args.T, 3, args.eps2),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "time_to_1e-6_rel_obj": oracle_tts(sig, theta, args.eps2, args.T),
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     return line
@@ -234,13 +300,12 @@ def run_reference(args, info):
 
 def main():
     args = parse()
-    from pasc_inference_gb300 import dist
-    info = dist.init()
+    info = dist_init()
     if args.impl == "reference":
         line = run_reference(args, info)
         if line is not None:
             print(json.dumps(line), flush=True)
-        dist.finalize(info)
+        dist_finalize(info)
         return
 
     from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Problem, capi, datagen
@@ -265,7 +330,7 @@ def main():
     if args.warmup:
         p.spgqp_iterate(args.warmup, poll=False)
 
-    dist.barrier(info)
+    dist_barrier(info)
     sampler = ClockSampler(dev) if info.rank == 0 else None
     if sampler:
         sampler.start()
@@ -288,8 +353,8 @@ def main():
         done += n
     t_wall = time.perf_counter() - t_wall0
     clocks = sampler.stop() if sampler else None
-    dist.barrier(info)
-    ms_max = dist.max_over_ranks(info, ms_total)
+    dist_barrier(info)
+    ms_max = max_over_ranks(info, ms_total)
     value = info.world_size * args.steps / (ms_max / 1000.0)
     ms_per_step = ms_max / args.steps
 
@@ -306,21 +371,22 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "T": T, "K": K, "epssqr": args.eps2,
-                   "parallelism": f"replicas x{info.world_size}",
-                   "l2": "inputs larger than L2 (x 120 MB + data 40 MB read, x 120 MB written per step)",
-                   "wall_s_timed": t_wall, "restarts": restarts,
-                   "sweep_kernel": {0: "one timestep per thread", 1: "bulk-copy tiles, 4 timesteps per thread"}[variant]},
+        "config": bench_config(T, K, args.eps2),
+        "run": {"wall_s_timed": t_wall, "restarts": restarts,
+                "bytes_per_step": "x 120 MB + data 40 MB read, x 120 MB written",
+                "sweep_kernel": {0: "one timestep per thread", 1: "bulk-copy tiles, 4 timesteps per thread"}[variant]},
         "gpu_launches": launches,
         "roofline": roofline,
         "clocks": clocks,
     }
     p.close()
 
-    if info.rank == 0 and not args.no_e2e:
-        result["e2e"] = measure_e2e(sig, theta, args.eps2, dev)
+    fstar = None
     if info.rank == 0 and not args.no_tts:
-        result["time_to_1e-6_rel_obj"] = measure_tts(sig, theta, args.eps2, dev)
+        result["time_to_1e-6_rel_obj"] = measure_tts(sig, theta, dev)
+        fstar = result["time_to_1e-6_rel_obj"].get(f"epssqr={args.eps2:g}", {}).get("f_star_fp64")
+    if info.rank == 0 and not args.no_e2e:
+        result["e2e"] = measure_e2e(sig, theta, args.eps2, dev, fstar)
     if info.rank == 0 and not args.no_batched:
         result["batched"] = measure_batched(dev, peak, qp=args.batched_qp)
     if info.rank == 0 and not args.no_multichannel:
@@ -336,86 +402,149 @@ def main():
                                   "sample": f"5 SPG iterations of the FP64 oracle on the full T={T} "
                                             f"signal ({dt:.1f} s, OpenMP)",
                                   "one_thread": {"value": rate1, "unit": UNIT, "cores": 1,
-                                                 "sample": f"2 SPG iterations, same signal ({dt1:.1f} s)"}}
+                                                 "sample": f"2 SPG iterations, same signal ({dt1:.1f} s)"},
+                                  "time_to_1e-6_rel_obj": oracle_tts(sig, theta, args.eps2, T)}
     if info.rank == 0:
         print(json.dumps(result), flush=True)
-    dist.finalize(info)
+    dist_finalize(info)
 
 
-def _pinned(n):
-    """A page-locked host array of n doubles (torch's pinned allocator; the numpy view is what
-    the C ABI receives)."""
-    import torch
-    t = torch.empty(n, dtype=torch.float64).pin_memory()
-    return t, t.numpy()
-
-
-def measure_e2e(sig, theta, eps2, dev, steps=2):
-    """Public API with host buffers in pinned memory; copies inside the timed region."""
+def measure_e2e(sig, theta, eps2, dev, fstar, steps=2):
+    """The public API end to end with host buffers in page-locked memory from the library's
+    allocator (pasc_gb300_host_alloc); the copies are inside the timed region.  Each step:
+    set_data, set_gamma, permute, set_theta, update_b, spgqp_solve with the reference's default
+    stop rule (|f - f_old| < 1e-9, GLL m 10; it ends within 1e-6 relative of the FP64 optimum
+    here, checked below), get_gamma, get_fx.  Two forms: FP32 host buffers (the mixed path's
+    device format) and FP64 host buffers (the reference's vector type)."""
     from pasc_inference_gb300 import PASC_PREC_MIXED, Problem, capi
     T, K = sig.T, sig.K
-    keep_g, gamma_h = _pinned(T * K)
-    keep_d, data_h = _pinned(T)
-    keep_o, out = _pinned(T * K)
-    gamma_h[:] = sig.gamma0
-    data_h[:] = sig.data
-    opts = capi.spgqp_opts(m=10, eps=1e-6)
-    with Problem(T, K, eps2, precision=PASC_PREC_MIXED, device=dev) as p:
-        its, secs, launches = 0, 0.0, 0
-        for rep in range(steps + 1):
-            t0 = time.perf_counter()
-            p.set_data(data_h)
-            p.set_gamma(gamma_h)
-            p.permute_gamma()
-            p.set_theta(theta)
-            p.update_b()
-            st = p.spgqp_solve(opts)
-            p.get_gamma_into(out)
-            fx = p.get_fx()
-            dt = time.perf_counter() - t0
-            if rep > 0:
-                its += st.it
-                secs += dt
-                launches += st.kernel_launches
-    return {"value": its / secs, "unit": UNIT, "h2d_bytes_per_step": 8 * T + 8 * T * K + 8 * K,
-            "d2h_bytes_per_step": 8 * T * K + 8, "host_buffers": "pinned", "spg_it_per_step": its / steps,
-            "s_per_step": secs / steps, "fx": fx, "gpu_launches_per_step": launches / steps}
+    opts = capi.spgqp_opts(m=10, eps=1e-9)
+    out = {}
+    for form, dt in (("f32_host", np.float32), ("f64_host", np.float64)):
+        hb = [capi.host_empty(n, dt) for n in (T, T * K, T * K)]
+        data_h, gamma_h, out_h = (h.array for h in hb)
+        data_h[:] = sig.data
+        gamma_h[:] = sig.gamma0
+        with Problem(T, K, eps2, precision=PASC_PREC_MIXED, device=dev) as p:
+            its, secs, launches, fx = 0, 0.0, 0, None
+            for rep in range(steps + 1):
+                t0 = time.perf_counter()
+                if dt == np.float32:
+                    p.set_data_f32(data_h)
+                    p.set_gamma_f32(gamma_h)
+                else:
+                    p.set_data(data_h)
+                    p.set_gamma(gamma_h)
+                p.permute_gamma()
+                p.set_theta(theta)
+                p.update_b()
+                st = p.spgqp_solve(opts)
+                if dt == np.float32:
+                    p.get_gamma_f32_into(out_h)
+                else:
+                    p.get_gamma_into(out_h)
+                fx = p.get_fx()
+                dt_s = time.perf_counter() - t0
+                if rep > 0:
+                    its += st.it
+                    secs += dt_s
+                    launches += st.kernel_launches
+        w = np.dtype(dt).itemsize
+        out[form] = {"value": its / secs, "unit": UNIT, "h2d_bytes_per_step": w * T + w * T * K + 8 * K,
+                     "d2h_bytes_per_step": w * T * K + 8, "host_buffers": "page-locked (pasc_gb300_host_alloc)",
+                     "spg_it_per_step": its / steps, "s_per_step": secs / steps, "fx": fx,
+                     "fx_rel_err_vs_fp64_optimum": abs(fx - fstar) / abs(fstar) if fstar else None,
+                     "stop": "|f - f_old| < 1e-9 (reference default)", "gpu_launches_per_step": launches / steps}
+        for h in hb:
+            h.close()
+    res = dict(out["f32_host"])
+    err = res["fx_rel_err_vs_fp64_optimum"]
+    res["time_to_1e-6_rel_obj_s"] = res["s_per_step"] if (err is not None and err <= 1e-6) else None
+    res["f64_host"] = out["f64_host"]
+    return res
 
 
-def measure_tts(sig, theta, eps2, dev):
-    """Time to an objective within 1e-6 (relative) of the converged FP64 objective."""
+def _fw_gap_rel(x, data, theta, T, K, eps2):
+    """Frank-Wolfe gap of x relative to |f(x)|, from the FP64 oracle's operator and residual:
+    an upper bound on (f(x) - f*) / |f(x)| for the QP over the simplex product."""
+    from oracle import pasc_oracle as orc
+    b = orc.residual_b(data, theta, T, K, nthreads=0)
+    g = orc.matmult(x, T, K, orc.A_coeff(eps2, T), nthreads=0) - b
+    f = 0.5 * (x @ (g + b)) - b @ x
+    G, X = g.reshape(T, K), x.reshape(T, K)
+    return float(np.sum(np.sum(X * G, axis=1) - G.min(axis=1))) / abs(f)
+
+
+TTS_PLAN = {1.0: (400, 4000), 10.0: (1600, 4000), 100.0: (2600, 6000), 1000.0: (16000, 25000)}
+
+
+def measure_tts(sig, theta, dev, eps_list=(1.0, 10.0, 100.0, 1000.0)):
+    """Time to an objective within 1e-6 (relative) of the FP64 optimum, for every epssqr of
+    the benchmark sweep: the plain FP64 GPU path (the reference's structure) and the mixed
+    path from the same gamma0, both run without a stopping test (fixed iteration budgets
+    that reach the optimum: TTS_PLAN) and traced every few iterations.  The FP64 end point
+    is the optimum, certified by its Frank-Wolfe gap under the oracle's FP64 operator; the
+    mixed path's end point is compared with it (objective and gamma)."""
     from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Problem, capi
     T, K = sig.T, sig.K
-    traces = {}
-    for name, prec, maxit, chunk in (("fp64_plain", PASC_PREC_FP64, 4000, 50),
-                                     ("mixed_fused", PASC_PREC_MIXED, 4000, 25)):
-        with Problem(T, K, eps2, precision=prec, device=dev) as p:
-            p.set_data(sig.data)
-            p.set_gamma(sig.gamma0)
-            p.permute_gamma()
-            p.set_theta(theta)
-            p.update_b()
-            o = capi.spgqp_opts(m=10, eps=1e-13 if prec == PASC_PREC_FP64 else 1e-12, maxit=maxit)
-            t0 = time.perf_counter()
-            p.spgqp_start(o)
-            tr = []
-            st = None
-            while True:
-                st = p.spgqp_iterate(chunk, poll=True)
-                tr.append((time.perf_counter() - t0, st.it, st.fx))
-                if st.status != capi.PASC_SPG_RUNNING:
-                    break
-            traces[name] = (tr, st)
-    fstar = traces["fp64_plain"][1].fx
-    res = {"f_star_fp64": fstar}
-    for name, (tr, st) in traces.items():
-        hit = next(((t, it) for t, it, f in tr if abs(f - fstar) <= 1e-6 * abs(fstar)), None)
-        res[name] = {"seconds": hit[0] if hit else None, "spg_it": hit[1] if hit else None,
-                     "final_rel_err": abs(st.fx - fstar) / abs(fstar), "final_it": st.it,
-                     "status": capi.STATUS_NAMES.get(st.status, st.status)}
-    a, b = res["fp64_plain"]["seconds"], res["mixed_fused"]["seconds"]
-    res["speedup_vs_fp64_plain"] = (a / b) if (a and b) else None
-    return res
+    out = {}
+    for eps2 in eps_list:
+        it64, itmx = TTS_PLAN.get(eps2, (4000, 8000))
+        traces = {}
+        for name, prec, maxit, chunk in (("fp64_plain", PASC_PREC_FP64, it64, 50),
+                                         ("mixed_fused", PASC_PREC_MIXED, itmx, 25)):
+            with Problem(T, K, eps2, precision=prec, device=dev) as p:
+                p.set_data(sig.data)
+                p.set_gamma(sig.gamma0)
+                p.permute_gamma()
+                p.set_theta(theta)
+                p.update_b()
+                o = capi.spgqp_opts(m=10, maxit=maxit, stop_difff=0)
+                t0 = time.perf_counter()
+                p.spgqp_start(o)
+                tr = []
+                while True:
+                    st = p.spgqp_iterate(chunk, poll=True)
+                    tr.append((time.perf_counter() - t0, st.it, st.fx))
+                    if st.status != capi.PASC_SPG_RUNNING:
+                        break
+                traces[name] = (tr, st, p.get_gamma())
+        tr64, st64, x64 = traces["fp64_plain"]
+        fstar = st64.fx
+        res = {"f_star_fp64": fstar, "fp64_optimum_fw_gap_rel": _fw_gap_rel(x64, sig.data, theta, T, K, eps2)}
+        for name, (tr, st, x) in traces.items():
+            hit = next(((t, it) for t, it, f in tr if abs(f - fstar) <= 1e-6 * abs(fstar)), None)
+            res[name] = {"seconds": hit[0] if hit else None, "spg_it": hit[1] if hit else None,
+                         "final_rel_err": abs(st.fx - fstar) / abs(fstar), "final_it": st.it,
+                         "status": capi.STATUS_NAMES.get(st.status, st.status)}
+        xm = traces["mixed_fused"][2]
+        res["mixed_fused"]["gamma_rel_err_vs_fp64_optimum"] = float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))
+        res["mixed_fused"]["labels_equal_frac"] = float(np.mean(np.argmax(xm.reshape(T, K), 1) ==
+                                                               np.argmax(x64.reshape(T, K), 1)))
+        a, b = res["fp64_plain"]["seconds"], res["mixed_fused"]["seconds"]
+        res["speedup_vs_fp64_plain"] = (a / b) if (a and b) else None
+        out[f"epssqr={eps2:g}"] = res
+    return out
+
+
+def oracle_tts(sig, theta, eps2, T, nthreads=0, maxit=600):
+    """The FP64 oracle on the host cores: time to an objective within 1e-6 (relative) of its
+    own objective at |f - f_old| < 1e-12 (the reference's SPG loop, traced)."""
+    from oracle import pasc_oracle as O
+    O.build()
+    K = sig.K
+    b = O.residual_b(sig.data, theta, T, K, nthreads=nthreads)
+    x0 = O.permute_blocked_to_interleaved(sig.gamma0, T, K)
+    t0 = time.perf_counter()
+    _, r, tr = O.spgqp_solve(b, x0, T, K, O.A_coeff(eps2, T), O.spg_opts(m=10, maxit=maxit, eps=1e-12),
+                             trace=True, nthreads=nthreads)
+    secs = time.perf_counter() - t0
+    f = tr[:, 0]
+    fend = f[-1]
+    hit = int(np.argmax(np.abs(f - fend) <= 1e-6 * abs(fend)))
+    return {"seconds": secs * hit / max(r.it, 1), "spg_it": hit, "f_ref": float(fend), "run_it": int(r.it),
+            "run_s": secs, "cores": nthreads if nthreads > 0 else cpu_cores(),
+            "f_ref_rule": "objective of the same run at |f - f_old| < 1e-12"}
 
 
 def measure_multichannel(dev, peak):

@@ -166,6 +166,23 @@ int pasc_gb300_get_gamma(pasc_gb300_problem *p, double *gamma);
 int pasc_gb300_set_theta(pasc_gb300_problem *p, const double *theta);
 int pasc_gb300_get_theta(pasc_gb300_problem *p, double *theta);
 
+/* The same vectors in FP32 host buffers (data T*xdim values, gamma N values, same layouts).
+ * The mixed path keeps data and gamma in FP32 on the device, so these calls move half the
+ * bytes of their FP64 forms and convert nothing on the way (the fp64 path widens or narrows on
+ * the device).  No counterpart in the reference, whose vectors are FP64 PETSc Vecs; a caller
+ * that holds FP64 arrays uses the calls above. */
+int pasc_gb300_set_data_f32(pasc_gb300_problem *p, const float *data);
+int pasc_gb300_set_gamma_f32(pasc_gb300_problem *p, const float *gamma);
+int pasc_gb300_get_gamma_f32(pasc_gb300_problem *p, float *gamma);
+
+/* Page-locked host memory (cudaHostAlloc, portable to every device) for the host buffers of
+ * this ABI: copies from and to it run at the host link's full rate and need no staging
+ * through the driver's bounce buffers.  The replacement for the host arrays PETSc's VecCreate
+ * allocates (src/petscvector/common/decomposition.cpp:200-245 creates the reference's
+ * vectors); free with pasc_gb300_host_free.  *ptr is NULL after a failure. */
+int pasc_gb300_host_alloc(void **ptr, unsigned long bytes);
+int pasc_gb300_host_free(void *ptr);
+
 /* TSSolver::gammavector_permute (include/general/solver/tssolver.h:760-775 ->
  * src/petscvector/common/decomposition.cpp:266-356): blocked k*T+t -> interleaved t*K+k. */
 int pasc_gb300_permute_gamma(pasc_gb300_problem *p);
@@ -377,19 +394,20 @@ int pasc_gb300_fem_reduce_f64(const double *g1_dev, double *g2_dev, long T1, lon
 int pasc_gb300_fem_prolongate_f64(const double *g2_dev, double *g1_dev, long T1, long T2, int K, int fem_type,
                                   void *stream);
 
-/* Theta update for callers that cannot allocate device memory when they need it: code
- * running while a stream is captured into a CUDA graph, hosts whose device memory belongs
- * to another framework's allocator, real-time loops that allow no allocation (nor the
- * device synchronisation cudaMalloc/cudaFree can imply) after start-up.  No counterpart in
- * the reference; it computes what pasc_gb300_update_theta computes
- * (theta_k = sum_t gamma_tk x_t / sum_t gamma_tk) on caller-owned device buffers: gamma_dev
- * (T*K floats, t*K + k), data_dev (T floats), theta_dev (K doubles, written).  It calls no
- * cudaMalloc, cudaFree or allocating library routine; its reduction scratch is a static
- * device array of the library (about 128 KiB, held on every GPU that loads the library until
- * the process exits), which limits K to 8.  The first call on a device looks up that array's
- * address (cudaGetSymbolAddress), so make it before any stream capture.  All calls share the
- * array: calls that overlap on the GPU (other streams, or before the previous call has
- * finished) race and must be avoided.  Asynchronous on `stream`. */
+/* Theta update for callers that cannot allocate device memory when they need it: hosts
+ * whose device memory belongs to another framework's allocator, real-time loops that allow
+ * no allocation (nor the device synchronisation cudaMalloc/cudaFree can imply) after
+ * start-up.  No counterpart in the reference; it computes what pasc_gb300_update_theta
+ * computes (theta_k = sum_t gamma_tk x_t / sum_t gamma_tk) on caller-owned device buffers:
+ * gamma_dev (T*K floats, t*K + k), data_dev (T floats), theta_dev (K doubles, written).  It
+ * calls no cudaMalloc, cudaFree or allocating library routine; its reduction scratch is a
+ * static device array of the library (about 128 KiB, held on every GPU that loads the
+ * library until the process exits), which limits K to 8.  The first call on a device looks
+ * up that array's address (cudaGetSymbolAddress) and keeps it, so make that call before any
+ * stream capture, and do not use the entry point on a device after cudaDeviceReset there
+ * (the kept address belonged to the context the reset ended).  All calls share the array:
+ * calls that overlap on the GPU (other streams, or before the previous call has finished)
+ * race and must be avoided.  Asynchronous on `stream`. */
 int pasc_gb300_theta_update_noalloc(const float *gamma_dev, const float *data_dev, long T, int K,
                                     double *theta_dev, void *stream);
 
@@ -414,6 +432,14 @@ int pasc_gb300_batch_set_gamma(pasc_gb300_batch *b, int i, const double *gamma);
 int pasc_gb300_batch_get_gamma(pasc_gb300_batch *b, int i, double *gamma);
 int pasc_gb300_batch_set_theta(pasc_gb300_batch *b, int i, const double *theta);
 int pasc_gb300_batch_get_theta(pasc_gb300_batch *b, int i, double *theta);
+/* How the batched solves below are driven (no reference counterpart).  device_loop = 1 (the
+ * default): each solve is ONE CUDA graph launch; conditional WHILE nodes repeat the sweeps and
+ * the outer iterations, and single-block control kernels decide on the device after every
+ * `chunk` sweeps (1..64, default 4) which signals still run and whether to go on -- no host
+ * round trip inside a solve.  The loops are bounded by the solve's maxit (sweeps) and the
+ * TSSolver's maxit (outer iterations).  device_loop = 0: the host launches the sweeps in
+ * chunks and reads the signals' states between chunks. */
+int pasc_gb300_batch_set_loop(pasc_gb300_batch *b, int device_loop, int chunk);
 /* pasc_gb300_spgqp_solve for every signal at once; st: n entries (nullable).  The
  * ||b||-scaled stopping tests are not supported (PASC_ERR_NOTSUPP). */
 int pasc_gb300_batch_spgqp_solve(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o,

@@ -355,15 +355,29 @@ void pasc_oracle_residual_b(const double *data, const double *theta, double *b, 
 void pasc_oracle_theta_update(const double *gamma, const double *data, double *theta, long T,
                               int K, int xdim, int nthreads)
 {
-    (void)nthreads;
-    for (int k = 0; k < K; k++) {
+    /* One task per (k, block of up to 16 channels): every sum runs over t in ascending order
+     * on one thread, so the result does not depend on the thread count. */
+    int nth = eff_threads(nthreads);
+    const int JB = 16;
+    const int njb = (xdim + JB - 1) / JB;
+    const long ntask = (long)K * njb;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nth) if (nth > 1)
+#endif
+    for (long task = 0; task < ntask; task++) {
+        const int k = (int)(task / njb);
+        const int j0 = (int)(task % njb) * JB;
+        const int nj = (xdim - j0 < JB) ? xdim - j0 : JB;
         double gsum = 0.0;
         for (long t = 0; t < T; t++) gsum += gamma[t * (long)K + k];
-        for (int j = 0; j < xdim; j++) {
-            double gx = 0.0;
-            for (long t = 0; t < T; t++) gx += data[t * (long)xdim + j] * gamma[t * (long)K + k];
-            theta[k * (long)xdim + j] = (gsum != 0) ? gx / gsum : 0.0;
+        double gx[16];
+        for (int j = 0; j < nj; j++) gx[j] = 0.0;
+        for (long t = 0; t < T; t++) {
+            const double gk = gamma[t * (long)K + k];
+            const double *row = data + t * (long)xdim + j0;
+            for (int j = 0; j < nj; j++) gx[j] += row[j] * gk;
         }
+        for (int j = 0; j < nj; j++) theta[k * (long)xdim + j0 + j] = (gsum != 0) ? gx[j] / gsum : 0.0;
     }
 }
 

@@ -191,9 +191,9 @@ def residual_b(data, theta, T, K, xdim=1, bscale=None, nthreads=1):
     return b
 
 
-def theta_update(gamma, data, T, K, xdim=1):
+def theta_update(gamma, data, T, K, xdim=1, nthreads=1):
     th = np.empty(K * xdim)
-    lib().pasc_oracle_theta_update(_f64(gamma), _f64(data), th, T, K, xdim, 1)
+    lib().pasc_oracle_theta_update(_f64(gamma), _f64(data), th, T, K, xdim, nthreads)
     return th
 
 

@@ -55,11 +55,19 @@ def ts_opts_from(options: dict | None) -> TsOpts:
 
 
 def _vec(a, n: int, what: str) -> np.ndarray:
-    """a as a contiguous float64 array of at least n values: the ABI reads n values from the
-    pointer it gets, so a shorter array is refused here (PASC_ERR_ARG) instead of being read
-    past its end (of a longer one the first n values are used)."""
+    """a as a contiguous float64 array of exactly n values: the ABI reads n values from the
+    pointer it gets, so an array of another size is refused here (PASC_ERR_ARG), as the C++
+    mirror refuses it; pass a slice where a prefix is meant."""
     v = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
-    if v.size < n:
+    if v.size != n:
+        raise PascError(capi.PASC_ERR_ARG, f"{what}: {n} values expected, got {v.size}")
+    return v
+
+
+def _vec32(a, n: int, what: str) -> np.ndarray:
+    """a as a contiguous float32 array of exactly n values (PASC_ERR_ARG otherwise)."""
+    v = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    if v.size != n:
         raise PascError(capi.PASC_ERR_ARG, f"{what}: {n} values expected, got {v.size}")
     return v
 
@@ -131,6 +139,21 @@ class Problem:
         if out.dtype != np.float64 or out.size != self.T * self.K or not out.flags.c_contiguous:
             raise ValueError("get_gamma_into: a contiguous float64 array of T*K values is needed")
         check(load().pasc_gb300_get_gamma(self._h, out))
+        return out
+
+    def set_data_f32(self, data):
+        """set_data from FP32 values (the mixed path's device format: half the bytes, no
+        conversion)."""
+        check(load().pasc_gb300_set_data_f32(self._h, _vec32(data, self.T * self.xdim, "set_data_f32")))
+
+    def set_gamma_f32(self, gamma):
+        check(load().pasc_gb300_set_gamma_f32(self._h, _vec32(gamma, self.T * self.K, "set_gamma_f32")))
+
+    def get_gamma_f32_into(self, out: np.ndarray) -> np.ndarray:
+        """gamma as FP32 values into a caller's array (e.g. page-locked host memory)."""
+        if out.dtype != np.float32 or out.size != self.T * self.K or not out.flags.c_contiguous:
+            raise ValueError("get_gamma_f32_into: a contiguous float32 array of T*K values is needed")
+        check(load().pasc_gb300_get_gamma_f32(self._h, out))
         return out
 
     def set_theta(self, theta):
@@ -320,6 +343,11 @@ class Batch:
             return np.ascontiguousarray(a, dtype=np.float64)
         T, K = int(self.T[i]), int(self.K[i])
         return _vec(a, {1: T, 2: T * K, 3: K}[what], name)
+
+    def set_loop(self, device_loop: bool = True, chunk: int = 4):
+        """device_loop: each solve is one graph launch whose loops are decided on the device
+        every `chunk` sweeps (default); False: the host drives the sweeps in chunks."""
+        check(load().pasc_gb300_batch_set_loop(self._h, 1 if device_loop else 0, int(chunk)))
 
     def set_data(self, i: int, data):
         check(load().pasc_gb300_batch_set_data(self._h, int(i), self._vec(i, data, 1, "batch_set_data")))

@@ -66,6 +66,7 @@ class PascError(RuntimeError):
 
 _dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_fp = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 LONG_DTYPE = np.int64 if C.sizeof(C.c_long) == 8 else np.int32
 _lp = np.ctypeslib.ndpointer(LONG_DTYPE, flags="C_CONTIGUOUS")
 _h = C.c_void_p
@@ -83,6 +84,11 @@ PROTOTYPES = {
     "pasc_gb300_set_data": (C.c_int, [_h, _dp]),
     "pasc_gb300_set_gamma": (C.c_int, [_h, _dp]),
     "pasc_gb300_get_gamma": (C.c_int, [_h, _dp]),
+    "pasc_gb300_set_data_f32": (C.c_int, [_h, _fp]),
+    "pasc_gb300_set_gamma_f32": (C.c_int, [_h, _fp]),
+    "pasc_gb300_get_gamma_f32": (C.c_int, [_h, _fp]),
+    "pasc_gb300_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_ulong]),
+    "pasc_gb300_host_free": (C.c_int, [C.c_void_p]),
     "pasc_gb300_set_theta": (C.c_int, [_h, _dp]),
     "pasc_gb300_get_theta": (C.c_int, [_h, _dp]),
     "pasc_gb300_permute_gamma": (C.c_int, [_h]),
@@ -136,6 +142,7 @@ PROTOTYPES = {
     "pasc_gb300_batch_create": (C.c_int, [C.POINTER(_h), C.c_int, _lp, _ip, _dp, C.c_int]),
     "pasc_gb300_batch_destroy": (C.c_int, [_h]),
     "pasc_gb300_batch_size": (C.c_int, [_h, C.POINTER(C.c_int)]),
+    "pasc_gb300_batch_set_loop": (C.c_int, [_h, C.c_int, C.c_int]),
     "pasc_gb300_batch_set_data": (C.c_int, [_h, C.c_int, _dp]),
     "pasc_gb300_batch_set_gamma": (C.c_int, [_h, C.c_int, _dp]),
     "pasc_gb300_batch_get_gamma": (C.c_int, [_h, C.c_int, _dp]),
@@ -204,3 +211,33 @@ def adjoint_opts(**kw) -> AdjointOpts:
             raise KeyError(k)
         setattr(o, k, v)
     return o
+
+
+class HostBuffer:
+    """Page-locked host memory from pasc_gb300_host_alloc, freed when the object goes; `array`
+    is a numpy view of it (keep the HostBuffer alive as long as the view is used)."""
+
+    def __init__(self, n: int, dtype=np.float64):
+        dt = np.dtype(dtype)
+        ptr = C.c_void_p()
+        check(load().pasc_gb300_host_alloc(C.byref(ptr), int(n) * dt.itemsize))
+        self._ptr = ptr
+        buf = (C.c_char * (int(n) * dt.itemsize)).from_address(ptr.value)
+        self.array = np.frombuffer(buf, dtype=dt, count=int(n))
+
+    def close(self):
+        if getattr(self, "_ptr", None) is not None and self._ptr.value:
+            self.array = None
+            load().pasc_gb300_host_free(self._ptr)
+            self._ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def host_empty(n: int, dtype=np.float64) -> HostBuffer:
+    """n values of page-locked host memory (see HostBuffer)."""
+    return HostBuffer(n, dtype)

@@ -26,6 +26,225 @@ int bfail(int code, const std::string &msg)
 
 }  // namespace
 
+// ---------------------------------------------------------------------------------------
+// device-driven loops.  The batched SPG solve and the batched TSSolver run as ONE CUDA graph
+// launch each: conditional WHILE nodes repeat the SPG sweeps of the running signals and the
+// outer (theta step, gamma step, |L - L_old| test) iterations, and small single-block control
+// kernels decide on the device whether to go on.  Every loop is bounded: the sweep loop ends
+// once `spg_maxit` sweeps have run, the outer loop after `ts_maxit` iterations, whatever the
+// signals' states, and both end on a device error (a bounded bulk-copy wait that gave up).
+// ---------------------------------------------------------------------------------------
+namespace pasc {
+
+struct BatchLoop {
+    // settings, written by the host before each launch
+    int ts_maxit, ts_relative, chunk, spg_maxit;
+    double ts_eps;
+    double eps, gamma, sigma1, sigma2, alphainit;
+    int maxit, m, stop_difff, stop_normgp, stop_Anormgp;
+    // progress
+    int outer_it, sweeps, error, launches;
+};
+
+struct BatchOuter {  // one signal's outer loop (TSSolver::solve, tssolver.h:550-645)
+    double L, dL;
+    int done, it_last, spg_it, spg_hm, incr, pad;
+};
+
+constexpr int BL_NT = 1024;
+
+// exclusive prefix sum over the block of one int per thread; *total gets the sum
+__device__ __forceinline__ int bl_scan(int v, int *s_warp, int *total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < (BL_NT / 32) ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        s_warp[32 + lane] = w;  // inclusive sums of the warps
+    }
+    __syncthreads();
+    const int before = (warp ? s_warp[32 + warp - 1] : 0) + x - v;
+    *total = s_warp[32 + BL_NT / 32 - 1];
+    __syncthreads();
+    return before;
+}
+
+// The work list: every segment of the signals with take[i] != 0, in signal order.
+template <class Take>
+__device__ void bl_worklist(const BatchArgs &a, int *work, int *nwork, Take take)
+{
+    __shared__ int s_warp[64];
+    int base = 0;
+    for (int i0 = 0; i0 < a.ninst; i0 += BL_NT) {
+        const int i = i0 + threadIdx.x;
+        const int cnt = (i < a.ninst && take(i)) ? a.inst[i].nseg : 0;
+        int total;
+        const int off = base + bl_scan(cnt, s_warp, &total);
+        for (int q = 0; q < cnt; q++) work[off + q] = a.inst[i].seg0 + q;
+        base += total;
+    }
+    if (threadIdx.x == 0) {
+        *nwork = base;
+        *a.next_job = 0u;
+    }
+}
+
+__device__ __forceinline__ int bl_count(int v)
+{
+    return __syncthreads_count(v);
+}
+
+__global__ void __launch_bounds__(BL_NT) bl_begin_kernel(BatchArgs a, BatchLoop *L, BatchOuter *O, int *active)
+{
+    for (int i = threadIdx.x; i < a.ninst; i += BL_NT) {
+        BatchOuter o;
+        o.L = DBL_MAX;
+        o.dL = DBL_MAX;
+        o.done = o.it_last = o.spg_it = o.spg_hm = o.incr = o.pad = 0;
+        O[i] = o;
+        active[i] = 1;
+    }
+    if (threadIdx.x == 0) {
+        L->outer_it = 0;
+        L->error = 0;
+        L->launches = 1;
+    }
+}
+
+// theta step of the signals still in their outer loop: work list and tickets
+__global__ void __launch_bounds__(BL_NT) bl_theta_head_kernel(BatchArgs a, int *work, int *nwork, BatchLoop *L)
+{
+    for (int i = threadIdx.x; i < a.ninst; i += BL_NT) a.ticket[i] = 0u;
+    bl_worklist(a, work, nwork, [&](int i) { return a.active[i] != 0; });
+    if (threadIdx.x == 0) L->launches += 2;
+}
+
+// start of an SPG solve of the active signals (the set-up of spgqpsolver.cpp:104-137 is the
+// INIT sweep that follows); the others are left as they are (status IDLE)
+__global__ void __launch_bounds__(BL_NT) bl_spg_setup_kernel(BatchArgs a, int *work, int *nwork, BatchLoop *L,
+                                                             const double *coeffA, const double *coeffB,
+                                                             cudaGraphConditionalHandle h_sweeps)
+{
+    const BatchLoop cfg = *L;
+    int nact = 0;
+    for (int i = threadIdx.x; i < a.ninst; i += BL_NT) {
+        SpgDevState &h = a.st[i];
+        const int cur = h.cur;
+        SpgDevState z;
+        memset(&z, 0, sizeof z);
+        z.alpha_prev = z.alpha_cur = cfg.alphainit;
+        z.coeff = coeffA[i];
+        z.bscale = coeffB[i];
+        z.eps = cfg.eps;
+        z.gamma = cfg.gamma;
+        z.sigma1 = cfg.sigma1;
+        z.sigma2 = cfg.sigma2;
+        z.maxit = cfg.maxit;
+        z.m = cfg.m;
+        z.stop_difff = cfg.stop_difff;
+        z.stop_normgp = cfg.stop_normgp;
+        z.stop_Anormgp = cfg.stop_Anormgp;
+        z.cur = cur;
+        z.status = a.active[i] ? PASC_SPG_RUNNING : 99;  // 99: takes no part (batch.cu IDLE)
+        h = z;
+        a.ticket[i] = 0u;
+        nact += a.active[i] ? 1 : 0;
+    }
+    nact = bl_count(nact > 0);
+    bl_worklist(a, work, nwork, [&](int i) { return a.active[i] != 0; });
+    if (threadIdx.x == 0) {
+        L->sweeps = 0;
+        L->launches += 2;  // this kernel and the INIT sweep
+        cudaGraphSetConditional(h_sweeps, nact > 0 ? 1u : 0u);
+    }
+}
+
+// after `chunk` sweeps: drop the signals whose solve ended from the work list and decide on
+// the next chunk
+__global__ void __launch_bounds__(BL_NT) bl_spg_poll_kernel(BatchArgs a, int *work, int *nwork, BatchLoop *L,
+                                                            cudaGraphConditionalHandle h_sweeps)
+{
+    int running = 0, err = 0;
+    for (int i = threadIdx.x; i < a.ninst; i += BL_NT) {
+        running |= a.st[i].status == PASC_SPG_RUNNING;
+        err |= a.st[i].error != 0;
+    }
+    running = bl_count(running);
+    err = bl_count(err);
+    bl_worklist(a, work, nwork, [&](int i) { return a.st[i].status == PASC_SPG_RUNNING; });
+    if (threadIdx.x == 0) {
+        const int sweeps = L->sweeps + L->chunk;
+        L->sweeps = sweeps;
+        L->launches += L->chunk + 1;
+        if (err) L->error = 1;
+        cudaGraphSetConditional(h_sweeps, (running > 0 && err == 0 && sweeps < L->spg_maxit) ? 1u : 0u);
+    }
+}
+
+// end of a batched SPG solve: a solve still running has used its iterations
+__global__ void __launch_bounds__(BL_NT) bl_spg_final_kernel(BatchArgs a, BatchLoop *L)
+{
+    for (int i = threadIdx.x; i < a.ninst; i += BL_NT)
+        if (a.st[i].status == PASC_SPG_RUNNING) a.st[i].status = PASC_SPG_MAXIT;
+    if (threadIdx.x == 0) L->launches += 1;
+}
+
+// end of an outer iteration (tssolver.h:618-645): L, |L - L_old| and the stopping test of
+// every active signal; a signal whose test holds leaves the loop
+__global__ void __launch_bounds__(BL_NT) bl_outer_tail_kernel(BatchArgs a, BatchLoop *L, BatchOuter *O, int *active,
+                                                              cudaGraphConditionalHandle h_outer)
+{
+    const int it = L->outer_it;
+    const int ts_maxit = L->ts_maxit;
+    int left = 0;
+    for (int i = threadIdx.x; i < a.ninst; i += BL_NT) {
+        if (!active[i]) continue;
+        SpgDevState &h = a.st[i];
+        if (h.status == PASC_SPG_RUNNING) h.status = PASC_SPG_MAXIT;
+        BatchOuter o = O[i];
+        o.spg_it += h.it;
+        o.spg_hm += h.hessmult;
+        const double L_old = o.L;
+        o.L = h.fx;
+        o.dL = fabs(o.L - L_old);
+        if (o.L - L_old > 0) o.incr++;
+        o.it_last = it;
+        const bool stop = L->ts_relative ? (o.dL < L->ts_eps * fabs(o.L)) : (o.dL < L->ts_eps);
+        if (stop) {
+            o.done = 1;
+            active[i] = 0;
+        } else {
+            if (it == ts_maxit - 1) o.it_last = ts_maxit;
+            left = 1;
+        }
+        O[i] = o;
+    }
+    left = bl_count(left);
+    int err = 0;
+    for (int i = threadIdx.x; i < a.ninst; i += BL_NT) err |= a.st[i].error != 0;
+    err = bl_count(err);
+    if (threadIdx.x == 0) {
+        L->outer_it = it + 1;
+        L->launches += 1;
+        if (err) L->error = 1;
+        cudaGraphSetConditional(h_outer, (left > 0 && err == 0 && L->error == 0 && it + 1 < ts_maxit) ? 1u : 0u);
+    }
+}
+
+}  // namespace pasc
+
 #define BCU(call)                                                                                  \
     do {                                                                                           \
         cudaError_t e_ = (call);                                                                   \
@@ -63,6 +282,16 @@ struct pasc_gb300_batch {
     cudaGraphExec_t chunk = nullptr;
     pasc_gb300_spgqp_opts o{};
     int launches = 0;
+    // device-driven loops (one graph launch per solve): control state, per-signal outer-loop
+    // records, the graphs (SPG solve; TSSolver without / with the theta step) and the capture
+    // streams of the loop bodies
+    int device_loop = 1;
+    int loop_chunk = 4;
+    BatchLoop *loop_d = nullptr, *loop_h = nullptr;
+    BatchOuter *outer_d = nullptr, *outer_h = nullptr;
+    double *coeffA_d = nullptr, *coeffB_d = nullptr;
+    cudaGraphExec_t g_spg = nullptr, g_ts[2] = {nullptr, nullptr};
+    cudaStream_t aux[2] = {nullptr, nullptr};
 };
 
 static constexpr int BATCH_CHUNK = 16;
@@ -72,8 +301,14 @@ static void batch_free(pasc_gb300_batch *b)
     if (!b) return;
     cudaSetDevice(b->device);
     if (b->chunk) cudaGraphExecDestroy(b->chunk);
+    for (cudaGraphExec_t g : {b->g_spg, b->g_ts[0], b->g_ts[1]})
+        if (g) cudaGraphExecDestroy(g);
+    for (cudaStream_t q : b->aux)
+        if (q) cudaStreamDestroy(q);
+    if (b->loop_h) cudaFreeHost(b->loop_h);
+    if (b->outer_h) cudaFreeHost(b->outer_h);
     void *dev[] = {b->inst_d, b->seg_inst_d, b->work_d, b->nwork_d, b->xb[0], b->xb[1], b->data, b->stage64, b->st_d, b->partials,
-                   b->theta64, b->ticket, b->next_job, b->active_d};
+                   b->theta64, b->ticket, b->next_job, b->active_d, b->loop_d, b->outer_d, b->coeffA_d, b->coeffB_d};
     for (void *p : dev)
         if (p) cudaFree(p);
     if (b->st_h) cudaFreeHost(b->st_h);
@@ -174,12 +409,22 @@ int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const 
         !dal((void **)&b->st_d, sizeof(SpgDevState) * n) || !dal((void **)&b->partials, sizeof(double) * 16 * b->nseg) ||
         !dal((void **)&b->theta64, sizeof(double) * 8 * n) || !dal((void **)&b->ticket, sizeof(unsigned int) * n) ||
         !dal((void **)&b->next_job, sizeof(unsigned int)) || !dal((void **)&b->active_d, sizeof(int) * n) ||
-        !dal((void **)&b->work_d, sizeof(int) * b->nseg) || !dal((void **)&b->nwork_d, sizeof(int)))
+        !dal((void **)&b->work_d, sizeof(int) * b->nseg) || !dal((void **)&b->nwork_d, sizeof(int)) ||
+        !dal((void **)&b->loop_d, sizeof(BatchLoop)) || !dal((void **)&b->outer_d, sizeof(BatchOuter) * n) ||
+        !dal((void **)&b->coeffA_d, sizeof(double) * n) || !dal((void **)&b->coeffB_d, sizeof(double) * n))
         return bail(bfail(PASC_ERR_ALLOC, "batch_create: device allocation failed"));
     if (cudaMallocHost((void **)&b->st_h, sizeof(SpgDevState) * n) != cudaSuccess ||
         cudaMallocHost((void **)&b->active_h, sizeof(int) * n) != cudaSuccess ||
-        cudaMallocHost((void **)&b->work_h, sizeof(int) * (b->nseg + 1)) != cudaSuccess)
+        cudaMallocHost((void **)&b->work_h, sizeof(int) * (b->nseg + 1)) != cudaSuccess ||
+        cudaMallocHost((void **)&b->loop_h, sizeof(BatchLoop)) != cudaSuccess ||
+        cudaMallocHost((void **)&b->outer_h, sizeof(BatchOuter) * n) != cudaSuccess)
         return bail(bfail(PASC_ERR_ALLOC, "batch_create: pinned allocation failed"));
+    if (cudaStreamCreateWithFlags(&b->aux[0], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->aux[1], cudaStreamNonBlocking) != cudaSuccess)
+        return bail(bfail(PASC_ERR_CUDA, "batch_create: stream creation failed"));
+    memset(b->loop_h, 0, sizeof(BatchLoop));
+    cudaMemcpy(b->coeffA_d, b->coeffA.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(b->coeffB_d, b->coeffB.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
     memset(b->st_h, 0, sizeof(SpgDevState) * n);
     cudaMemset(b->xb[0], 0, sizeof(float) * b->nx);  // pads stay zero: kernels write 0 <= t < T only
     cudaMemset(b->xb[1], 0, sizeof(float) * b->nx);
@@ -203,6 +448,23 @@ int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const 
 int pasc_gb300_batch_destroy(pasc_gb300_batch *b)
 {
     batch_free(b);
+    return PASC_OK;
+}
+
+int pasc_gb300_batch_set_loop(pasc_gb300_batch *b, int device_loop, int chunk)
+{
+    if (!b) return bfail(PASC_ERR_ARG, "batch_set_loop: NULL handle");
+    if (chunk < 1 || chunk > 64) return bfail(PASC_ERR_ARG, "batch_set_loop: chunk must be in [1, 64]");
+    BCU(cudaSetDevice(b->device));
+    BCU(cudaStreamSynchronize(b->stream));
+    if (chunk != b->loop_chunk) {
+        for (cudaGraphExec_t *g : {&b->g_spg, &b->g_ts[0], &b->g_ts[1]}) {
+            if (*g) cudaGraphExecDestroy(*g);
+            *g = nullptr;
+        }
+        b->loop_chunk = chunk;
+    }
+    b->device_loop = device_loop ? 1 : 0;
     return PASC_OK;
 }
 
@@ -331,12 +593,198 @@ static int ensure_batch_graph(pasc_gb300_batch *b)
     return PASC_OK;
 }
 
+// ---------------------------------------------------------------------------------------
+// graphs of the device-driven loops
+// ---------------------------------------------------------------------------------------
+
+// A conditional handle for a node of the graph stream s is capturing into.
+static cudaError_t capture_handle(cudaStream_t s, unsigned int dflt, unsigned int flags, cudaGraphConditionalHandle *h)
+{
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr);
+    if (e != cudaSuccess) return e;
+    if (cs != cudaStreamCaptureStatusActive || !g) return cudaErrorStreamCaptureInvalidated;
+    return cudaGraphConditionalHandleCreate(h, g, dflt, flags);
+}
+
+// Appends a WHILE node on handle h to the capture of s (after the captured work so far) and
+// makes it the capture's only dependency; *body receives the node's body graph.
+static cudaError_t capture_while(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraph_t *body)
+{
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return e;
+    if (cs != cudaStreamCaptureStatusActive || !g) return cudaErrorStreamCaptureInvalidated;
+    std::vector<cudaGraphNode_t> dv(deps, deps + nd);
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    e = cudaGraphAddNode(&node, g, dv.empty() ? nullptr : dv.data(), nullptr, dv.size(), &np);
+    if (e != cudaSuccess) return e;
+    *body = np.conditional.phGraph_out[0];
+    return cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+// Captures the SPG solve of the active signals on s: set-up, INIT sweep, then a WHILE loop
+// of `loop_chunk` sweeps and a poll, as long as a signal runs (bounded by spg_maxit sweeps).
+static cudaError_t capture_spg(pasc_gb300_batch *b, cudaStream_t s, cudaStream_t body_stream)
+{
+    BatchArgs a = batch_args(b);
+    cudaGraphConditionalHandle hs;
+    cudaError_t e = capture_handle(s, 0u, 0u, &hs);
+    if (e != cudaSuccess) return e;
+    bl_spg_setup_kernel<<<1, BL_NT, 0, s>>>(a, b->work_d, b->nwork_d, b->loop_d, b->coeffA_d, b->coeffB_d, hs);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = launch_batch_sweep(b->KB, true, b->grid_init, a, s)) != cudaSuccess) return e;
+    cudaGraph_t body = nullptr;
+    if ((e = capture_while(s, hs, &body)) != cudaSuccess) return e;
+    // the loop body, captured on its own stream into the node's body graph
+    if ((e = cudaStreamBeginCaptureToGraph(body_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess)
+        return e;
+    for (int q = 0; q < b->loop_chunk && e == cudaSuccess; q++) {
+        e = cudaMemsetAsync(b->next_job, 0, sizeof(unsigned int), body_stream);
+        if (e == cudaSuccess) e = launch_batch_sweep(b->KB, false, b->grid, a, body_stream);
+    }
+    if (e == cudaSuccess) {
+        bl_spg_poll_kernel<<<1, BL_NT, 0, body_stream>>>(a, b->work_d, b->nwork_d, b->loop_d, hs);
+        e = cudaGetLastError();
+    }
+    cudaGraph_t out = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(body_stream, &out);
+    return e != cudaSuccess ? e : e2;
+}
+
+static int instantiate(cudaStream_t s, cudaError_t e, cudaGraphExec_t *exec, const char *what)
+{
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(s, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        *exec = nullptr;
+        cudaGetLastError();
+        return bfail(PASC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+    return PASC_OK;
+}
+
+// The batched SPG solve as one graph.
+static int ensure_spg_loop_graph(pasc_gb300_batch *b)
+{
+    if (b->g_spg) return PASC_OK;
+    BCU(cudaStreamSynchronize(b->stream));
+    BCU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = capture_spg(b, b->stream, b->aux[1]);
+    if (e == cudaSuccess) {
+        bl_spg_final_kernel<<<1, BL_NT, 0, b->stream>>>(batch_args(b), b->loop_d);
+        e = cudaGetLastError();
+    }
+    return instantiate(b->stream, e, &b->g_spg, "batch SPG loop graph");
+}
+
+// The batched TSSolver as one graph: WHILE (a signal is in its outer loop) { theta step,
+// SPG solve (its own WHILE loop), |L - L_old| test }.
+static int ensure_ts_loop_graph(pasc_gb300_batch *b, int thetasolved)
+{
+    cudaGraphExec_t *exec = &b->g_ts[thetasolved ? 1 : 0];
+    if (*exec) return PASC_OK;
+    BCU(cudaStreamSynchronize(b->stream));
+    BatchArgs a = batch_args(b);
+    BCU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    bl_begin_kernel<<<1, BL_NT, 0, b->stream>>>(a, b->loop_d, b->outer_d, b->active_d);
+    e = cudaGetLastError();
+    cudaGraphConditionalHandle ho;
+    cudaGraph_t body = nullptr;
+    if (e == cudaSuccess) e = capture_handle(b->stream, 1u, cudaGraphCondAssignDefault, &ho);
+    if (e == cudaSuccess) e = capture_while(b->stream, ho, &body);
+    if (e == cudaSuccess) {
+        cudaStream_t s = b->aux[0];
+        e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            if (!thetasolved) {
+                bl_theta_head_kernel<<<1, BL_NT, 0, s>>>(a, b->work_d, b->nwork_d, b->loop_d);
+                e = cudaGetLastError();
+                if (e == cudaSuccess) e = launch_theta_batch(b->grid_theta, a, s);
+            }
+            if (e == cudaSuccess) e = capture_spg(b, s, b->aux[1]);
+            if (e == cudaSuccess) {
+                bl_outer_tail_kernel<<<1, BL_NT, 0, s>>>(a, b->loop_d, b->outer_d, b->active_d, ho);
+                e = cudaGetLastError();
+            }
+            cudaGraph_t out = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(s, &out);
+            if (e == cudaSuccess) e = e2;
+        }
+    }
+    return instantiate(b->stream, e, exec, "batch TSSolver loop graph");
+}
+
+static void loop_settings(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o)
+{
+    BatchLoop &L = *b->loop_h;
+    L.eps = o->eps;
+    L.gamma = o->gamma;
+    L.sigma1 = o->sigma1;
+    L.sigma2 = o->sigma2;
+    L.alphainit = o->alphainit;
+    L.maxit = o->maxit;
+    L.m = o->m;
+    L.stop_difff = o->stop_difff;
+    L.stop_normgp = o->stop_normgp;
+    L.stop_Anormgp = o->stop_Anormgp;
+    L.spg_maxit = o->maxit;
+    L.chunk = b->loop_chunk;
+    L.outer_it = L.sweeps = L.error = L.launches = 0;
+}
+
+// Uploads the settings and each signal's current buffer index, launches `g` and reads the
+// states back.
+static int run_loop_graph(pasc_gb300_batch *b, cudaGraphExec_t g, double *elapsed_ms)
+{
+    cudaStream_t s = b->stream;
+    BCU(cudaStreamSynchronize(s));
+    for (int i = 0; i < b->n; i++) b->st_h[i].cur = b->cur[i];
+    BCU(cudaMemcpyAsync(b->st_d, b->st_h, sizeof(SpgDevState) * b->n, cudaMemcpyHostToDevice, s));
+    BCU(cudaMemcpyAsync(b->loop_d, b->loop_h, sizeof(BatchLoop), cudaMemcpyHostToDevice, s));
+    BCU(cudaMemcpyAsync(b->active_d, b->active_h, sizeof(int) * b->n, cudaMemcpyHostToDevice, s));
+    BCU(cudaEventRecord(b->ev0, s));
+    BCU(cudaGraphLaunch(g, s));
+    BCU(cudaEventRecord(b->ev1, s));
+    BCU(cudaMemcpyAsync(b->st_h, b->st_d, sizeof(SpgDevState) * b->n, cudaMemcpyDeviceToHost, s));
+    BCU(cudaMemcpyAsync(b->loop_h, b->loop_d, sizeof(BatchLoop), cudaMemcpyDeviceToHost, s));
+    BCU(cudaMemcpyAsync(b->outer_h, b->outer_d, sizeof(BatchOuter) * b->n, cudaMemcpyDeviceToHost, s));
+    BCU(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    if (elapsed_ms) *elapsed_ms += ms;
+    for (int i = 0; i < b->n; i++) b->cur[i] = b->st_h[i].cur;
+    std::fill(b->in_work.begin(), b->in_work.end(), 2);  // the device rewrote the work list
+    b->launches += b->loop_h->launches;
+    if (b->loop_h->error) return bfail(PASC_ERR_TIMEOUT, "batch: a bounded wait for a bulk copy gave up");
+    return PASC_OK;
+}
+
 // SPG solves of the signals with active_h[i] != 0 (the others stay untouched).
 static int batch_spgqp(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o, double *elapsed_ms)
 {
     if (o->stop_normgp_normb || o->stop_Anormgp_normb)
         return bfail(PASC_ERR_NOTSUPP, "batch: ||b||-scaled stopping tests are not supported");
     if (o->m < 1 || o->m > MMAX_STATE) return bfail(PASC_ERR_ARG, "batch: m must be in [1, 64]");
+    if (b->device_loop) {
+        BCHK(ensure_spg_loop_graph(b));
+        loop_settings(b, o);
+        return run_loop_graph(b, b->g_spg, elapsed_ms);
+    }
     BCHK(ensure_batch_graph(b));
     cudaStream_t s = b->stream;
     BCU(cudaStreamSynchronize(s));  // the pinned state mirror may still be feeding an upload
@@ -451,6 +899,38 @@ int pasc_gb300_batch_ts_solve(pasc_gb300_batch *b, const pasc_gb300_ts_opts *ts,
     BCU(cudaSetDevice(b->device));
     auto t0 = std::chrono::steady_clock::now();
     const int n = b->n;
+    if (b->device_loop) {
+        if (spg->stop_normgp_normb || spg->stop_Anormgp_normb)
+            return bfail(PASC_ERR_NOTSUPP, "batch: ||b||-scaled stopping tests are not supported");
+        if (spg->m < 1 || spg->m > MMAX_STATE) return bfail(PASC_ERR_ARG, "batch: m must be in [1, 64]");
+        BCHK(ensure_ts_loop_graph(b, ts->thetasolved ? 1 : 0));
+        b->launches = 0;
+        if (ts->init_permute) BCHK(batch_permute(b));
+        loop_settings(b, spg);
+        b->loop_h->ts_maxit = ts->maxit;
+        b->loop_h->ts_eps = ts->eps;
+        b->loop_h->ts_relative = ts->relative;
+        for (int i = 0; i < n; i++) b->active_h[i] = 1;
+        if (ts->maxit > 0) BCHK(run_loop_graph(b, b->g_ts[ts->thetasolved ? 1 : 0], nullptr));
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (st) {
+            for (int i = 0; i < n; i++) {
+                const BatchOuter &o = b->outer_h[i];
+                const bool ran = ts->maxit > 0;
+                st[i].it_last = ran ? o.it_last : 0;
+                st[i].it_sum = st[i].it_last;
+                st[i].spg_it_sum = ran ? o.spg_it : 0;
+                st[i].spg_hessmult_sum = ran ? o.spg_hm : 0;
+                st[i].kernel_launches = b->launches;
+                st[i].L_increased = ran ? o.incr : 0;
+                st[i].L = ran ? o.L : DBL_MAX;
+                st[i].deltaL = ran ? o.dL : DBL_MAX;
+                st[i].aic = 2 * log(st[i].L) + b->K[i];
+                st[i].time_s = secs;
+            }
+        }
+        return PASC_OK;
+    }
     std::vector<double> L(n, DBL_MAX), dL(n, DBL_MAX);
     std::vector<int> done(n, 0), it_last(n, 0), spg_it(n, 0), spg_hm(n, 0), incr(n, 0);
     b->launches = 0;

@@ -1,10 +1,9 @@
 // noalloc.cu -- a theta update (K-means step of the FEM-H1 model) that allocates nothing.
 //
 // Some callers of this library cannot allocate device memory at the point where they need
-// the theta step: code that runs while a CUDA stream is being captured into a graph, hosts
-// whose device memory is owned by another framework's allocator, and real-time loops that
-// forbid allocation (and the implicit device synchronisation cudaMalloc/cudaFree may cause)
-// after start-up.  For them this file offers pasc_gb300_theta_update_noalloc: the caller
+// the theta step: hosts whose device memory is owned by another framework's allocator, and
+// real-time loops that forbid allocation (and the implicit device synchronisation
+// cudaMalloc/cudaFree may cause) after start-up.  For them this file offers pasc_gb300_theta_update_noalloc: the caller
 // passes its own device buffers for the inputs and the output, and the reduction's scratch
 // (per-block partial sums and the last-block ticket) lives in the file-scope array below,
 // which every GPU that loads the library holds until the process exits.
@@ -86,7 +85,9 @@ double *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
 
 // Device address of the scratch array on the current device.  The array's name is only a
 // host-side stand-in for the symbol, so the address is looked up once per device (with that
-// device current) and remembered.
+// device current) and remembered for the life of the process: a cudaDeviceReset ends the
+// context the address belongs to, and the entry point is not to be used on that device
+// after one.
 cudaError_t noalloc_scratch(int dev, double **out)
 {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);

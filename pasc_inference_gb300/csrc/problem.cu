@@ -68,7 +68,7 @@ static void free_all(pasc_gb300_problem *p)
                    p->d, p->Ad, p->b, p->data32_raw, p->theta32, p->xb_raw[0], p->xb_raw[1], p->st,
                    p->partials, p->xbf, p->xnorm, p->bmat_raw, p->theta_split, p->theta_f32, p->tnorm,
                    p->mc_partials, p->mc_err, p->tp_ck64, p->tp_kw32, p->gptr, p->gidx, p->db_raw[0],
-                   p->db_raw[1], p->gpartials};
+                   p->db_raw[1], p->gpartials, p->stage32};
     for (void *q : dev)
         if (q) cudaFree(q);
     if (p->st_h) cudaFreeHost(p->st_h);
@@ -414,12 +414,9 @@ static int fem_update_b_async(pasc_gb300_problem *p, int *launches)
 
 extern "C" {
 
-int pasc_gb300_set_data(pasc_gb300_problem *p, const double *data)
+// after data64 holds the new data (FP64 on the device): the derived device copies
+static int data_uploaded(pasc_gb300_problem *p)
 {
-    if (!p || !data) return fail(PASC_ERR_ARG, "set_data: NULL argument");
-    p->run.started = false;
-    CU(cudaSetDevice(p->device));
-    CU(cudaMemcpyAsync(p->data64, data, sizeof(double) * p->T * p->xdim, cudaMemcpyHostToDevice, p->stream));
     if (p->xdim > 1) {
         // multichannel: X is kept in BF16 (rounded to nearest), with ||X_t||^2 of the rounded
         // values; b follows from the current theta
@@ -432,6 +429,41 @@ int pasc_gb300_set_data(pasc_gb300_problem *p, const double *data)
     CHK(mc_check_error(p));
     p->have_data = true;
     return PASC_OK;
+}
+
+int pasc_gb300_set_data(pasc_gb300_problem *p, const double *data)
+{
+    if (!p || !data) return fail(PASC_ERR_ARG, "set_data: NULL argument");
+    p->run.started = false;
+    CU(cudaSetDevice(p->device));
+    CU(cudaMemcpyAsync(p->data64, data, sizeof(double) * p->T * p->xdim, cudaMemcpyHostToDevice, p->stream));
+    return data_uploaded(p);
+}
+
+int pasc_gb300_set_data_f32(pasc_gb300_problem *p, const float *data)
+{
+    if (!p || !data) return fail(PASC_ERR_ARG, "set_data_f32: NULL argument");
+    p->run.started = false;
+    CU(cudaSetDevice(p->device));
+    const long n = p->T * p->xdim;
+    if (p->xdim == 1 && p->precision == PASC_PREC_MIXED) {
+        // the sweeps read FP32 data: copy it in place, widen it for the FP64 consumers
+        CU(cudaMemcpyAsync(p->data32, data, sizeof(float) * n, cudaMemcpyHostToDevice, p->stream));
+        CU(launch_f32_to_f64(p->data32, p->data64, n, p->stream));
+        CU(cudaStreamSynchronize(p->stream));
+        p->have_data = true;
+        return PASC_OK;
+    }
+    float *stage = nullptr;
+    if (n <= 2 * p->N) {
+        stage = reinterpret_cast<float *>(p->stage64);
+    } else {
+        if (!p->stage32) CHK(dalloc(&p->stage32, (size_t)n));
+        stage = p->stage32;
+    }
+    CU(cudaMemcpyAsync(stage, data, sizeof(float) * n, cudaMemcpyHostToDevice, p->stream));
+    CU(launch_f32_to_f64(stage, p->data64, n, p->stream));
+    return data_uploaded(p);
 }
 
 int pasc_gb300_set_gamma(pasc_gb300_problem *p, const double *gamma)
@@ -470,6 +502,57 @@ int pasc_gb300_get_gamma(pasc_gb300_problem *p, double *gamma)
     CHK(gamma64(p, &g64));
     CU(cudaMemcpyAsync(gamma, g64, sizeof(double) * p->N, cudaMemcpyDeviceToHost, p->stream));
     CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_set_gamma_f32(pasc_gb300_problem *p, const float *gamma)
+{
+    if (!p || !gamma) return fail(PASC_ERR_ARG, "set_gamma_f32: NULL argument");
+    p->run.started = false;
+    CU(cudaSetDevice(p->device));
+    if (p->precision == PASC_PREC_FP64) {
+        float *stage = reinterpret_cast<float *>(p->stage64);
+        CU(cudaMemcpyAsync(stage, gamma, sizeof(float) * p->N, cudaMemcpyHostToDevice, p->stream));
+        CU(launch_f32_to_f64(stage, p->x, p->N, p->stream));
+    } else {
+        CU(cudaMemcpyAsync(p->xb[p->cur], gamma, sizeof(float) * p->N, cudaMemcpyHostToDevice, p->stream));
+    }
+    CU(cudaStreamSynchronize(p->stream));
+    p->have_fx = false;
+    return PASC_OK;
+}
+
+int pasc_gb300_get_gamma_f32(pasc_gb300_problem *p, float *gamma)
+{
+    if (!p || !gamma) return fail(PASC_ERR_ARG, "get_gamma_f32: NULL argument");
+    CU(cudaSetDevice(p->device));
+    const float *src = p->xb[p->cur];
+    if (p->precision == PASC_PREC_FP64) {
+        float *stage = reinterpret_cast<float *>(p->stage64);
+        CU(launch_f64_to_f32(p->x, stage, p->N, p->stream));
+        src = stage;
+    }
+    CU(cudaMemcpyAsync(gamma, src, sizeof(float) * p->N, cudaMemcpyDeviceToHost, p->stream));
+    CU(cudaStreamSynchronize(p->stream));
+    return PASC_OK;
+}
+
+int pasc_gb300_host_alloc(void **ptr, unsigned long bytes)
+{
+    if (!ptr) return fail(PASC_ERR_ARG, "host_alloc: NULL argument");
+    *ptr = nullptr;
+    cudaError_t e = cudaHostAlloc(ptr, bytes > 0 ? bytes : 1, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return fail(PASC_ERR_ALLOC, "cudaHostAlloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    }
+    return PASC_OK;
+}
+
+int pasc_gb300_host_free(void *ptr)
+{
+    if (!ptr) return PASC_OK;
+    CU(cudaFreeHost(ptr));
     return PASC_OK;
 }
 

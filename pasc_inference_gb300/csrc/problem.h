@@ -42,6 +42,7 @@ struct pasc_gb300_problem {
     double *data64 = nullptr;     // T (fp64 path; mixed path uses it as upload staging)
     double *theta64 = nullptr;    // K*xdim
     double *stage64 = nullptr;    // N (mixed: conversions; fp64: permutation temp)
+    float *stage32 = nullptr;     // T*xdim, only where FP32 host data does not fit in stage64
     double *red = nullptr;        // reduction scratch (dot_partials_size doubles)
     double *red_out = nullptr;    // 8 doubles
     double *red_out_h = nullptr;  // pinned mirror

@@ -1,7 +1,7 @@
 """Generates tests/golden/golden_ref.npz from the reference's own code.
 
-Run in a checkout where the PASC_inference tree is available (default /root/reference, or
-$PASC_REFERENCE):  python tests/golden/make_golden.py
+Run with the PASC_inference tree named on the command line (or in $PASC_REFERENCE):
+  python tests/golden/make_golden.py <PASC_inference tree>
 It builds oracle/_ref/libpasc_ref.so (oracle/build_ref.sh: the reference's generic
 SPGQPSolver / TSSolver / SPG_fs / SimplexFeasibleSet_Local templates compiled unmodified
 against host-array shims) and records inputs and outputs of:
@@ -30,7 +30,10 @@ from oracle import pasc_oracle as O  # noqa: E402
 from pasc_inference_gb300 import datagen  # noqa: E402
 from pasc_inference_gb300.petscio import load_vec  # noqa: E402
 
-REF = os.environ.get("PASC_REFERENCE", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PASC_REFERENCE", "")
+if not os.path.isfile(os.path.join(REF, "include/general/solver/spgqpsolver.h")):
+    sys.exit("make_golden: give the PASC_inference tree as the first argument or in PASC_REFERENCE")
+os.environ["PASC_REFERENCE"] = REF  # oracle/build_ref.sh compiles from the same tree
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden_ref.npz")
 
 

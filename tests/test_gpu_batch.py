@@ -182,3 +182,65 @@ def test_batch_bad_arguments(gpulib):
             bt.spgqp_solve(capi.spgqp_opts(stop_normgp_normb=1))
         with pytest.raises(capi.PascError):
             bt.ts_solve(capi.ts_opts(annealing=3))
+
+
+def _ts_batch(sigs, eps, device_loop, chunk=4, theta0=None, **ts_kw):
+    bt = Batch([s.T for s in sigs], [s.K for s in sigs], eps)
+    bt.set_loop(device_loop, chunk)
+    for i, s in enumerate(sigs):
+        bt.set_data(i, s.data)
+        bt.set_gamma(i, s.gamma0)
+        bt.set_theta(i, np.zeros(s.K) if theta0 is None else theta0[i])
+    st = bt.ts_solve(capi.ts_opts(**ts_kw), capi.spgqp_opts(m=10, eps=1e-9, maxit=5000))
+    out = [(x.L, x.it_last, x.spg_it_sum, x.L_increased, bt.get_theta(i), bt.get_gamma(i)) for i, x in enumerate(st)]
+    bt.close()
+    return out
+
+
+@pytest.mark.parametrize("chunk", [1, 4, 7])
+def test_batch_device_loop_equals_host_loop(gpulib, chunk):
+    """The device-driven loops (one graph launch per solve, conditional WHILE nodes, control
+    on the device every `chunk` sweeps) make exactly the iterations of the host-driven loop:
+    every signal's SPG and TSSolver results are bit-identical (each signal's sweeps do not
+    depend on how the sweeps are grouped)."""
+    sigs = [datagen.signal1d(g["T"], g["K"], g["levels"], g["smin"], g["smax"], g["sigma"], g["seed"])
+            for g, _ in TS_CASES]
+    eps = [e for _, e in TS_CASES]
+    host = _ts_batch(sigs, eps, False, maxit=50, eps=1e-9)
+    dev = _ts_batch(sigs, eps, True, chunk, maxit=50, eps=1e-9)
+    for i, (h, d) in enumerate(zip(host, dev)):
+        assert h[:4] == d[:4], (i, h[:4], d[:4])
+        np.testing.assert_array_equal(h[4], d[4])
+        np.testing.assert_array_equal(h[5], d[5])
+    # theta given (TSSolver::set_solution_theta): the graph without the theta step
+    th = [np.linspace(0.0, 2.0, s.K) for s in sigs]
+    host = _ts_batch(sigs, eps, False, theta0=th, maxit=3, thetasolved=1)
+    dev = _ts_batch(sigs, eps, True, chunk, theta0=th, maxit=3, thetasolved=1)
+    for h, d in zip(host, dev):
+        assert h[:4] == d[:4]
+        np.testing.assert_array_equal(h[5], d[5])
+
+
+def test_batch_device_loop_spg_equals_host_loop(gpulib, oracle):
+    res = []
+    for device_loop in (False, True):
+        bt, probs = _load(SPG_CASES, oracle, seed0=3)
+        with bt:
+            bt.set_loop(device_loop, 4)
+            st = bt.spgqp_solve(capi.spgqp_opts(m=10, eps=1e-10, maxit=4000))
+            res.append(([(s.it, s.status, s.fx) for s in st], [bt.get_gamma(i) for i in range(len(SPG_CASES))]))
+            st0 = bt.spgqp_solve(capi.spgqp_opts(maxit=0))  # maxit 0: the set-up only
+            assert all(s.it == 0 and s.status == capi.PASC_SPG_MAXIT for s in st0)
+    assert res[0][0] == res[1][0]
+    for a, b in zip(res[0][1], res[1][1]):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_batch_set_loop_arguments(gpulib):
+    with Batch([100, 200], [3, 2], [1.0, 1.0]) as bt:
+        with pytest.raises(capi.PascError):
+            bt.set_loop(True, 0)
+        with pytest.raises(capi.PascError):
+            bt.set_loop(True, 65)
+        bt.set_loop(False, 1)
+        bt.set_loop(True, 64)

@@ -1,0 +1,154 @@
+"""The benchmark configurations at their full sizes against the FP64 oracle.
+
+Signal workload: T = 1e7, K = 3 (levels {0, 1, 2} in random order per segment, segment lengths
+U[1e3, 1e5], noise 0.5), theta fixed at the levels, for every epssqr of the sweep
+{1, 10, 100, 1000}.  For each epssqr:
+  * the fp64 GPU path makes the oracle's iterations: the objectives of the first 30 iterations
+    from the same gamma0 agree to 1e-11 relative (both FP64; the dot products are summed in
+    another order);
+  * the fp64 GPU path driven until its objective stops changing (or ||d||^2 < 1e-20) is the
+    optimum: its Frank-Wolfe gap sum_t (gamma_t'g_t - min_k g_tk), an upper bound on f - f*
+    computed from the oracle's operator and residual, is below 1e-10 |f|, and the oracle's own
+    SPG iteration started from that point changes the objective by less than 1e-12 relative in
+    20 iterations;
+  * for epssqr 1 and 10 the oracle is also driven to its optimum from gamma0 (about a minute
+    of host time); the two optima agree to 1e-12 (objective) and 1e-6 (gamma, relative 2-norm).
+    Gamma is compared more loosely than the objective because at epssqr = 1 the objective is
+    flat along some directions (timesteps whose residuals to two levels nearly tie, coupled
+    only through A = 1e-7 A_hat): there the oracle's iteration moves an optimal FP64 gamma by
+    1.5e-7 (relative 2-norm) while the objective stays the same to 1e-12;
+  * the mixed path run to its fixed point (25000 iterations; about 17500 are needed at epssqr
+    1000, where the smooth modes have curvature ~1e-4 below the largest) has, against that
+    optimum, the objective within 1e-6 relative (both the value the device reports and the
+    oracle's FP64 objective of the returned FP32 gamma), gamma within 1e-5 relative (2-norm;
+    measured 2e-8 to 2.6e-6) and argmax labels equal on >= 99.99% of the timesteps.
+The optimum of this convex QP does not depend on the start, so the oracle's fixed-point check
+from the GPU's FP64 end point pins it as well as a solve from gamma0 would; at epssqr 100 and
+1000 the latter takes the oracle 2250 and 15000 iterations (about 2 and 12 minutes on 16 host
+cores), longer than a test should run.
+
+Multichannel workload: T = 1e6 timesteps of n = 128 channels, K = 8 (Markov labels with
+self-transition 0.999, centroids N(0, I), noise 0.8, epssqr 50; X rounded to BF16 for both
+sides), the TSSolver from an informative gamma0 (true labels weighted 1 plus uniform noise;
+from a uniform gamma0 the K-means alternation's fixed point depends on rounding) with the
+reference's stopping rules (SPG |f - f_old| < 1e-9, outer |L - L_old| < 1e-9): L within 1e-6
+relative of the oracle's (device-reported, and recomputed in FP64 from the returned gamma and
+theta), theta within 1e-5 of its scale, gamma within 1e-5 relative (2-norm), labels equal on
+>= 99.99% of the timesteps."""
+import numpy as np
+import pytest
+
+from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Problem, capi, datagen
+
+pytestmark = pytest.mark.gpu
+
+THETA = np.array([0.0, 1.0, 2.0])
+SPG64_TIGHT = dict(m=10, maxit=25000, eps=1e-20, stop_difff=1, stop_normgp=1)
+
+
+@pytest.fixture(scope="module")
+def signal(oracle):
+    sig = datagen.signal1d_cfg1()
+    T, K = sig.T, sig.K
+    b = oracle.residual_b(sig.data, THETA, T, K, nthreads=0)
+    x0 = oracle.permute_blocked_to_interleaved(sig.gamma0, T, K)
+    return sig, b, x0
+
+
+def _load(sig, eps2, prec):
+    p = Problem(sig.T, sig.K, eps2, precision=prec)
+    p.set_data(sig.data)
+    p.set_gamma(sig.gamma0)
+    p.permute_gamma()
+    p.set_theta(THETA)
+    p.update_b()
+    return p
+
+
+def _rel_l2(a, ref):
+    return float(np.linalg.norm(a - ref) / np.linalg.norm(ref))
+
+
+def _objective_and_gap(oracle, x, b, T, K, coeff):
+    """FP64 objective 1/2 x'Ax - b'x and Frank-Wolfe gap of x (oracle operator)."""
+    g = oracle.matmult(x, T, K, coeff, nthreads=0) - b
+    f = 0.5 * (x @ (g + b)) - b @ x
+    G, X = g.reshape(T, K), x.reshape(T, K)
+    gap = float(np.sum(np.sum(X * G, axis=1) - G.min(axis=1)))
+    return float(f), gap
+
+
+@pytest.mark.parametrize("eps2", [1.0, 10.0, 100.0, 1000.0])
+def test_signal_1e7_k3_vs_oracle(gpulib, oracle, signal, eps2):
+    sig, b, x0 = signal
+    T, K = sig.T, sig.K
+    coeff = oracle.A_coeff(eps2, T)
+
+    # the fp64 GPU path makes the oracle's first iterations
+    _, _, tr_o = oracle.spgqp_solve(b, x0, T, K, coeff, oracle.spg_opts(m=10, maxit=30, stop_difff=0),
+                                    trace=True, nthreads=0)
+    with _load(sig, eps2, PASC_PREC_FP64) as p:
+        p.spgqp_start(capi.spgqp_opts(m=10, maxit=30, stop_difff=0))
+        done = 0
+        for it in (1, 2, 5, 10, 30):
+            st = p.spgqp_iterate(it - done, poll=True)
+            done = it
+            assert st.it == it
+            assert abs(st.fx - tr_o[it, 0]) <= 1e-11 * abs(tr_o[it, 0]), (eps2, it, st.fx, tr_o[it, 0])
+
+    # fp64 GPU driven to the optimum, certified by the oracle
+    with _load(sig, eps2, PASC_PREC_FP64) as p:
+        st64 = p.spgqp_solve(capi.spgqp_opts(**SPG64_TIGHT))
+        x64 = p.get_gamma()
+    f64, gap64 = _objective_and_gap(oracle, x64, b, T, K, coeff)
+    assert abs(f64 - st64.fx) <= 1e-12 * abs(f64), (eps2, f64, st64.fx)
+    assert gap64 <= 1e-10 * abs(f64), (eps2, gap64, st64.it, st64.status)
+    xw, rw, _ = oracle.spgqp_solve(b, x64, T, K, coeff, oracle.spg_opts(m=10, maxit=20, stop_difff=0), nthreads=0)
+    assert abs(rw.fx - f64) <= 1e-12 * abs(f64), (eps2, rw.fx, f64)
+    assert _rel_l2(xw, x64) <= 1e-6, (eps2, _rel_l2(xw, x64))
+    fstar, xstar = f64, x64
+
+    if eps2 <= 10.0:
+        xo, ro, _ = oracle.spgqp_solve(b, x0, T, K, coeff, oracle.spg_opts(**SPG64_TIGHT), nthreads=0)
+        assert abs(ro.fx - f64) <= 1e-12 * abs(f64), (eps2, ro.fx, f64, ro.it)
+        assert _rel_l2(x64, xo) <= 1e-6, (eps2, _rel_l2(x64, xo))
+        fstar, xstar = ro.fx, xo
+
+    # the mixed path at its fixed point
+    with _load(sig, eps2, PASC_PREC_MIXED) as p:
+        st = p.spgqp_solve(capi.spgqp_opts(m=10, maxit=25000, stop_difff=0))
+        assert st.status in (capi.PASC_SPG_MAXIT, capi.PASC_SPG_DAD_ZERO), st.status
+        xm = p.get_gamma()
+    fm, _ = _objective_and_gap(oracle, xm, b, T, K, coeff)
+    assert abs(st.fx - fstar) <= 1e-6 * abs(fstar), (eps2, st.fx, fstar)
+    assert abs(fm - fstar) <= 1e-6 * abs(fstar), (eps2, fm, fstar)
+    err = _rel_l2(xm, xstar)
+    assert err <= 1e-5, (eps2, err)
+    lab = np.argmax(xm.reshape(T, K), axis=1) == np.argmax(xstar.reshape(T, K), axis=1)
+    assert np.mean(lab) >= 0.9999, (eps2, np.mean(lab))
+
+
+def test_multichannel_1e6_n128_k8_vs_oracle(gpulib, oracle):
+    mc = datagen.multichannel()
+    T, n, K = mc.T, mc.n, mc.K
+    g0 = mc.gamma0.reshape(K, T).copy()
+    g0[mc.labels, np.arange(T)] += 1.0
+    g0 = g0.ravel()
+    go, tho, ro, _ = oracle.tssolver_solve(mc.data, g0, np.zeros(K * n), T, K, mc.epssqr, xdim=n,
+                                           ts=oracle.ts_opts(maxit=300, eps=1e-9),
+                                           spg=oracle.spg_opts(m=10, eps=1e-9, maxit=20000), nthreads=0)
+    with Problem(T, K, mc.epssqr, precision=PASC_PREC_MIXED, xdim=n) as p:
+        p.set_data(mc.data)
+        p.set_gamma(g0)
+        p.set_theta(np.zeros(K * n))
+        st = p.ts_solve(capi.ts_opts(maxit=300, eps=1e-9), capi.spgqp_opts(m=10, eps=1e-9, maxit=20000))
+        g = p.get_gamma()
+        th = p.get_theta()
+    assert abs(st.L - ro.L) <= 1e-6 * abs(ro.L), (st.L, ro.L)
+    bo = oracle.residual_b(mc.data, th, T, K, xdim=n, nthreads=0)
+    L_host = 0.5 * g @ oracle.matmult(g, T, K, oracle.A_coeff(mc.epssqr, T), nthreads=0) - bo @ g
+    assert abs(L_host - ro.L) <= 1e-6 * abs(ro.L), (L_host, ro.L)
+    assert float(np.max(np.abs(th - tho)) / np.max(np.abs(tho))) <= 1e-5
+    assert _rel_l2(g, go) <= 1e-5, _rel_l2(g, go)
+    lab = np.argmax(g.reshape(T, K), axis=1) == np.argmax(go.reshape(T, K), axis=1)
+    assert np.mean(lab) >= 0.9999

@@ -89,13 +89,13 @@ def test_replica_timing_two_gloo_ranks(tmp_path):
     script.write_text(textwrap.dedent(f"""
         import os, sys, json
         sys.path.insert(0, {ROOT!r})
-        from pasc_inference_gb300 import dist
-        info = dist.init(timeout_s=60)
-        dist.barrier(info)
-        mx = dist.max_over_ranks(info, 10.0 + info.rank)
-        sm = dist.sum_over_ranks(info, 1.0)
+        import bench
+        info = bench.dist_init(timeout_s=60)
+        bench.dist_barrier(info)
+        mx = bench.max_over_ranks(info, 10.0 + info.rank)
+        sm = bench.sum_over_ranks(info, 1.0)
         print(json.dumps({{"rank": info.rank, "ws": info.world_size, "max": mx, "sum": sm}}))
-        dist.finalize(info)
+        bench.dist_finalize(info)
     """))
     port = _free_port()
     procs = []

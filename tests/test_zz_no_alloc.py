@@ -1,7 +1,6 @@
 """The allocation-free theta update (pasc_gb300_theta_update_noalloc), for callers that cannot
-allocate device memory when they need the theta step -- code running during a CUDA graph
-capture, hosts whose device memory belongs to another framework's allocator, real-time loops
-that allow no allocation after start-up.  It is checked through the C ABI against the
+allocate device memory when they need the theta step -- hosts whose device memory belongs to
+another framework's allocator, real-time loops that allow no allocation after start-up.  It is checked through the C ABI against the
 problem-handle path (pasc_gb300_update_theta), which computes the same reduction with scratch
 the handle allocated: relative difference <= 1e-12 (both sum the same FP32 values in the same
 order, so the results are expected to be identical).  Two calls in a row share the static
