@@ -117,6 +117,30 @@ inline void save_vec(const std::string &path, const std::vector<double> &v)
 // ---------------------------------------------------------------------------------------
 // RAII handles
 // ---------------------------------------------------------------------------------------
+// Page-locked host memory from pasc_gb300_host_alloc (copies at the host link's full rate),
+// freed with the object.  The reference's vectors live in PETSc-allocated host arrays.
+template <typename V>
+class HostBuffer {
+public:
+    explicit HostBuffer(size_t n) : n_(n)
+    {
+        void *p = nullptr;
+        check(pasc_gb300_host_alloc(&p, (unsigned long)(n * sizeof(V))));
+        p_.reset(static_cast<V *>(p));
+    }
+    V *data() { return p_.get(); }
+    const V *data() const { return p_.get(); }
+    size_t size() const { return n_; }
+    V &operator[](size_t i) { return p_.get()[i]; }
+
+private:
+    struct Del {
+        void operator()(V *p) const { pasc_gb300_host_free(p); }
+    };
+    std::unique_ptr<V, Del> p_;
+    size_t n_;
+};
+
 class Problem {
 public:
     Problem(long T, int K, double epssqr, int precision = PASC_PREC_MIXED, int xdim = 1, int device = 0)
@@ -154,6 +178,10 @@ public:
         check(pasc_gb300_get_gamma(h_.get(), g.data()));
         return g;
     }
+    // FP32 host buffers (the mixed path's device format: half the bytes, no conversion)
+    void set_data_f32(const float *x, size_t n) { need_n(n, (size_t)T_ * xdim_); check(pasc_gb300_set_data_f32(h_.get(), x)); }
+    void set_gamma_f32(const float *g, size_t n) { need_n(n, (size_t)T_ * K_); check(pasc_gb300_set_gamma_f32(h_.get(), g)); }
+    void get_gamma_f32(float *g, size_t n) const { need_n(n, (size_t)T_ * K_); check(pasc_gb300_get_gamma_f32(h_.get(), g)); }
     std::vector<double> get_theta() const
     {
         std::vector<double> t((size_t)K_ * xdim_);
@@ -227,9 +255,10 @@ private:
     struct Del {
         void operator()(pasc_gb300_problem *p) const { pasc_gb300_destroy(p); }
     };
-    static void need(const std::vector<double> &v, size_t n)
+    static void need(const std::vector<double> &v, size_t n) { need_n(v.size(), n); }
+    static void need_n(size_t got, size_t n)
     {
-        if (v.size() != n) throw Error(PASC_ERR_ARG, "expected " + std::to_string(n) + " values, got " + std::to_string(v.size()));
+        if (got != n) throw Error(PASC_ERR_ARG, "expected " + std::to_string(n) + " values, got " + std::to_string(got));
     }
     std::unique_ptr<pasc_gb300_problem, Del> h_;
     long T_;
@@ -247,6 +276,8 @@ public:
         h_.reset(b);
     }
     int size() const { return (int)T_.size(); }
+    // one graph launch per solve with the loops decided on the device (default), or host-driven
+    void set_loop(bool device_loop, int chunk = 4) { check(pasc_gb300_batch_set_loop(h_.get(), device_loop ? 1 : 0, chunk)); }
     void set_data(int i, const std::vector<double> &x) { check(pasc_gb300_batch_set_data(h_.get(), i, x.data())); }
     void set_gamma(int i, const std::vector<double> &g) { check(pasc_gb300_batch_set_gamma(h_.get(), i, g.data())); }
     void set_theta(int i, const std::vector<double> &t) { check(pasc_gb300_batch_set_theta(h_.get(), i, t.data())); }

@@ -20,9 +20,13 @@ def descend_log_epssqr(problem, clean, steps: int = 20, lr: float | None = None,
                        spg=None, adj=None, min_epssqr: float = 1e-8):
     """Runs `steps` gradient steps on u = log(epssqr), starting from problem.epssqr, the
     problem's data, theta and current gamma (each solve warm-starts from the previous gamma).
-    lr None: chosen so that the first step moves u by `first_step`.  Returns one record per
-    step: epssqr, loss, dloss/du, SPG iterations, CG iterations, solve and adjoint seconds."""
-    spg = spg or capi.spgqp_opts(m=10, eps=1e-12, maxit=20000)
+    lr None: chosen so that the first step moves u by `first_step`.  spg None: each solve runs
+    20000 SPG iterations with no stopping test, which brings the mixed path to its fixed point
+    on the benchmark sizes (T <= 1e6): the gradient jumps where the free set changes, so it
+    has to be taken at the fixed point, not where a |f - f_old| test happened to stop.
+    Returns one record per step: epssqr, loss, dloss/du, SPG iterations, CG iterations,
+    solve and adjoint seconds."""
+    spg = spg or capi.spgqp_opts(m=10, maxit=20000, stop_difff=0)
     u = math.log(problem.epssqr)
     out = []
     for step in range(steps + 1):

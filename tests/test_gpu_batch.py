@@ -184,8 +184,8 @@ def test_batch_bad_arguments(gpulib):
             bt.ts_solve(capi.ts_opts(annealing=3))
 
 
-def _ts_batch(sigs, eps, device_loop, chunk=4, theta0=None, **ts_kw):
-    bt = Batch([s.T for s in sigs], [s.K for s in sigs], eps)
+def _ts_batch(sigs, epssqr, device_loop, chunk=4, theta0=None, **ts_kw):
+    bt = Batch([s.T for s in sigs], [s.K for s in sigs], epssqr)
     bt.set_loop(device_loop, chunk)
     for i, s in enumerate(sigs):
         bt.set_data(i, s.data)
