@@ -278,6 +278,14 @@ public:
     int size() const { return (int)T_.size(); }
     // one graph launch per solve with the loops decided on the device (default), or host-driven
     void set_loop(bool device_loop, int chunk = 4) { check(pasc_gb300_batch_set_loop(h_.get(), device_loop ? 1 : 0, chunk)); }
+    // bulk-copy tiles per segment; 0: chosen by the batch's tuner at the first solve
+    void set_segment_tiles(int tiles) { check(pasc_gb300_batch_set_segment_tiles(h_.get(), tiles)); }
+    int get_segment_tiles() const
+    {
+        int t = 0;
+        check(pasc_gb300_batch_get_segment_tiles(h_.get(), &t, nullptr));
+        return t;
+    }
     void set_data(int i, const std::vector<double> &x) { check(pasc_gb300_batch_set_data(h_.get(), i, x.data())); }
     void set_gamma(int i, const std::vector<double> &g) { check(pasc_gb300_batch_set_gamma(h_.get(), i, g.data())); }
     void set_theta(int i, const std::vector<double> &t) { check(pasc_gb300_batch_set_theta(h_.get(), i, t.data())); }

@@ -440,6 +440,14 @@ int pasc_gb300_batch_get_theta(pasc_gb300_batch *b, int i, double *theta);
  * TSSolver's maxit (outer iterations).  device_loop = 0: the host launches the sweeps in
  * chunks and reads the signals' states between chunks. */
 int pasc_gb300_batch_set_loop(pasc_gb300_batch *b, int device_loop, int chunk);
+/* Segment size of the batched sweeps (no reference counterpart): every signal is cut into
+ * segments of `tiles` bulk-copy tiles of 504 timesteps, the unit of work a block takes from
+ * the work list (longest signals first).  tiles = 0 (the default): the batch's tuner picks it
+ * at the first solve among {2, 4, 8, 16, 32} by timing sweeps of all signals and of the
+ * longest eighth alone; 2..64 pins it.  get: the size in use and (nullable, 5 values) the
+ * tuner's measured score of each candidate in ms (0 before tuning). */
+int pasc_gb300_batch_set_segment_tiles(pasc_gb300_batch *b, int tiles);
+int pasc_gb300_batch_get_segment_tiles(pasc_gb300_batch *b, int *tiles, double *tune_ms);
 /* pasc_gb300_spgqp_solve for every signal at once; st: n entries (nullable).  The
  * ||b||-scaled stopping tests are not supported (PASC_ERR_NOTSUPP). */
 int pasc_gb300_batch_spgqp_solve(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o,

@@ -349,6 +349,18 @@ class Batch:
         every `chunk` sweeps (default); False: the host drives the sweeps in chunks."""
         check(load().pasc_gb300_batch_set_loop(self._h, 1 if device_loop else 0, int(chunk)))
 
+    def set_segment_tiles(self, tiles: int = 0):
+        """Bulk-copy tiles per segment of the batched sweeps; 0: chosen by the tuner at the
+        first solve."""
+        check(load().pasc_gb300_batch_set_segment_tiles(self._h, int(tiles)))
+
+    def get_segment_tiles(self):
+        """(tiles in use, the tuner's score in ms of each candidate 2, 4, 8, 16, 32)."""
+        t = C.c_int()
+        ms = np.zeros(5)
+        check(load().pasc_gb300_batch_get_segment_tiles(self._h, C.byref(t), ms.ctypes.data))
+        return t.value, ms
+
     def set_data(self, i: int, data):
         check(load().pasc_gb300_batch_set_data(self._h, int(i), self._vec(i, data, 1, "batch_set_data")))
 

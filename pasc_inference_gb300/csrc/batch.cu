@@ -81,18 +81,19 @@ __device__ __forceinline__ int bl_scan(int v, int *s_warp, int *total)
     return before;
 }
 
-// The work list: every segment of the signals with take[i] != 0, in signal order.
+// The work list: every segment of the signals with take(i), longest signals first.
 template <class Take>
 __device__ void bl_worklist(const BatchArgs &a, int *work, int *nwork, Take take)
 {
     __shared__ int s_warp[64];
     int base = 0;
-    for (int i0 = 0; i0 < a.ninst; i0 += BL_NT) {
-        const int i = i0 + threadIdx.x;
-        const int cnt = (i < a.ninst && take(i)) ? a.inst[i].nseg : 0;
+    for (int q0 = 0; q0 < a.ninst; q0 += BL_NT) {
+        const int q = q0 + threadIdx.x;
+        const int i = q < a.ninst ? a.order[q] : 0;
+        const int cnt = (q < a.ninst && take(i)) ? a.inst[i].nseg : 0;
         int total;
         const int off = base + bl_scan(cnt, s_warp, &total);
-        for (int q = 0; q < cnt; q++) work[off + q] = a.inst[i].seg0 + q;
+        for (int s = 0; s < cnt; s++) work[off + s] = a.inst[i].seg0 + s;
         base += total;
     }
     if (threadIdx.x == 0) {
@@ -267,10 +268,18 @@ struct pasc_gb300_batch {
     std::vector<int> cur;  // buffer holding each signal's gamma
     BatchInstDev *inst_d = nullptr;
     int *seg_inst_d = nullptr;
-    int nseg = 0;
+    int nseg = 0, nseg_max = 0;
+    // segment size: bulk-copy tiles per segment (0 in seg_pinned: chosen by the tuner at the
+    // first solve), and the order of the work lists (signals by decreasing T)
+    int seg_tiles = 8, seg_pinned = 0;
+    bool tuned = false;
+    std::vector<int> order_h;
+    int *order_d = nullptr;
+    double tune_ms[8] = {0};
     // work list: the segments of the signals taking part in the next launches
     int *work_d = nullptr, *nwork_d = nullptr, *work_h = nullptr;
-    std::vector<char> in_work;  // signals in the uploaded list
+    std::vector<char> in_work;  // signals in the uploaded list (valid while work_valid)
+    bool work_valid = false;
     long nx = 0, nd = 0, maxN = 0;
     float *xb[2] = {nullptr, nullptr}, *data = nullptr;
     double *stage64 = nullptr;
@@ -278,7 +287,7 @@ struct pasc_gb300_batch {
     double *partials = nullptr, *theta64 = nullptr;
     unsigned int *ticket = nullptr, *next_job = nullptr;
     int *active_d = nullptr, *active_h = nullptr;
-    int grid = 0, grid_init = 0, grid_theta = 0;
+    int grid = 0, grid_init = 0, grid_theta = 0, occ = 1, occ_init = 1;
     cudaGraphExec_t chunk = nullptr;
     pasc_gb300_spgqp_opts o{};
     int launches = 0;
@@ -295,6 +304,7 @@ struct pasc_gb300_batch {
 };
 
 static constexpr int BATCH_CHUNK = 16;
+static constexpr int BATCH_MIN_SEG_TILES = 2;  // the smallest segment the tuner tries
 
 static void batch_free(pasc_gb300_batch *b)
 {
@@ -308,7 +318,8 @@ static void batch_free(pasc_gb300_batch *b)
     if (b->loop_h) cudaFreeHost(b->loop_h);
     if (b->outer_h) cudaFreeHost(b->outer_h);
     void *dev[] = {b->inst_d, b->seg_inst_d, b->work_d, b->nwork_d, b->xb[0], b->xb[1], b->data, b->stage64, b->st_d, b->partials,
-                   b->theta64, b->ticket, b->next_job, b->active_d, b->loop_d, b->outer_d, b->coeffA_d, b->coeffB_d};
+                   b->theta64, b->ticket, b->next_job, b->active_d, b->loop_d, b->outer_d, b->coeffA_d, b->coeffB_d,
+                   b->order_d};
     for (void *p : dev)
         if (p) cudaFree(p);
     if (b->st_h) cudaFreeHost(b->st_h);
@@ -318,6 +329,37 @@ static void batch_free(pasc_gb300_batch *b)
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
+}
+
+// Cuts every signal into segments of seg_tiles tiles (segment numbers in signal order, as the
+// per-signal reductions expect) and sizes the grids.  Drops the cached graphs (they hold the
+// launch shapes) and the uploaded work list (it numbers segments of the old layout).
+static int batch_layout(pasc_gb300_batch *b, int seg_tiles)
+{
+    std::vector<int> seg_inst;
+    // the device copy holds the theta the batched theta step wrote last
+    BCU(cudaStreamSynchronize(b->stream));
+    BCU(cudaMemcpy(b->inst_h.data(), b->inst_d, sizeof(BatchInstDev) * b->n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < b->n; i++) {
+        BatchInstDev &I = b->inst_h[i];
+        I.seg0 = (int)seg_inst.size();
+        I.nseg = (I.tiles + seg_tiles - 1) / seg_tiles;
+        for (int s = 0; s < I.nseg; s++) seg_inst.push_back(i);
+    }
+    if ((int)seg_inst.size() > b->nseg_max) return bfail(PASC_ERR_STATE, "batch: segment table overflow");
+    b->seg_tiles = seg_tiles;
+    b->nseg = (int)seg_inst.size();
+    b->grid = std::max(1, std::min(b->occ * b->sms, b->nseg));
+    b->grid_init = std::max(1, std::min(b->occ_init * b->sms, b->nseg));
+    b->grid_theta = std::max(1, std::min(b->sms * 4, b->nseg));
+    BCU(cudaMemcpy(b->inst_d, b->inst_h.data(), sizeof(BatchInstDev) * b->n, cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy(b->seg_inst_d, seg_inst.data(), sizeof(int) * b->nseg, cudaMemcpyHostToDevice));
+    for (cudaGraphExec_t *g : {&b->chunk, &b->g_spg, &b->g_ts[0], &b->g_ts[1]}) {
+        if (*g) cudaGraphExecDestroy(*g);
+        *g = nullptr;
+    }
+    b->work_valid = false;
+    return PASC_OK;
 }
 
 static BatchArgs batch_args(pasc_gb300_batch *b)
@@ -338,6 +380,8 @@ static BatchArgs batch_args(pasc_gb300_batch *b)
     a.next_job = b->next_job;
     a.active = b->active_d;
     a.theta64 = b->theta64;
+    a.order = b->order_d;
+    a.seg_tiles = b->seg_tiles;
     return a;
 }
 
@@ -367,9 +411,8 @@ int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const 
     b->K.assign(K, K + n);
     b->epssqr.assign(epssqr, epssqr + n);
     b->cur.assign(n, 0);
-    const int W = batch_tile_width(), ST = batch_segment_timesteps();
+    const int W = batch_tile_width();
     const long PADB = batch_max_tile();
-    std::vector<int> seg_inst;
     b->inst_h.resize(n);
     long xo = 0, doff = 0;
     for (int i = 0; i < n; i++) {
@@ -386,9 +429,7 @@ int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const 
         xo += ((BPAD_FRONT + T[i] + PADB) * K[i] + 3) / 4 * 4;  // next signal starts 16-byte aligned
         doff += (BPAD_FRONT + T[i] + PADB + 3) / 4 * 4;
         I.tiles = (int)((T[i] + W - 1) / W);
-        I.seg0 = (int)seg_inst.size();
-        I.nseg = (int)((T[i] + ST - 1) / ST);
-        for (int s = 0; s < I.nseg; s++) seg_inst.push_back(i);
+        b->nseg_max += (I.tiles + BATCH_MIN_SEG_TILES - 1) / BATCH_MIN_SEG_TILES;
         b->maxN = std::max(b->maxN, T[i] * (long)K[i]);
         double c = epssqr[i] * (1.0 / (double)T[i]);  // graphh1fem.cpp:146-151
         b->coeffA.push_back(c);
@@ -396,26 +437,29 @@ int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const 
     }
     b->nx = xo;
     b->nd = doff;
-    b->nseg = (int)seg_inst.size();
+    b->order_h.resize(n);
+    for (int i = 0; i < n; i++) b->order_h[i] = i;
+    std::stable_sort(b->order_h.begin(), b->order_h.end(), [&](int x, int y) { return T[x] > T[y]; });
     if (cudaSetDevice(device) != cudaSuccess) return bail(bfail(PASC_ERR_CUDA, "cudaSetDevice failed"));
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
         return bail(bfail(PASC_ERR_CUDA, "batch_create: stream/event creation failed"));
     auto dal = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes > 0 ? bytes : 1) == cudaSuccess; };
-    if (!dal((void **)&b->inst_d, sizeof(BatchInstDev) * n) || !dal((void **)&b->seg_inst_d, sizeof(int) * b->nseg) ||
+    if (!dal((void **)&b->inst_d, sizeof(BatchInstDev) * n) || !dal((void **)&b->seg_inst_d, sizeof(int) * b->nseg_max) ||
         !dal((void **)&b->xb[0], sizeof(float) * b->nx) || !dal((void **)&b->xb[1], sizeof(float) * b->nx) ||
         !dal((void **)&b->data, sizeof(float) * b->nd) || !dal((void **)&b->stage64, sizeof(double) * b->maxN) ||
-        !dal((void **)&b->st_d, sizeof(SpgDevState) * n) || !dal((void **)&b->partials, sizeof(double) * 16 * b->nseg) ||
+        !dal((void **)&b->st_d, sizeof(SpgDevState) * n) || !dal((void **)&b->partials, sizeof(double) * 16 * b->nseg_max) ||
         !dal((void **)&b->theta64, sizeof(double) * 8 * n) || !dal((void **)&b->ticket, sizeof(unsigned int) * n) ||
         !dal((void **)&b->next_job, sizeof(unsigned int)) || !dal((void **)&b->active_d, sizeof(int) * n) ||
-        !dal((void **)&b->work_d, sizeof(int) * b->nseg) || !dal((void **)&b->nwork_d, sizeof(int)) ||
+        !dal((void **)&b->work_d, sizeof(int) * b->nseg_max) || !dal((void **)&b->nwork_d, sizeof(int)) ||
+        !dal((void **)&b->order_d, sizeof(int) * n) ||
         !dal((void **)&b->loop_d, sizeof(BatchLoop)) || !dal((void **)&b->outer_d, sizeof(BatchOuter) * n) ||
         !dal((void **)&b->coeffA_d, sizeof(double) * n) || !dal((void **)&b->coeffB_d, sizeof(double) * n))
         return bail(bfail(PASC_ERR_ALLOC, "batch_create: device allocation failed"));
     if (cudaMallocHost((void **)&b->st_h, sizeof(SpgDevState) * n) != cudaSuccess ||
         cudaMallocHost((void **)&b->active_h, sizeof(int) * n) != cudaSuccess ||
-        cudaMallocHost((void **)&b->work_h, sizeof(int) * (b->nseg + 1)) != cudaSuccess ||
+        cudaMallocHost((void **)&b->work_h, sizeof(int) * (b->nseg_max + 1)) != cudaSuccess ||
         cudaMallocHost((void **)&b->loop_h, sizeof(BatchLoop)) != cudaSuccess ||
         cudaMallocHost((void **)&b->outer_h, sizeof(BatchOuter) * n) != cudaSuccess)
         return bail(bfail(PASC_ERR_ALLOC, "batch_create: pinned allocation failed"));
@@ -435,11 +479,11 @@ int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const 
     cudaMemset(b->nwork_d, 0, sizeof(int));
     b->in_work.assign(n, 0);
     cudaMemcpy(b->inst_d, b->inst_h.data(), sizeof(BatchInstDev) * n, cudaMemcpyHostToDevice);
-    cudaMemcpy(b->seg_inst_d, seg_inst.data(), sizeof(int) * b->nseg, cudaMemcpyHostToDevice);
-    b->grid = std::max(1, std::min(batch_blocks_per_sm(b->KB, false) * b->sms, b->nseg));
-    b->grid_init = std::max(1, std::min(batch_blocks_per_sm(b->KB, true) * b->sms, b->nseg));
-    b->grid_theta = std::max(1, std::min(b->sms * 4, b->nseg));
-    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    cudaMemcpy(b->order_d, b->order_h.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+    b->occ = batch_blocks_per_sm(b->KB, false);
+    b->occ_init = batch_blocks_per_sm(b->KB, true);
+    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess ||
+        batch_layout(b, b->seg_tiles) != PASC_OK || cudaDeviceSynchronize() != cudaSuccess)
         return bail(bfail(PASC_ERR_CUDA, "batch_create: initialisation failed"));
     *out = b;
     return PASC_OK;
@@ -465,6 +509,28 @@ int pasc_gb300_batch_set_loop(pasc_gb300_batch *b, int device_loop, int chunk)
         b->loop_chunk = chunk;
     }
     b->device_loop = device_loop ? 1 : 0;
+    return PASC_OK;
+}
+
+int pasc_gb300_batch_set_segment_tiles(pasc_gb300_batch *b, int tiles)
+{
+    if (!b) return bfail(PASC_ERR_ARG, "batch_set_segment_tiles: NULL handle");
+    if (tiles != 0 && (tiles < BATCH_MIN_SEG_TILES || tiles > 64))
+        return bfail(PASC_ERR_ARG, "batch_set_segment_tiles: tiles must be 0 (tuned) or in [2, 64]");
+    BCU(cudaSetDevice(b->device));
+    b->seg_pinned = tiles;
+    b->tuned = false;
+    for (double &v : b->tune_ms) v = 0.0;
+    if (tiles) return batch_layout(b, tiles);
+    return PASC_OK;
+}
+
+int pasc_gb300_batch_get_segment_tiles(pasc_gb300_batch *b, int *tiles, double *tune_ms)
+{
+    if (!b || !tiles) return bfail(PASC_ERR_ARG, "batch_get_segment_tiles: NULL argument");
+    *tiles = b->seg_tiles;
+    if (tune_ms)
+        for (int c = 0; c < 5; c++) tune_ms[c] = b->tune_ms[c];
     return PASC_OK;
 }
 
@@ -551,21 +617,96 @@ static int batch_permute(pasc_gb300_batch *b)
 template <class Pred>
 static int update_worklist(pasc_gb300_batch *b, Pred take)
 {
-    bool same = true;
+    bool same = b->work_valid;
     for (int i = 0; i < b->n && same; i++) same = (b->in_work[i] != 0) == take(i);
     if (same) return PASC_OK;
     BCU(cudaStreamSynchronize(b->stream));  // the pinned list may still be feeding an upload
     int cnt = 0;
-    for (int i = 0; i < b->n; i++) {
+    for (int q = 0; q < b->n; q++) {
+        const int i = b->order_h[q];
         b->in_work[i] = take(i) ? 1 : 0;
         if (!b->in_work[i]) continue;
         const BatchInstDev &I = b->inst_h[i];
         for (int s = 0; s < I.nseg; s++) b->work_h[1 + cnt++] = I.seg0 + s;
     }
     b->work_h[0] = cnt;
+    b->work_valid = true;
     BCU(cudaMemcpyAsync(b->nwork_d, b->work_h, sizeof(int), cudaMemcpyHostToDevice, b->stream));
     if (cnt) BCU(cudaMemcpyAsync(b->work_d, b->work_h + 1, sizeof(int) * cnt, cudaMemcpyHostToDevice, b->stream));
     return PASC_OK;
+}
+
+// One INIT sweep (a pure function of each signal's current gamma: it reads buffer cur and
+// writes the other one, and the solve that follows starts over from buffer cur) of the signals
+// with take(i), timed with CUDA events; best of `reps`.
+template <class Pred>
+static int time_init_sweep(pasc_gb300_batch *b, Pred take, int reps, float *best)
+{
+    cudaStream_t s = b->stream;
+    BatchArgs a = batch_args(b);
+    *best = 1e30f;
+    for (int r = 0; r < reps + 1; r++) {
+        BCU(cudaStreamSynchronize(s));
+        for (int i = 0; i < b->n; i++) {
+            SpgDevState &h = b->st_h[i];
+            memset(&h, 0, sizeof h);
+            h.alpha_prev = h.alpha_cur = 2.0;
+            h.coeff = b->coeffA[i];
+            h.bscale = b->coeffB[i];
+            h.gamma = 0.9;
+            h.sigma2 = 1.0;
+            h.maxit = 1;
+            h.m = 1;
+            h.cur = b->cur[i];
+            h.status = take(i) ? PASC_SPG_RUNNING : IDLE;
+        }
+        BCU(cudaMemcpyAsync(b->st_d, b->st_h, sizeof(SpgDevState) * b->n, cudaMemcpyHostToDevice, s));
+        BCU(cudaMemsetAsync(b->ticket, 0, sizeof(unsigned int) * b->n, s));
+        BCHK(update_worklist(b, take));
+        BCU(cudaMemsetAsync(b->next_job, 0, sizeof(unsigned int), s));
+        BCU(cudaEventRecord(b->ev0, s));
+        BCU(launch_batch_sweep(b->KB, true, b->grid_init, a, s));
+        BCU(cudaEventRecord(b->ev1, s));
+        BCU(cudaEventSynchronize(b->ev1));
+        float ms = 0.f;
+        BCU(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+        if (r > 0 && ms < *best) *best = ms;  // the first run warms up
+    }
+    BCU(cudaMemcpyAsync(b->st_h, b->st_d, sizeof(SpgDevState) * b->n, cudaMemcpyDeviceToHost, s));
+    BCU(cudaStreamSynchronize(s));
+    for (int i = 0; i < b->n; i++)
+        if (b->st_h[i].error) return bfail(PASC_ERR_TIMEOUT, "batch: a bounded wait for a bulk copy gave up");
+    return PASC_OK;
+}
+
+// The batch's tuner, run at its first solve unless the segment size was pinned: for each
+// segment size in {2, 4, 8, 16, 32} tiles it times one sweep of every signal and one sweep of
+// the longest eighth of the signals alone (the end of a solve, when only long signals still
+// run, is where short segments pay off and long ones leave SMs idle), and keeps the size with
+// the smallest sum of the two.
+static int batch_tune(pasc_gb300_batch *b)
+{
+    if (b->tuned) return PASC_OK;
+    b->tuned = true;
+    if (b->seg_pinned) return PASC_OK;
+    const int nlong = std::max(1, b->n / 8);
+    std::vector<char> is_long(b->n, 0);
+    for (int q = 0; q < nlong; q++) is_long[b->order_h[q]] = 1;
+    const int cand[] = {2, 4, 8, 16, 32};
+    int best = b->seg_tiles;
+    double best_ms = 1e300;
+    for (int c = 0; c < 5; c++) {
+        BCHK(batch_layout(b, cand[c]));
+        float t_all = 0.f, t_long = 0.f;
+        BCHK(time_init_sweep(b, [](int) { return true; }, 3, &t_all));
+        BCHK(time_init_sweep(b, [&](int i) { return is_long[i] != 0; }, 3, &t_long));
+        b->tune_ms[c] = (double)t_all + (double)t_long;
+        if (b->tune_ms[c] < best_ms) {
+            best_ms = b->tune_ms[c];
+            best = cand[c];
+        }
+    }
+    return batch_layout(b, best);
 }
 
 static int ensure_batch_graph(pasc_gb300_batch *b)
@@ -768,7 +909,7 @@ static int run_loop_graph(pasc_gb300_batch *b, cudaGraphExec_t g, double *elapse
     cudaEventElapsedTime(&ms, b->ev0, b->ev1);
     if (elapsed_ms) *elapsed_ms += ms;
     for (int i = 0; i < b->n; i++) b->cur[i] = b->st_h[i].cur;
-    std::fill(b->in_work.begin(), b->in_work.end(), 2);  // the device rewrote the work list
+    b->work_valid = false;  // the device rewrote the work list
     b->launches += b->loop_h->launches;
     if (b->loop_h->error) return bfail(PASC_ERR_TIMEOUT, "batch: a bounded wait for a bulk copy gave up");
     return PASC_OK;
@@ -780,6 +921,7 @@ static int batch_spgqp(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o, doub
     if (o->stop_normgp_normb || o->stop_Anormgp_normb)
         return bfail(PASC_ERR_NOTSUPP, "batch: ||b||-scaled stopping tests are not supported");
     if (o->m < 1 || o->m > MMAX_STATE) return bfail(PASC_ERR_ARG, "batch: m must be in [1, 64]");
+    BCHK(batch_tune(b));
     if (b->device_loop) {
         BCHK(ensure_spg_loop_graph(b));
         loop_settings(b, o);
@@ -903,6 +1045,7 @@ int pasc_gb300_batch_ts_solve(pasc_gb300_batch *b, const pasc_gb300_ts_opts *ts,
         if (spg->stop_normgp_normb || spg->stop_Anormgp_normb)
             return bfail(PASC_ERR_NOTSUPP, "batch: ||b||-scaled stopping tests are not supported");
         if (spg->m < 1 || spg->m > MMAX_STATE) return bfail(PASC_ERR_ARG, "batch: m must be in [1, 64]");
+        BCHK(batch_tune(b));
         BCHK(ensure_ts_loop_graph(b, ts->thetasolved ? 1 : 0));
         b->launches = 0;
         if (ts->init_permute) BCHK(batch_permute(b));
@@ -931,6 +1074,7 @@ int pasc_gb300_batch_ts_solve(pasc_gb300_batch *b, const pasc_gb300_ts_opts *ts,
         }
         return PASC_OK;
     }
+    BCHK(batch_tune(b));
     std::vector<double> L(n, DBL_MAX), dL(n, DBL_MAX);
     std::vector<int> done(n, 0), it_last(n, 0), spg_it(n, 0), spg_hm(n, 0), incr(n, 0);
     b->launches = 0;

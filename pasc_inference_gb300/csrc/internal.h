@@ -119,6 +119,8 @@ struct BatchArgs {
     unsigned int *next_job;  // work-list counter (zeroed before every launch)
     const int *active;       // theta step: signals still in their outer loop
     double *theta64;         // 8 per signal
+    const int *order;        // signals by decreasing T: the order of the work lists
+    int seg_tiles;           // bulk-copy tiles per segment
 };
 
 // Multichannel data (kernels_mc.cu).
@@ -173,7 +175,6 @@ int image_sweep_tiles(int W, int H);
 cudaError_t launch_image_sweep(int K, bool init, int grid, const ImageSweepArgs &a, cudaStream_t s);
 
 int batch_tile_width();
-int batch_segment_timesteps();
 int batch_max_tile();
 int batch_blocks_per_sm(int KB, bool init);
 cudaError_t launch_batch_sweep(int KB, bool init, int grid, const BatchArgs &a, cudaStream_t s);

@@ -5,10 +5,10 @@
 // restarts of examples/test_signal1D/test_signal1D.cpp:268-353, include/general/solver/
 // tssolver.h:522-698; independent signals are separate runs).  Here all of them share a
 // persistent grid:
-//   - each signal is cut into segments of SEG_TILES bulk-copy tiles (sweep_tma.cuh); the
-//     segments of the signals still running form one work list (rebuilt by the host whenever
-//     it reads the signals' states), and blocks take segments in turn from an atomic counter,
-//     so long and short signals balance across the GPU;
+//   - each signal is cut into segments of seg_tiles bulk-copy tiles (sweep_tma.cuh; chosen by
+//     the batch's tuner); the segments of the signals still running form one work list, longest
+//     signals first (rebuilt whenever the signals' states are read), and blocks take segments
+//     in turn from an atomic counter, so long and short signals balance across the GPU;
 //   - a segment is computed by one block with the tile pipeline of the single-signal kernel
 //     (K dispatched at run time) and leaves its four partial sums in its own slot, so the
 //     sums do not depend on which block took which segment (deterministic);
@@ -23,12 +23,10 @@
 namespace pasc {
 
 constexpr int BATCH_NT = 128;
-constexpr int BATCH_SEG_TILES = 8;
 constexpr int BATCH_W = BATCH_NT * TMA_R - 2 * TMA_HALO;  // owned timesteps per tile
-constexpr int BATCH_SEG_T = BATCH_SEG_TILES * BATCH_W;      // timesteps per segment
+// tiles per segment (BatchArgs::seg_tiles) are chosen at run time by the batch's tuner
 
 int batch_tile_width() { return BATCH_W; }
-int batch_segment_timesteps() { return BATCH_SEG_T; }
 int batch_max_tile() { return BATCH_NT * TMA_R; }
 
 // Computes one segment of signal `q` (all threads of the block).  j counts the tiles this
@@ -55,8 +53,14 @@ __device__ __forceinline__ bool batch_segment(TmaSmem<KB, BATCH_NT> &sm, const B
     for (int k = 0; k < K; k++) sc.theta[k] = I.theta[k];
 
     const int lseg = seg - I.seg0;
-    const int tlo = lseg * BATCH_SEG_TILES;
-    const int thi = min(tlo + BATCH_SEG_TILES, I.tiles);
+    const int tlo = lseg * a.seg_tiles;
+    const int thi = min(tlo + a.seg_tiles, I.tiles);
+    if (lseg < 0 || lseg >= I.nseg || tlo >= thi) {
+        // not a segment of this signal (a work list out of step with the segment table): issue
+        // no copy, report it
+        if (threadIdx.x == 0) atomicExch(&st->error, 1);
+        return true;
+    }
     if (threadIdx.x == 0) {
         fence_proxy_async_smem();  // the stages were last read through the generic proxy
         tma_issue<K>(sm, j & 1, sc.xin, sc.data, tlo * BATCH_W - TMA_HALO);
@@ -119,6 +123,7 @@ __global__ void __launch_bounds__(BATCH_NT, batch_min_blocks(KB)) spg_batch_swee
         const int job = sm.job;
         if (job >= *a.nwork) break;
         const int seg = a.work[job];
+        if ((unsigned)seg >= (unsigned)a.nseg) continue;  // never for a list of the current layout
         const int q = a.seg_inst[seg];
         if (a.st[q].status != PASC_SPG_RUNNING) continue;  // this signal's solve ended in this chunk
         bool ok = true;
@@ -149,8 +154,9 @@ __device__ __forceinline__ void theta_segment(const BatchArgs &a, int q, int seg
     const BatchInstDev &I = a.inst[q];
     const float *gam = (a.st[q].cur ? a.xb1 : a.xb0) + I.xoff;
     const float *dat = a.data + I.doff;
-    const long t_lo = (long)(seg - I.seg0) * BATCH_SEG_T;
-    const long t_hi = t_lo + BATCH_SEG_T < I.T ? t_lo + BATCH_SEG_T : I.T;
+    const long seg_t = (long)a.seg_tiles * BATCH_W;
+    const long t_lo = (long)(seg - I.seg0) * seg_t;
+    const long t_hi = t_lo + seg_t < I.T ? t_lo + seg_t : I.T;
     KahanF sx[K], sg[K];
     for (long t = t_lo + threadIdx.x; t < t_hi; t += BATCH_THETA_NT) {
         const float x = __ldg(dat + t);
@@ -202,6 +208,7 @@ __global__ void __launch_bounds__(BATCH_THETA_NT) theta_batch_kernel(BatchArgs a
         const int job = s_job;
         if (job >= *a.nwork) break;
         const int seg = a.work[job];
+        if ((unsigned)seg >= (unsigned)a.nseg) continue;  // never for a list of the current layout
         const int q = a.seg_inst[seg];
         if (!a.active[q]) continue;
         switch (a.inst[q].K) {

@@ -244,3 +244,50 @@ def test_batch_set_loop_arguments(gpulib):
             bt.set_loop(True, 65)
         bt.set_loop(False, 1)
         bt.set_loop(True, 64)
+
+
+def test_batch_segment_tiles_tuned_and_pinned(gpulib, oracle):
+    """The tuner picks one of its candidate segment sizes at the first solve (and reports the
+    score it measured for each); pinned sizes give the same converged objectives (segments
+    change only the order of the FP64 sums of block partials)."""
+    fx = {}
+    for tiles in (0, 2, 32):
+        bt, probs = _load(SPG_CASES, oracle, seed0=5)
+        with bt:
+            bt.set_segment_tiles(tiles)
+            st = bt.spgqp_solve(capi.spgqp_opts(maxit=3000, stop_difff=0))
+            used, ms = bt.get_segment_tiles()
+            if tiles == 0:
+                assert used in (2, 4, 8, 16, 32) and np.all(ms > 0), (used, ms)
+            else:
+                assert used == tiles and np.all(ms == 0)
+            fx[tiles] = np.array([s.fx for s in st])
+    for tiles in (2, 32):
+        np.testing.assert_allclose(fx[tiles], fx[0], rtol=1e-6, atol=1e-12)
+    with Batch([100, 200], [3, 2], [1.0, 1.0]) as bt:
+        for bad in (1, 65, -1):
+            with pytest.raises(capi.PascError):
+                bt.set_segment_tiles(bad)
+
+
+def test_batch_retuned_after_solves_keeps_theta(gpulib):
+    """Changing the segment size after a TSSolver run (whose theta steps updated the device
+    copy of every signal's theta) keeps those thetas: the objective of the final gamma,
+    evaluated by a zero-iteration solve, is the same with and without the change."""
+    sigs = [datagen.signal1d(g["T"], g["K"], g["levels"], g["smin"], g["smax"], g["sigma"], g["seed"])
+            for g, _ in TS_CASES]
+    eps = [e for _, e in TS_CASES]
+    fx = []
+    for relayout in (False, True):
+        with Batch([s.T for s in sigs], [s.K for s in sigs], eps) as bt:
+            bt.set_segment_tiles(8)
+            for i, s in enumerate(sigs):
+                bt.set_data(i, s.data)
+                bt.set_gamma(i, s.gamma0)
+                bt.set_theta(i, np.zeros(s.K))
+            bt.ts_solve(capi.ts_opts(maxit=5), capi.spgqp_opts(m=10, eps=1e-9))
+            if relayout:
+                bt.set_segment_tiles(2)
+            st = bt.spgqp_solve(capi.spgqp_opts(maxit=0))
+            fx.append(np.array([x.fx for x in st]))
+    np.testing.assert_allclose(fx[1], fx[0], rtol=1e-9)
