@@ -221,6 +221,12 @@ int pasc_gb300_spgqp_last_iterate(pasc_gb300_problem *p, double *ms, int *launch
  * first solve, measured on the solve's own first sweep. */
 int pasc_gb300_set_sweep_variant(pasc_gb300_problem *p, int variant);
 int pasc_gb300_get_sweep_variant(pasc_gb300_problem *p, int *variant);
+/* The sweep configuration in use: kernel (-1 before the first solve), blocks of its grid,
+ * and the sweep time (ms) the tuner measured for it (0 when pinned or taken from an earlier
+ * problem of the same shape).  With variant -1 the first solve times both kernels at every
+ * grid of 1, 2, ... blocks per SM up to their occupancy, on the solve's own start point
+ * (gamma is saved and restored around the timing runs). */
+int pasc_gb300_get_sweep_tuning(pasc_gb300_problem *p, int *variant, int *blocks, double *sweep_ms);
 
 /* Measurement: device time per call (CUDA events on the handle's stream) of `reps`
  * back-to-back launches of the theta update (which = 1, as pasc_gb300_update_theta) or of the

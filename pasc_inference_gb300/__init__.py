@@ -202,6 +202,12 @@ class Problem:
         check(load().pasc_gb300_get_sweep_variant(self._h, C.byref(v)))
         return v.value
 
+    def get_sweep_tuning(self):
+        """(kernel, blocks of its grid, tuned sweep time in ms)."""
+        v, g, ms = C.c_int(), C.c_int(), C.c_double()
+        check(load().pasc_gb300_get_sweep_tuning(self._h, C.byref(v), C.byref(g), C.byref(ms)))
+        return v.value, g.value, ms.value
+
     def time_model_kernels(self, which: int, reps: int = 10) -> float:
         """ms per call of the theta update (which=1) or the residual (which=2)."""
         v = C.c_double()

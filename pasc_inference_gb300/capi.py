@@ -100,6 +100,7 @@ PROTOTYPES = {
     "pasc_gb300_spgqp_last_iterate": (C.c_int, [_h, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "pasc_gb300_set_sweep_variant": (C.c_int, [_h, C.c_int]),
     "pasc_gb300_get_sweep_variant": (C.c_int, [_h, C.POINTER(C.c_int)]),
+    "pasc_gb300_get_sweep_tuning": (C.c_int, [_h, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "pasc_gb300_get_b": (C.c_int, [_h, _dp]),
     "pasc_gb300_set_fem": (C.c_int, [_h, C.c_double, C.c_int]),
     "pasc_gb300_get_fem": (C.c_int, [_h, C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_long)]),

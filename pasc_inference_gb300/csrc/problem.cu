@@ -247,6 +247,8 @@ int pasc_gb300_create(pasc_gb300_problem **out, long T, int K, int xdim, int pre
         const long nt_tma = (T + sweep_tma_tile_width() - 1) / sweep_tma_tile_width();
         p->grid_sweep[1] = grid(sweep_tma_blocks_per_sm(K, false, xdim > 1), nt_tma);
         p->grid_sweep_init[1] = grid(sweep_tma_blocks_per_sm(K, true, xdim > 1), nt_tma);
+        p->grid_sweep_max[0] = p->grid_sweep[0];
+        p->grid_sweep_max[1] = p->grid_sweep[1];
         long gt = (long)p->sms * 4;
         long tb = (T + 255) / 256;
         p->grid_theta = (int)(gt < tb ? gt : tb);
@@ -964,8 +966,11 @@ struct VariantKey {
         return std::tie(device, K, form, tbucket) < std::tie(o.device, o.K, o.form, o.tbucket);
     }
 };
+struct VariantChoice {
+    int variant, blocks_per_sm;
+};
 static std::mutex variant_cache_mutex;
-static std::map<VariantKey, int> variant_cache;
+static std::map<VariantKey, VariantChoice> variant_cache;
 
 static VariantKey variant_key(const pasc_gb300_problem *p)
 {
@@ -974,14 +979,20 @@ static VariantKey variant_key(const pasc_gb300_problem *p)
     return VariantKey{p->device, p->K, p->bmat ? 1 : (p->tp ? 2 : 0), tb};
 }
 
-// Chooses the sweep kernel by timing.  The INIT sweep reads only buffer `cur` and the data
-// and writes the other buffer and the state, so it can be repeated with either kernel
-// without changing the solve; the faster kernel is kept for the problem's lifetime (and for
-// later problems of the same shape).
+// Chooses the sweep kernel and its grid by timing: every kernel (one timestep per thread;
+// bulk-copy tiles) at every grid of 1, 2, ... blocks per SM up to its occupancy (each block
+// walks the tiles grid-stride).  A candidate runs the solve's own INIT sweep and then four
+// regular sweeps, of which the fastest of the last three is its time; gamma is saved first
+// and put back afterwards, so the solve that follows is unchanged.  The choice is kept for
+// the problem's lifetime and for later problems of the same device, K, sweep form and
+// power-of-two bucket of T.  A start point that is already stationary (the sweeps stop at
+// once) says nothing about speed: the bulk-copy kernel at full occupancy is taken untimed.
 static int autotune_variant(pasc_gb300_problem *p)
 {
     if (p->graph && p->variant < 0) p->variant = p->img_W > 0 ? 1 : 0;  // the fused image sweep where it applies
     if (p->variant >= 0) return PASC_OK;
+    int *gs = p->tp ? p->grid_sweep_tp : p->grid_sweep;
+    const int *gmax = p->tp ? p->grid_sweep_tp_max : p->grid_sweep_max;
     if (!sweep_tma_supported(p->K)) {
         p->variant = 0;
         return PASC_OK;
@@ -991,39 +1002,82 @@ static int autotune_variant(pasc_gb300_problem *p)
         std::lock_guard<std::mutex> g(variant_cache_mutex);
         auto it = variant_cache.find(key);
         if (it != variant_cache.end()) {
-            p->variant = it->second;
+            const int v = it->second.variant;
+            const long g2 = (long)it->second.blocks_per_sm * p->sms;
+            p->variant = v;
+            gs[v] = (int)(g2 < gmax[v] ? g2 : gmax[v]);
             return PASC_OK;
         }
     }
     cudaStream_t s = p->stream;
     SweepArgs a;
     sweep_args(p, &a);
+    const int cur0 = p->cur;
+    float *saved = reinterpret_cast<float *>(p->stage64);  // N doubles: room for the N floats of gamma
+    CU(cudaMemcpyAsync(saved, p->xb[cur0], sizeof(float) * p->N, cudaMemcpyDeviceToDevice, s));
     float best = 1e30f;
-    int bestv = 0;
-    for (int v = 0; v < 2; v++) {
-        float tot = 0.f;
-        for (int rep = 0; rep < 4; rep++) {
+    int bestv = 0, bestm = 1;
+    bool untimed = false;
+    cudaEvent_t evs[5];
+    for (int q = 0; q < 5; q++) CU(cudaEventCreate(&evs[q]));
+    int rc = PASC_OK;
+    for (int v = 0; v < 2 && rc == PASC_OK && !untimed; v++) {
+        const int mmax = (gmax[v] + p->sms - 1) / p->sms;
+        for (int m = 1; m <= mmax && rc == PASC_OK && !untimed; m++) {
+            const long g = (long)m * p->sms;
+            gs[v] = (int)(g < gmax[v] ? g : gmax[v]);
             fill_device_state(p, p->st_h);
-            CU(cudaMemcpyAsync(p->st, p->st_h, sizeof(SpgDevState), cudaMemcpyHostToDevice, s));
-            CU(cudaEventRecord(p->ev0, s));
-            CU(launch_variant(p, v, true, a));
-            CU(cudaEventRecord(p->ev1, s));
-            CU(cudaEventSynchronize(p->ev1));
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, p->ev0, p->ev1);
-            if (rep > 0) tot += ms;  // the first launch also pays one-time set-up
-        }
-        CU(cudaMemcpyAsync(p->st_h, p->st, sizeof(SpgDevState), cudaMemcpyDeviceToHost, s));
-        CU(cudaStreamSynchronize(s));
-        CHK(check_device_error(p));
-        if (tot < best) {
-            best = tot;
-            bestv = v;
+            p->st_h->maxit = 1 << 30;
+            p->st_h->stop_difff = p->st_h->stop_normgp = p->st_h->stop_Anormgp = 0;
+            cudaError_t e = cudaMemcpyAsync(p->st, p->st_h, sizeof(SpgDevState), cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = launch_variant(p, v, true, a);
+            for (int q = 0; q < 4 && e == cudaSuccess; q++) {
+                e = cudaEventRecord(evs[q], s);
+                if (e == cudaSuccess) e = launch_variant(p, v, false, a);
+            }
+            if (e == cudaSuccess) e = cudaEventRecord(evs[4], s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(p->st_h, p->st, sizeof(SpgDevState), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) {
+                rc = fail(PASC_ERR_CUDA, "sweep tuning: %s", cudaGetErrorString(e));
+                break;
+            }
+            if (p->st_h->error) break;
+            if (p->st_h->status != PASC_SPG_RUNNING) {
+                untimed = true;
+                break;
+            }
+            float t = 1e30f;
+            for (int q = 1; q < 4; q++) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, evs[q], evs[q + 1]);
+                t = ms < t ? ms : t;
+            }
+            if (t < best) {
+                best = t;
+                bestv = v;
+                bestm = m;
+            }
         }
     }
+    for (int q = 0; q < 5; q++) cudaEventDestroy(evs[q]);
+    CU(cudaMemcpyAsync(p->xb[cur0], saved, sizeof(float) * p->N, cudaMemcpyDeviceToDevice, s));
+    CU(cudaStreamSynchronize(s));
+    p->cur = cur0;
+    gs[0] = gmax[0];
+    gs[1] = gmax[1];
+    if (rc != PASC_OK) return rc;
+    CHK(check_device_error(p));
+    if (untimed) {
+        p->variant = 1;
+        return PASC_OK;
+    }
     p->variant = bestv;
-    std::lock_guard<std::mutex> g(variant_cache_mutex);
-    variant_cache[key] = bestv;
+    const long g = (long)bestm * p->sms;
+    gs[bestv] = (int)(g < gmax[bestv] ? g : gmax[bestv]);
+    p->tune_ms = best;
+    std::lock_guard<std::mutex> lk(variant_cache_mutex);
+    variant_cache[key] = VariantChoice{bestv, bestm};
     return PASC_OK;
 }
 
@@ -1349,6 +1403,22 @@ int pasc_gb300_set_sweep_variant(pasc_gb300_problem *p, int variant)
         return fail(PASC_ERR_NOTSUPP, "set_sweep_variant: the fused image sweep needs T = 1 on a pixel grid (H >= 2)");
     p->variant = variant;
     p->run.started = false;
+    // a pinned kernel runs at full occupancy; -1 tunes kernel and grid again
+    for (int v = 0; v < 2; v++) {
+        p->grid_sweep[v] = p->grid_sweep_max[v];
+        if (p->tp) p->grid_sweep_tp[v] = p->grid_sweep_tp_max[v];
+    }
+    p->tune_ms = 0.f;
+    return PASC_OK;
+}
+
+int pasc_gb300_get_sweep_tuning(pasc_gb300_problem *p, int *variant, int *blocks, double *sweep_ms)
+{
+    if (!p || !variant || !blocks || !sweep_ms) return fail(PASC_ERR_ARG, "get_sweep_tuning: NULL argument");
+    *variant = p->variant;
+    const int v = p->variant < 0 ? 1 : p->variant;
+    *blocks = p->tp ? p->grid_sweep_tp[v] : p->grid_sweep[v];
+    *sweep_ms = p->tune_ms;
     return PASC_OK;
 }
 
@@ -1390,6 +1460,7 @@ int pasc_gb300_set_fem(pasc_gb300_problem *p, double fem_reduce, int fem_type)
         const long nt_tma = (T2 + sweep_tma_tile_width() - 1) / sweep_tma_tile_width();
         long g = (long)sweep_tma_blocks_per_sm(p->K, false, true) * q->sms;
         q->grid_sweep[1] = (int)(g < nt_tma ? (g < 1 ? 1 : g) : nt_tma);
+        q->grid_sweep_max[1] = q->grid_sweep[1];
         g = (long)sweep_tma_blocks_per_sm(p->K, true, true) * q->sms;
         q->grid_sweep_init[1] = (int)(g < nt_tma ? (g < 1 ? 1 : g) : nt_tma);
     }
@@ -1523,10 +1594,12 @@ int pasc_gb300_set_usethetainpenalty(pasc_gb300_problem *p, int on)
             g = g < cap ? g : cap;
             return (int)(g < 1 ? 1 : g);
         };
-        p->grid_sweep_tp[0] = grid(sweep_blocks_per_sm(p->K, false, true), nt_thread, p->grid_sweep[0]);
+        p->grid_sweep_tp[0] = grid(sweep_blocks_per_sm(p->K, false, true), nt_thread, p->grid_sweep_max[0]);
+        p->grid_sweep_tp_max[0] = p->grid_sweep_tp[0];
         p->grid_sweep_init_tp[0] = grid(sweep_blocks_per_sm(p->K, true, true), nt_thread, p->grid_sweep_init[0]);
         if (sweep_tma_supported(p->K)) {
-            p->grid_sweep_tp[1] = grid(sweep_tma_blocks_per_sm(p->K, false, false, true), nt_tma, p->grid_sweep[1]);
+            p->grid_sweep_tp[1] = grid(sweep_tma_blocks_per_sm(p->K, false, false, true), nt_tma, p->grid_sweep_max[1]);
+            p->grid_sweep_tp_max[1] = p->grid_sweep_tp[1];
             p->grid_sweep_init_tp[1] =
                 grid(sweep_tma_blocks_per_sm(p->K, true, false, true), nt_tma, p->grid_sweep_init[1]);
         }

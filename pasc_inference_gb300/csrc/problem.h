@@ -60,7 +60,9 @@ struct pasc_gb300_problem {
     int cur = 0;
     // sweep kernels: 0 = one timestep per thread, 1 = bulk-copy tiles, 4 timesteps per thread
     int grid_sweep[2] = {0, 0}, grid_sweep_init[2] = {0, 0}, grid_theta = 0;
-    int variant = -1;             // -1: chosen by timing at the first solve
+    int grid_sweep_max[2] = {0, 0};  // the grids the partials buffer was sized for (occupancy)
+    int variant = -1;             // -1: kernel and grid chosen by timing at the first solve
+    float tune_ms = 0.f;          // the chosen configuration's sweep time in the tuning runs
     cudaGraphExec_t chunk_graph = nullptr;
     int chunk_graph_len = 0, chunk_graph_variant = -1;
 
@@ -105,7 +107,7 @@ struct pasc_gb300_problem {
     bool tp = false;
     double *tp_ck64 = nullptr;
     float *tp_kw32 = nullptr;
-    int grid_sweep_tp[2] = {0, 0}, grid_sweep_init_tp[2] = {0, 0};
+    int grid_sweep_tp[2] = {0, 0}, grid_sweep_init_tp[2] = {0, 0}, grid_sweep_tp_max[2] = {0, 0};
 
     pasc::SpgRun run;
     pasc::AdjointWork *adj = nullptr;  // allocated by the first adjoint call

@@ -103,3 +103,25 @@ def test_pads_stay_zero_and_buffers_untouched_outside(gpulib, oracle):
             st = p.spgqp_solve(opts)
             np.testing.assert_array_equal(p.get_gamma(), g_ref)
             assert st.fx == st_ref.fx
+
+
+def test_tuner_picks_kernel_and_grid(gpulib, oracle):
+    """With the kernel left to the tuner the first solve times both kernels over their grids
+    (gamma saved and restored around the timing runs): the solve then makes the same
+    iterations as with the chosen kernel pinned (objective within 1e-6), and the reported
+    grid is a multiple of the SM count or the kernel's full grid."""
+    T, K, eps2 = 2_000_003, 3, 10.0
+    data, theta, x0, b, coeff = _qp(T, K, eps2, 11, oracle)
+    opts = capi.spgqp_opts(maxit=60, stop_difff=0, m=10)
+    with Problem(T, K, eps2, precision=PASC_PREC_MIXED) as p:
+        p.set_data(data)
+        p.set_theta(theta)
+        p.set_gamma(x0)
+        p.update_b()
+        assert p.get_sweep_tuning()[0] == -1
+        st = p.spgqp_solve(opts)
+        v, blocks, ms = p.get_sweep_tuning()
+    assert v in (0, 1) and blocks >= 1 and ms >= 0.0, (v, blocks, ms)
+    st_pinned, _ = _solve(T, K, eps2, data, theta, x0, v, opts)
+    assert st.it == st_pinned.it == 60
+    assert abs(st.fx - st_pinned.fx) <= 1e-6 * abs(st_pinned.fx), (st.fx, st_pinned.fx)
