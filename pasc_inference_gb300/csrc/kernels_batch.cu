@@ -67,18 +67,21 @@ __device__ __forceinline__ bool batch_segment(TmaSmem<KB, BATCH_NT> &sm, const B
         if (tlo + 1 < thi) tma_issue<K>(sm, (j + 1) & 1, sc.xin, sc.data, (tlo + 1) * BATCH_W - TMA_HALO);
     }
     TileAcc acc;
+    TilePending<K> pend;
+    pend.valid = false;
     for (int tile = tlo; tile < thi; tile++, j++) {
         const int s = j & 1;
         const bool arrived = mbar_wait(&sm.bar[s], (parity >> s) & 1u);
-        if (!__syncthreads_and(arrived)) {
+        if (!tma_tile<K, KB, BATCH_NT, INIT>(sm, s, j, arrived, tile * BATCH_W - TMA_HALO, sc, acc, pend,
+                                             tile + 2 < thi ? (tile + 2) * BATCH_W - TMA_HALO : TMA_NO_REFILL)) {
             mbar_wait(&sm.bar[s], (parity >> s) & 1u);
             if (tile + 1 < thi) mbar_wait(&sm.bar[s ^ 1], (parity >> (s ^ 1)) & 1u);
             return false;
         }
         parity ^= 1u << s;
-        tma_tile<K, KB, BATCH_NT, INIT>(sm, s, tile * BATCH_W - TMA_HALO, sc, acc,
-                                        tile + 2 < thi ? (tile + 2) * BATCH_W - TMA_HALO : TMA_NO_REFILL);
     }
+    __syncthreads();
+    tma_flush_pending<K, KB, BATCH_NT, false, false, TMA_R>(sm, sc, acc, pend);  // the segment's last tile: its pair terms belong to this signal
 
     double v[4] = {acc.f.value(), (double)acc.dd, (double)acc.dAd, (double)acc.gd};
     block_sum<4>(v, sm.red);

@@ -34,8 +34,13 @@ struct TmaShape {
     static constexpr int NT = 512 / R;
 };
 
+// resident blocks per SM the register allocation is held to (0: the compiler's choice)
+#ifndef PASC_TMA_MIN_BLOCKS
+#define PASC_TMA_MIN_BLOCKS 0
+#endif
+
 template <int K, int NT, bool INIT, int MODE>
-__global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
+__global__ void __launch_bounds__(NT, PASC_TMA_MIN_BLOCKS) spg_sweep_tma_kernel(SweepArgs a)
 {
     constexpr bool BM = MODE == 1, TP = MODE == 2;
     constexpr int R = TmaShape<K>::R;
@@ -81,24 +86,29 @@ __global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
     }
 
     TileAcc acc;
+    TilePending<K> pend;
+    pend.valid = false;
     unsigned int parity = 0u;  // bit s: phase parity of stage s
     int j = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, j++) {
         const int s = j & 1;
         const bool arrived = mbar_wait(&sm.bar[s], (parity >> s) & 1u);
-        if (!__syncthreads_and(arrived)) {
-            // a bulk copy did not arrive in time: record it, wait (bounded) once more for the
-            // copies this block has in flight, and leave the tile loop
+        const int next2 = tile + 2 * (int)gridDim.x;
+        if (!tma_tile<K, K, NT, INIT, BM, TP, R>(sm, s, j, arrived, tile * W - TMA_HALO, sc, acc, pend,
+                                                 next2 < ntiles ? next2 * W - TMA_HALO : TMA_NO_REFILL)) {
+            // a bulk copy did not arrive in time (the tile's barrier voted on it, before any
+            // further copy was issued): record it, wait (bounded) once more for the copies this
+            // block has in flight, and leave the tile loop
             if (i == 0) atomicExch(&st->error, 1);
             mbar_wait(&sm.bar[s], (parity >> s) & 1u);
             if (tile + (int)gridDim.x < ntiles) mbar_wait(&sm.bar[s ^ 1], (parity >> (s ^ 1)) & 1u);
+            pend.valid = false;
             break;
         }
         parity ^= 1u << s;
-        const int next2 = tile + 2 * (int)gridDim.x;
-        tma_tile<K, K, NT, INIT, BM, TP, R>(sm, s, tile * W - TMA_HALO, sc, acc,
-                                            next2 < ntiles ? next2 * W - TMA_HALO : TMA_NO_REFILL);
     }
+    __syncthreads();
+    tma_flush_pending<K, K, NT, BM, TP, R>(sm, sc, acc, pend);  // the last tile's pair terms
 
     // block and grid reductions
     double v[4] = {acc.f.value(), (double)acc.dd, (double)acc.dAd, (double)acc.gd};

@@ -84,9 +84,10 @@ struct TmaSmem {
     alignas(16) float x[2][P * KB];  // gamma tile, two stages (stride K for K <= KB)
     alignas(16) float dat[2][BM ? P * KB : P];  // data tile (BM: b tile), two stages
     // x^{c+1} of each thread's first / last timestep and d_{c+2} of its first timestep (layout:
-    // nbr_idx)
-    float yl[NT * KB], yr[NT * KB];
-    float dl[NT * KB];
+    // nbr_idx), double buffered by tile parity: one block barrier per tile separates their
+    // writes from their reads (tma_tile_body)
+    float yl[2][NT * KB], yr[2][NT * KB];
+    float dl[2][NT * KB];
     double red[4 * (NT / 32)];
     unsigned long long bar[2];
     int job;                          // batched kernel: the work item this block took
@@ -118,6 +119,32 @@ struct TileAcc {
     float dd = 0.f, dAd = 0.f, gd = 0.f;
 };
 
+// The d'Ad term of the pair (last timestep of this thread, first timestep of the next thread)
+// of a tile, left for after the next block barrier (the next tile's, or the one that ends the
+// block's tiles) so that the tile needs no barrier between writing d_{c+2} and reading it.
+template <int K>
+struct TilePending {
+    float dlast[K];
+    int j;       // tile parity whose dl buffer holds the neighbour's value
+    bool valid;  // this thread owns the pair and both timesteps lie in the signal
+};
+
+// Adds the pending pair term; call after a block barrier that follows the tile's phase C.
+template <int K, int KB, int NT, bool BM, bool TP, int R>
+__device__ __forceinline__ void tma_flush_pending(const TmaSmem<KB, NT, BM, R> &sm, const TileScalars<K> &sc,
+                                                  TileAcc &acc, TilePending<K> &pend)
+{
+    if (pend.valid) {
+        const int ri = threadIdx.x + 1;  // owners are never the last thread
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const float df = sm.dl[pend.j & 1][nbr_idx<K, NT>(ri, k)] - pend.dlast[k];
+            acc.dAd = fmaf(TP ? df * sc.kw[k] : df, df, acc.dAd);
+        }
+    }
+    pend.valid = false;
+}
+
 // Thread 0: bring the tile starting at timestep t0 into stage s.
 template <int K, int KB, int NT, bool BM, int R>
 __device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM, R> &sm, int s, const float *xin, const float *data,
@@ -130,10 +157,15 @@ __device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM, R> &sm, int s, con
     bulk_g2s(sm.dat[s], data + (long)t0 * (BM ? K : 1), bytes_d, &sm.bar[s]);
 }
 
-// One tile whose stage s has arrived: phases A-D of the sweep.  After phase B (the stage's
-// last read: b values, when they come from the stage, are read into registers in phase A)
-// thread 0 refills stage s with the tile at refill_t0 unless it is TMA_NO_REFILL.  Contains
-// three __syncthreads(); all threads of the block must call it.
+// One tile (the block's j-th) in stage s: phases A-D of the sweep.  `arrived`: this thread saw
+// the stage's copy complete (its own bounded mbarrier wait).  The tile has ONE block barrier,
+// after phase B, which also votes on `arrived`: if any thread's wait gave up, every thread
+// returns false there (before any further copy is issued).  After the barrier thread 0 refills
+// stage s with the tile at refill_t0 unless it is TMA_NO_REFILL (phase A was the stage's last
+// reader), and the pending pair term of the block's previous tile is added.  The neighbour
+// arrays are double buffered by j: a tile writes its parity's buffers before (yl, yr) or after
+// (dl) its barrier and they are read after that barrier, while the next tile writes the other
+// parity.  All threads of the block must call it.
 //
 // The FEM-H1 row is formed from shared neighbour differences: with D_j = x_{tb+j} -
 // x_{tb+j-1} (zero when the pair crosses an end of the signal, t_j <= 0 or t_j > T-1),
@@ -143,9 +175,11 @@ __device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM, R> &sm, int s, con
 // (all but the first and last of a signal) run without them.  TP: theta in the penalty, the
 // operator of cluster k is scaled by sc.kw[k] (and so is its share of d'Ad).
 template <int K, int KB, int NT, bool INIT, bool BM, bool EDGE, bool TP = false, int R = TMA_R>
-__device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s, int t0, const TileScalars<K> &sc,
-                                              TileAcc &acc, int refill_t0)
+__device__ __forceinline__ bool tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s, int j, bool arrived, int t0,
+                                              const TileScalars<K> &sc, TileAcc &acc, TilePending<K> &pend,
+                                              int refill_t0)
 {
+    const int jb = j & 1;
     constexpr int HT = TMA_HALO / R;  // halo threads at each end of the tile
     const int i = threadIdx.x;
     const int li = i > 0 ? i - 1 : i, ri = i < NT - 1 ? i + 1 : i;  // clamped neighbours
@@ -312,16 +346,18 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
     }
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        sm.yl[nbr_idx<K, NT>(i, k)] = x1[0][k];
-        sm.yr[nbr_idx<K, NT>(i, k)] = x1[R - 1][k];
+        sm.yl[jb][nbr_idx<K, NT>(i, k)] = x1[0][k];
+        sm.yr[jb][nbr_idx<K, NT>(i, k)] = x1[R - 1][k];
     }
-    __syncthreads();
+    if (!__syncthreads_and(arrived)) return false;
 
     // the stage is free (phase A was its last reader): refill it
     if (i == 0 && refill_t0 != TMA_NO_REFILL) {
         fence_proxy_async_smem();
         tma_issue<K>(sm, s, sc.xin, sc.data, refill_t0);
     }
+    // the previous tile's d_{c+2} was written before this barrier
+    tma_flush_pending<K, KB, NT, BM, TP, R>(sm, sc, acc, pend);
 
     // phase C: g^{c+1}, objective, d_{c+2}
     float g1[R][K], d1[R][K];
@@ -330,10 +366,10 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
 #pragma unroll
         for (int k = 0; k < K; k++) {
             float E[R + 1];
-            E[0] = x1[0][k] - sm.yr[nbr_idx<K, NT>(li, k)];
+            E[0] = x1[0][k] - sm.yr[jb][nbr_idx<K, NT>(li, k)];
 #pragma unroll
             for (int r = 1; r < R; r++) E[r] = x1[r][k] - x1[r - 1][k];
-            E[R] = sm.yl[nbr_idx<K, NT>(ri, k)] - x1[R - 1][k];
+            E[R] = sm.yl[jb][nbr_idx<K, NT>(ri, k)] - x1[R - 1][k];
 #pragma unroll
             for (int j = 0; j <= R; j++) E[j] = dm[j] ? E[j] : 0.f;
 #pragma unroll
@@ -353,23 +389,26 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
         }
     }
 #pragma unroll
-    for (int k = 0; k < K; k++) sm.dl[nbr_idx<K, NT>(i, k)] = d1[0][k];
-    __syncthreads();
+    for (int k = 0; k < K; k++) sm.dl[jb][nbr_idx<K, NT>(i, k)] = d1[0][k];
 
-    // phase D: dots of d_{c+2} and the store of x^{c+1}
+    // phase D: dots of d_{c+2} and the store of x^{c+1}; the pair with the next thread's first
+    // timestep waits for the next barrier (TilePending)
     if (owner) {
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const float dnext = sm.dl[nbr_idx<K, NT>(ri, k)];
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 acc.dd = fmaf(d1[r][k], d1[r][k], acc.dd);
                 acc.gd = fmaf(g1[r][k], d1[r][k], acc.gd);
-                const float nb = r == R - 1 ? dnext : d1[r < R - 1 ? r + 1 : R - 1][k];
-                const float df = dm[r + 1] ? nb - d1[r][k] : 0.f;  // pair (t_r, t_r + 1) inside
-                acc.dAd = fmaf(TP ? df * sc.kw[k] : df, df, acc.dAd);
+                if (r < R - 1) {
+                    const float df = dm[r + 1] ? d1[r + 1][k] - d1[r][k] : 0.f;  // pair (t_r, t_r + 1) inside
+                    acc.dAd = fmaf(TP ? df * sc.kw[k] : df, df, acc.dAd);
+                }
             }
+            pend.dlast[k] = d1[R - 1][k];
         }
+        pend.valid = dm[R];
+        pend.j = j;
         if (!EDGE || in[R - 1]) {
             // all R timesteps inside: 16-byte stores when R*K is a multiple of 4 (tb*K*4 bytes is
             // then a multiple of 16: tb is a multiple of R), 8-byte stores otherwise
@@ -397,17 +436,17 @@ __device__ __forceinline__ void tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
                     for (int k = 0; k < K; k++) sc.xout[(long)(tb + r) * K + k] = x1[r][k];
         }
     }
-    // the neighbour arrays are rewritten by the next tile's phase B only after its own
-    // __syncthreads-separated phase A, so no barrier is needed here
+    return true;
 }
 
 template <int K, int KB, int NT, bool INIT, bool BM = false, bool TP = false, int R = TMA_R>
-__device__ __forceinline__ void tma_tile(TmaSmem<KB, NT, BM, R> &sm, int s, int t0, const TileScalars<K> &sc,
-                                         TileAcc &acc, int refill_t0)
+__device__ __forceinline__ bool tma_tile(TmaSmem<KB, NT, BM, R> &sm, int s, int j, bool arrived, int t0,
+                                         const TileScalars<K> &sc, TileAcc &acc, TilePending<K> &pend, int refill_t0)
 {
     constexpr int P = NT * R;
-    if (t0 >= 1 && t0 + P <= sc.T - 1) tma_tile_body<K, KB, NT, INIT, BM, false, TP, R>(sm, s, t0, sc, acc, refill_t0);
-    else tma_tile_body<K, KB, NT, INIT, BM, true, TP, R>(sm, s, t0, sc, acc, refill_t0);
+    if (t0 >= 1 && t0 + P <= sc.T - 1)
+        return tma_tile_body<K, KB, NT, INIT, BM, false, TP, R>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
+    return tma_tile_body<K, KB, NT, INIT, BM, true, TP, R>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
 }
 
 }  // namespace pasc
