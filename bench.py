@@ -13,24 +13,29 @@ timed region so that no step is skipped.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Besides the headline line it measures, on rank 0:
-  e2e        the same metric through the public API with host buffers: set_data, set_gamma,
-             set_theta, spgqp_solve (reference stopping rule, eps 1e-6, m 10), get_gamma, get_fx;
-             host<->device copies inside the timed region.
-  tts        time to an objective within 1e-6 relative of the converged FP64 objective, for the
-             mixed path and for the plain FP64 GPU path on the same problem.
+  tts        for every epssqr of the sweep {1, 10, 100, 1000}: time to an objective within 1e-6
+             relative of the FP64 optimum, for the mixed path and for the plain FP64 GPU path
+             on the same problem; the FP64 end point certified by its Frank-Wolfe gap under the
+             oracle's operator, and the mixed end point's objective and gamma errors against it.
+  e2e        the same metric through the public API with host buffers in page-locked memory
+             (pasc_gb300_host_alloc): set_data, set_gamma, permute, set_theta, update_b,
+             spgqp_solve (the reference's default stop, |f - f_old| < 1e-9, m 10), get_gamma,
+             get_fx; host<->device copies inside the timed region.  FP32 host buffers (the
+             mixed path's device format) for the line's value, FP64 host buffers beside it.
   roofline   the sweep kernel's algorithmic bytes (8*K*T + 4*T per iteration: gamma read and
              written in FP32, the data read once) over its CUDA-event time, against the
              measured HBM copy bandwidth.
   cpu_baseline  the FP64 CPU oracle (a port of the reference's CPU path) on all host cores, and
-             on one (`one_thread`).
+             on one (`one_thread`), and its time to 1e-6 relative objective.
   batched    the 256-signal uneven workload (T log-uniform in [1e3, 1e6], K in 2..5, epssqr
              log-uniform in [1, 1000]): every signal's TSSolver (SPG eps 1e-6, m 10; outer loop
-             to 1e-6 relative change of L) solved by one batch handle (one launch per SPG
-             iteration for all running signals) and, for comparison, one signal at a time with
-             the plain FP64 GPU path and with the single-signal mixed path; plus the batch
-             sweep's HBM throughput with all 256 signals running.  With --batched-qp also the
-             gamma-step QP of every signal at fixed theta (its true levels; stop |f - f_old| <
-             1e-9) by the batch and by the plain FP64 path, objectives compared signal by signal.
+             to 1e-6 relative change of L) solved by one batch handle (one CUDA graph launch
+             whose conditional nodes loop on the device) and, for comparison, one signal at a
+             time with the plain FP64 GPU path and with the single-signal mixed path; the
+             batch sweep's HBM throughput with all 256 signals running; and the gamma-step QP
+             of every signal at fixed theta by the batch and by the plain FP64 path under the
+             same stop rule, objectives compared signal by signal and with the best objective
+             any run reached (--no-batched-qp skips it).
   adjoint    derivatives through the converged gamma step at T = 1e6, K = 3 (the benchmark
              signal generator, clean copy kept): dloss/d epssqr of the reconstruction MSE from
              the adjoint, checked against central differences (1e-4 relative) through FP64 GPU
@@ -138,9 +143,9 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-multichannel", action="store_true")
     ap.add_argument("--no-image", action="store_true")
-    ap.add_argument("--batched-qp", action="store_true",
-                    help="also solve every batched signal's gamma-step QP at fixed theta by the batch and by "
-                         "the plain FP64 path one signal at a time (adds about two minutes)")
+    ap.add_argument("--no-batched-qp", action="store_true",
+                    help="skip the batched gamma-step QP at fixed theta (the plain FP64 path one signal at a "
+                         "time takes about two minutes of it)")
     ap.add_argument("--variant", type=int, default=-1, choices=[-1, 0, 1],
                     help="sweep kernel: -1 chosen by timing (default), 0 one timestep per thread, "
                          "1 bulk-copy tiles (pin it when profiling: a profiler distorts the timing)")
@@ -388,7 +393,7 @@ def main():
     if info.rank == 0 and not args.no_e2e:
         result["e2e"] = measure_e2e(sig, theta, args.eps2, dev, fstar)
     if info.rank == 0 and not args.no_batched:
-        result["batched"] = measure_batched(dev, peak, qp=args.batched_qp)
+        result["batched"] = measure_batched(dev, peak, qp=not args.no_batched_qp)
     if info.rank == 0 and not args.no_multichannel:
         result["multichannel"] = measure_multichannel(dev, peak)
     if info.rank == 0 and not args.no_adjoint:
@@ -771,25 +776,34 @@ def measure_adjoint(dev, peak, eps0=300.0):
     return res
 
 
-def measure_batched(dev, peak, qp=False):
+def measure_batched(dev, peak, qp=True):
+    """The 256-signal uneven workload through one batch handle: the sweep's HBM throughput with
+    every signal running, the TSSolver of every signal (device-driven loop; and the host-driven
+    loop for comparison) against one signal at a time on the plain FP64 GPU path and on the
+    single-signal mixed path, and the gamma-step QP at fixed theta (batch vs plain FP64 one at a
+    time, the same stop rule; and the batch alone driven much further, to find how far each
+    stop leaves every signal from its optimum)."""
     from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Batch, Problem, capi, datagen
     inst = datagen.batched()
     n = len(inst)
     ts = capi.ts_opts(eps=1e-6, relative=1)
     spg = capi.spgqp_opts(m=10, eps=1e-6)
 
-    def load_batch(theta0):
+    def load_batch(theta0, device_loop=True):
         bt = Batch([s.T for s in inst], [s.K for s in inst], [s.epssqr for s in inst], device=dev)
+        bt.set_loop(device_loop, 4)
         for i, s in enumerate(inst):
             bt.set_data(i, s.data)
             bt.set_gamma(i, s.gamma0)
             bt.set_theta(i, theta0(s))
         return bt
 
-    # sweep throughput with every signal running: 200 iterations, stopping tests off
+    # sweep throughput with every signal running (stopping tests off), after the tuner chose
+    # the segment size on the batch's first solve
     B_sweep = float(sum((8 * s.K + 4) * s.T for s in inst))
     with load_batch(lambda s: np.linspace(0.0, 4.0, s.K)) as bt:
         bt.spgqp_solve(capi.spgqp_opts(maxit=20, stop_difff=0))
+        seg_tiles, tune_ms = bt.get_segment_tiles()
         for i, s in enumerate(inst):
             bt.set_gamma(i, s.gamma0)
         st = bt.spgqp_solve(capi.spgqp_opts(maxit=200, stop_difff=0))
@@ -797,15 +811,16 @@ def measure_batched(dev, peak, qp=False):
         sweep_s = st[0].time_s / (200 + 1)
     gbs = B_sweep / sweep_s / 1e9
 
-    walls, L_b = [], None
-    for rep in range(2):
-        with load_batch(lambda s: np.zeros(s.K)) as bt:
+    walls, L_b = {True: [], False: []}, None
+    for device_loop in (True, True, False):
+        with load_batch(lambda s: np.zeros(s.K), device_loop) as bt:
             t0 = time.perf_counter()
             st = bt.ts_solve(ts, spg)
-            walls.append(time.perf_counter() - t0)
-            L_b = np.array([x.L for x in st])
-            spg_it_b = int(sum(x.spg_it_sum for x in st))
-            launches_b = st[0].kernel_launches
+            walls[device_loop].append(time.perf_counter() - t0)
+            if device_loop:
+                L_b = np.array([x.L for x in st])
+                spg_it_b = int(sum(x.spg_it_sum for x in st))
+                launches_b = st[0].kernel_launches
     seq = {}
     for name, prec in (("fp64_plain", PASC_PREC_FP64), ("mixed_single", PASC_PREC_MIXED)):
         tot, its, Ls = 0.0, 0, []
@@ -820,9 +835,8 @@ def measure_batched(dev, peak, qp=False):
                 its += r.spg_it_sum
                 Ls.append(r.L)
         seq[name] = (tot, its, np.array(Ls))
-    wall_b = min(walls)
+    wall_b = min(walls[True])
     rel = np.abs(L_b - seq["fp64_plain"][2]) / np.abs(seq["fp64_plain"][2])
-
     # The alternating loop starts from random gamma: its first theta step gives nearly equal
     # levels, and rounding-level differences in the first gamma steps decide which local
     # minimum a signal ends in, so L is compared here only as a distribution.
@@ -831,7 +845,9 @@ def measure_batched(dev, peak, qp=False):
         "workload": "256 signals, T log-U[1e3,1e6], K U{2..5}, epssqr log-U[1,1000], sorted levels U[0,4], "
                     "segments U[T/50,T/5], sigma U[0.2,1]; TSSolver SPG eps 1e-6 m 10, outer 1e-6 relative",
         "signals": n, "timesteps": int(sum(s.T for s in inst)),
-        "batch_s": wall_b, "batch_spg_it_sum": spg_it_b, "batch_gpu_launches": launches_b,
+        "segment_tiles_tuned": seg_tiles, "tuner_ms_per_candidate_2_4_8_16_32": [float(x) for x in tune_ms],
+        "batch_s": wall_b, "batch_host_loop_s": min(walls[False]), "batch_spg_it_sum": spg_it_b,
+        "batch_gpu_launches": launches_b, "batch_loop": "one CUDA graph launch (conditional WHILE nodes)",
         "fp64_plain_sequential_s": seq["fp64_plain"][0], "fp64_plain_spg_it_sum": int(seq["fp64_plain"][1]),
         "mixed_single_sequential_s": seq["mixed_single"][0],
         "mixed_single_spg_it_sum": int(seq["mixed_single"][1]),
@@ -847,24 +863,33 @@ def measure_batched(dev, peak, qp=False):
     }
 
 
+def _dist(f, fbest):
+    r = (np.asarray(f) - fbest) / np.abs(fbest)
+    return {"median": float(np.median(r)), "max": float(np.max(r)), "frac_within_1e-6": float(np.mean(r <= 1e-6)),
+            "frac_within_1e-5": float(np.mean(r <= 1e-5))}
+
+
 def measure_batched_qp(inst, load_batch, dev):
     """The gamma-step QP of every batched signal at fixed theta (its sorted true levels) from
-    the same random start, a convex problem, solved by the batch and by the plain FP64 path one
-    signal at a time under the reference's default stop rule (|f - f_old| < 1e-9, GLL m 10);
-    objectives compared signal by signal.  The rule ends each path where one non-monotone step
-    happens to change f by less than 1e-9, so on slowly converging signals the two stop at
-    different distances from the optimum."""
+    the same random start, a convex problem: the batch and the plain FP64 path one signal at a
+    time under the same stop rule (the reference's default, |f - f_old| < 1e-9, GLL m 10, maxit
+    20000), and the batch again with |f - f_old| < 1e-14 and maxit 200000.  f_best per signal is
+    the lowest objective any of the three runs reached; each run's distance from it (relative)
+    shows where its stop left the signals, and the two paths under the same rule are compared
+    signal by signal."""
     from pasc_inference_gb300 import PASC_PREC_FP64, Problem, capi
     qp_spg = capi.spgqp_opts(m=10, eps=1e-9, maxit=20000)
-    qwalls = []
-    for rep in range(2):
-        with load_batch(lambda s: s.levels) as bt:
-            t0 = time.perf_counter()
-            qst = bt.spgqp_solve(qp_spg)
-            qwalls.append(time.perf_counter() - t0)
-    f_b = np.array([x.fx for x in qst])
-    it_qb = int(sum(x.it for x in qst))
-    status_qb = [x.status for x in qst]
+    tight = capi.spgqp_opts(m=10, eps=1e-14, maxit=200000)
+    runs = {}
+    for name, o in (("batch", qp_spg), ("batch_tight", tight)):
+        walls = []
+        for rep in range(2 if name == "batch" else 1):
+            with load_batch(lambda s: s.levels) as bt:
+                t0 = time.perf_counter()
+                qst = bt.spgqp_solve(o)
+                walls.append(time.perf_counter() - t0)
+        runs[name] = (min(walls), np.array([x.fx for x in qst]), int(sum(x.it for x in qst)),
+                      int(sum(1 for x in qst if x.status == capi.PASC_SPG_CONVERGED)))
     q64_s, q64_it, f_64, conv64 = 0.0, 0, [], 0
     for s in inst:
         with Problem(s.T, s.K, s.epssqr, precision=PASC_PREC_FP64, device=dev) as p:
@@ -879,15 +904,20 @@ def measure_batched_qp(inst, load_batch, dev):
             conv64 += r.status == capi.PASC_SPG_CONVERGED
             f_64.append(r.fx)
     f_64 = np.array(f_64)
-    qrel = np.abs(f_b - f_64) / np.abs(f_64)
-    qp = {"theta": "sorted true levels of each signal, fixed", "stop": "|f - f_old| < 1e-9, GLL m 10, maxit 20000",
-          "batch_s": min(qwalls), "batch_spg_it_sum": it_qb,
-          "batch_converged": int(sum(1 for x in status_qb if x == capi.PASC_SPG_CONVERGED)),
-          "fp64_plain_sequential_s": q64_s, "fp64_plain_spg_it_sum": q64_it, "fp64_converged": int(conv64),
-          "speedup_vs_fp64_plain_sequential": q64_s / min(qwalls),
-          "f_rel_diff_vs_fp64": {"median": float(np.median(qrel)), "max": float(np.max(qrel)),
-                                 "frac_within_1e-6": float(np.mean(qrel <= 1e-6))}}
-    return qp
+    fbest = np.minimum(np.minimum(runs["batch"][1], runs["batch_tight"][1]), f_64)
+    qrel = np.abs(runs["batch"][1] - f_64) / np.abs(f_64)
+    return {"theta": "sorted true levels of each signal, fixed",
+            "stop": "|f - f_old| < 1e-9, GLL m 10, maxit 20000 (both paths)",
+            "batch_s": runs["batch"][0], "batch_spg_it_sum": runs["batch"][2], "batch_converged": runs["batch"][3],
+            "fp64_plain_sequential_s": q64_s, "fp64_plain_spg_it_sum": q64_it, "fp64_converged": int(conv64),
+            "speedup_vs_fp64_plain_sequential": q64_s / runs["batch"][0],
+            "f_rel_diff_batch_vs_fp64_same_rule": {"median": float(np.median(qrel)), "max": float(np.max(qrel)),
+                                                    "frac_within_1e-6": float(np.mean(qrel <= 1e-6)),
+                                                    "frac_batch_lower": float(np.mean(runs["batch"][1] < f_64))},
+            "distance_from_f_best": {"batch": _dist(runs["batch"][1], fbest), "fp64_plain": _dist(f_64, fbest),
+                                     "batch_tight": _dist(runs["batch_tight"][1], fbest)},
+            "batch_tight": {"stop": "|f - f_old| < 1e-14, maxit 200000", "s": runs["batch_tight"][0],
+                            "spg_it_sum": runs["batch_tight"][2], "converged": runs["batch_tight"][3]}}
 
 
 if __name__ == "__main__":
