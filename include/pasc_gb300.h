@@ -390,6 +390,38 @@ int pasc_gb300_fem_h1_matmult_f64(const double *x_dev, double *y_dev, long T, in
 int pasc_gb300_fem_h1_matmult_f32(const float *x_dev, float *y_dev, long T, int K,
                                   float coeff, void *stream);
 
+/* The vector level of the reference's backend interface on FP64 device buffers, for a
+ * backend that keeps the reference's own generic solvers and gives them device vectors
+ * (include/pasc/gb300_backend.hpp): GeneralVector<VectorBase> (include/general/algebra/
+ * vector/generalvector.h:58-106) over the PETSc operations its GPU backend calls
+ * (include/external/petscvector/algebra/vector/petscvector.h: VecDuplicate/VecCreate ->
+ * vec_alloc, VecCopy -> vec_copy, VecAXPY -> vec_axpy, VecWAXPY -> vec_waxpy, VecScale ->
+ * vec_scale, VecDot -> vec_dot; VecNorm is sqrt(vec_dot(x, x))).  FP64, each element in the
+ * reference's operation order; vec_dot is a deterministic block tree (its result waits for the
+ * stream); vec_alloc returns zeroed memory on `device` (which it makes current).  Operations
+ * take the device of their buffers as current. */
+int pasc_gb300_vec_alloc(double **v_dev, long n, int device);
+int pasc_gb300_vec_free(double *v_dev);
+int pasc_gb300_vec_set(double *v_dev, const double *host, long n);
+int pasc_gb300_vec_get(const double *v_dev, double *host, long n);
+int pasc_gb300_vec_copy(double *y_dev, const double *x_dev, long n, void *stream);                 /* y = x */
+int pasc_gb300_vec_axpy(double *y_dev, double a, const double *x_dev, long n, void *stream);       /* y += a x */
+int pasc_gb300_vec_waxpy(double *w_dev, double a, const double *x_dev, const double *y_dev, long n,
+                         void *stream);                                                            /* w = a x + y */
+int pasc_gb300_vec_scale(double *x_dev, double a, long n, void *stream);                          /* x = a x */
+int pasc_gb300_vec_dot(const double *x_dev, const double *y_dev, long n, double *out, void *stream);
+/* Decomposition::permute_TRK (src/petscvector/common/decomposition.cpp:266-356, R = 1):
+ * blocked k*T + t -> interleaved t*K + k, out of place. */
+int pasc_gb300_permute_f64(const double *src_dev, double *dst_dev, long T, int K, void *stream);
+/* GraphH1FEMModel::updatebeforesolve_gammasolver (src/petscvector/model/graphh1fem.cpp:237-289)
+ * on device buffers: b_tk = bscale (x_t - theta_k)^2 (theta_dev: K values on the device). */
+int pasc_gb300_residual_f64(const double *data_dev, const double *theta_dev, double *b_dev, long T, int K,
+                            double bscale, void *stream);
+/* GraphH1FEMModel::updatebeforesolve_thetasolver (graphh1fem.cpp:347-380) on device buffers:
+ * theta_k = sum_t gamma_tk x_t / sum_t gamma_tk; waits for the result. */
+int pasc_gb300_theta_update_f64(const double *gamma_dev, const double *data_dev, double *theta_dev, long T, int K,
+                                void *stream);
+
 /* Fem::reduce_gamma / prolongate_gamma (src/petscvector/common/fem.cpp:32-190,
  * femhat.cpp:27-215) on device buffers: g1 T1*K fine values, g2 T2*K coarse values
  * (interleaved t*K + k), fem_type 0 FEM-SUM or 1 FEM-HAT (T2 >= 2).  The reference's CUDA

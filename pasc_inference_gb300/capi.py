@@ -136,6 +136,19 @@ PROTOTYPES = {
                                                 C.c_void_p]),
     "pasc_gb300_theta_update_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p,
                                                   C.c_void_p]),
+    "pasc_gb300_vec_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_long, C.c_int]),
+    "pasc_gb300_vec_free": (C.c_int, [C.c_void_p]),
+    "pasc_gb300_vec_set": (C.c_int, [C.c_void_p, _dp, C.c_long]),
+    "pasc_gb300_vec_get": (C.c_int, [C.c_void_p, _dp, C.c_long]),
+    "pasc_gb300_vec_copy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_void_p]),
+    "pasc_gb300_vec_axpy": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_long, C.c_void_p]),
+    "pasc_gb300_vec_waxpy": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_long, C.c_void_p]),
+    "pasc_gb300_vec_scale": (C.c_int, [C.c_void_p, C.c_double, C.c_long, C.c_void_p]),
+    "pasc_gb300_vec_dot": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.POINTER(C.c_double), C.c_void_p]),
+    "pasc_gb300_permute_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p]),
+    "pasc_gb300_residual_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_double,
+                                          C.c_void_p]),
+    "pasc_gb300_theta_update_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p]),
     "pasc_gb300_adjoint_default_opts": (None, [C.POINTER(AdjointOpts)]),
     "pasc_gb300_recon_mse": (C.c_int, [_h, _dp, C.POINTER(C.c_double)]),
     "pasc_gb300_adjoint": (C.c_int, [_h, C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(C.c_double), C.c_void_p,

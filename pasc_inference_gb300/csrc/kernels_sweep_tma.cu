@@ -34,13 +34,8 @@ struct TmaShape {
     static constexpr int NT = 512 / R;
 };
 
-// resident blocks per SM the register allocation is held to (0: the compiler's choice)
-#ifndef PASC_TMA_MIN_BLOCKS
-#define PASC_TMA_MIN_BLOCKS 0
-#endif
-
 template <int K, int NT, bool INIT, int MODE>
-__global__ void __launch_bounds__(NT, PASC_TMA_MIN_BLOCKS) spg_sweep_tma_kernel(SweepArgs a)
+__global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
 {
     constexpr bool BM = MODE == 1, TP = MODE == 2;
     constexpr int R = TmaShape<K>::R;

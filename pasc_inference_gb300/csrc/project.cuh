@@ -134,68 +134,6 @@ __device__ __forceinline__ void project_reg(float (&x)[K])
 }
 
 // ---------------------------------------------------------------------------------------
-// FP32 on pairs of timesteps: x[k] holds cluster k of two timesteps (.x, .y).  The same
-// operations in the same order as project_reg, element for element (identical results); the
-// sums, candidates and shifts run as packed two-wide FP32 instructions (sm_100 family), the
-// comparisons per timestep.
-// ---------------------------------------------------------------------------------------
-__device__ __forceinline__ float2 pk_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 pk_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-// a - b, rounded once (b * -1 is exact)
-__device__ __forceinline__ float2 pk_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
-__device__ __forceinline__ float2 pk_splat(float v) { return make_float2(v, v); }
-
-template <int K>
-__device__ __forceinline__ void project_reg2(float2 (&x)[K])
-{
-    const float2 m1 = pk_splat(-1.f);
-    float2 sum = x[0];
-#pragma unroll
-    for (int k = 1; k < K; k++) sum = pk_add(sum, x[k]);
-    float2 tau;
-    if (K == 1) {
-        tau = pk_add(sum, m1);
-    } else if (K == 2) {
-        const float2 mx = make_float2(fmaxf(x[0].x, x[1].x), fmaxf(x[0].y, x[1].y));
-        const float2 c1 = pk_add(mx, m1), c2 = pk_mul(pk_add(sum, m1), pk_splat(0.5f));
-        tau = make_float2(fmaxf(c1.x, c2.x), fmaxf(c1.y, c2.y));
-    } else if (K == 3) {
-        const float2 mx = make_float2(fmaxf(fmaxf(x[0].x, x[1].x), x[2].x), fmaxf(fmaxf(x[0].y, x[1].y), x[2].y));
-        const float2 mn = make_float2(fminf(fminf(x[0].x, x[1].x), x[2].x), fminf(fminf(x[0].y, x[1].y), x[2].y));
-        const float2 c1 = pk_add(mx, m1);
-        const float2 c2 = pk_mul(pk_add(pk_sub(sum, mn), m1), pk_splat(0.5f));
-        const float2 c3 = pk_mul(pk_add(sum, m1), pk_splat(1.f / 3.f));
-        tau = make_float2(fmaxf(fmaxf(c1.x, c2.x), c3.x), fmaxf(fmaxf(c1.y, c2.y), c3.y));
-    } else {
-        float sx[K], sy[K];
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            sx[k] = x[k].x;
-            sy[k] = x[k].y;
-        }
-        sort_net<K>(sx);
-        sort_net<K>(sy);
-        float2 acc = pk_splat(0.f);
-        tau = pk_splat(-FLT_MAX);
-#pragma unroll
-        for (int i = K - 1; i >= 0; i--) {
-            acc = pk_add(acc, make_float2(sx[i], sy[i]));
-            const float2 c = pk_mul(pk_add(acc, m1), pk_splat(1.f / (float)(K - i)));
-            tau = make_float2(fmaxf(tau.x, c.x), fmaxf(tau.y, c.y));
-        }
-    }
-    // a block holding a NaN gets a NaN threshold and so becomes all zeros (as project_reg)
-    if (sum.x != sum.x) tau.x = sum.x;
-    if (sum.y != sum.y) tau.y = sum.y;
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-        const float2 v = pk_sub(x[k], tau);
-        x[k] = make_float2(fmaxf(v.x, 0.f), fmaxf(v.y, 0.f));
-    }
-}
-
-// ---------------------------------------------------------------------------------------
 // FP32, G lanes per timestep (G a power of two, 2..32), lane k of the group holds x_k for
 // k < K.  All lanes of the warp must call it (shuffles use the full mask); lanes whose group
 // has no valid timestep pass valid = false.

@@ -20,11 +20,6 @@ constexpr int TMA_R = 4;          // timesteps per thread
 constexpr int TMA_HALO = 4;       // halo timesteps on each side of a tile
 constexpr unsigned int TMA_WAIT_LIMIT = 1u << 24;  // try_wait rounds before giving up
 constexpr int TMA_NO_REFILL = -(1 << 30);
-// R = 4 tiles run the packed two-wide FP32 form of the tile (tma_tile_body_pk)
-#ifndef PASC_TMA_PACKED
-#define PASC_TMA_PACKED 1
-#endif
-constexpr bool TMA_PACKED = PASC_TMA_PACKED != 0;
 
 __device__ __forceinline__ unsigned int smem_addr(const void *p)
 {
@@ -444,318 +439,14 @@ __device__ __forceinline__ bool tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
     return true;
 }
 
-// The same tile for R = 4 with the arithmetic on pairs of timesteps: packed two-wide FP32
-// instructions (FADD2/FMUL2/FFMA2 of the sm_100 family) carry the elementwise operations of
-// phases A-D, and project_reg2 the projections.  Every value is computed by the same
-// operations in the same order as tma_tile_body (the packed instructions round each lane as
-// the scalar ones do); only the per-thread FP32 partial sums of f, d'd, g'd and d'Ad are kept
-// in two lanes and added at the end of the tile.  Pair A holds timesteps (0, 2) of the thread
-// and pair B timesteps (1, 3), so that the stencil's neighbour differences of one pair come
-// from the other pair without moving values between lanes.
-template <int K, int KB, int NT, bool INIT, bool BM, bool EDGE, bool TP = false>
-__device__ __forceinline__ bool tma_tile_body_pk(TmaSmem<KB, NT, BM, 4> &sm, int s, int j, bool arrived, int t0,
-                                                 const TileScalars<K> &sc, TileAcc &acc, TilePending<K> &pend,
-                                                 int refill_t0)
-{
-    constexpr int R = 4;
-    constexpr int HT = TMA_HALO / R;
-    const int jb = j & 1;
-    const int i = threadIdx.x;
-    const int li = i > 0 ? i - 1 : i, ri = i < NT - 1 ? i + 1 : i;
-    const bool owner = i >= HT && i <= NT - 1 - HT;
-    const int T = sc.T;
-    const int tb = t0 + i * R;
-    const float c2 = 2.f * sc.coeff;
-
-    bool in[R], dm[R + 1];
-#pragma unroll
-    for (int r = 0; r < R; r++) in[r] = EDGE ? (unsigned)(tb + r) < (unsigned)T : true;
-#pragma unroll
-    for (int q = 0; q <= R; q++) dm[q] = EDGE ? (unsigned)(tb + q - 1) < (unsigned)(T - 1) : true;
-
-    // element (r, k) lives in pair r & 1, lane r >> 1
-    auto get = [](const float2 &v, int r) { return (r >> 1) ? v.y : v.x; };
-    auto put = [](float2 &v, int r, float x) {
-        if (r >> 1) v.y = x;
-        else v.x = x;
-    };
-
-    // phase A: x^c and -b of the thread's 4 timesteps, the neighbours' edge values
-    float2 xc[2][K], nb[2][K];
-    float xlft[K], xrgt[K];
-    {
-        float xs[R * K];
-        if constexpr ((R * K) % 4 == 0) {
-            const float4 *src = reinterpret_cast<const float4 *>(&sm.x[s][i * R * K]);
-#pragma unroll
-            for (int q = 0; q < R * K / 4; q++) {
-                const float4 v = src[q];
-                xs[4 * q] = v.x; xs[4 * q + 1] = v.y; xs[4 * q + 2] = v.z; xs[4 * q + 3] = v.w;
-            }
-        } else {
-            const float2 *src = reinterpret_cast<const float2 *>(&sm.x[s][i * R * K]);
-#pragma unroll
-            for (int q = 0; q < R * K / 2; q++) {
-                const float2 v = src[q];
-                xs[2 * q] = v.x; xs[2 * q + 1] = v.y;
-            }
-        }
-#pragma unroll
-        for (int r = 0; r < R; r++)
-#pragma unroll
-            for (int k = 0; k < K; k++) put(xc[r & 1][k], r, xs[r * K + k]);
-        const float *nl = &sm.x[s][(li * R + R - 1) * K], *nr = &sm.x[s][(ri * R) * K];
-        if constexpr (K % 4 == 0) {
-#pragma unroll
-            for (int q = 0; q < K / 4; q++) {
-                const float4 a = reinterpret_cast<const float4 *>(nl)[q];
-                const float4 c = reinterpret_cast<const float4 *>(nr)[q];
-                xlft[4 * q] = a.x; xlft[4 * q + 1] = a.y; xlft[4 * q + 2] = a.z; xlft[4 * q + 3] = a.w;
-                xrgt[4 * q] = c.x; xrgt[4 * q + 1] = c.y; xrgt[4 * q + 2] = c.z; xrgt[4 * q + 3] = c.w;
-            }
-        } else if constexpr (K % 2 == 0 && K >= 4) {
-#pragma unroll
-            for (int q = 0; q < K / 2; q++) {
-                const float2 a = reinterpret_cast<const float2 *>(nl)[q];
-                const float2 c = reinterpret_cast<const float2 *>(nr)[q];
-                xlft[2 * q] = a.x; xlft[2 * q + 1] = a.y;
-                xrgt[2 * q] = c.x; xrgt[2 * q + 1] = c.y;
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < K; k++) {
-                xlft[k] = nl[k];
-                xrgt[k] = nr[k];
-            }
-        }
-        if (BM) {
-            float bs[R * K];
-            if constexpr ((R * K) % 4 == 0) {
-                const float4 *b4 = reinterpret_cast<const float4 *>(&sm.dat[s][i * R * K]);
-#pragma unroll
-                for (int q = 0; q < R * K / 4; q++) {
-                    const float4 v = b4[q];
-                    bs[4 * q] = v.x; bs[4 * q + 1] = v.y; bs[4 * q + 2] = v.z; bs[4 * q + 3] = v.w;
-                }
-            } else {
-                const float2 *b2 = reinterpret_cast<const float2 *>(&sm.dat[s][i * R * K]);
-#pragma unroll
-                for (int q = 0; q < R * K / 2; q++) {
-                    const float2 v = b2[q];
-                    bs[2 * q] = v.x; bs[2 * q + 1] = v.y;
-                }
-            }
-#pragma unroll
-            for (int r = 0; r < R; r++)
-#pragma unroll
-                for (int k = 0; k < K; k++) put(nb[r & 1][k], r, -bs[r * K + k]);
-        } else {
-            const float4 d4 = *reinterpret_cast<const float4 *>(&sm.dat[s][i * R]);
-            const float2 dA = make_float2(d4.x, d4.z), dB = make_float2(d4.y, d4.w);
-            const float2 nbs = pk_splat(-sc.bscale);
-#pragma unroll
-            for (int k = 0; k < K; k++) {
-                const float2 th = pk_splat(sc.theta[k]);
-                const float2 rA = pk_sub(dA, th), rB = pk_sub(dB, th);
-                nb[0][k] = pk_mul(nbs, pk_mul(rA, rA));  // -(bscale (rr rr)), exactly
-                nb[1][k] = pk_mul(nbs, pk_mul(rB, rB));
-            }
-        }
-    }
-    if (INIT) {
-        project_reg2<K>(xc[0]);
-        project_reg2<K>(xc[1]);
-        project_reg<K>(xlft);
-        project_reg<K>(xrgt);
-    }
-    if (EDGE) {
-#pragma unroll
-        for (int r = 0; r < R; r++)
-#pragma unroll
-            for (int k = 0; k < K; k++)
-                if (!in[r]) put(xc[r & 1][k], r, 0.f);
-        const bool inl = (unsigned)(tb - 1) < (unsigned)T, inr = (unsigned)(tb + R) < (unsigned)T;
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            xlft[k] = inl ? xlft[k] : 0.f;
-            xrgt[k] = inr ? xrgt[k] : 0.f;
-        }
-    }
-
-    // half rows of A_hat for the pairs from x and its neighbour values:
-    // LA = (D0 - D1, D2 - D3), LB = (D1 - D2, D3 - D4) with D_q = x_q - x_{q-1}
-    auto rows = [&](const float2 &a, const float2 &b, float lft, float rgt, float2 &LA, float2 &LB) {
-        float2 DB = pk_sub(b, a);                      // (D1, D3)
-        float2 DA = pk_sub(a, make_float2(lft, b.x));  // (D0, D2)
-        float D4 = rgt - b.y;
-        if (EDGE) {
-            DA.x = dm[0] ? DA.x : 0.f;
-            DB.x = dm[1] ? DB.x : 0.f;
-            DA.y = dm[2] ? DA.y : 0.f;
-            DB.y = dm[3] ? DB.y : 0.f;
-            D4 = dm[4] ? D4 : 0.f;
-        }
-        LA = pk_sub(DA, DB);
-        LB = pk_sub(DB, make_float2(DA.y, D4));
-    };
-
-    // phase B: x^{c+1}
-    float2 x1[2][K];
-    if (INIT) {
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            x1[0][k] = xc[0][k];
-            x1[1][k] = xc[1][k];
-        }
-    } else {
-        const float2 na0 = pk_splat(-sc.a0);
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            float2 LA, LB;
-            rows(xc[0][k], xc[1][k], xlft[k], xrgt[k], LA, LB);
-            const float2 ck = pk_splat(TP ? c2 * sc.kw[k] : c2);
-            const float2 gA = pk_fma(ck, LA, nb[0][k]), gB = pk_fma(ck, LB, nb[1][k]);
-            x1[0][k] = pk_fma(na0, gA, xc[0][k]);  // z before the projection
-            x1[1][k] = pk_fma(na0, gB, xc[1][k]);
-        }
-        project_reg2<K>(x1[0]);
-        project_reg2<K>(x1[1]);
-        const float2 bt = pk_splat(sc.beta);
-#pragma unroll
-        for (int p = 0; p < 2; p++)
-#pragma unroll
-            for (int k = 0; k < K; k++) x1[p][k] = pk_fma(bt, pk_sub(x1[p][k], xc[p][k]), xc[p][k]);
-        if (EDGE) {
-#pragma unroll
-            for (int r = 0; r < R; r++)
-#pragma unroll
-                for (int k = 0; k < K; k++)
-                    if (!in[r]) put(x1[r & 1][k], r, 0.f);
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-        sm.yl[jb][nbr_idx<K, NT>(i, k)] = x1[0][k].x;  // timestep 0
-        sm.yr[jb][nbr_idx<K, NT>(i, k)] = x1[1][k].y;  // timestep 3
-    }
-    if (!__syncthreads_and(arrived)) return false;
-
-    if (i == 0 && refill_t0 != TMA_NO_REFILL) {
-        fence_proxy_async_smem();
-        tma_issue<K>(sm, s, sc.xin, sc.data, refill_t0);
-    }
-    tma_flush_pending<K, KB, NT, BM, TP, R>(sm, sc, acc, pend);
-
-    // phase C: g^{c+1}, objective, d_{c+2}
-    float2 g1[2][K], d1[2][K];
-    {
-        float2 fp = pk_splat(0.f);
-        const float2 na1 = pk_splat(-sc.a1);
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            float2 LA, LB;
-            rows(x1[0][k], x1[1][k], sm.yr[jb][nbr_idx<K, NT>(li, k)], sm.yl[jb][nbr_idx<K, NT>(ri, k)], LA, LB);
-            const float2 ck = pk_splat(TP ? c2 * sc.kw[k] : c2);
-            g1[0][k] = pk_fma(ck, LA, nb[0][k]);
-            g1[1][k] = pk_fma(ck, LB, nb[1][k]);
-            // (g - b) x; x is zero outside the signal, so these terms vanish there
-            fp = pk_fma(pk_add(g1[0][k], nb[0][k]), x1[0][k], fp);
-            fp = pk_fma(pk_add(g1[1][k], nb[1][k]), x1[1][k], fp);
-            d1[0][k] = pk_fma(na1, g1[0][k], x1[0][k]);
-            d1[1][k] = pk_fma(na1, g1[1][k], x1[1][k]);
-        }
-        if (owner) acc.f.add(fp.x + fp.y);
-        project_reg2<K>(d1[0]);
-        project_reg2<K>(d1[1]);
-#pragma unroll
-        for (int p = 0; p < 2; p++)
-#pragma unroll
-            for (int k = 0; k < K; k++) d1[p][k] = pk_sub(d1[p][k], x1[p][k]);
-        if (EDGE) {
-#pragma unroll
-            for (int r = 0; r < R; r++)
-#pragma unroll
-                for (int k = 0; k < K; k++)
-                    if (!in[r]) put(d1[r & 1][k], r, 0.f);
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < K; k++) sm.dl[jb][nbr_idx<K, NT>(i, k)] = d1[0][k].x;
-
-    // phase D: dots of d_{c+2} (the pair with the next thread's first timestep waits for the
-    // next barrier) and the store of x^{c+1}
-    if (owner) {
-        float2 dd = pk_splat(0.f), gd = pk_splat(0.f), dA = pk_splat(0.f);
-        float dmid = 0.f;
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            dd = pk_fma(d1[0][k], d1[0][k], dd);
-            dd = pk_fma(d1[1][k], d1[1][k], dd);
-            gd = pk_fma(g1[0][k], d1[0][k], gd);
-            gd = pk_fma(g1[1][k], d1[1][k], gd);
-            // pairs (0,1) and (2,3) packed; pair (1,2) on its own
-            float2 df = pk_sub(d1[1][k], d1[0][k]);
-            float dfm = d1[0][k].y - d1[1][k].x;
-            if (EDGE) {
-                df.x = dm[1] ? df.x : 0.f;
-                df.y = dm[3] ? df.y : 0.f;
-                dfm = dm[2] ? dfm : 0.f;
-            }
-            if (TP) {
-                dA = pk_fma(pk_mul(df, pk_splat(sc.kw[k])), df, dA);
-                dmid = fmaf(dfm * sc.kw[k], dfm, dmid);
-            } else {
-                dA = pk_fma(df, df, dA);
-                dmid = fmaf(dfm, dfm, dmid);
-            }
-            pend.dlast[k] = d1[1][k].y;
-        }
-        acc.dd += dd.x + dd.y;
-        acc.gd += gd.x + gd.y;
-        acc.dAd += (dA.x + dA.y) + dmid;
-        pend.valid = dm[R];
-        pend.j = j;
-        float xs[R * K];
-#pragma unroll
-        for (int r = 0; r < R; r++)
-#pragma unroll
-            for (int k = 0; k < K; k++) xs[r * K + k] = get(x1[r & 1][k], r);
-        if (!EDGE || in[R - 1]) {
-            if constexpr ((R * K) % 4 == 0) {
-                float4 *dst = reinterpret_cast<float4 *>(sc.xout + (long)tb * K);
-#pragma unroll
-                for (int q = 0; q < R * K / 4; q++)
-                    dst[q] = make_float4(xs[4 * q], xs[4 * q + 1], xs[4 * q + 2], xs[4 * q + 3]);
-            } else {
-                float2 *dst = reinterpret_cast<float2 *>(sc.xout + (long)tb * K);
-#pragma unroll
-                for (int q = 0; q < R * K / 2; q++) dst[q] = make_float2(xs[2 * q], xs[2 * q + 1]);
-            }
-        } else {
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                if (in[r])
-#pragma unroll
-                    for (int k = 0; k < K; k++) sc.xout[(long)(tb + r) * K + k] = xs[r * K + k];
-        }
-    }
-    return true;
-}
-
 template <int K, int KB, int NT, bool INIT, bool BM = false, bool TP = false, int R = TMA_R>
 __device__ __forceinline__ bool tma_tile(TmaSmem<KB, NT, BM, R> &sm, int s, int j, bool arrived, int t0,
                                          const TileScalars<K> &sc, TileAcc &acc, TilePending<K> &pend, int refill_t0)
 {
     constexpr int P = NT * R;
-    if constexpr (R == 4 && TMA_PACKED) {
-        if (t0 >= 1 && t0 + P <= sc.T - 1)
-            return tma_tile_body_pk<K, KB, NT, INIT, BM, false, TP>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
-        return tma_tile_body_pk<K, KB, NT, INIT, BM, true, TP>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
-    } else {
-        if (t0 >= 1 && t0 + P <= sc.T - 1)
-            return tma_tile_body<K, KB, NT, INIT, BM, false, TP, R>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
-        return tma_tile_body<K, KB, NT, INIT, BM, true, TP, R>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
-    }
+    if (t0 >= 1 && t0 + P <= sc.T - 1)
+        return tma_tile_body<K, KB, NT, INIT, BM, false, TP, R>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
+    return tma_tile_body<K, KB, NT, INIT, BM, true, TP, R>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
 }
 
 }  // namespace pasc

@@ -104,7 +104,7 @@ for name, (res, args) in capi.PROTOTYPES.items():
 
 def test_null_handles_and_pointers_are_refused(lib):
     """Every entry point that takes a handle or device pointer first, called with NULL for it
-    and NULL / 0 for everything else, returns an error code (destroy, host_free: OK) instead of crashing;
+    and NULL / 0 for everything else, returns an error code (destroy, host_free, vec_free: OK) instead of crashing;
     the constructors refuse a NULL output pointer.  Run in a child process so that a crash
     fails this test and not the session."""
     r = subprocess.run([sys.executable, "-c", NULL_SWEEP, ROOT], capture_output=True, text=True, timeout=120)
@@ -112,7 +112,7 @@ def test_null_handles_and_pointers_are_refused(lib):
     rcs = dict(line.rsplit(" ", 1) for line in r.stdout.split("\n") if line.strip())
     assert len(rcs) >= 50, rcs
     for name, rc in rcs.items():
-        if name in ("pasc_gb300_destroy", "pasc_gb300_batch_destroy", "pasc_gb300_host_free"):
+        if name in ("pasc_gb300_destroy", "pasc_gb300_batch_destroy", "pasc_gb300_host_free", "pasc_gb300_vec_free"):
             assert int(rc) == capi.PASC_OK, name
         else:
             assert int(rc) == capi.PASC_ERR_ARG, (name, rc)
