@@ -21,3 +21,16 @@ ${CXX:-g++} -std=c++14 -O2 -fPIC -shared -ffp-contract=off -w \
     "$REF/src/general/model/generalmodel.cpp" \
     -o "$HERE/_ref/libpasc_ref.so"
 echo "build_ref: $HERE/_ref/libpasc_ref.so"
+# The test driver of the GB300 backend (tests/cpp/gb300_backend_driver.cpp, include/pasc/
+# gb300_backend.hpp) over the reference's generic solver templates, as one translation unit
+# with the reference's headers and the shims inlined (this repository's headers stay
+# includes), for tests/test_gpu_backend.py to compile where the reference tree is absent.
+ROOT=$(cd "$HERE/.." && pwd)
+python3 "$HERE/flatten_sources.py" "$HERE/_ref/backend/gb300_backend_driver_flat.cpp" \
+    "$ROOT/tests/cpp/gb300_backend_driver.cpp" \
+    "$REF/src/general/solver/spg_fs.cpp" \
+    "$REF/src/general/solver/generalsolver.cpp" \
+    "$REF/src/general/data/generaldata.cpp" \
+    "$REF/src/general/model/generalmodel.cpp" \
+    -I "$HERE/ref_shim" -I "$REF/include" -I "$REF/src"
+echo "build_ref: $HERE/_ref/backend/gb300_backend_driver_flat.cpp"
