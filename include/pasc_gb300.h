@@ -481,9 +481,10 @@ int pasc_gb300_batch_set_loop(pasc_gb300_batch *b, int device_loop, int chunk);
 /* Segment size of the batched sweeps (no reference counterpart): every signal is cut into
  * segments of `tiles` bulk-copy tiles of 504 timesteps, the unit of work a block takes from
  * the work list (longest signals first).  tiles = 0 (the default): the batch's tuner picks it
- * at the first solve among {2, 4, 8, 16, 32} by timing sweeps of all signals and of the
- * longest eighth alone; 2..64 pins it.  get: the size in use and (nullable, 5 values) the
- * tuner's measured score of each candidate in ms (0 before tuning). */
+ * at the first solve among {2, 4, 8, 16, 32} by timing sweeps of all signals, of the longest
+ * eighth alone and of the longest signal alone (score t_all + t_eighth + 8 t_longest); 2..64
+ * pins it.  get: the size in use and (nullable, 5 values) the tuner's score of each candidate
+ * in ms (0 before tuning). */
 int pasc_gb300_batch_set_segment_tiles(pasc_gb300_batch *b, int tiles);
 int pasc_gb300_batch_get_segment_tiles(pasc_gb300_batch *b, int *tiles, double *tune_ms);
 /* pasc_gb300_spgqp_solve for every signal at once; st: n entries (nullable).  The

@@ -680,10 +680,12 @@ static int time_init_sweep(pasc_gb300_batch *b, Pred take, int reps, float *best
 }
 
 // The batch's tuner, run at its first solve unless the segment size was pinned: for each
-// segment size in {2, 4, 8, 16, 32} tiles it times one sweep of every signal and one sweep of
-// the longest eighth of the signals alone (the end of a solve, when only long signals still
-// run, is where short segments pay off and long ones leave SMs idle), and keeps the size with
-// the smallest sum of the two.
+// segment size in {2, 4, 8, 16, 32} tiles it times one sweep of every signal, one of the
+// longest eighth of the signals alone and one of the longest signal alone, and keeps the size
+// with the smallest t_all + t_eighth + 8 t_longest.  Most sweeps of a batched solve run with
+// few signals left (measured on the 256-signal workload: about 30 times more sweeps than the
+// mean signal's iterations), where short segments keep the SMs busy and long ones leave them
+// idle; the full sweep is where long segments save their per-segment set-up.
 static int batch_tune(pasc_gb300_batch *b)
 {
     if (b->tuned) return PASC_OK;
@@ -697,10 +699,12 @@ static int batch_tune(pasc_gb300_batch *b)
     double best_ms = 1e300;
     for (int c = 0; c < 5; c++) {
         BCHK(batch_layout(b, cand[c]));
-        float t_all = 0.f, t_long = 0.f;
+        float t_all = 0.f, t_long = 0.f, t_one = 0.f;
+        const int longest = b->order_h[0];
         BCHK(time_init_sweep(b, [](int) { return true; }, 3, &t_all));
         BCHK(time_init_sweep(b, [&](int i) { return is_long[i] != 0; }, 3, &t_long));
-        b->tune_ms[c] = (double)t_all + (double)t_long;
+        BCHK(time_init_sweep(b, [&](int i) { return i == longest; }, 3, &t_one));
+        b->tune_ms[c] = (double)t_all + (double)t_long + 8.0 * (double)t_one;
         if (b->tune_ms[c] < best_ms) {
             best_ms = b->tune_ms[c];
             best = cand[c];
