@@ -798,12 +798,11 @@ def measure_batched(dev, peak, qp=True):
             bt.set_theta(i, theta0(s))
         return bt
 
-    # sweep throughput with every signal running (stopping tests off), after the tuner chose
-    # the segment size on the batch's first solve
+    # sweep throughput with every signal running (stopping tests off; work items sized for that)
     B_sweep = float(sum((8 * s.K + 4) * s.T for s in inst))
     with load_batch(lambda s: np.linspace(0.0, 4.0, s.K)) as bt:
         bt.spgqp_solve(capi.spgqp_opts(maxit=20, stop_difff=0))
-        seg_tiles, tune_ms = bt.get_segment_tiles()
+        seg_tiles, item_tiles = bt.get_segment_tiles()
         for i, s in enumerate(inst):
             bt.set_gamma(i, s.gamma0)
         st = bt.spgqp_solve(capi.spgqp_opts(maxit=200, stop_difff=0))
@@ -845,7 +844,9 @@ def measure_batched(dev, peak, qp=True):
         "workload": "256 signals, T log-U[1e3,1e6], K U{2..5}, epssqr log-U[1,1000], sorted levels U[0,4], "
                     "segments U[T/50,T/5], sigma U[0.2,1]; TSSolver SPG eps 1e-6 m 10, outer 1e-6 relative",
         "signals": n, "timesteps": int(sum(s.T for s in inst)),
-        "segment_tiles_tuned": seg_tiles, "tuner_ms_per_candidate_2_4_8_16_32": [float(x) for x in tune_ms],
+        "work_items": {"segment_tiles": seg_tiles, "item_tiles_all_running": item_tiles,
+                       "sizing": "items of 4..32 tiles, about 4 per resident block, resized at every "
+                                 "rebuild of the work list"},
         "batch_s": wall_b, "batch_host_loop_s": min(walls[False]), "batch_spg_it_sum": spg_it_b,
         "batch_gpu_launches": launches_b, "batch_loop": "one CUDA graph launch (conditional WHILE nodes)",
         "fp64_plain_sequential_s": seq["fp64_plain"][0], "fp64_plain_spg_it_sum": int(seq["fp64_plain"][1]),

@@ -278,7 +278,8 @@ public:
     int size() const { return (int)T_.size(); }
     // one graph launch per solve with the loops decided on the device (default), or host-driven
     void set_loop(bool device_loop, int chunk = 4) { check(pasc_gb300_batch_set_loop(h_.get(), device_loop ? 1 : 0, chunk)); }
-    // bulk-copy tiles per segment; 0: chosen by the batch's tuner at the first solve
+    // work items of the batched sweeps: 0 sized from the segments still running, -c with about
+    // c items per resident block, 2..64 fixed items of that many tiles
     void set_segment_tiles(int tiles) { check(pasc_gb300_batch_set_segment_tiles(h_.get(), tiles)); }
     int get_segment_tiles() const
     {

@@ -478,15 +478,16 @@ int pasc_gb300_batch_get_theta(pasc_gb300_batch *b, int i, double *theta);
  * TSSolver's maxit (outer iterations).  device_loop = 0: the host launches the sweeps in
  * chunks and reads the signals' states between chunks. */
 int pasc_gb300_batch_set_loop(pasc_gb300_batch *b, int device_loop, int chunk);
-/* Segment size of the batched sweeps (no reference counterpart): every signal is cut into
- * segments of `tiles` bulk-copy tiles of 504 timesteps, the unit of work a block takes from
- * the work list (longest signals first).  tiles = 0 (the default): the batch's tuner picks it
- * at the first solve among {2, 4, 8, 16, 32} by timing sweeps of all signals, of the longest
- * eighth alone and of the longest signal alone (score t_all + t_eighth + 8 t_longest); 2..64
- * pins it.  get: the size in use and (nullable, 5 values) the tuner's score of each candidate
- * in ms (0 before tuning). */
+/* Work items of the batched sweeps (no reference counterpart): every signal is cut into
+ * segments of bulk-copy tiles of 504 timesteps, and a block takes work items (consecutive
+ * segments of one signal) from a list ordered longest signals first.  tiles = 0 (the default):
+ * segments of 4 tiles, merged at every rebuild of the list into items sized from the number of
+ * segments still running -- about four items per resident block, 4 to 32 tiles each (long
+ * items while every signal runs, short ones when few remain); -c (1 <= c <= 16): the same
+ * with about c items per resident block; 2..64: every item is one segment of that many tiles.
+ * get: the segment size and (nullable) the item size with every signal running, in tiles. */
 int pasc_gb300_batch_set_segment_tiles(pasc_gb300_batch *b, int tiles);
-int pasc_gb300_batch_get_segment_tiles(pasc_gb300_batch *b, int *tiles, double *tune_ms);
+int pasc_gb300_batch_get_segment_tiles(pasc_gb300_batch *b, int *seg_tiles, int *item_tiles);
 /* pasc_gb300_spgqp_solve for every signal at once; st: n entries (nullable).  The
  * ||b||-scaled stopping tests are not supported (PASC_ERR_NOTSUPP). */
 int pasc_gb300_batch_spgqp_solve(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o,

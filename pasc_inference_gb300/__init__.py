@@ -356,16 +356,17 @@ class Batch:
         check(load().pasc_gb300_batch_set_loop(self._h, 1 if device_loop else 0, int(chunk)))
 
     def set_segment_tiles(self, tiles: int = 0):
-        """Bulk-copy tiles per segment of the batched sweeps; 0: chosen by the tuner at the
-        first solve."""
+        """Work items of the batched sweeps: 0 (default) sized at every rebuild of the work list
+        from the segments still running (4-tile segments, items of 4 to 32 tiles, about four per
+        resident block); -c the same with about c items per resident block; 2..64 fixed items of
+        that many tiles."""
         check(load().pasc_gb300_batch_set_segment_tiles(self._h, int(tiles)))
 
     def get_segment_tiles(self):
-        """(tiles in use, the tuner's score in ms of each candidate 2, 4, 8, 16, 32)."""
-        t = C.c_int()
-        ms = np.zeros(5)
-        check(load().pasc_gb300_batch_get_segment_tiles(self._h, C.byref(t), ms.ctypes.data))
-        return t.value, ms
+        """(tiles per segment, tiles per work item with every signal running)."""
+        t, it = C.c_int(), C.c_int()
+        check(load().pasc_gb300_batch_get_segment_tiles(self._h, C.byref(t), C.byref(it)))
+        return t.value, it.value
 
     def set_data(self, i: int, data):
         check(load().pasc_gb300_batch_set_data(self._h, int(i), self._vec(i, data, 1, "batch_set_data")))

@@ -158,7 +158,7 @@ PROTOTYPES = {
     "pasc_gb300_batch_size": (C.c_int, [_h, C.POINTER(C.c_int)]),
     "pasc_gb300_batch_set_loop": (C.c_int, [_h, C.c_int, C.c_int]),
     "pasc_gb300_batch_set_segment_tiles": (C.c_int, [_h, C.c_int]),
-    "pasc_gb300_batch_get_segment_tiles": (C.c_int, [_h, C.POINTER(C.c_int), C.c_void_p]),
+    "pasc_gb300_batch_get_segment_tiles": (C.c_int, [_h, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "pasc_gb300_batch_set_data": (C.c_int, [_h, C.c_int, _dp]),
     "pasc_gb300_batch_set_gamma": (C.c_int, [_h, C.c_int, _dp]),
     "pasc_gb300_batch_get_gamma": (C.c_int, [_h, C.c_int, _dp]),

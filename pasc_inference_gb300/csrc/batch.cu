@@ -81,23 +81,33 @@ __device__ __forceinline__ int bl_scan(int v, int *s_warp, int *total)
     return before;
 }
 
-// The work list: every segment of the signals with take(i), longest signals first.
+// The work list: the items of the signals with take(i), longest signals first (the same list
+// update_worklist builds on the host).
 template <class Take>
 __device__ void bl_worklist(const BatchArgs &a, int *work, int *nwork, Take take)
 {
     __shared__ int s_warp[64];
+    int nseg = 0;
+    for (int q0 = 0; q0 < a.ninst; q0 += BL_NT) {
+        const int q = q0 + threadIdx.x;
+        int total;
+        bl_scan((q < a.ninst && take(a.order[q])) ? a.inst[a.order[q]].nseg : 0, s_warp, &total);
+        nseg += total;
+    }
+    const int m = batch_merge(nseg, a.merge_target, a.merge_max);
     int base = 0;
     for (int q0 = 0; q0 < a.ninst; q0 += BL_NT) {
         const int q = q0 + threadIdx.x;
         const int i = q < a.ninst ? a.order[q] : 0;
-        const int cnt = (q < a.ninst && take(i)) ? a.inst[i].nseg : 0;
+        const int cnt = (q < a.ninst && take(i)) ? (a.inst[i].nseg + m - 1) / m : 0;
         int total;
         const int off = base + bl_scan(cnt, s_warp, &total);
-        for (int s = 0; s < cnt; s++) work[off + s] = a.inst[i].seg0 + s;
+        for (int c = 0; c < cnt; c++) work[off + c] = a.inst[i].seg0 + c * m;
         base += total;
     }
     if (threadIdx.x == 0) {
-        *nwork = base;
+        nwork[0] = base;
+        nwork[1] = m;
         *a.next_job = 0u;
     }
 }
@@ -257,6 +267,16 @@ __global__ void __launch_bounds__(BL_NT) bl_outer_tail_kernel(BatchArgs a, Batch
         if (r_ != PASC_OK) return r_;  \
     } while (0)
 
+static constexpr int BATCH_CHUNK = 16;
+static constexpr int BATCH_MIN_SEG_TILES = 2;  // the smallest segment size
+// automatic work items: segments of 4 tiles merged into items of up to 32 tiles, about four
+// items per resident block (measured on 256 signals of 1e3..1e6 timesteps: fixed 4-tile items
+// were best for the TSSolver, whose late sweeps run few signals, fixed 16-tile items for
+// long QP solves of all signals)
+static constexpr int BATCH_AUTO_SEG_TILES = 4;
+static constexpr int BATCH_MERGE_MAX_TILES = 32;
+static constexpr int BATCH_AUTO_ITEMS_PER_BLOCK = 4;
+
 struct pasc_gb300_batch {
     int n = 0, device = 0, sms = 0, KB = 0;
     cudaStream_t stream = nullptr;
@@ -269,14 +289,14 @@ struct pasc_gb300_batch {
     BatchInstDev *inst_d = nullptr;
     int *seg_inst_d = nullptr;
     int nseg = 0, nseg_max = 0;
-    // segment size: bulk-copy tiles per segment (0 in seg_pinned: chosen by the tuner at the
-    // first solve), and the order of the work lists (signals by decreasing T)
-    int seg_tiles = 8, seg_pinned = 0;
-    bool tuned = false;
+    // segments: bulk-copy tiles per segment; merge_per_block > 0: work items of up to
+    // BATCH_MERGE_MAX_TILES tiles sized for about merge_per_block items per resident block of
+    // the sweep grid, 0: one segment per item (a pinned size).  order: signals by decreasing T
+    int seg_tiles = BATCH_AUTO_SEG_TILES, merge_per_block = BATCH_AUTO_ITEMS_PER_BLOCK;
     std::vector<int> order_h;
     int *order_d = nullptr;
-    double tune_ms[8] = {0};
-    // work list: the segments of the signals taking part in the next launches
+    // work list: the items of the signals taking part in the next launches; nwork_d holds
+    // {items, segments per item}
     int *work_d = nullptr, *nwork_d = nullptr, *work_h = nullptr;
     std::vector<char> in_work;  // signals in the uploaded list (valid while work_valid)
     bool work_valid = false;
@@ -303,8 +323,6 @@ struct pasc_gb300_batch {
     cudaStream_t aux[2] = {nullptr, nullptr};
 };
 
-static constexpr int BATCH_CHUNK = 16;
-static constexpr int BATCH_MIN_SEG_TILES = 2;  // the smallest segment the tuner tries
 
 static void batch_free(pasc_gb300_batch *b)
 {
@@ -382,6 +400,8 @@ static BatchArgs batch_args(pasc_gb300_batch *b)
     a.theta64 = b->theta64;
     a.order = b->order_d;
     a.seg_tiles = b->seg_tiles;
+    a.merge_target = b->merge_per_block * b->grid;
+    a.merge_max = std::max(1, BATCH_MERGE_MAX_TILES / b->seg_tiles);
     return a;
 }
 
@@ -452,14 +472,14 @@ int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const 
         !dal((void **)&b->st_d, sizeof(SpgDevState) * n) || !dal((void **)&b->partials, sizeof(double) * 16 * b->nseg_max) ||
         !dal((void **)&b->theta64, sizeof(double) * 8 * n) || !dal((void **)&b->ticket, sizeof(unsigned int) * n) ||
         !dal((void **)&b->next_job, sizeof(unsigned int)) || !dal((void **)&b->active_d, sizeof(int) * n) ||
-        !dal((void **)&b->work_d, sizeof(int) * b->nseg_max) || !dal((void **)&b->nwork_d, sizeof(int)) ||
+        !dal((void **)&b->work_d, sizeof(int) * b->nseg_max) || !dal((void **)&b->nwork_d, 2 * sizeof(int)) ||
         !dal((void **)&b->order_d, sizeof(int) * n) ||
         !dal((void **)&b->loop_d, sizeof(BatchLoop)) || !dal((void **)&b->outer_d, sizeof(BatchOuter) * n) ||
         !dal((void **)&b->coeffA_d, sizeof(double) * n) || !dal((void **)&b->coeffB_d, sizeof(double) * n))
         return bail(bfail(PASC_ERR_ALLOC, "batch_create: device allocation failed"));
     if (cudaMallocHost((void **)&b->st_h, sizeof(SpgDevState) * n) != cudaSuccess ||
         cudaMallocHost((void **)&b->active_h, sizeof(int) * n) != cudaSuccess ||
-        cudaMallocHost((void **)&b->work_h, sizeof(int) * (b->nseg_max + 1)) != cudaSuccess ||
+        cudaMallocHost((void **)&b->work_h, sizeof(int) * (b->nseg_max + 2)) != cudaSuccess ||
         cudaMallocHost((void **)&b->loop_h, sizeof(BatchLoop)) != cudaSuccess ||
         cudaMallocHost((void **)&b->outer_h, sizeof(BatchOuter) * n) != cudaSuccess)
         return bail(bfail(PASC_ERR_ALLOC, "batch_create: pinned allocation failed"));
@@ -476,7 +496,7 @@ int pasc_gb300_batch_create(pasc_gb300_batch **out, int n, const long *T, const 
     cudaMemset(b->st_d, 0, sizeof(SpgDevState) * n);
     cudaMemset(b->ticket, 0, sizeof(unsigned int) * n);
     cudaMemset(b->theta64, 0, sizeof(double) * 8 * n);
-    cudaMemset(b->nwork_d, 0, sizeof(int));
+    cudaMemset(b->nwork_d, 0, 2 * sizeof(int));
     b->in_work.assign(n, 0);
     cudaMemcpy(b->inst_d, b->inst_h.data(), sizeof(BatchInstDev) * n, cudaMemcpyHostToDevice);
     cudaMemcpy(b->order_d, b->order_h.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
@@ -515,22 +535,26 @@ int pasc_gb300_batch_set_loop(pasc_gb300_batch *b, int device_loop, int chunk)
 int pasc_gb300_batch_set_segment_tiles(pasc_gb300_batch *b, int tiles)
 {
     if (!b) return bfail(PASC_ERR_ARG, "batch_set_segment_tiles: NULL handle");
-    if (tiles != 0 && (tiles < BATCH_MIN_SEG_TILES || tiles > 64))
-        return bfail(PASC_ERR_ARG, "batch_set_segment_tiles: tiles must be 0 (tuned) or in [2, 64]");
+    if (tiles > 64 || tiles == 1 || tiles < -16)
+        return bfail(PASC_ERR_ARG, "batch_set_segment_tiles: tiles must be in [2, 64], 0 (automatic) or in [-16, -1]");
     BCU(cudaSetDevice(b->device));
-    b->seg_pinned = tiles;
-    b->tuned = false;
-    for (double &v : b->tune_ms) v = 0.0;
-    if (tiles) return batch_layout(b, tiles);
-    return PASC_OK;
+    if (tiles > 0) {
+        b->merge_per_block = 0;
+        return batch_layout(b, tiles);
+    }
+    b->merge_per_block = tiles < 0 ? -tiles : BATCH_AUTO_ITEMS_PER_BLOCK;
+    b->work_valid = false;
+    return b->seg_tiles == BATCH_AUTO_SEG_TILES ? PASC_OK : batch_layout(b, BATCH_AUTO_SEG_TILES);
 }
 
-int pasc_gb300_batch_get_segment_tiles(pasc_gb300_batch *b, int *tiles, double *tune_ms)
+int pasc_gb300_batch_get_segment_tiles(pasc_gb300_batch *b, int *seg_tiles, int *item_tiles)
 {
-    if (!b || !tiles) return bfail(PASC_ERR_ARG, "batch_get_segment_tiles: NULL argument");
-    *tiles = b->seg_tiles;
-    if (tune_ms)
-        for (int c = 0; c < 5; c++) tune_ms[c] = b->tune_ms[c];
+    if (!b || !seg_tiles) return bfail(PASC_ERR_ARG, "batch_get_segment_tiles: NULL argument");
+    *seg_tiles = b->seg_tiles;
+    if (item_tiles) {
+        const BatchArgs a = batch_args(b);
+        *item_tiles = batch_merge(b->nseg, a.merge_target, a.merge_max) * b->seg_tiles;
+    }
     return PASC_OK;
 }
 
@@ -613,7 +637,8 @@ static int batch_permute(pasc_gb300_batch *b)
 }
 
 // Rebuilds the work list from take[i] (signal i takes part) when that set changed since the
-// last upload; the list holds all segments of every signal taking part, in signal order.
+// last upload: the items of every signal taking part, longest signals first (the list
+// bl_worklist builds on the device, item for item).
 template <class Pred>
 static int update_worklist(pasc_gb300_batch *b, Pred take)
 {
@@ -621,96 +646,26 @@ static int update_worklist(pasc_gb300_batch *b, Pred take)
     for (int i = 0; i < b->n && same; i++) same = (b->in_work[i] != 0) == take(i);
     if (same) return PASC_OK;
     BCU(cudaStreamSynchronize(b->stream));  // the pinned list may still be feeding an upload
+    int nseg = 0;
+    for (int i = 0; i < b->n; i++) {
+        b->in_work[i] = take(i) ? 1 : 0;
+        if (b->in_work[i]) nseg += b->inst_h[i].nseg;
+    }
+    const BatchArgs a = batch_args(b);
+    const int m = batch_merge(nseg, a.merge_target, a.merge_max);
     int cnt = 0;
     for (int q = 0; q < b->n; q++) {
         const int i = b->order_h[q];
-        b->in_work[i] = take(i) ? 1 : 0;
         if (!b->in_work[i]) continue;
         const BatchInstDev &I = b->inst_h[i];
-        for (int s = 0; s < I.nseg; s++) b->work_h[1 + cnt++] = I.seg0 + s;
+        for (int s = 0; s < I.nseg; s += m) b->work_h[2 + cnt++] = I.seg0 + s;
     }
     b->work_h[0] = cnt;
+    b->work_h[1] = m;
     b->work_valid = true;
-    BCU(cudaMemcpyAsync(b->nwork_d, b->work_h, sizeof(int), cudaMemcpyHostToDevice, b->stream));
-    if (cnt) BCU(cudaMemcpyAsync(b->work_d, b->work_h + 1, sizeof(int) * cnt, cudaMemcpyHostToDevice, b->stream));
+    BCU(cudaMemcpyAsync(b->nwork_d, b->work_h, 2 * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    if (cnt) BCU(cudaMemcpyAsync(b->work_d, b->work_h + 2, sizeof(int) * cnt, cudaMemcpyHostToDevice, b->stream));
     return PASC_OK;
-}
-
-// One INIT sweep (a pure function of each signal's current gamma: it reads buffer cur and
-// writes the other one, and the solve that follows starts over from buffer cur) of the signals
-// with take(i), timed with CUDA events; best of `reps`.
-template <class Pred>
-static int time_init_sweep(pasc_gb300_batch *b, Pred take, int reps, float *best)
-{
-    cudaStream_t s = b->stream;
-    BatchArgs a = batch_args(b);
-    *best = 1e30f;
-    for (int r = 0; r < reps + 1; r++) {
-        BCU(cudaStreamSynchronize(s));
-        for (int i = 0; i < b->n; i++) {
-            SpgDevState &h = b->st_h[i];
-            memset(&h, 0, sizeof h);
-            h.alpha_prev = h.alpha_cur = 2.0;
-            h.coeff = b->coeffA[i];
-            h.bscale = b->coeffB[i];
-            h.gamma = 0.9;
-            h.sigma2 = 1.0;
-            h.maxit = 1;
-            h.m = 1;
-            h.cur = b->cur[i];
-            h.status = take(i) ? PASC_SPG_RUNNING : IDLE;
-        }
-        BCU(cudaMemcpyAsync(b->st_d, b->st_h, sizeof(SpgDevState) * b->n, cudaMemcpyHostToDevice, s));
-        BCU(cudaMemsetAsync(b->ticket, 0, sizeof(unsigned int) * b->n, s));
-        BCHK(update_worklist(b, take));
-        BCU(cudaMemsetAsync(b->next_job, 0, sizeof(unsigned int), s));
-        BCU(cudaEventRecord(b->ev0, s));
-        BCU(launch_batch_sweep(b->KB, true, b->grid_init, a, s));
-        BCU(cudaEventRecord(b->ev1, s));
-        BCU(cudaEventSynchronize(b->ev1));
-        float ms = 0.f;
-        BCU(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
-        if (r > 0 && ms < *best) *best = ms;  // the first run warms up
-    }
-    BCU(cudaMemcpyAsync(b->st_h, b->st_d, sizeof(SpgDevState) * b->n, cudaMemcpyDeviceToHost, s));
-    BCU(cudaStreamSynchronize(s));
-    for (int i = 0; i < b->n; i++)
-        if (b->st_h[i].error) return bfail(PASC_ERR_TIMEOUT, "batch: a bounded wait for a bulk copy gave up");
-    return PASC_OK;
-}
-
-// The batch's tuner, run at its first solve unless the segment size was pinned: for each
-// segment size in {2, 4, 8, 16, 32} tiles it times one sweep of every signal, one of the
-// longest eighth of the signals alone and one of the longest signal alone, and keeps the size
-// with the smallest t_all + t_eighth + 8 t_longest.  Most sweeps of a batched solve run with
-// few signals left (measured on the 256-signal workload: about 30 times more sweeps than the
-// mean signal's iterations), where short segments keep the SMs busy and long ones leave them
-// idle; the full sweep is where long segments save their per-segment set-up.
-static int batch_tune(pasc_gb300_batch *b)
-{
-    if (b->tuned) return PASC_OK;
-    b->tuned = true;
-    if (b->seg_pinned) return PASC_OK;
-    const int nlong = std::max(1, b->n / 8);
-    std::vector<char> is_long(b->n, 0);
-    for (int q = 0; q < nlong; q++) is_long[b->order_h[q]] = 1;
-    const int cand[] = {2, 4, 8, 16, 32};
-    int best = b->seg_tiles;
-    double best_ms = 1e300;
-    for (int c = 0; c < 5; c++) {
-        BCHK(batch_layout(b, cand[c]));
-        float t_all = 0.f, t_long = 0.f, t_one = 0.f;
-        const int longest = b->order_h[0];
-        BCHK(time_init_sweep(b, [](int) { return true; }, 3, &t_all));
-        BCHK(time_init_sweep(b, [&](int i) { return is_long[i] != 0; }, 3, &t_long));
-        BCHK(time_init_sweep(b, [&](int i) { return i == longest; }, 3, &t_one));
-        b->tune_ms[c] = (double)t_all + (double)t_long + 8.0 * (double)t_one;
-        if (b->tune_ms[c] < best_ms) {
-            best_ms = b->tune_ms[c];
-            best = cand[c];
-        }
-    }
-    return batch_layout(b, best);
 }
 
 static int ensure_batch_graph(pasc_gb300_batch *b)
@@ -925,7 +880,6 @@ static int batch_spgqp(pasc_gb300_batch *b, const pasc_gb300_spgqp_opts *o, doub
     if (o->stop_normgp_normb || o->stop_Anormgp_normb)
         return bfail(PASC_ERR_NOTSUPP, "batch: ||b||-scaled stopping tests are not supported");
     if (o->m < 1 || o->m > MMAX_STATE) return bfail(PASC_ERR_ARG, "batch: m must be in [1, 64]");
-    BCHK(batch_tune(b));
     if (b->device_loop) {
         BCHK(ensure_spg_loop_graph(b));
         loop_settings(b, o);
@@ -1049,8 +1003,7 @@ int pasc_gb300_batch_ts_solve(pasc_gb300_batch *b, const pasc_gb300_ts_opts *ts,
         if (spg->stop_normgp_normb || spg->stop_Anormgp_normb)
             return bfail(PASC_ERR_NOTSUPP, "batch: ||b||-scaled stopping tests are not supported");
         if (spg->m < 1 || spg->m > MMAX_STATE) return bfail(PASC_ERR_ARG, "batch: m must be in [1, 64]");
-        BCHK(batch_tune(b));
-        BCHK(ensure_ts_loop_graph(b, ts->thetasolved ? 1 : 0));
+            BCHK(ensure_ts_loop_graph(b, ts->thetasolved ? 1 : 0));
         b->launches = 0;
         if (ts->init_permute) BCHK(batch_permute(b));
         loop_settings(b, spg);
@@ -1078,7 +1031,6 @@ int pasc_gb300_batch_ts_solve(pasc_gb300_batch *b, const pasc_gb300_ts_opts *ts,
         }
         return PASC_OK;
     }
-    BCHK(batch_tune(b));
     std::vector<double> L(n, DBL_MAX), dL(n, DBL_MAX);
     std::vector<int> done(n, 0), it_last(n, 0), spg_it(n, 0), spg_hm(n, 0), incr(n, 0);
     b->launches = 0;

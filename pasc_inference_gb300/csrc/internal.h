@@ -109,7 +109,8 @@ struct BatchArgs {
     BatchInstDev *inst;
     const int *seg_inst;     // segment -> signal
     const int *work;         // segments to visit in this launch (those of signals still taking part)
-    const int *nwork;        // length of work (device memory: rewritten between captured launches)
+    const int *nwork;        // length of work and segments per item (device memory: rewritten
+                             // between captured launches)
     int nseg, ninst;
     float *xb0, *xb1;        // packed gamma, ping-pong (each signal's half given by its state's cur)
     const float *data;       // packed data
@@ -121,7 +122,19 @@ struct BatchArgs {
     double *theta64;         // 8 per signal
     const int *order;        // signals by decreasing T: the order of the work lists
     int seg_tiles;           // bulk-copy tiles per segment
+    int merge_target;        // work items wanted per list (0: one segment per item)
+    int merge_max;           // most segments in one work item
 };
+
+// Segments per work item of a list over s segments: about `target` items, between 1 and mmax
+// segments each (target 0: 1).  nwork[1] holds it for the list in use; the work list names
+// the first segment of every item, and an item never crosses into the next signal.
+__host__ __device__ inline int batch_merge(int s, int target, int mmax)
+{
+    if (target <= 0) return 1;
+    const int m = s / target;
+    return m < 1 ? 1 : (m > mmax ? mmax : m);
+}
 
 // Multichannel data (kernels_mc.cu).
 struct McArgs {

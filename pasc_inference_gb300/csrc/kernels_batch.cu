@@ -5,14 +5,16 @@
 // restarts of examples/test_signal1D/test_signal1D.cpp:268-353, include/general/solver/
 // tssolver.h:522-698; independent signals are separate runs).  Here all of them share a
 // persistent grid:
-//   - each signal is cut into segments of seg_tiles bulk-copy tiles (sweep_tma.cuh; chosen by
-//     the batch's tuner); the segments of the signals still running form one work list, longest
-//     signals first (rebuilt whenever the signals' states are read), and blocks take segments
-//     in turn from an atomic counter, so long and short signals balance across the GPU;
-//   - a segment is computed by one block with the tile pipeline of the single-signal kernel
-//     (K dispatched at run time) and leaves its four partial sums in its own slot, so the
-//     sums do not depend on which block took which segment (deterministic);
-//   - the block that completes the last segment of a signal (per-signal ticket) reduces that
+//   - each signal is cut into segments of seg_tiles bulk-copy tiles (sweep_tma.cuh); the
+//     segments of the signals still running, grouped into work items of m consecutive
+//     segments of one signal (m sized from how many segments are running: long items while
+//     the GPU is full, short ones when few signals remain), form one work list, longest
+//     signals first (rebuilt whenever the signals' states are read), and blocks take items in
+//     turn from an atomic counter, so long and short signals balance across the GPU;
+//   - an item is computed by one block with the tile pipeline of the single-signal kernel
+//     (K dispatched at run time) and leaves its four partial sums in the slot of its first
+//     segment, so the sums do not depend on which block took which item (deterministic);
+//   - the block that completes the last item of a signal (per-signal ticket) reduces that
 //     signal's slots in order and applies the reference's step-length, GLL and stopping rules
 //     to that signal alone (sweep_common.cuh): every signal converges on its own, and the
 //     segments of a signal whose solve has ended are skipped (per-signal convergence mask).
@@ -29,11 +31,12 @@ constexpr int BATCH_W = BATCH_NT * TMA_R - 2 * TMA_HALO;  // owned timesteps per
 int batch_tile_width() { return BATCH_W; }
 int batch_max_tile() { return BATCH_NT * TMA_R; }
 
-// Computes one segment of signal `q` (all threads of the block).  j counts the tiles this
-// block has computed (it selects the stage) and parity holds the stages' phase bits; both
-// persist across segments.  Returns false if a bulk copy did not arrive in time.
+// Computes one work item of signal `q`, the m segments from `seg` on (all threads of the
+// block).  j counts the tiles this block has computed (it selects the stage) and parity holds
+// the stages' phase bits; both persist across items.  Returns false if a bulk copy did not
+// arrive in time.
 template <int K, int KB, bool INIT>
-__device__ __forceinline__ bool batch_segment(TmaSmem<KB, BATCH_NT> &sm, const BatchArgs &a, int q, int seg,
+__device__ __forceinline__ bool batch_segment(TmaSmem<KB, BATCH_NT> &sm, const BatchArgs &a, int q, int seg, int m,
                                               int &j, unsigned int &parity)
 {
     const BatchInstDev &I = a.inst[q];
@@ -54,9 +57,9 @@ __device__ __forceinline__ bool batch_segment(TmaSmem<KB, BATCH_NT> &sm, const B
 
     const int lseg = seg - I.seg0;
     const int tlo = lseg * a.seg_tiles;
-    const int thi = min(tlo + a.seg_tiles, I.tiles);
-    if (lseg < 0 || lseg >= I.nseg || tlo >= thi) {
-        // not a segment of this signal (a work list out of step with the segment table): issue
+    const int thi = min(tlo + m * a.seg_tiles, I.tiles);
+    if (lseg < 0 || lseg >= I.nseg || lseg % m != 0 || tlo >= thi) {
+        // not an item of this signal (a work list out of step with the segment table): issue
         // no copy, report it
         if (threadIdx.x == 0) atomicExch(&st->error, 1);
         return true;
@@ -83,20 +86,9 @@ __device__ __forceinline__ bool batch_segment(TmaSmem<KB, BATCH_NT> &sm, const B
     __syncthreads();
     tma_flush_pending<K, KB, BATCH_NT, false, false, TMA_R>(sm, sc, acc, pend);  // the segment's last tile: its pair terms belong to this signal
 
-    double v[4] = {acc.f.value(), (double)acc.dd, (double)acc.dAd, (double)acc.gd};
-    block_sum<4>(v, sm.red);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int r = 0; r < 4; r++) a.partials[(long)seg * 4 + r] = v[r];
-    }
-    if (!last_block_done_count(&a.ticket[q], (unsigned int)I.nseg)) return true;
-    double w[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int b = threadIdx.x; b < I.nseg; b += BATCH_NT) {
-#pragma unroll
-        for (int r = 0; r < 4; r++) w[r] += __ldcg(a.partials + (long)(I.seg0 + b) * 4 + r);
-    }
-    block_sum<4>(w, sm.red);
-    if (threadIdx.x == 0) {
+    double w[4];
+    if (sweep_grid_sum4(acc.f, acc.dd, acc.dAd, acc.gd, reinterpret_cast<float2 *>(a.partials), seg, &a.ticket[q],
+                        (unsigned int)((I.nseg + m - 1) / m), I.seg0, m, reinterpret_cast<float2 *>(sm.red), w)) {
         a.ticket[q] = 0;
         spg_finish_sweep<INIT>(st, cur, w);
     }
@@ -119,12 +111,13 @@ __global__ void __launch_bounds__(BATCH_NT, batch_min_blocks(KB)) spg_batch_swee
     }
     int j = 0;
     unsigned int parity = 0u;
+    const int nwork = a.nwork[0], m = max(a.nwork[1], 1);
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) sm.job = (int)atomicAdd(a.next_job, 1u);
         __syncthreads();
         const int job = sm.job;
-        if (job >= *a.nwork) break;
+        if (job >= nwork) break;
         const int seg = a.work[job];
         if ((unsigned)seg >= (unsigned)a.nseg) continue;  // never for a list of the current layout
         const int q = a.seg_inst[seg];
@@ -132,7 +125,7 @@ __global__ void __launch_bounds__(BATCH_NT, batch_min_blocks(KB)) spg_batch_swee
         bool ok = true;
         switch (a.inst[q].K) {
 #define PASC_CASE(KK) \
-    case KK: if (KK <= KB) ok = batch_segment<(KK <= KB ? KK : 1), KB, INIT>(sm, a, q, seg, j, parity); break;
+    case KK: if (KK <= KB) ok = batch_segment<(KK <= KB ? KK : 1), KB, INIT>(sm, a, q, seg, m, j, parity); break;
             PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
             PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
 #undef PASC_CASE
@@ -146,20 +139,21 @@ __global__ void __launch_bounds__(BATCH_NT, batch_min_blocks(KB)) spg_batch_swee
 }
 
 // ---------------------------------------------------------------------------------------
-// batched theta step (graphh1fem.cpp:347-380) on the same work list: a segment sums
-// gamma_tk x_t and gamma_tk over its timesteps; the last segment of a signal divides.
+// batched theta step (graphh1fem.cpp:347-380) on the same work list: an item sums
+// gamma_tk x_t and gamma_tk over its timesteps; the last item of a signal divides.
 // ---------------------------------------------------------------------------------------
 constexpr int BATCH_THETA_NT = 256;
 
 template <int K>
-__device__ __forceinline__ void theta_segment(const BatchArgs &a, int q, int seg, double *s_red)
+__device__ __forceinline__ void theta_segment(const BatchArgs &a, int q, int seg, int m, double *s_red)
 {
     const BatchInstDev &I = a.inst[q];
     const float *gam = (a.st[q].cur ? a.xb1 : a.xb0) + I.xoff;
     const float *dat = a.data + I.doff;
     const long seg_t = (long)a.seg_tiles * BATCH_W;
     const long t_lo = (long)(seg - I.seg0) * seg_t;
-    const long t_hi = t_lo + seg_t < I.T ? t_lo + seg_t : I.T;
+    const long t_hi = t_lo + m * seg_t < I.T ? t_lo + m * seg_t : I.T;
+    const int nitems = (I.nseg + m - 1) / m;
     KahanF sx[K], sg[K];
     for (long t = t_lo + threadIdx.x; t < t_hi; t += BATCH_THETA_NT) {
         const float x = __ldg(dat + t);
@@ -181,13 +175,13 @@ __device__ __forceinline__ void theta_segment(const BatchArgs &a, int q, int seg
 #pragma unroll
         for (int r = 0; r < 2 * K; r++) a.partials[(long)seg * 16 + r] = v[r];
     }
-    if (!last_block_done_count(&a.ticket[q], (unsigned int)I.nseg)) return;
+    if (!last_block_done_count(&a.ticket[q], (unsigned int)nitems)) return;
     double w[2 * K];
 #pragma unroll
     for (int r = 0; r < 2 * K; r++) w[r] = 0.0;
-    for (int b = threadIdx.x; b < I.nseg; b += BATCH_THETA_NT) {
+    for (int b = threadIdx.x; b < nitems; b += BATCH_THETA_NT) {
 #pragma unroll
-        for (int r = 0; r < 2 * K; r++) w[r] += __ldcg(a.partials + (long)(I.seg0 + b) * 16 + r);
+        for (int r = 0; r < 2 * K; r++) w[r] += __ldcg(a.partials + ((long)I.seg0 + (long)b * m) * 16 + r);
     }
     block_sum<2 * K>(w, s_red);
     if (threadIdx.x == 0) {
@@ -204,18 +198,23 @@ __global__ void __launch_bounds__(BATCH_THETA_NT) theta_batch_kernel(BatchArgs a
 {
     __shared__ double s_red[2 * 8 * (BATCH_THETA_NT / 32)];
     __shared__ int s_job;
+    const int nwork = a.nwork[0], m = max(a.nwork[1], 1);
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_job = (int)atomicAdd(a.next_job, 1u);
         __syncthreads();
         const int job = s_job;
-        if (job >= *a.nwork) break;
+        if (job >= nwork) break;
         const int seg = a.work[job];
         if ((unsigned)seg >= (unsigned)a.nseg) continue;  // never for a list of the current layout
         const int q = a.seg_inst[seg];
         if (!a.active[q]) continue;
+        if ((seg - a.inst[q].seg0) % m != 0) {  // not the first segment of an item
+            if (threadIdx.x == 0) atomicExch(&a.st[q].error, 1);
+            continue;
+        }
         switch (a.inst[q].K) {
-#define PASC_CASE(KK) case KK: theta_segment<KK>(a, q, seg, s_red); break;
+#define PASC_CASE(KK) case KK: theta_segment<KK>(a, q, seg, m, s_red); break;
             PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
             PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
 #undef PASC_CASE

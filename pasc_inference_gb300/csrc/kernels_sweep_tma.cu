@@ -28,14 +28,18 @@ namespace pasc {
 // Timesteps per thread and threads per block of the tile: 4 x 128, or for K >= 6 (whose
 // per-thread arrays of 4 timesteps need ~165 registers, 3 blocks per SM) 2 x 256; the tile is
 // 512 timesteps either way.
+// MinBlocks: resident blocks per SM the registers are held to (0: the compiler's choice).  At
+// K <= 3 the compiler's own choice was 72 registers with a 16-byte local-memory spill (7
+// blocks per SM); held to 8 blocks it fits 64 registers without one.
 template <int K>
 struct TmaShape {
     static constexpr int R = K >= 6 ? 2 : 4;
     static constexpr int NT = 512 / R;
+    static constexpr int MinBlocks = K <= 3 ? 8 : (K == 4 ? 6 : (K == 5 ? 5 : 0));
 };
 
 template <int K, int NT, bool INIT, int MODE>
-__global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
+__global__ void __launch_bounds__(NT, TmaShape<K>::MinBlocks) spg_sweep_tma_kernel(SweepArgs a)
 {
     constexpr bool BM = MODE == 1, TP = MODE == 2;
     constexpr int R = TmaShape<K>::R;
@@ -105,22 +109,11 @@ __global__ void __launch_bounds__(NT) spg_sweep_tma_kernel(SweepArgs a)
     __syncthreads();
     tma_flush_pending<K, K, NT, BM, TP, R>(sm, sc, acc, pend);  // the last tile's pair terms
 
-    // block and grid reductions
-    double v[4] = {acc.f.value(), (double)acc.dd, (double)acc.dAd, (double)acc.gd};
-    block_sum<4>(v, sm.red);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int q = 0; q < 4; q++) a.partials[blockIdx.x * 4 + q] = v[q];
-    }
-    if (!last_block_done(&st->counter)) return;
-
-    double w[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += NT) {
-#pragma unroll
-        for (int q = 0; q < 4; q++) w[q] += __ldcg(a.partials + b * 4 + q);
-    }
-    block_sum<4>(w, sm.red);
-    if (threadIdx.x != 0) return;
+    // block and grid reductions (float-float; the step logic in FP64)
+    double w[4];
+    if (!sweep_grid_sum4(acc.f, acc.dd, acc.dAd, acc.gd, reinterpret_cast<float2 *>(a.partials), blockIdx.x,
+                         &st->counter, gridDim.x, 0, 1, reinterpret_cast<float2 *>(sm.red), w))
+        return;
     spg_finish_sweep<INIT>(st, cur, w);
 }
 
@@ -142,6 +135,10 @@ static int tma_blocks_per_sm_mode()
     const size_t smem = sizeof(TmaSmem<K, NT, MODE == 1, TmaShape<K>::R>);
     cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
+    // all of the unified L1/shared array as shared memory: the tiles arrive by bulk copy, and
+    // the default split held K = 3 to 7 blocks per SM
+    cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxShared);
     int nb = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_tma_kernel<K, NT, INIT, MODE>, NT, smem);
     return nb > 0 ? nb : 1;

@@ -97,22 +97,31 @@ __device__ __forceinline__ void sort_net(float (&s)[K])
 // active set attains it.  Taking the maximum needs no search and no branch; for K <= 3 it
 // needs no sort either (the largest, the sum minus the smallest, the sum).  An already
 // feasible block yields t = 0 and is returned unchanged, as in the reference's early exit.
-// The divisions are multiplications by compile-time reciprocals (within one ulp).
+// The divisions are multiplications by compile-time reciprocals (within one ulp), fused with
+// the subtraction of 1.
 template <int K>
 __device__ __forceinline__ void project_reg(float (&x)[K])
 {
     float sum = 0.f;
 #pragma unroll
     for (int k = 0; k < K; k++) sum += x[k];
+    // (s - 1)/j is taken as fmaf(s, 1/j, -1/j): one rounding of the exact c*s - c (zero at
+    // s = 1 exactly, so a feasible block keeps t = 0).  fmaxf drops NaN operands: the last
+    // candidate, the one over all K entries, is merged by a comparison instead, so that a block
+    // holding a NaN (a NaN sum) gets a NaN threshold and becomes all zeros, as in the reference
+    // (whose comparisons with NaN all fail).
     float tau;
     if (K == 1) {
         tau = sum - 1.f;
     } else if (K == 2) {
-        tau = fmaxf(fmaxf(x[0], x[1]) - 1.f, (sum - 1.f) * 0.5f);
+        const float t1 = fmaxf(x[0], x[1]) - 1.f, t2 = fmaf(sum, 0.5f, -0.5f);
+        tau = t1 >= t2 ? t1 : t2;
     } else if (K == 3) {
         const float mx = fmaxf(fmaxf(x[0], x[1]), x[2]);
         const float mn = fminf(fminf(x[0], x[1]), x[2]);
-        tau = fmaxf(fmaxf(mx - 1.f, (sum - mn - 1.f) * 0.5f), (sum - 1.f) * (1.f / 3.f));
+        const float t12 = fmaxf(mx - 1.f, fmaf(sum - mn, 0.5f, -0.5f));
+        const float t3 = fmaf(sum, 1.f / 3.f, -1.f / 3.f);
+        tau = t12 >= t3 ? t12 : t3;
     } else {
         float s[K];
 #pragma unroll
@@ -121,14 +130,13 @@ __device__ __forceinline__ void project_reg(float (&x)[K])
         float acc = 0.f;
         tau = -FLT_MAX;
 #pragma unroll
-        for (int i = K - 1; i >= 0; i--) {
+        for (int i = K - 1; i >= 1; i--) {
             acc += s[i];
-            tau = fmaxf(tau, (acc - 1.f) * (1.f / (float)(K - i)));
+            tau = fmaxf(tau, fmaf(acc, 1.f / (float)(K - i), -1.f / (float)(K - i)));
         }
+        const float tk = fmaf(sum, 1.f / (float)K, -1.f / (float)K);
+        tau = tau >= tk ? tau : tk;
     }
-    // fmaxf drops NaN operands; a block holding a NaN gets a NaN threshold and so becomes all
-    // zeros, as in the reference (whose comparisons with NaN all fail)
-    if (sum != sum) tau = sum;
 #pragma unroll
     for (int k = 0; k < K; k++) x[k] = fmaxf(x[k] - tau, 0.f);
 }

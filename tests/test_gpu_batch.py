@@ -246,28 +246,50 @@ def test_batch_set_loop_arguments(gpulib):
         bt.set_loop(True, 64)
 
 
-def test_batch_segment_tiles_tuned_and_pinned(gpulib, oracle):
-    """The tuner picks one of its candidate segment sizes at the first solve (and reports the
-    score it measured for each); pinned sizes give the same converged objectives (segments
-    change only the order of the FP64 sums of block partials)."""
+def test_batch_work_items_automatic_and_pinned(gpulib, oracle):
+    """Work items sized from the segments still running (the default, and with another number
+    of items per block) and fixed segment sizes give the same converged objectives (the item
+    size changes only the grouping of the block partials in the per-signal sums)."""
     fx = {}
-    for tiles in (0, 2, 32):
+    for tiles in (0, -1, -16, 2, 32):
         bt, probs = _load(SPG_CASES, oracle, seed0=5)
         with bt:
             bt.set_segment_tiles(tiles)
             st = bt.spgqp_solve(capi.spgqp_opts(maxit=3000, stop_difff=0))
-            used, ms = bt.get_segment_tiles()
-            if tiles == 0:
-                assert used in (2, 4, 8, 16, 32) and np.all(ms > 0), (used, ms)
+            seg, item = bt.get_segment_tiles()
+            if tiles <= 0:
+                assert seg == 4 and item % 4 == 0 and 4 <= item <= 32, (tiles, seg, item)
             else:
-                assert used == tiles and np.all(ms == 0)
+                assert seg == item == tiles
             fx[tiles] = np.array([s.fx for s in st])
-    for tiles in (2, 32):
+    for tiles in (-1, -16, 2, 32):
         np.testing.assert_allclose(fx[tiles], fx[0], rtol=1e-6, atol=1e-12)
     with Batch([100, 200], [3, 2], [1.0, 1.0]) as bt:
-        for bad in (1, 65, -1):
+        for bad in (1, 65, -17):
             with pytest.raises(capi.PascError):
                 bt.set_segment_tiles(bad)
+
+
+def test_batch_items_merge_with_many_segments(gpulib):
+    """With every signal long enough that the list is merged (items of several segments), the
+    automatic list and the same solve with one segment per item agree: the per-signal sums
+    collect every item exactly once (a lost or doubled item would change f)."""
+    sigs = [datagen.signal1d(T, 3, [0.0, 1.0, 2.0], 500, 5000, 0.5, 40 + q)
+            for q, T in enumerate([6_000_000, 4_000_000, 2_500_000, 900_000, 3_000])]
+    fx = {}
+    for tiles in (0, -1, 4):
+        with Batch([s.T for s in sigs], [3] * len(sigs), [10.0] * len(sigs)) as bt:
+            bt.set_segment_tiles(tiles)
+            for i, s in enumerate(sigs):
+                bt.set_data(i, s.data)
+                bt.set_gamma(i, s.gamma0)
+                bt.set_theta(i, np.array([0.0, 1.0, 2.0]))
+            st = bt.spgqp_solve(capi.spgqp_opts(maxit=200, stop_difff=0))
+            fx[tiles] = np.array([x.fx for x in st])
+            if tiles <= 0:
+                assert bt.get_segment_tiles()[1] > 4
+    np.testing.assert_allclose(fx[0], fx[4], rtol=1e-6)
+    np.testing.assert_allclose(fx[-1], fx[4], rtol=1e-6)
 
 
 def test_batch_retuned_after_solves_keeps_theta(gpulib):
