@@ -247,20 +247,11 @@ __global__ void __launch_bounds__(IMG_NT) image_sweep_kernel(ImageSweepArgs a)
     }
 
     // d'A_hat d = 1/2 sum_p sum_n (d_p - d_n)^2; the finish step takes dAd = 2 coeff w[2]
-    double v[4] = {acc_f.value(), (double)acc_dd, 0.25 * (double)acc_dad, (double)acc_gd};
-    block_sum<4>(v, sm.red);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int q = 0; q < 4; q++) a.partials[blockIdx.x * 4 + q] = v[q];
-    }
-    if (!last_block_done(&st->counter)) return;
-    double w[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += IMG_NT) {
-#pragma unroll
-        for (int q = 0; q < 4; q++) w[q] += __ldcg(a.partials + b * 4 + q);
-    }
-    block_sum<4>(w, sm.red);
-    if (threadIdx.x != 0) return;
+    // (the factor 1/4 is exact in FP32)
+    double w[4];
+    if (!sweep_grid_sum4(acc_f, acc_dd, 0.25f * acc_dad, acc_gd, reinterpret_cast<float2 *>(a.partials), blockIdx.x,
+                         &st->counter, gridDim.x, 0, 1, reinterpret_cast<float2 *>(sm.red), w))
+        return;
     spg_finish_sweep<INIT>(st, cur, w);
 }
 

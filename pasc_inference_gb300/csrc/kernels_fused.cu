@@ -238,23 +238,11 @@ __global__ void __launch_bounds__(SWEEP_NT, K <= 4 ? 6 : (K <= 6 ? 4 : 3)) spg_s
         }
     }
 
-    // block and grid reductions
-    double v[4] = {acc_f.value(), (double)acc_dd, (double)acc_dAd, (double)acc_gd};
-    block_sum<4>(v, s_red);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int q = 0; q < 4; q++) a.partials[blockIdx.x * 4 + q] = v[q];
-    }
-    if (!last_block_done(&st->counter)) return;
-
-    double w[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += SWEEP_NT) {
-#pragma unroll
-        for (int q = 0; q < 4; q++) w[q] += __ldcg(a.partials + b * 4 + q);
-    }
-    block_sum<4>(w, s_red);
-    if (threadIdx.x != 0) return;
-
+    // block and grid reductions (float-float; the step logic in FP64)
+    double w[4];
+    if (!sweep_grid_sum4(acc_f, acc_dd, acc_dAd, acc_gd, reinterpret_cast<float2 *>(a.partials), blockIdx.x,
+                         &st->counter, gridDim.x, 0, 1, reinterpret_cast<float2 *>(s_red), w))
+        return;
     spg_finish_sweep<INIT>(st, cur, w);
 }
 
