@@ -21,9 +21,10 @@
 // serves as an independent check of the tensor-core kernel.
 //
 // Theta update on the CUDA cores in FP32 (products of FP32 gamma and BF16 X, FP32 partial sums
-// over 64 timesteps folded into FP64), per-block FP64 partials, then one block per cluster sums
-// them in block order (deterministic) and prepares what the residual needs: the BF16 split,
-// the FP32 copy and ||theta_k||^2.
+// folded into float-float pairs, common.cuh), per-block float-float partials, then one block per
+// cluster sums them in a fixed order and prepares what the residual needs: the BF16 split, the
+// FP32 copy and ||theta_k||^2.  No FP64 arithmetic runs in the sums: on this part a dependent
+// FP64 add takes 63 cycles, and the folds of every block ran at the same moment.
 #include <cuda_bf16.h>
 #include <string.h>
 #include <algorithm>
@@ -382,23 +383,24 @@ cudaError_t launch_mc_residual_simt(int K, int grid, const McArgs &a, cudaStream
 // theta update
 // ---------------------------------------------------------------------------------------
 constexpr int MC_THETA_NT = 128;
-constexpr int MC_THETA_FOLD = 64;  // timesteps summed in FP32 before folding into FP64
+constexpr int MC_THETA_FOLD = 64;  // timesteps summed in FP32 before folding into a pair
 
-// partials[g * (K*n + K) + k*n + j] = sum_t gamma_tk X_tj, [.. + K*n + k] = sum_t gamma_tk
-// over block g's timesteps; thread = channel (NJ channels per thread, n <= 128 * NJ)
+// partials (float-float pairs) [g * (K*n + K) + k*n + j] = sum_t gamma_tk X_tj,
+// [.. + K*n + k] = sum_t gamma_tk over block g's timesteps; thread = channel (NJ channels per
+// thread, n <= 128 * NJ)
 template <int NJ, int K>
 __global__ void __launch_bounds__(MC_THETA_NT) mc_theta_partial_kernel(McArgs a, const float *gamma)
 {
     const int n = a.n;
     const long per = (a.T + gridDim.x - 1) / gridDim.x;
     const long t0 = blockIdx.x * per, t1 = t0 + per < a.T ? t0 + per : a.T;
-    double acc[NJ][K], den[K];
+    FF acc[NJ][K], den[K];
 #pragma unroll
     for (int q = 0; q < NJ; q++)
 #pragma unroll
-        for (int k = 0; k < K; k++) acc[q][k] = 0.0;
+        for (int k = 0; k < K; k++) acc[q][k] = ff_make(0.f);
 #pragma unroll
-    for (int k = 0; k < K; k++) den[k] = 0.0;
+    for (int k = 0; k < K; k++) den[k] = ff_make(0.f);
     for (long tb = t0; tb < t1; tb += MC_THETA_FOLD) {
         const long te = tb + MC_THETA_FOLD < t1 ? tb + MC_THETA_FOLD : t1;
         float f[NJ][K], fd[K];
@@ -426,21 +428,21 @@ __global__ void __launch_bounds__(MC_THETA_NT) mc_theta_partial_kernel(McArgs a,
 #pragma unroll
         for (int q = 0; q < NJ; q++)
 #pragma unroll
-            for (int k = 0; k < K; k++) acc[q][k] += (double)f[q][k];
+            for (int k = 0; k < K; k++) acc[q][k] = ff_add(acc[q][k], ff_make(f[q][k]));
 #pragma unroll
-        for (int k = 0; k < K; k++) den[k] += (double)fd[k];
+        for (int k = 0; k < K; k++) den[k] = ff_add(den[k], ff_make(fd[k]));
     }
-    double *P = a.partials + (long)blockIdx.x * (K * n + K);
+    float2 *P = reinterpret_cast<float2 *>(a.partials) + (long)blockIdx.x * (K * n + K);
 #pragma unroll
     for (int q = 0; q < NJ; q++) {
         const int jj = threadIdx.x + q * MC_THETA_NT;
         if (jj < n)
 #pragma unroll
-            for (int k = 0; k < K; k++) P[k * n + jj] = acc[q][k];
+            for (int k = 0; k < K; k++) P[k * n + jj] = make_float2(acc[q][k].hi, acc[q][k].lo);
     }
     if (threadIdx.x == 0)
 #pragma unroll
-        for (int k = 0; k < K; k++) P[K * n + k] = den[k];
+        for (int k = 0; k < K; k++) P[K * n + k] = make_float2(den[k].hi, den[k].lo);
 }
 
 // Vectorised form for n in {8, 16, 32, 64, 128, 256}: a thread owns 8 consecutive channels of a
@@ -449,7 +451,8 @@ __global__ void __launch_bounds__(MC_THETA_NT) mc_theta_partial_kernel(McArgs a,
 // Clusters with gamma_tk == 0 contribute nothing and are skipped (near convergence most
 // timesteps sit at a vertex of the simplex, so this removes most of the multiply-adds).
 // Block sums: shuffles across the rows of a warp, then warps in a fixed order through shared
-// memory in FP64 (deterministic); one partial per block in the layout of the kernel above.
+// memory in float-float pairs (deterministic); one partial per block in the layout of the
+// kernel above.
 constexpr int MC_THETA_VNT = 256;
 constexpr int MC_THETA_ROWS = 1024;
 
@@ -459,7 +462,7 @@ __global__ void __launch_bounds__(MC_THETA_VNT, K >= 7 ? 1 : 2) mc_theta_partial
     constexpr int RPB = MC_THETA_VNT / TPR;  // rows per step
     constexpr int NW = MC_THETA_VNT / 32;
     const int n = TPR * 8;
-    __shared__ double s_sum[TPR * 8 * K + K];
+    __shared__ float2 s_sum[TPR * 8 * K + K];
     const int tid = threadIdx.x, c = tid % TPR, r0 = tid / TPR;
     const long t0 = (long)blockIdx.x * MC_THETA_ROWS;
     const long t1 = t0 + MC_THETA_ROWS < a.T ? t0 + MC_THETA_ROWS : a.T;
@@ -509,19 +512,21 @@ __global__ void __launch_bounds__(MC_THETA_VNT, K >= 7 ? 1 : 2) mc_theta_partial
             for (int q = 0; q < 8; q++)
 #pragma unroll
                 for (int k = 0; k < K; k++) {
-                    double &dst = s_sum[k * n + c * 8 + q];
-                    dst = (w == 0 ? 0.0 : dst) + (double)acc[q][k];
+                    float2 &dst = s_sum[k * n + c * 8 + q];
+                    const FF r = ff_add(w == 0 ? ff_make(0.f) : FF{dst.x, dst.y}, ff_make(acc[q][k]));
+                    dst = make_float2(r.hi, r.lo);
                 }
             if (c == 0)
 #pragma unroll
                 for (int k = 0; k < K; k++) {
-                    double &dst = s_sum[K * n + k];
-                    dst = (w == 0 ? 0.0 : dst) + (double)den[k];
+                    float2 &dst = s_sum[K * n + k];
+                    const FF r = ff_add(w == 0 ? ff_make(0.f) : FF{dst.x, dst.y}, ff_make(den[k]));
+                    dst = make_float2(r.hi, r.lo);
                 }
         }
         __syncthreads();
     }
-    double *P = a.partials + (long)blockIdx.x * (K * n + K);
+    float2 *P = reinterpret_cast<float2 *>(a.partials) + (long)blockIdx.x * (K * n + K);
     for (int i = tid; i < K * n + K; i += MC_THETA_VNT) P[i] = s_sum[i];
 }
 
@@ -541,7 +546,7 @@ template <int K, int TPR>
 __host__ __device__ constexpr size_t mc_theta_tma_smem()
 {
     return (size_t)MC_TC_STAGES * (MC_TC_ROWS * TPR * 4 * 2 + MC_TC_ROWS * K * 4) + (size_t)(TPR * 4 * K + K) * 8 +
-           MC_TC_STAGES * 8 + 128;
+           MC_TC_STAGES * 8 + 128;  // the block sums: TPR*4*K + K float-float pairs
 }
 
 template <int K, int TPR>
@@ -555,7 +560,7 @@ __global__ void __launch_bounds__(MC_THETA_VNT) mc_theta_tma_kernel(McArgs a, co
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char *xs = smem_raw;
     float *gs = reinterpret_cast<float *>(smem_raw + MC_TC_STAGES * XB);
-    double *s_sum = reinterpret_cast<double *>(smem_raw + MC_TC_STAGES * (XB + GB));
+    float2 *s_sum = reinterpret_cast<float2 *>(smem_raw + MC_TC_STAGES * (XB + GB));
     unsigned long long *bar = reinterpret_cast<unsigned long long *>(s_sum + n * K + K);
 
     const int tid = threadIdx.x, c = tid % TPR, r0 = tid / TPR;
@@ -590,7 +595,7 @@ __global__ void __launch_bounds__(MC_THETA_VNT) mc_theta_tma_kernel(McArgs a, co
         for (int k = 0; k < K; k++) tot[q][k] = 0.f;
 #pragma unroll
     for (int k = 0; k < K; k++) dtot[k] = 0.f;
-    for (int i = tid; i < n * K + K; i += MC_THETA_VNT) s_sum[i] = 0.0;  // a row may span warps
+    for (int i = tid; i < n * K + K; i += MC_THETA_VNT) s_sum[i] = make_float2(0.f, 0.f);  // a row may span warps
     unsigned int parity = 0u;
     bool failed = false;
     int j = 0;
@@ -617,9 +622,20 @@ __global__ void __launch_bounds__(MC_THETA_VNT) mc_theta_tma_kernel(McArgs a, co
             const uint2 xv = *reinterpret_cast<const uint2 *>(xc + (r * n + c * 4) * 2);
             const float x[4] = {__uint_as_float(xv.x << 16), __uint_as_float(xv.x & 0xFFFF0000u),
                                 __uint_as_float(xv.y << 16), __uint_as_float(xv.y & 0xFFFF0000u)};
+            float gr[K];  // the row's weights: 16-byte shared loads where the row is 16-byte aligned
+            if constexpr (K % 4 == 0) {
+#pragma unroll
+                for (int k4 = 0; k4 < K / 4; k4++) {
+                    const float4 v = reinterpret_cast<const float4 *>(gc + r * K)[k4];
+                    gr[4 * k4] = v.x; gr[4 * k4 + 1] = v.y; gr[4 * k4 + 2] = v.z; gr[4 * k4 + 3] = v.w;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < K; k++) gr[k] = gc[r * K + k];
+            }
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                const float g = gc[r * K + k];
+                const float g = gr[k];
                 den[k] += g;
                 if (g != 0.f) {
 #pragma unroll
@@ -651,7 +667,7 @@ __global__ void __launch_bounds__(MC_THETA_VNT) mc_theta_tma_kernel(McArgs a, co
         }
         return;
     }
-    // rows of a warp that share channel chunk c, then warps in a fixed order (FP64)
+    // rows of a warp that share channel chunk c, then warps in a fixed order (float-float)
 #pragma unroll
     for (int off = TPR; off < 32; off <<= 1) {
 #pragma unroll
@@ -667,14 +683,22 @@ __global__ void __launch_bounds__(MC_THETA_VNT) mc_theta_tma_kernel(McArgs a, co
 #pragma unroll
             for (int q = 0; q < 4; q++)
 #pragma unroll
-                for (int k = 0; k < K; k++) s_sum[k * n + c * 4 + q] += (double)tot[q][k];
+                for (int k = 0; k < K; k++) {
+                    float2 &dst = s_sum[k * n + c * 4 + q];
+                    const FF r = ff_add(FF{dst.x, dst.y}, ff_make(tot[q][k]));
+                    dst = make_float2(r.hi, r.lo);
+                }
             if (c == 0)
 #pragma unroll
-                for (int k = 0; k < K; k++) s_sum[K * n + k] += (double)dtot[k];
+                for (int k = 0; k < K; k++) {
+                    float2 &dst = s_sum[K * n + k];
+                    const FF r = ff_add(FF{dst.x, dst.y}, ff_make(dtot[k]));
+                    dst = make_float2(r.hi, r.lo);
+                }
         }
         __syncthreads();
     }
-    double *P = a.partials + (long)blockIdx.x * (K * n + K);
+    float2 *P = reinterpret_cast<float2 *>(a.partials) + (long)blockIdx.x * (K * n + K);
     for (int i = tid; i < K * n + K; i += MC_THETA_VNT) P[i] = s_sum[i];
 }
 
@@ -739,28 +763,48 @@ int mc_theta_tma_blocks_per_sm(int K, int n)
 int mc_theta_vec_supported(int n) { return n == 8 || n == 16 || n == 32 || n == 64 || n == 128 || n == 256; }
 int mc_theta_vec_grid(long T) { return (int)((T + MC_THETA_ROWS - 1) / MC_THETA_ROWS); }
 
-// One block per cluster k (blockDim >= n, a multiple of 32).  from_partials: theta_k from the
-// partial sums of `nparts` blocks (summed in block order); otherwise theta64 as given.  Then:
-// the FP32 copy, the three BF16 parts (rows k, K + k, 2K + k of theta_split) and ||theta_k||^2.
+// One block per cluster k: blockDim = nb * S, nb = n rounded up to a multiple of 32, S slices.
+// from_partials: theta_k from the float-float partial sums of `nparts` blocks -- slice s sums
+// the parts s, s + S, ... in order, then the S slice sums are added in slice order (fixed
+// order, deterministic; S dependent chains of nparts/S additions instead of one of nparts),
+// and one FP64 division per channel; otherwise theta64 as given (S = 1).  Then, in slice 0: the
+// FP32 copy, the three BF16 parts (rows k, K + k, 2K + k of theta_split) and ||theta_k||^2.
+constexpr int MC_PREP_MAX_THREADS = 1024;
+
 template <int K>
-__global__ void mc_theta_prepare_kernel(McArgs a, int nparts, int from_partials)
+__global__ void __launch_bounds__(MC_PREP_MAX_THREADS) mc_theta_prepare_kernel(McArgs a, int nparts, int from_partials)
 {
     __shared__ double s_red[32];
-    const int k = blockIdx.x, j = threadIdx.x, n = a.n;
+    __shared__ float2 s_part[MC_PREP_MAX_THREADS + 8];
+    const int k = blockIdx.x, n = a.n, nb = (n + 31) / 32 * 32;
+    const int j = threadIdx.x % nb, sl = threadIdx.x / nb, S = blockDim.x / nb;
     double th = 0.0;
     if (from_partials) {
-        double num = 0.0, den = 0.0;
-        for (int g = 0; g < nparts; g++) {
-            const double *P = a.partials + (long)g * (K * n + K);
-            if (j < n) num += P[k * n + j];
-            den += P[K * n + k];
+        const float2 *P = reinterpret_cast<const float2 *>(a.partials);
+        FF num = ff_make(0.f), den = ff_make(0.f);
+        for (int g = sl; g < nparts; g += S) {
+            const float2 *Pg = P + (long)g * (K * n + K);
+            if (j < n) num = ff_add(num, FF{Pg[k * n + j].x, Pg[k * n + j].y});
+            if (j == 0) den = ff_add(den, FF{Pg[K * n + k].x, Pg[K * n + k].y});
         }
-        th = (j < n && den != 0.0) ? num / den : 0.0;
-        if (j < n) a.theta64[k * n + j] = th;
-    } else if (j < n) {
+        s_part[threadIdx.x] = make_float2(num.hi, num.lo);
+        if (j == 0) s_part[MC_PREP_MAX_THREADS + (sl & 7)] = make_float2(den.hi, den.lo);
+        __syncthreads();
+        if (sl == 0) {
+            num = ff_make(0.f);
+            den = ff_make(0.f);
+            for (int q = 0; q < S; q++) {
+                num = ff_add(num, FF{s_part[q * nb + j].x, s_part[q * nb + j].y});
+                den = ff_add(den, FF{s_part[MC_PREP_MAX_THREADS + q].x, s_part[MC_PREP_MAX_THREADS + q].y});
+            }
+            const double dd = ff_value(den);
+            th = (j < n && dd != 0.0) ? ff_value(num) / dd : 0.0;
+            if (j < n) a.theta64[k * n + j] = th;
+        }
+    } else if (j < n && sl == 0) {
         th = a.theta64[k * n + j];
     }
-    if (j < n) {
+    if (sl == 0 && j < n) {
         a.theta_f32[k * n + j] = (float)th;
         const __nv_bfloat16 p1 = __double2bfloat16(th);
         const double r1 = th - (double)__bfloat162float(p1);
@@ -771,14 +815,14 @@ __global__ void mc_theta_prepare_kernel(McArgs a, int nparts, int from_partials)
         a.theta_split[(long)(K + k) * n + j] = __bfloat16_as_ushort(p2);
         a.theta_split[(long)(2 * K + k) * n + j] = __bfloat16_as_ushort(p3);
     }
-    double v = th * th;
+    double v = th * th;  // 0 outside slice 0
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if ((j & 31) == 0) s_red[j >> 5] = v;
+    if (sl == 0 && (j & 31) == 0) s_red[j >> 5] = v;
     __syncthreads();
-    if (j == 0) {
+    if (threadIdx.x == 0) {
         double s = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += s_red[w];
+        for (int w = 0; w < nb / 32; w++) s += s_red[w];
         a.tnorm[k] = (float)s;
     }
 }
@@ -787,11 +831,12 @@ template <int NKA, int K>
 static cudaError_t launch_theta_t(int grid, const McArgs &a, const float *gamma, cudaStream_t s)
 {
     const int nb = ((a.n + 31) / 32) * 32;
+    const int np = nb * std::min(8, std::max(1, MC_PREP_MAX_THREADS / nb));  // prepare: up to 8 slices
     if (gamma && a.theta_tma_grid > 0) {
         int r = -1;
         PASC_MC_TPR_SWITCH_R(r, a.n, ThetaTma<K>::template launch, a.theta_tma_grid, a, gamma, s)
         if (r < 0) return cudaErrorInvalidValue;
-        mc_theta_prepare_kernel<K><<<K, nb, 0, s>>>(a, a.theta_tma_grid, 1);
+        mc_theta_prepare_kernel<K><<<K, np, 0, s>>>(a, a.theta_tma_grid, 1);
     } else if (gamma && mc_theta_vec_supported(a.n)) {
         const int g = mc_theta_vec_grid(a.T);
         switch (a.n / 8) {
@@ -803,11 +848,11 @@ static cudaError_t launch_theta_t(int grid, const McArgs &a, const float *gamma,
             case 32: mc_theta_partial_vec_kernel<K, 32><<<g, MC_THETA_VNT, 0, s>>>(a, gamma); break;
             default: return cudaErrorInvalidValue;
         }
-        mc_theta_prepare_kernel<K><<<K, nb, 0, s>>>(a, g, 1);
+        mc_theta_prepare_kernel<K><<<K, np, 0, s>>>(a, g, 1);
     } else if (gamma) {
         if (a.n <= 128) mc_theta_partial_kernel<1, K><<<grid, MC_THETA_NT, 0, s>>>(a, gamma);
         else mc_theta_partial_kernel<2, K><<<grid, MC_THETA_NT, 0, s>>>(a, gamma);
-        mc_theta_prepare_kernel<K><<<K, nb, 0, s>>>(a, grid, 1);
+        mc_theta_prepare_kernel<K><<<K, np, 0, s>>>(a, grid, 1);
     } else {
         mc_theta_prepare_kernel<K><<<K, nb, 0, s>>>(a, 0, 0);
     }
