@@ -26,7 +26,10 @@ Besides the headline line it measures, on rank 0:
              written in FP32, the data read once) over its CUDA-event time, against the
              measured HBM copy bandwidth.
   cpu_baseline  the FP64 CPU oracle (a port of the reference's CPU path) on all host cores, and
-             on one (`one_thread`), and its time to 1e-6 relative objective.
+             on one (`one_thread`), and its time to 1e-6 relative objective; beside them the
+             reference's own SPGQPSolver template compiled from its headers (oracle/_ref, one
+             thread, `reference_one_thread`) on the same QP, with a check that its objective
+             equals the port's bit for bit.
   batched    the 256-signal uneven workload (T log-uniform in [1e3, 1e6], K in 2..5, epssqr
              log-uniform in [1, 1000]): every signal's TSSolver (SPG eps 1e-6, m 10; outer loop
              to 1e-6 relative change of L) solved by one batch handle (one CUDA graph launch
@@ -268,6 +271,36 @@ def oracle_iter_rate(sig, theta, eps2, T, iters, nthreads):
     return r.it / dt, dt
 
 
+def reference_iter_rate(sig, theta, eps2, T, iters):
+    """SPG iterations/s of the reference's own SPGQPSolver template, compiled from its headers
+    with host-array vectors (oracle/_ref; one thread), on the same QP; also whether its
+    objective after `iters` iterations equals the oracle port's bit for bit.  None where the
+    library could not be built."""
+    from oracle import pasc_oracle as O
+    try:
+        if O.build_ref() is None:
+            return None
+    except Exception:
+        return None
+    K = sig.K
+    gam = O.permute_blocked_to_interleaved(sig.gamma0, T, K)
+    b = O.residual_b(sig.data, theta, T, K, nthreads=0)
+    coeff = O.A_coeff(eps2, T)
+    t0 = time.perf_counter()
+    O.ref_spgqp_solve(b, gam, T, K, coeff, spgqpsolver_maxit=0, spgqpsolver_m=10, spgqpsolver_stop_difff=0)
+    t_init = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    _, it, _, fx = O.ref_spgqp_solve(b, gam, T, K, coeff, spgqpsolver_maxit=iters, spgqpsolver_m=10,
+                                     spgqpsolver_stop_difff=0)
+    dt = max(time.perf_counter() - t0 - t_init, 1e-9)
+    # the port on one thread sums in the template's order (its OpenMP sums on more threads do not)
+    _, r, _ = O.spgqp_solve(b, gam, T, K, coeff, O.spg_opts(maxit=iters, m=10, stop_difff=0), nthreads=1)
+    return {"value": it / dt, "unit": UNIT, "cores": 1, "kind": "reference",
+            "sample": f"{it} SPG iterations of the reference's SPGQPSolver template (oracle/_ref, "
+                      f"host-array vectors) on the full T={T} signal ({dt:.1f} s)",
+            "objective_equals_port": bool(fx == r.fx)}
+
+
 def run_reference(args, info):
     """The reference path's CPU implementation (the FP64 oracle port), rank 0 only."""
     from pasc_inference_gb300 import datagen
@@ -408,6 +441,7 @@ def main():
                                             f"signal ({dt:.1f} s, OpenMP)",
                                   "one_thread": {"value": rate1, "unit": UNIT, "cores": 1,
                                                  "sample": f"2 SPG iterations, same signal ({dt1:.1f} s)"},
+                                  "reference_one_thread": reference_iter_rate(sig, theta, args.eps2, T, 2),
                                   "time_to_1e-6_rel_obj": oracle_tts(sig, theta, args.eps2, T)}
     if info.rank == 0:
         print(json.dumps(result), flush=True)
@@ -487,9 +521,10 @@ def measure_tts(sig, theta, dev, eps_list=(1.0, 10.0, 100.0, 1000.0)):
     """Time to an objective within 1e-6 (relative) of the FP64 optimum, for every epssqr of
     the benchmark sweep: the plain FP64 GPU path (the reference's structure) and the mixed
     path from the same gamma0, both run without a stopping test (fixed iteration budgets
-    that reach the optimum: TTS_PLAN) and traced every few iterations.  The FP64 end point
-    is the optimum, certified by its Frank-Wolfe gap under the oracle's FP64 operator; the
-    mixed path's end point is compared with it (objective and gamma)."""
+    that reach the optimum: TTS_PLAN) and traced every few iterations.  The FP64 end point,
+    polished (pasc_gb300_polish), is the optimum, certified by its Frank-Wolfe gap under the
+    oracle's FP64 operator; the mixed path's end point is compared with it (objective and
+    gamma), before and after its own polish."""
     from pasc_inference_gb300 import PASC_PREC_FP64, PASC_PREC_MIXED, Problem, capi
     T, K = sig.T, sig.K
     out = {}
@@ -513,19 +548,28 @@ def measure_tts(sig, theta, dev, eps_list=(1.0, 10.0, 100.0, 1000.0)):
                     tr.append((time.perf_counter() - t0, st.it, st.fx))
                     if st.status != capi.PASC_SPG_RUNNING:
                         break
-                traces[name] = (tr, st, p.get_gamma())
-        tr64, st64, x64 = traces["fp64_plain"]
-        fstar = st64.fx
-        res = {"f_star_fp64": fstar, "fp64_optimum_fw_gap_rel": _fw_gap_rel(x64, sig.data, theta, T, K, eps2)}
-        for name, (tr, st, x) in traces.items():
+                x_end = p.get_gamma()
+                t0 = time.perf_counter()
+                ps = p.polish()
+                t_pol = time.perf_counter() - t0
+                traces[name] = (tr, st, x_end, p.get_gamma(), ps, t_pol)
+        tr64, st64, x64_end, x64, ps64, _ = traces["fp64_plain"]
+        fstar = ps64.fx
+        res = {"f_star_fp64": fstar, "fp64_optimum_fw_gap_rel": _fw_gap_rel(x64, sig.data, theta, T, K, eps2),
+               "fp64_end_gamma_rel_to_polished": float(np.linalg.norm(x64_end - x64) / np.linalg.norm(x64))}
+        for name, (tr, st, x, _, _, _) in traces.items():
             hit = next(((t, it) for t, it, f in tr if abs(f - fstar) <= 1e-6 * abs(fstar)), None)
             res[name] = {"seconds": hit[0] if hit else None, "spg_it": hit[1] if hit else None,
                          "final_rel_err": abs(st.fx - fstar) / abs(fstar), "final_it": st.it,
                          "status": capi.STATUS_NAMES.get(st.status, st.status)}
-        xm = traces["mixed_fused"][2]
+        _, _, xm, xmp, psm, t_pol = traces["mixed_fused"]
         res["mixed_fused"]["gamma_rel_err_vs_fp64_optimum"] = float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))
         res["mixed_fused"]["labels_equal_frac"] = float(np.mean(np.argmax(xm.reshape(T, K), 1) ==
                                                                np.argmax(x64.reshape(T, K), 1)))
+        res["mixed_fused"]["polished"] = {
+            "gamma_rel_err_vs_fp64_optimum": float(np.linalg.norm(xmp - x64) / np.linalg.norm(x64)),
+            "f_rel_err": abs(psm.fx - fstar) / abs(fstar), "rounds": psm.rounds, "cg_it": psm.cg_it,
+            "seconds": t_pol, "device_s": psm.time_s}
         a, b = res["fp64_plain"]["seconds"], res["mixed_fused"]["seconds"]
         res["speedup_vs_fp64_plain"] = (a / b) if (a and b) else None
         out[f"epssqr={eps2:g}"] = res
@@ -717,6 +761,8 @@ def measure_adjoint(dev, peak, eps0=300.0):
         t0 = time.perf_counter()
         st = p.spgqp_solve(spg_mixed)
         t1 = time.perf_counter()
+        pol = p.polish()
+        t1p = time.perf_counter()
         loss = p.recon_mse(sig.clean)
         deps, dX, dth, a = p.adjoint()
         t2 = time.perf_counter()
@@ -727,13 +773,16 @@ def measure_adjoint(dev, peak, eps0=300.0):
     B_cg = 40.0 * N + 4.0 * T
     cg_s = a.time_s / max(a.cg_it, 1)
     res.update({"loss": loss, "dloss_depssqr": deps, "solve_s": t1 - t0, "spg_it": st.it,
-                "adjoint_s": t2 - t1, "adjoint_device_s": a.time_s, "cg_it": a.cg_it,
+                "polish": {"s": t1p - t1, "device_s": pol.time_s, "rounds": pol.rounds, "cg_it": pol.cg_it,
+                           "step_rel": pol.step_rel, "face_changes": pol.face_changes},
+                "adjoint_s": t2 - t1p, "adjoint_device_s": a.time_s, "cg_it": a.cg_it,
                 "free_dims": a.free_dims,
                 "cg_iteration": {"us": cg_s * 1e6, "bytes": B_cg, "achieved": B_cg / cg_s / 1e9, "unit": "GB/s",
                                  "peak": peak, "frac": B_cg / cg_s / 1e9 / peak}})
     # FP64 GPU: gradient and central differences
     with loaded(PASC_PREC_FP64, eps0) as p:
         p.spgqp_solve(spg64)
+        p.polish()
         x0 = p.get_gamma()
         p.recon_mse(sig.clean)
         deps64, _, _, _ = p.adjoint()
@@ -744,6 +793,7 @@ def measure_adjoint(dev, peak, eps0=300.0):
             p.set_gamma(x0)
             p.update_b()
             p.spgqp_solve(spg64)
+            p.polish()
             lo.append(p.recon_mse(sig.clean))
     fd = (lo[0] - lo[1]) / (2 * h * eps0)
     # FP64 oracle on the host: solve (the reference's stop rule, |f - f_old| < 1e-12) + adjoint,
@@ -756,13 +806,14 @@ def measure_adjoint(dev, peak, eps0=300.0):
     _, dgo, _ = orc.recon_mse(xo, theta, sig.clean, T, K)
     orc.adjoint(xo, sig.data, theta, dgo, T, K, eps0)
     t_cpu = time.perf_counter() - t0
-    # the oracle's adjoint at the FP64 fixed point (the FP64 GPU solve above, ||d||^2 < 1e-26)
+    # the oracle's adjoint at the FP64 optimum (the FP64 GPU solve above, ||d||^2 < 1e-26, polished)
     _, dgo, _ = orc.recon_mse(x0, theta, sig.clean, T, K)
     deps_o = orc.adjoint(x0, sig.data, theta, dgo, T, K, eps0, cg_tol=1e-12)[0]
     res["checks"] = {"fd_central_h1e-4_fp64": fd, "adjoint_fp64": deps64, "oracle_fp64_at_fixed_point": deps_o,
                      "rel_mixed_vs_fd": abs(deps - fd) / abs(fd), "rel_fp64_vs_fd": abs(deps64 - fd) / abs(fd),
                      "rel_mixed_vs_oracle": abs(deps - deps_o) / abs(deps_o),
-                     "mixed_solve": "20000 SPG iterations, no stopping test (FP32 fixed point)"}
+                     "mixed_solve": "20000 SPG iterations, no stopping test (FP32 fixed point), then "
+                                    "pasc_gb300_polish (FP64 face-Newton rounds to the optimum)"}
     res["cpu_baseline_gradient_s"] = t_cpu
     res["cpu_baseline_cores"] = cpu_cores()
     # 20 gradient steps on log epssqr

@@ -369,6 +369,44 @@ int pasc_gb300_adjoint(pasc_gb300_problem *p, const double *dloss_dgamma, const 
                        double *dloss_depssqr, double *dloss_ddata, double *dloss_dtheta,
                        pasc_gb300_adjoint_stats *st);
 
+/* Polish (no reference counterpart): refines the problem's gamma to the optimum of its QP
+ * on the face the solve ended on.  The mixed path's FP32 iteration stalls where its updates
+ * drop below half an FP32 ulp of gamma, ~1e-6..1e-5 (relative 2-norm) from the optimum on
+ * ill-conditioned problems, at a point that depends on the rounding of the sums; each round
+ * here reads the free set F_t from one projected-gradient step (as the adjoint does), moves
+ * gamma onto that face (entries outside F_t to 0, their mass spread over F_t), solves
+ * P A P delta = -P (A gamma - b) on S in FP64 (FP32 conjugate gradients inside FP64 iterative
+ * refinement on mixed problems, the adjoint's solver), adds delta in FP64 and projects the
+ * timesteps that left their face back onto the simplex; a round that does not lower the FP64
+ * objective is undone, and the rounds end when a step stays on its face or the projected
+ * gradient is at the rounding level of b.  Mixed problems keep the result rounded once to FP32.  Afterwards get_fx returns
+ * the FP64 objective of the polished gamma; a dloss/dgamma kept by recon_mse is dropped.  Same
+ * restrictions as the adjoint (K <= 8, 1-D, no FEM reduction, theta not in the penalty). */
+typedef struct {
+    int rounds;             /* at most this many face-Newton rounds (4) */
+    double act_tol;         /* z_tk > act_tol is free (0: every entry a projected-gradient step
+                               leaves positive, so that small free entries of the optimum stay free) */
+    double cg_tol;          /* relative residual of each solve (1e-6: a round gains about six
+                               digits on the face; the next round starts from its end) */
+    int cg_maxit;           /* conjugate-gradient iterations per solve (2000) */
+} pasc_gb300_polish_opts;
+
+typedef struct {
+    int rounds;             /* rounds done */
+    int cg_it;              /* conjugate-gradient iterations, all rounds */
+    int kernel_launches;
+    long face_changes;      /* timesteps projected back onto the simplex in the last round */
+    int cg_status;          /* last solve: 1 converged, 2 cg_maxit reached, 4 stopped at the
+                               rounding level (p'Ap <= 0), 0 none run */
+    double cg_relres;       /* last solve: ||r|| / ||r_0|| at its end */
+    double step_rel;        /* ||delta|| / ||gamma|| of the last round */
+    double fx;              /* FP64 objective of the polished gamma */
+    double time_s;          /* device time (CUDA events) */
+} pasc_gb300_polish_stats;
+
+void pasc_gb300_polish_default_opts(pasc_gb300_polish_opts *o);
+int pasc_gb300_polish(pasc_gb300_problem *p, const pasc_gb300_polish_opts *o, pasc_gb300_polish_stats *st);
+
 /* ---------------------------------------------------------------------------------------
  * device-pointer kernels: the reference's GPU-side operations, usable on caller buffers
  * ------------------------------------------------------------------------------------- */

@@ -59,10 +59,18 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+REF_FLAT_PATH = os.path.join(HERE, "_ref", "libpasc_ref_flat.cpp")
+
+
 def build_ref() -> str | None:
-    """Compile the reference's own solver templates (needs the reference tree); None if absent."""
+    """Compile the reference's own solver templates: from the reference tree where it is
+    (build_ref.sh), else from the single translation unit that recipe wrote into oracle/_ref
+    (a machine without the tree, given a copy of this checkout); None if neither exists."""
     script = os.path.join(HERE, "build_ref.sh")
     subprocess.check_call(["sh", script])
+    if not os.path.exists(REF_LIB_PATH) and os.path.exists(REF_FLAT_PATH):
+        subprocess.check_call([os.environ.get("CXX", "g++"), "-std=c++14", "-O2", "-fPIC", "-shared",
+                               "-ffp-contract=off", "-w", REF_FLAT_PATH, "-o", REF_LIB_PATH])
     return REF_LIB_PATH if os.path.exists(REF_LIB_PATH) else None
 
 

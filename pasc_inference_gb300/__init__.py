@@ -296,6 +296,13 @@ class Problem:
         check(load().pasc_gb300_recon_mse(self._h, _vec(clean, self.T, "recon_mse"), C.byref(v)))
         return v.value
 
+    def polish(self, opts: capi.PolishOpts | None = None) -> capi.PolishStats:
+        """Refine gamma to the optimum of the QP on the face the solve ended on (FP64
+        face-Newton rounds; see pasc_gb300_polish)."""
+        st = capi.PolishStats()
+        check(load().pasc_gb300_polish(self._h, C.byref(opts or capi.polish_opts()), C.byref(st)))
+        return st
+
     def adjoint(self, dloss_dgamma=None, opts: capi.AdjointOpts | None = None):
         """Returns (dloss/d epssqr, dloss/d data [T], dloss/d theta [K], AdjointStats)."""
         deps = C.c_double()

@@ -58,6 +58,16 @@ class AdjointStats(C.Structure):
                 ("free_dims", C.c_long), ("cg_relres", C.c_double), ("time_s", C.c_double)]
 
 
+class PolishOpts(C.Structure):
+    _fields_ = [("rounds", C.c_int), ("act_tol", C.c_double), ("cg_tol", C.c_double), ("cg_maxit", C.c_int)]
+
+
+class PolishStats(C.Structure):
+    _fields_ = [("rounds", C.c_int), ("cg_it", C.c_int), ("kernel_launches", C.c_int),
+                ("face_changes", C.c_long), ("cg_status", C.c_int), ("cg_relres", C.c_double),
+                ("step_rel", C.c_double), ("fx", C.c_double), ("time_s", C.c_double)]
+
+
 class PascError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"pasc_gb300 error {code}: {msg}")
@@ -151,6 +161,8 @@ PROTOTYPES = {
     "pasc_gb300_theta_update_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p]),
     "pasc_gb300_adjoint_default_opts": (None, [C.POINTER(AdjointOpts)]),
     "pasc_gb300_recon_mse": (C.c_int, [_h, _dp, C.POINTER(C.c_double)]),
+    "pasc_gb300_polish_default_opts": (None, [C.POINTER(PolishOpts)]),
+    "pasc_gb300_polish": (C.c_int, [_h, C.POINTER(PolishOpts), C.POINTER(PolishStats)]),
     "pasc_gb300_adjoint": (C.c_int, [_h, C.c_void_p, C.POINTER(AdjointOpts), C.POINTER(C.c_double), C.c_void_p,
                                      C.c_void_p, C.POINTER(AdjointStats)]),
     "pasc_gb300_batch_create": (C.c_int, [C.POINTER(_h), C.c_int, _lp, _ip, _dp, C.c_int]),
@@ -212,6 +224,16 @@ def spgqp_opts(**kw) -> SpgqpOpts:
 def ts_opts(**kw) -> TsOpts:
     o = TsOpts()
     load().pasc_gb300_ts_default_opts(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
+
+
+def polish_opts(**kw) -> PolishOpts:
+    o = PolishOpts()
+    load().pasc_gb300_polish_default_opts(C.byref(o))
     for k, v in kw.items():
         if not hasattr(o, k):
             raise KeyError(k)

@@ -56,6 +56,10 @@ struct AdjDevState {
     unsigned int fall;  // clusters free at every timestep (their cluster-constant, zero-sum
                         // vectors are the null space of P A P on S)
     double nullc[8];    // component of lambda along that null space, per cluster
+    double rr64;        // FP32 refinement: FP64 r'r of the last residual
+    double rscale;      // FP32 refinement: the residual is handed to the FP32 solve times this
+                        // (its rms brought to 1: a small residual would otherwise lose its
+                        // products p'q to FP32 underflow), the correction divided by it
 };
 
 struct AdjointWork {
@@ -180,23 +184,24 @@ __global__ void __launch_bounds__(ADJ_NT) recon_mse_kernel(const double *gam, co
     }
 }
 
-// free sets (from z = Proj(gamma - a g), see the head of the file), r = P dl/dgamma,
-// lambda = 0, both search-direction buffers 0, r'r and dim S.
-template <int K>
+// free sets (from z = Proj(gamma - a g), see the head of the file), r = P dl/dgamma
+// (POLISH: r = -P g, the face-Newton step's right-hand side), lambda = 0, both
+// search-direction buffers 0, r'r and dim S.
+template <int K, bool POLISH = false>
 __global__ void __launch_bounds__(ADJ_NT) adj_setup_kernel(const double *gam, const double *gl, const double *data,
                                                            const double *theta, long T, double coeff, double bscale,
                                                            double act_tol, unsigned int *mask, double *lam,
                                                            double *r, double *p0, double *p1,
                                                            double *partials, AdjDevState *st)
 {
-    __shared__ double scratch[(2 + K) * (ADJ_NT / 32)];
+    __shared__ double scratch[(3 + K) * (ADJ_NT / 32)];
     const double a = 1.0 / (8.0 * coeff + fabs(bscale));
-    double v2[2 + K];
+    double v2[3 + K];
 #pragma unroll
-    for (int j = 0; j < 2 + K; j++) v2[j] = 0.0;
+    for (int j = 0; j < 3 + K; j++) v2[j] = 0.0;
     for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
         const double x = data[t];
-        double z[K], zs[K];
+        double z[K], zs[K], grad[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const double gc = gam[t * K + k];
@@ -204,17 +209,25 @@ __global__ void __launch_bounds__(ADJ_NT) adj_setup_kernel(const double *gam, co
             if (t > 0) ag += 2.0 * (gc - gam[(t - 1) * K + k]);
             if (t < T - 1) ag += 2.0 * (gc - gam[(t + 1) * K + k]);
             const double res = x - theta[k];
-            z[k] = gc - a * (coeff * ag - bscale * res * res);
+            grad[k] = coeff * ag - bscale * res * res;
+            v2[2 + K] += (bscale * res * res) * (bscale * res * res);
+            z[k] = gc - a * grad[k];
         }
-        project_ref_f64(z, K, zs);
         unsigned int m = 0u;
         double v[K];
+        if (POLISH) {
+            m = mask[t];  // the face gamma was snapped onto (adj_polish_mask_kernel, adj_polish_snap_kernel)
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            m |= (z[k] > act_tol ? 1u : 0u) << k;
-            v[k] = gl[t * K + k];
+            for (int k = 0; k < K; k++) v[k] = -grad[k];
+        } else {
+            project_ref_f64(z, K, zs);
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                m |= (z[k] > act_tol ? 1u : 0u) << k;
+                v[k] = gl[t * K + k];
+            }
+            mask[t] = m;
         }
-        mask[t] = m;
         proj_free<K>(v, m);
 #pragma unroll
         for (int k = 0; k < K; k++) {
@@ -229,8 +242,8 @@ __global__ void __launch_bounds__(ADJ_NT) adj_setup_kernel(const double *gam, co
 #pragma unroll
         for (int k = 0; k < K; k++) v2[2 + k] += (double)((m >> k) & 1u);
     }
-    double w[2 + K];
-    if (!grid_sum<2 + K>(v2, partials, &st->counter, scratch, w)) return;
+    double w[3 + K];
+    if (!grid_sum<3 + K>(v2, partials, &st->counter, scratch, w)) return;
     if (threadIdx.x == 0) {
         st->rr = st->rr0 = w[0];
         st->free_dims = w[1];
@@ -242,6 +255,9 @@ __global__ void __launch_bounds__(ADJ_NT) adj_setup_kernel(const double *gam, co
         st->beta = 0.0;
         st->pcur = 0;
         st->status = (w[0] > 0.0) ? ADJ_RUNNING : ADJ_CONVERGED;
+        // POLISH: a projected gradient at the rounding level of b (||P g|| <= 1e-12 ||b||) is
+        // stationary already; a solve on it would only fit noise
+        if (POLISH && w[0] <= 1e-24 * w[2 + K]) st->status = ADJ_CONVERGED;
         if (!isfinite(w[0])) st->status = ADJ_BREAKDOWN;
     }
 }
@@ -367,6 +383,7 @@ __global__ void __launch_bounds__(ADJ_NT) adj_residual_kernel(const unsigned int
                                                               AdjDevState *st)
 {
     __shared__ double scratch[1 * (ADJ_NT / 32)];
+    const double rscale = st->rscale;
     double v[1] = {0.0};
     for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
         double y[K];
@@ -383,7 +400,7 @@ __global__ void __launch_bounds__(ADJ_NT) adj_residual_kernel(const unsigned int
         for (int k = 0; k < K; k++) {
             const long i = t * K + k;
             const double rv = rhs[i] - y[k];
-            r32[i] = (float)rv;
+            r32[i] = (float)(rv * rscale);
             p0[i] = 0.f;
             p1[i] = 0.f;
             d32[i] = 0.f;
@@ -393,8 +410,9 @@ __global__ void __launch_bounds__(ADJ_NT) adj_residual_kernel(const unsigned int
     double w[1];
     if (!grid_sum<1>(v, partials, &st->counter, scratch, w)) return;
     if (threadIdx.x == 0) {
-        st->rr = w[0];
-        st->rr_in0 = w[0];
+        st->rr64 = w[0];
+        st->rr = w[0] * rscale * rscale;  // r'r of the scaled FP32 residual the inner solve starts from
+        st->rr_in0 = st->rr;
         st->beta = 0.0;
         st->pcur = 0;
         if (!isfinite(w[0])) st->status = ADJ_BREAKDOWN;
@@ -506,12 +524,13 @@ __global__ void __launch_bounds__(ADJ_NT) adj_update32_kernel(float *d, float *r
 // amplified by the solve of the next step)
 template <int K>
 __global__ void __launch_bounds__(ADJ_NT) adj_accum_kernel(double *lam, const float *d, const unsigned int *mask,
-                                                           long T)
+                                                           long T, const AdjDevState *st)
 {
+    const double inv = 1.0 / st->rscale;
     for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
         double v[K];
 #pragma unroll
-        for (int k = 0; k < K; k++) v[k] = lam[t * K + k] + (double)d[t * K + k];
+        for (int k = 0; k < K; k++) v[k] = lam[t * K + k] + (double)d[t * K + k] * inv;
         proj_free<K>(v, mask[t]);
 #pragma unroll
         for (int k = 0; k < K; k++) lam[t * K + k] = v[k];
@@ -597,6 +616,153 @@ __global__ void __launch_bounds__(ADJ_NT) adj_output_kernel(const double *lam, c
 #pragma unroll
         for (int k = 0; k < K; k++) out[1 + k] = w[1 + k];
     }
+}
+
+// Polish, first pass: the free set of every timestep from one projected-gradient step (as in
+// adj_setup_kernel).
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_polish_mask_kernel(const double *gam, const double *data,
+                                                                 const double *theta, long T, double coeff,
+                                                                 double bscale, double act_tol, unsigned int *mask)
+{
+    const double a = 1.0 / (8.0 * coeff + fabs(bscale));
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        const double x = data[t];
+        double z[K], zs[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const double gc = gam[t * K + k];
+            double ag = 0.0;
+            if (t > 0) ag += 2.0 * (gc - gam[(t - 1) * K + k]);
+            if (t < T - 1) ag += 2.0 * (gc - gam[(t + 1) * K + k]);
+            const double res = x - theta[k];
+            z[k] = gc - a * (coeff * ag - bscale * res * res);
+        }
+        project_ref_f64(z, K, zs);
+        unsigned int m = 0u;
+#pragma unroll
+        for (int k = 0; k < K; k++) m |= (z[k] > act_tol ? 1u : 0u) << k;
+        mask[t] = m;
+    }
+}
+
+// Polish, second pass: gamma onto its face -- entries outside the free set to 0, their mass
+// spread evenly over the free ones (the sum stays 1); the Newton step then starts on the face.
+// (A timestep with no free entry -- not possible for z on the simplex with act_tol < 1/K --
+// is left as it is.)
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_polish_snap_kernel(double *gam, const unsigned int *mask, long T)
+{
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        const unsigned int m = mask[t];
+        const int nf = __popc(m);
+        if (nf == 0 || nf == K) continue;
+        double y[K], out = 0.0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            y[k] = gam[t * K + k];
+            if (!((m >> k) & 1u)) out += y[k];
+        }
+        const double share = out / nf;
+#pragma unroll
+        for (int k = 0; k < K; k++) gam[t * K + k] = ((m >> k) & 1u) ? y[k] + share : 0.0;
+    }
+}
+
+// Polish: gamma += delta (delta = lambda of the face-Newton solve, in S: zero off the free
+// set, zero sum per timestep); a timestep with a negative entry left its face and is projected
+// back onto the simplex (FP64, the reference's order).  x32: the FP32 state, rounded from the
+// result (mixed problems; may be null).  out[0..2] = projected timesteps, sum delta^2,
+// sum gamma^2.
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_polish_apply_kernel(const double *lam, double *gam, float *x32, long T,
+                                                                  double *partials, unsigned int *ticket, double *out)
+{
+    __shared__ double scratch[3 * (ADJ_NT / 32)];
+    double v[3] = {0.0, 0.0, 0.0};
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        double y[K], ys[K], d2 = 0.0;
+        bool neg = false;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const double dk = lam[t * K + k];
+            y[k] = gam[t * K + k] + dk;
+            d2 += dk * dk;
+            neg |= !(y[k] >= 0.0);
+        }
+        if (neg) project_ref_f64(y, K, ys);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            gam[t * K + k] = y[k];
+            if (x32) x32[t * K + k] = (float)y[k];
+            v[2] += y[k] * y[k];
+        }
+        v[0] += neg ? 1.0 : 0.0;
+        v[1] += d2;
+    }
+    double w[3];
+    if (!grid_sum<3>(v, partials, ticket, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        out[0] = w[0];
+        out[1] = w[1];
+        out[2] = w[2];
+    }
+}
+
+// Polish: the right-hand side -P g minus its component in the null space of P A P (the
+// st->nullc adj_nullmean_kernel found for it); r'r starts the solve.  Where clusters are free
+// at every timestep, moving their weights by constants that sum to zero changes f only
+// linearly, g'v, which vanishes at the optimum: the Newton step on the face ignores it (the
+// solve needs a right-hand side in the range of P A P).
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_polish_rhs_kernel(double *r, long T, double *partials, AdjDevState *st)
+{
+    __shared__ double scratch[1 * (ADJ_NT / 32)];
+    double c[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) c[k] = st->nullc[k];
+    double v[1] = {0.0};
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const double y = r[t * K + k] - c[k];
+            r[t * K + k] = y;
+            v[0] += y * y;
+        }
+    }
+    double w[1];
+    if (!grid_sum<1>(v, partials, &st->counter, scratch, w)) return;
+    if (threadIdx.x == 0) {
+        st->rr = st->rr0 = w[0];
+        st->status = (w[0] > 0.0) ? ADJ_RUNNING : ADJ_CONVERGED;
+        if (!isfinite(w[0])) st->status = ADJ_BREAKDOWN;
+    }
+}
+
+// out[0] = 1/2 gamma'A gamma - b'gamma in FP64 (A = coeff A_hat, b = bscale (x - theta)^2)
+template <int K>
+__global__ void __launch_bounds__(ADJ_NT) adj_objective_kernel(const double *gam, const double *data,
+                                                               const double *theta, long T, double coeff,
+                                                               double bscale, double *partials,
+                                                               unsigned int *ticket, double *out)
+{
+    __shared__ double scratch[1 * (ADJ_NT / 32)];
+    double v[1] = {0.0};
+    for (long t = blockIdx.x * (long)ADJ_NT + threadIdx.x; t < T; t += (long)gridDim.x * ADJ_NT) {
+        const double x = data[t];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const double gc = gam[t * K + k];
+            double ag = 0.0;
+            if (t > 0) ag += 2.0 * (gc - gam[(t - 1) * K + k]);
+            if (t < T - 1) ag += 2.0 * (gc - gam[(t + 1) * K + k]);
+            const double res = x - theta[k];
+            v[0] += gc * (0.5 * coeff * ag - bscale * res * res);
+        }
+    }
+    double w[1];
+    if (!grid_sum<1>(v, partials, ticket, scratch, w)) return;
+    if (threadIdx.x == 0) out[0] = w[0];
 }
 
 // ---------------------------------------------------------------------------------------
@@ -743,7 +909,12 @@ static int adj_refine(pasc_gb300_problem *p, AdjDevState *h, int *launches)
 {
     AdjointWork *w = p->adj;
     cudaStream_t s = p->stream;
+    double rr_last = h->rr0;  // FP64 r'r of the last residual (the right-hand side's at first)
     auto residual = [&]() -> int {
+        // scale of the next FP32 solve from the last residual: its rms about 1 (then 1e-4 after
+        // each further inner solve, well inside the FP32 range)
+        h->rscale = rr_last > 0.0 && isfinite(rr_last) ? 1.0 / sqrt(rr_last / (double)p->N) : 1.0;
+        ACU(cudaMemcpyAsync(&w->st->rscale, &h->rscale, sizeof(double), cudaMemcpyHostToDevice, s));
         PASC_ADJ_DISPATCH(p->K, (adj_residual_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(
                                     w->mask, w->lam, w->r, w->r32, w->pb32[0], w->pb32[1], w->d32, p->T, p->coeffA,
                                     w->partials, w->st)));
@@ -751,6 +922,7 @@ static int adj_refine(pasc_gb300_problem *p, AdjDevState *h, int *launches)
         *launches += 1;
         ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
         ACU(cudaStreamSynchronize(s));
+        rr_last = h->rr64;
         return PASC_OK;
     };
     ACHK(residual());  // lambda = 0: r32 = the right-hand side
@@ -762,7 +934,8 @@ static int adj_refine(pasc_gb300_problem *p, AdjDevState *h, int *launches)
             ACU(cudaStreamSynchronize(s));
         }
         if (h->status != ADJ_INNER_DONE) break;  // breakdown
-        PASC_ADJ_DISPATCH(p->K, (adj_accum_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(w->lam, w->d32, w->mask, p->T)));
+        PASC_ADJ_DISPATCH(p->K, (adj_accum_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(w->lam, w->d32, w->mask, p->T,
+                                                                                   w->st)));
         ACU(cudaGetLastError());
         *launches += 1;
         ACHK(residual());
@@ -884,12 +1057,170 @@ int pasc_gb300_adjoint(pasc_gb300_problem *p, const double *dloss_dgamma, const 
         stats->status = h->status;
         stats->kernel_launches = launches;
         stats->free_dims = (long)h->free_dims;
-        stats->cg_relres = h->rr0 > 0.0 ? sqrt(h->rr / h->rr0) : 0.0;
+        stats->cg_relres = h->rr0 > 0.0 ? sqrt((mixed ? h->rr64 : h->rr) / h->rr0) : 0.0;
         stats->time_s = ms * 1e-3;
     }
     if (h->status == ADJ_BREAKDOWN)
         return afail(PASC_ERR_STATE, "adjoint: conjugate gradients broke down (non-finite values, or the "
                                      "right-hand side has a component in the null space of P A P)");
+    return PASC_OK;
+}
+
+void pasc_gb300_polish_default_opts(pasc_gb300_polish_opts *o)
+{
+    if (!o) return;
+    o->rounds = 4;
+    o->act_tol = 0.0;
+    o->cg_tol = 1e-6;
+    o->cg_maxit = 2000;
+}
+
+int pasc_gb300_polish(pasc_gb300_problem *p, const pasc_gb300_polish_opts *o, pasc_gb300_polish_stats *stats)
+{
+    if (!p) return afail(PASC_ERR_ARG, "polish: NULL problem");
+    pasc_gb300_polish_opts od;
+    pasc_gb300_polish_default_opts(&od);
+    if (!o) o = &od;
+    if (o->rounds < 0 || o->cg_maxit < 0 || !(o->cg_tol >= 0.0)) return afail(PASC_ERR_ARG, "polish: bad options");
+    ACU(cudaSetDevice(p->device));
+    ACHK(ensure_work(p));
+    AdjointWork *w = p->adj;
+    cudaStream_t s = p->stream;
+    const bool mixed = p->precision == PASC_PREC_MIXED;
+    // the FP64 gamma the rounds refine: the problem's own (fp64) or a widened copy of the FP32
+    // state, written back rounded once at the end (mixed)
+    double *gam = mixed ? w->gam : p->x;
+    double *backup = w->gl;  // gamma at the start of a round (a kept dloss/dgamma is dropped anyway)
+    if (mixed) ACU(launch_f32_to_f64(p->xb[p->cur], gam, p->N, s));
+    if (mixed) ACHK(ensure_adj_graph32(p));
+    else ACHK(ensure_adj_graph(p));
+    ACU(cudaEventRecord(p->ev0, s));
+    AdjDevState *h = w->st_h;
+    int launches = mixed ? 1 : 0, rounds = 0, cg_it = 0, cg_status = 0;
+    double face_changes = 0.0, step_rel = 0.0, cg_relres = 0.0;
+    auto objective = [&](double *f) -> int {
+        PASC_ADJ_DISPATCH(p->K, (adj_objective_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(
+                                    gam, p->data64, p->theta64, p->T, p->coeffA, p->coeffB, w->partials, w->ticket,
+                                    w->out)));
+        ACU(cudaGetLastError());
+        launches++;
+        ACU(cudaMemcpyAsync(w->out_h, w->out, sizeof(double), cudaMemcpyDeviceToHost, s));
+        ACU(cudaStreamSynchronize(s));
+        *f = w->out_h[0];
+        return PASC_OK;
+    };
+    double f = 0.0;
+    ACHK(objective(&f));
+    for (int r = 0; r < o->rounds; r++) {
+        memset(h, 0, sizeof *h);
+        h->tol = o->cg_tol;
+        h->maxit = o->cg_maxit;
+        ACU(cudaMemcpyAsync(w->st, h, sizeof *h, cudaMemcpyHostToDevice, s));
+        ACU(cudaMemcpyAsync(backup, gam, sizeof(double) * p->N, cudaMemcpyDeviceToDevice, s));
+        PASC_ADJ_DISPATCH(p->K, {
+            adj_polish_mask_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(gam, p->data64, p->theta64, p->T, p->coeffA,
+                                                                  p->coeffB, o->act_tol, w->mask);
+            adj_polish_snap_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(gam, w->mask, p->T);
+        });
+        ACU(cudaGetLastError());
+        launches += 2;
+        PASC_ADJ_DISPATCH(p->K, (adj_setup_kernel<KK, true><<<w->grid, ADJ_NT, 0, s>>>(
+                                    gam, nullptr, p->data64, p->theta64, p->T, p->coeffA, p->coeffB, o->act_tol,
+                                    w->mask, w->lam, w->r, w->pb[0], w->pb[1], w->partials, w->st)));
+        ACU(cudaGetLastError());
+        launches++;
+        ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
+        ACU(cudaStreamSynchronize(s));
+        if (h->status == ADJ_RUNNING && __builtin_popcount(h->fall) >= 2) {
+            PASC_ADJ_DISPATCH(p->K, {
+                adj_nullmean_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(w->r, p->T, w->partials, w->st);
+                adj_polish_rhs_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(w->r, p->T, w->partials, w->st);
+            });
+            ACU(cudaGetLastError());
+            launches += 2;
+            ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
+            ACU(cudaStreamSynchronize(s));
+        }
+        if (h->status == ADJ_CONVERGED) {  // stationary on the face (to rounding): keep the snap if it did not raise f
+            double fs = 0.0;
+            ACHK(objective(&fs));
+            if (fs <= f + 1e-15 * fabs(f)) f = fs;
+            else ACU(cudaMemcpyAsync(gam, backup, sizeof(double) * p->N, cudaMemcpyDeviceToDevice, s));
+            face_changes = 0.0;
+            break;
+        }
+        if (h->status != ADJ_RUNNING) return afail(PASC_ERR_STATE, "polish: non-finite gradient");
+        const double rr0 = h->rr0;
+        if (mixed) {
+            ACHK(adj_refine(p, h, &launches));
+        } else {
+            while (h->status == ADJ_RUNNING) {
+                ACU(cudaGraphLaunch(w->chunk, s));
+                launches += 2 * ADJ_CHUNK;
+                ACU(cudaMemcpyAsync(h, w->st, sizeof *h, cudaMemcpyDeviceToHost, s));
+                ACU(cudaStreamSynchronize(s));
+            }
+        }
+        cg_it += h->it;
+        cg_status = h->status == ADJ_INNER_DONE ? ADJ_CONVERGED : h->status;
+        cg_relres = h->rr0 > 0.0 ? sqrt((mixed ? h->rr64 : h->rr) / h->rr0) : 0.0;
+        // conjugate gradients stop short (p'q <= 0) only where the residual has reached the
+        // rounding level of the operator: lambda is then the last iterate (fp64; it is kept
+        // only if it reduced the residual) or the corrections of the completed refinement
+        // steps (mixed)
+        if (h->status == ADJ_BREAKDOWN && !mixed && !(h->rr < rr0)) break;
+        if (__builtin_popcount(h->fall) >= 2) {  // the step orthogonal to the null space, as in the adjoint
+            PASC_ADJ_DISPATCH(p->K, {
+                adj_nullmean_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(w->lam, p->T, w->partials, w->st);
+                adj_nullsub_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(w->lam, p->T, w->st);
+            });
+            ACU(cudaGetLastError());
+            launches += 2;
+        }
+        PASC_ADJ_DISPATCH(p->K, (adj_polish_apply_kernel<KK><<<w->grid, ADJ_NT, 0, s>>>(
+                                    w->lam, gam, nullptr, p->T, w->partials, w->ticket, w->out)));
+        ACU(cudaGetLastError());
+        launches++;
+        ACU(cudaMemcpyAsync(w->out_h, w->out, sizeof(double) * 3, cudaMemcpyDeviceToHost, s));
+        ACU(cudaStreamSynchronize(s));
+        const double fc = w->out_h[0], sr = w->out_h[2] > 0.0 ? sqrt(w->out_h[1] / w->out_h[2]) : 0.0;
+        double fnew = 0.0;
+        ACHK(objective(&fnew));
+        if (!(fnew <= f + 1e-15 * fabs(f))) {  // no descent: keep the round's starting gamma and stop
+            ACU(cudaMemcpyAsync(gam, backup, sizeof(double) * p->N, cudaMemcpyDeviceToDevice, s));
+            break;
+        }
+        f = fnew;
+        rounds = r + 1;
+        face_changes = fc;
+        step_rel = sr;
+        if (face_changes == 0.0) break;  // the step stayed on its face: a further round would only
+                                         // repeat the solve to its tolerance
+    }
+    if (mixed) {
+        ACU(launch_f64_to_f32(gam, p->xb[p->cur], p->N, s));
+        launches++;
+        ACU(launch_f32_to_f64(p->xb[p->cur], gam, p->N, s));
+        ACHK(objective(&f));  // of the gamma kept: the FP32 rounding of the polished one
+    }
+    ACU(cudaEventRecord(p->ev1, s));
+    ACU(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+    p->fx_last = f;
+    p->have_fx = true;
+    w->have_gl = false;  // a stored dloss/dgamma belongs to the gamma before the polish
+    if (stats) {
+        stats->rounds = rounds;
+        stats->cg_it = cg_it;
+        stats->kernel_launches = launches;
+        stats->face_changes = (long)face_changes;
+        stats->cg_status = cg_status;
+        stats->cg_relres = cg_relres;
+        stats->step_rel = step_rel;
+        stats->fx = f;
+        stats->time_s = ms * 1e-3;
+    }
     return PASC_OK;
 }
 

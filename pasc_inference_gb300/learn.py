@@ -17,13 +17,15 @@ from . import capi
 
 
 def descend_log_epssqr(problem, clean, steps: int = 20, lr: float | None = None, first_step: float = 0.5,
-                       spg=None, adj=None, min_epssqr: float = 1e-8):
+                       spg=None, adj=None, min_epssqr: float = 1e-8, polish: bool = True):
     """Runs `steps` gradient steps on u = log(epssqr), starting from problem.epssqr, the
     problem's data, theta and current gamma (each solve warm-starts from the previous gamma).
     lr None: chosen so that the first step moves u by `first_step`.  spg None: each solve runs
     20000 SPG iterations with no stopping test, which brings the mixed path to its fixed point
     on the benchmark sizes (T <= 1e6): the gradient jumps where the free set changes, so it
     has to be taken at the fixed point, not where a |f - f_old| test happened to stop.
+    polish: after each solve, Problem.polish moves gamma from the solve's end point (on the
+    mixed path an FP32 stall 1e-6..1e-5 from the optimum) onto the optimum of its face.
     Returns one record per step: epssqr, loss, dloss/du, SPG iterations, CG iterations,
     solve and adjoint seconds."""
     spg = spg or capi.spgqp_opts(m=10, maxit=20000, stop_difff=0)
@@ -35,6 +37,8 @@ def descend_log_epssqr(problem, clean, steps: int = 20, lr: float | None = None,
         problem.update_b()
         t0 = time.perf_counter()
         st = problem.spgqp_solve(spg)
+        if polish:
+            problem.polish()
         t1 = time.perf_counter()
         loss = problem.recon_mse(clean)
         deps, _, _, ast = problem.adjoint(None, adj)

@@ -26,6 +26,9 @@ U[1e3, 1e5], noise 0.5), theta fixed at the levels, for every epssqr of the swee
     1.3e-5 from the FP64 optimum, depending on the rounding of the compiled sweep (measured on
     four builds): the slow modes, flat to 1e-4 of the largest curvature, magnify the FP32
     rounding of gamma and of its gradient.
+  * the mixed end point polished (pasc_gb300_polish: FP64 Newton rounds on its face) is the
+    optimum rounded to FP32: gamma within 1e-6 (measured 1.4e-8 at every epssqr), objective
+    within 1e-9, labels equal on >= 99.999%.
 The optimum of this convex QP does not depend on the start, so the oracle's fixed-point check
 from the GPU's FP64 end point pins it as well as a solve from gamma0 would; at epssqr 100 and
 1000 the latter takes the oracle 2250 and 15000 iterations (about 2 and 12 minutes on 16 host
@@ -126,11 +129,13 @@ def test_signal_1e7_k3_vs_oracle(gpulib, oracle, signal, eps2):
         assert _rel_l2(x64, xo) <= 1e-6, (eps2, _rel_l2(x64, xo))
         fstar, xstar = ro.fx, xo
 
-    # the mixed path at its fixed point
+    # the mixed path at its fixed point, then polished
     with _load(sig, eps2, PASC_PREC_MIXED) as p:
         st = p.spgqp_solve(capi.spgqp_opts(m=10, maxit=25000, stop_difff=0))
         assert st.status in (capi.PASC_SPG_MAXIT, capi.PASC_SPG_DAD_ZERO), st.status
         xm = p.get_gamma()
+        ps = p.polish()
+        xp = p.get_gamma()
     fm, _ = _objective_and_gap(oracle, xm, b, T, K, coeff)
     assert abs(st.fx - fstar) <= 1e-6 * abs(fstar), (eps2, st.fx, fstar)
     assert abs(fm - fstar) <= 1e-6 * abs(fstar), (eps2, fm, fstar)
@@ -138,6 +143,11 @@ def test_signal_1e7_k3_vs_oracle(gpulib, oracle, signal, eps2):
     assert err <= (2e-5 if eps2 >= 1000.0 else 1e-5), (eps2, err)
     lab = np.argmax(xm.reshape(T, K), axis=1) == np.argmax(xstar.reshape(T, K), axis=1)
     assert np.mean(lab) >= 0.9999, (eps2, np.mean(lab))
+    # polished: the optimum rounded to FP32 (measured 1.4e-8 for every epssqr)
+    errp = _rel_l2(xp, xstar)
+    assert errp <= 1e-6, (eps2, err, errp, ps.rounds, ps.cg_status)
+    assert abs(ps.fx - fstar) <= 1e-9 * abs(fstar), (eps2, ps.fx, fstar)
+    assert np.mean(np.argmax(xp.reshape(T, K), axis=1) == np.argmax(xstar.reshape(T, K), axis=1)) >= 0.99999
 
 
 def test_multichannel_1e6_n128_k8_vs_oracle(gpulib, oracle):
