@@ -56,6 +56,12 @@ struct SweepArgs {
     // theta in the penalty (GraphH1FEMModel with usethetainpenalty): block k of A is
     // coeff * kw[k] * A_hat with kw[k] = theta_k^2; null: every block is coeff * A_hat
     const float *kw = nullptr;
+    // bulk-copy sweep with 16 values per thread (K = 4, 8): tensor maps of the two gamma
+    // buffers and of the materialised b as rows of 16 floats from the start of their front
+    // pads (swz != 0: the tiles come in with the 64-byte swizzle, sweep_tma.cuh), and the row
+    // of timestep 0
+    CUtensorMap tm_x[2], tm_b;
+    int swz = 0, roff = 0;
 };
 
 // Graph (R > 1) mode, mixed path (graph.cu): x and d ping-pong, buffer st->cur current.
@@ -207,6 +213,13 @@ int sweep_tma_tile_width();
 int sweep_tma_max_tile();
 // bmat: the materialised-b form; tp: the theta-in-penalty form (SweepArgs::kw set)
 int sweep_tma_blocks_per_sm(int K, bool init, bool bmat = false, bool tp = false);
+// tensor map over n floats at base (16-byte aligned, n a multiple of 16) as rows of 16 floats,
+// box 16 x rows_per_box, 64-byte swizzle
+cudaError_t sweep_tma_make_rowmap(CUtensorMap *map, const float *base, long n, int rows_per_box);
+// threads per block of the bulk-copy sweep for K (its tile rows), and whether it reads 16
+// values per thread (the swizzled form applies)
+int sweep_tma_threads(int K);
+bool sweep_tma_rows16(int K);
 cudaError_t launch_sweep_tma(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);
 cudaError_t launch_theta_f32(int K, int grid, const ThetaArgs &a, cudaStream_t s);
 cudaError_t launch_project_f32(float *x, long T, int K, cudaStream_t s);

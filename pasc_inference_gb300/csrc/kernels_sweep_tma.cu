@@ -20,6 +20,8 @@
 // Every wait on an mbarrier is bounded: a wait that gives up sets the error word of the
 // device state (the host then reports PASC_ERR_TIMEOUT), the block waits once more, bounded,
 // for the copies it has in flight, and leaves its tile loop.
+#include <string.h>
+
 #include "sweep_tma.cuh"
 #include "sweep_common.cuh"
 
@@ -38,15 +40,18 @@ struct TmaShape {
     static constexpr int MinBlocks = K <= 3 ? 8 : (K == 4 ? 6 : (K == 5 ? 5 : 0));
 };
 
-template <int K, int NT, bool INIT, int MODE>
-__global__ void __launch_bounds__(NT, TmaShape<K>::MinBlocks) spg_sweep_tma_kernel(SweepArgs a)
+// SWZ (R*K == 16 only): tiles by tensor copies with the 64-byte swizzle (sweep_tma.cuh); the
+// stages then start at a 512-byte aligned shared address (512 bytes more dynamic memory).
+template <int K, int NT, bool INIT, int MODE, bool SWZ = false>
+__global__ void __launch_bounds__(NT, TmaShape<K>::MinBlocks) spg_sweep_tma_kernel(const __grid_constant__ SweepArgs a)
 {
     constexpr bool BM = MODE == 1, TP = MODE == 2;
     constexpr int R = TmaShape<K>::R;
     constexpr int P = NT * R;
     constexpr int W = P - 2 * TMA_HALO;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    TmaSmem<K, NT, BM, R> &sm = *reinterpret_cast<TmaSmem<K, NT, BM, R> *>(smem_raw);
+    unsigned char *smem_base = SWZ ? smem_raw + ((512u - (smem_addr(smem_raw) & 511u)) & 511u) : smem_raw;
+    TmaSmem<K, NT, BM, R> &sm = *reinterpret_cast<TmaSmem<K, NT, BM, R> *>(smem_base);
 
     SpgDevState *st = a.st;
     if (st->status != PASC_SPG_RUNNING) return;  // uniform across the grid
@@ -56,6 +61,9 @@ __global__ void __launch_bounds__(NT, TmaShape<K>::MinBlocks) spg_sweep_tma_kern
     sc.xin = cur ? a.xb1 : a.xb0;
     sc.xout = cur ? a.xb0 : a.xb1;
     sc.data = BM ? a.bmat : a.data;
+    sc.tmx = &a.tm_x[cur];
+    sc.tmb = &a.tm_b;
+    sc.roff = a.roff;
     sc.a0 = (float)st->alpha_prev;
     sc.beta = (float)st->beta;
     sc.a1 = (float)st->alpha_cur;
@@ -80,7 +88,10 @@ __global__ void __launch_bounds__(NT, TmaShape<K>::MinBlocks) spg_sweep_tma_kern
 #pragma unroll
         for (int s = 0; s < 2; s++) {
             const int tile = blockIdx.x + s * gridDim.x;
-            if (tile < ntiles) tma_issue<K>(sm, s, sc.xin, sc.data, tile * W - TMA_HALO);  // >= -4: front pad
+            if (tile < ntiles) {  // t0 >= -4: the front pad
+                if constexpr (SWZ) tma_issue_swz<K>(sm, s, sc, tile * W - TMA_HALO);
+                else tma_issue<K>(sm, s, sc.xin, sc.data, tile * W - TMA_HALO);
+            }
         }
     }
 
@@ -93,7 +104,7 @@ __global__ void __launch_bounds__(NT, TmaShape<K>::MinBlocks) spg_sweep_tma_kern
         const int s = j & 1;
         const bool arrived = mbar_wait(&sm.bar[s], (parity >> s) & 1u);
         const int next2 = tile + 2 * (int)gridDim.x;
-        if (!tma_tile<K, K, NT, INIT, BM, TP, R>(sm, s, j, arrived, tile * W - TMA_HALO, sc, acc, pend,
+        if (!tma_tile<K, K, NT, INIT, BM, TP, R, SWZ>(sm, s, j, arrived, tile * W - TMA_HALO, sc, acc, pend,
                                                  next2 < ntiles ? next2 * W - TMA_HALO : TMA_NO_REFILL)) {
             // a bulk copy did not arrive in time (the tile's barrier voted on it, before any
             // further copy was issued): record it, wait (bounded) once more for the copies this
@@ -117,31 +128,58 @@ __global__ void __launch_bounds__(NT, TmaShape<K>::MinBlocks) spg_sweep_tma_kern
     spg_finish_sweep<INIT>(st, cur, w);
 }
 
+template <int K, int NT, bool INIT, int MODE, bool SWZ>
+static constexpr size_t tma_smem_bytes()
+{
+    return sizeof(TmaSmem<K, NT, MODE == 1, TmaShape<K>::R>) + (SWZ ? 512 : 0);
+}
+
+template <int K, int NT, bool INIT, int MODE>
+static cudaError_t launch_tma_mode(int grid, const SweepArgs &a, cudaStream_t s)
+{
+    if constexpr (TmaShape<K>::R * K == 16) {
+        if (a.swz) {
+            spg_sweep_tma_kernel<K, NT, INIT, MODE, true><<<grid, NT, tma_smem_bytes<K, NT, INIT, MODE, true>(), s>>>(a);
+            return cudaGetLastError();
+        }
+    }
+    spg_sweep_tma_kernel<K, NT, INIT, MODE, false><<<grid, NT, tma_smem_bytes<K, NT, INIT, MODE, false>(), s>>>(a);
+    return cudaGetLastError();
+}
+
 template <int K, int NT, bool INIT>
 static cudaError_t launch_tma_t(int grid, const SweepArgs &a, cudaStream_t s)
 {
     // the dynamic shared memory limit was raised by tma_blocks_per_sm_t at problem creation
     // (no attribute call here: launches may be inside a stream capture)
-    constexpr int R = TmaShape<K>::R;
-    if (a.bmat) spg_sweep_tma_kernel<K, NT, INIT, 1><<<grid, NT, sizeof(TmaSmem<K, NT, true, R>), s>>>(a);
-    else if (a.kw) spg_sweep_tma_kernel<K, NT, INIT, 2><<<grid, NT, sizeof(TmaSmem<K, NT, false, R>), s>>>(a);
-    else spg_sweep_tma_kernel<K, NT, INIT, 0><<<grid, NT, sizeof(TmaSmem<K, NT, false, R>), s>>>(a);
-    return cudaGetLastError();
+    if (a.bmat) return launch_tma_mode<K, NT, INIT, 1>(grid, a, s);
+    if (a.kw) return launch_tma_mode<K, NT, INIT, 2>(grid, a, s);
+    return launch_tma_mode<K, NT, INIT, 0>(grid, a, s);
 }
 
-template <int K, int NT, bool INIT, int MODE>
-static int tma_blocks_per_sm_mode()
+template <int K, int NT, bool INIT, int MODE, bool SWZ>
+static int tma_blocks_per_sm_form()
 {
-    const size_t smem = sizeof(TmaSmem<K, NT, MODE == 1, TmaShape<K>::R>);
-    cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const size_t smem = tma_smem_bytes<K, NT, INIT, MODE, SWZ>();
+    cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT, MODE, SWZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     // all of the unified L1/shared array as shared memory: the tiles arrive by bulk copy, and
     // the default split held K = 3 to 7 blocks per SM
-    cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(spg_sweep_tma_kernel<K, NT, INIT, MODE, SWZ>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxShared);
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_tma_kernel<K, NT, INIT, MODE>, NT, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_sweep_tma_kernel<K, NT, INIT, MODE, SWZ>, NT, smem);
     return nb > 0 ? nb : 1;
+}
+
+// occupancy of the form in use (the swizzled one where it applies: K = 4, 8); the attributes of
+// both forms are set
+template <int K, int NT, bool INIT, int MODE>
+static int tma_blocks_per_sm_mode()
+{
+    const int n0 = tma_blocks_per_sm_form<K, NT, INIT, MODE, false>();
+    if constexpr (TmaShape<K>::R * K == 16) return tma_blocks_per_sm_form<K, NT, INIT, MODE, true>();
+    return n0;
 }
 
 // sets the shared-memory limit of the three forms; returns the occupancy of the form that
@@ -158,6 +196,47 @@ static int tma_blocks_per_sm_t(bool bm, bool tp)
 constexpr int TMA_P = 512;  // timesteps per tile, for every K (TmaShape)
 
 int sweep_tma_tile_width() { return TMA_P - 2 * TMA_HALO; }
+
+int sweep_tma_threads(int K)
+{
+    switch (K) {
+#define PASC_CASE(KK) case KK: return TmaShape<KK>::NT;
+        PASC_CASE(1) PASC_CASE(2) PASC_CASE(3) PASC_CASE(4)
+        PASC_CASE(5) PASC_CASE(6) PASC_CASE(7) PASC_CASE(8)
+#undef PASC_CASE
+        default: return 0;
+    }
+}
+
+bool sweep_tma_rows16(int K) { return K == 4 || K == 8; }  // TmaShape<K>::R * K == 16
+
+typedef CUresult (*PFN_encodeTiled_rows)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                         const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                                         CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                         CUtensorMapFloatOOBfill);
+
+cudaError_t sweep_tma_make_rowmap(CUtensorMap *map, const float *base, long n, int rows_per_box)
+{
+    static PFN_encodeTiled_rows fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
+        fn = (PFN_encodeTiled_rows)p;
+    }
+    if (n < 16 || n % 16 != 0 || rows_per_box < 1 || rows_per_box > 256) return cudaErrorInvalidValue;
+    memset(map, 0, sizeof *map);
+    const cuuint64_t dims[2] = {16, (cuuint64_t)(n / 16)};
+    const cuuint64_t strides[1] = {64};
+    const cuuint32_t box[2] = {16, (cuuint32_t)rows_per_box};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
 int sweep_tma_max_tile() { return TMA_P; }
 
 bool sweep_tma_supported(int K) { return K >= 1 && K <= 8; }

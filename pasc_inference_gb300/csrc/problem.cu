@@ -825,8 +825,37 @@ static int fp64_iterate(pasc_gb300_problem *p, long n)
 // ---------------------------------------------------------------------------------------
 // SPG-QP, mixed fused path: one sweep per iteration, state on the device, host polls.
 // ---------------------------------------------------------------------------------------
+// Tensor maps for the swizzled tiles of the bulk-copy sweep (K = 4, 8), rebuilt when the
+// buffers change; tm_ok false (the plain bulk-copy form runs) where they cannot be made.
+static void ensure_sweep_maps(pasc_gb300_problem *p)
+{
+    if (!sweep_tma_rows16(p->K) || p->precision != PASC_PREC_MIXED || !p->xb_raw[0]) {
+        p->tm_ok = false;
+        return;
+    }
+    if (p->tm_ok && p->tm_base[0] == p->xb_raw[0] && p->tm_base[1] == p->xb_raw[1] && p->tm_base[2] == p->bmat_raw)
+        return;
+    const long n = ((p->T + PAD_FRONT + PAD_BACK) * p->K) / 16 * 16;  // whole rows of 16 floats
+    const int rows = sweep_tma_threads(p->K);
+    bool ok = sweep_tma_make_rowmap(&p->tm_x[0], p->xb_raw[0], n, rows) == cudaSuccess &&
+              sweep_tma_make_rowmap(&p->tm_x[1], p->xb_raw[1], n, rows) == cudaSuccess;
+    if (ok && p->bmat_raw) ok = sweep_tma_make_rowmap(&p->tm_b, p->bmat_raw, n, rows) == cudaSuccess;
+    p->tm_ok = ok;
+    p->tm_base[0] = p->xb_raw[0];
+    p->tm_base[1] = p->xb_raw[1];
+    p->tm_base[2] = p->bmat_raw;
+}
+
 static int sweep_args(pasc_gb300_problem *p, SweepArgs *a)
 {
+    ensure_sweep_maps(p);
+    if (p->tm_ok) {
+        a->tm_x[0] = p->tm_x[0];
+        a->tm_x[1] = p->tm_x[1];
+        a->tm_b = p->tm_b;
+        a->swz = 1;
+        a->roff = (int)(PAD_FRONT * p->K / 16);
+    }
     a->bmat = p->bmat;  // set for multichannel data and for the inner handle of a reduced problem
     a->data = p->data32;
     a->theta = p->theta32;

@@ -72,6 +72,11 @@ struct pasc_gb300_problem {
     float *xnorm = nullptr;                // T
     float *bmat = nullptr;                 // T*K, past the front pad of bmat_raw
     float *bmat_raw = nullptr;             // zero pads as the gamma buffers (bulk-copy tiles)
+    // tensor maps of xb_raw[0], xb_raw[1] and bmat_raw for the swizzled bulk-copy sweep (K = 4,
+    // 8), built for the buffers in tm_base
+    CUtensorMap tm_x[2], tm_b;
+    const float *tm_base[3] = {nullptr, nullptr, nullptr};
+    bool tm_ok = false;
     unsigned short *theta_split = nullptr; // 32*xdim
     float *theta_f32 = nullptr;            // K*xdim
     float *tnorm = nullptr;                // K

@@ -112,7 +112,29 @@ struct TileScalars {
     const float *xin;
     float *xout;
     const float *data;  // BM: the materialised b (T*K, zero pads like gamma)
+    // SWZ tiles (R*K == 16): tensor maps of xin and of the materialised b over 64-byte rows,
+    // and the row of timestep 0 (the front pad's rows)
+    const CUtensorMap *tmx = nullptr, *tmb = nullptr;
+    int roff = 0;
 };
+
+// 2-D tiled TMA load of one box into shared memory, completing on `bar` (complete_tx).
+// x is the innermost coordinate (elements); x * element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, unsigned long long *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_addr(dst)),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// SWZ tiles: thread i's R*K = 16 values (64 bytes) are row i of the stage, brought in by a
+// tensor copy with the 64-byte swizzle, which stores 16-byte chunk c of row i at chunk
+// c ^ ((i >> 1) & 3) of that row (the stage base is 512-byte aligned).  Unswizzled, the rows
+// 64 bytes apart put a warp's 16-byte loads of one chunk on two of the eight 16-byte bank
+// groups (16 wavefronts instead of 4); swizzled, every group once per 8 lanes.
+__device__ __forceinline__ int swz_chunk(int row, int c) { return c ^ ((row >> 1) & 3); }
 
 struct TileAcc {
     KahanF f;
@@ -157,6 +179,23 @@ __device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM, R> &sm, int s, con
     bulk_g2s(sm.dat[s], data + (long)t0 * (BM ? K : 1), bytes_d, &sm.bar[s]);
 }
 
+// Thread 0: the same tile by tensor copies with the 64-byte swizzle (gamma, and b when BM; the
+// data values of a 1-D signal by a plain bulk copy).  The box is NT rows of 16 floats, row
+// (t0 * K) / 16 + roff of the map (t0 is a multiple of 4 and of 2 for K = 4 and 8, so this
+// is exact); rows past the end of a map read as zeros and count in the transaction bytes.
+template <int K, int KB, int NT, bool BM, int R>
+__device__ __forceinline__ void tma_issue_swz(TmaSmem<KB, NT, BM, R> &sm, int s, const TileScalars<K> &sc, int t0)
+{
+    static_assert(R * K == 16 && KB == K, "swizzled tiles hold one 64-byte row per thread");
+    constexpr int P = NT * R;
+    const unsigned int bytes_x = P * K * sizeof(float), bytes_d = (BM ? P * K : P) * sizeof(float);
+    const int row = (t0 * K) / 16 + sc.roff;
+    mbar_expect_tx(&sm.bar[s], bytes_x + bytes_d);
+    tma_load_2d(sm.x[s], sc.tmx, 0, row, &sm.bar[s]);
+    if (BM) tma_load_2d(sm.dat[s], sc.tmb, 0, row, &sm.bar[s]);
+    else bulk_g2s(sm.dat[s], sc.data + (long)t0, bytes_d, &sm.bar[s]);
+}
+
 // One tile (the block's j-th) in stage s: phases A-D of the sweep.  `arrived`: this thread saw
 // the stage's copy complete (its own bounded mbarrier wait).  The tile has ONE block barrier,
 // after phase B, which also votes on `arrived`: if any thread's wait gave up, every thread
@@ -174,7 +213,7 @@ __device__ __forceinline__ void tma_issue(TmaSmem<KB, NT, BM, R> &sm, int s, con
 // pair.  EDGE: the tile touches t <= 0 or t >= T-1 and needs the range masks; interior tiles
 // (all but the first and last of a signal) run without them.  TP: theta in the penalty, the
 // operator of cluster k is scaled by sc.kw[k] (and so is its share of d'Ad).
-template <int K, int KB, int NT, bool INIT, bool BM, bool EDGE, bool TP = false, int R = TMA_R>
+template <int K, int KB, int NT, bool INIT, bool BM, bool EDGE, bool TP = false, int R = TMA_R, bool SWZ = false>
 __device__ __forceinline__ bool tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s, int j, bool arrived, int t0,
                                               const TileScalars<K> &sc, TileAcc &acc, TilePending<K> &pend,
                                               int refill_t0)
@@ -212,7 +251,7 @@ __device__ __forceinline__ bool tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
             const float4 *src = reinterpret_cast<const float4 *>(&sm.x[s][i * R * K]);
 #pragma unroll
             for (int q = 0; q < R * K / 4; q++) {
-                const float4 v = src[q];
+                const float4 v = src[SWZ ? swz_chunk(i, q) : q];
                 const int e = 4 * q;
                 xc[(e + 0) / K][(e + 0) % K] = v.x;
                 xc[(e + 1) / K][(e + 1) % K] = v.y;
@@ -232,7 +271,20 @@ __device__ __forceinline__ bool tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
         // the neighbours' edge rows: vector loads for K = 4, 6, 8 (rows 16 or 8 bytes aligned),
         // which also spread a warp's loads over more banks (the rows lie R*K floats apart)
         const float *nl = &sm.x[s][(li * R + R - 1) * K], *nr = &sm.x[s][(ri * R) * K];
-        if constexpr (K % 4 == 0) {
+        if constexpr (SWZ) {
+            // rows li and ri: the chunks of the left neighbour's last timestep, of the right
+            // neighbour's first, each at its swizzled place
+            const float4 *rl = reinterpret_cast<const float4 *>(&sm.x[s][li * 16]);
+            const float4 *rr = reinterpret_cast<const float4 *>(&sm.x[s][ri * 16]);
+            constexpr int c0 = (R - 1) * K / 4;
+#pragma unroll
+            for (int q = 0; q < K / 4; q++) {
+                const float4 a = rl[swz_chunk(li, c0 + q)];
+                const float4 c = rr[swz_chunk(ri, q)];
+                xlft[4 * q] = a.x; xlft[4 * q + 1] = a.y; xlft[4 * q + 2] = a.z; xlft[4 * q + 3] = a.w;
+                xrgt[4 * q] = c.x; xrgt[4 * q + 1] = c.y; xrgt[4 * q + 2] = c.z; xrgt[4 * q + 3] = c.w;
+            }
+        } else if constexpr (K % 4 == 0) {
 #pragma unroll
             for (int q = 0; q < K / 4; q++) {
                 const float4 a = reinterpret_cast<const float4 *>(nl)[q];
@@ -262,7 +314,7 @@ __device__ __forceinline__ bool tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
                 const float4 *b4 = reinterpret_cast<const float4 *>(&sm.dat[s][i * R * K]);
 #pragma unroll
                 for (int q = 0; q < R * K / 4; q++) {
-                    const float4 v = b4[q];
+                    const float4 v = b4[SWZ ? swz_chunk(i, q) : q];
                     const int e = 4 * q;
                     bk[(e + 0) / K][(e + 0) % K] = v.x;
                     bk[(e + 1) / K][(e + 1) % K] = v.y;
@@ -354,7 +406,8 @@ __device__ __forceinline__ bool tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
     // the stage is free (phase A was its last reader): refill it
     if (i == 0 && refill_t0 != TMA_NO_REFILL) {
         fence_proxy_async_smem();
-        tma_issue<K>(sm, s, sc.xin, sc.data, refill_t0);
+        if constexpr (SWZ) tma_issue_swz<K>(sm, s, sc, refill_t0);
+        else tma_issue<K>(sm, s, sc.xin, sc.data, refill_t0);
     }
     // the previous tile's d_{c+2} was written before this barrier
     tma_flush_pending<K, KB, NT, BM, TP, R>(sm, sc, acc, pend);
@@ -439,14 +492,14 @@ __device__ __forceinline__ bool tma_tile_body(TmaSmem<KB, NT, BM, R> &sm, int s,
     return true;
 }
 
-template <int K, int KB, int NT, bool INIT, bool BM = false, bool TP = false, int R = TMA_R>
+template <int K, int KB, int NT, bool INIT, bool BM = false, bool TP = false, int R = TMA_R, bool SWZ = false>
 __device__ __forceinline__ bool tma_tile(TmaSmem<KB, NT, BM, R> &sm, int s, int j, bool arrived, int t0,
                                          const TileScalars<K> &sc, TileAcc &acc, TilePending<K> &pend, int refill_t0)
 {
     constexpr int P = NT * R;
     if (t0 >= 1 && t0 + P <= sc.T - 1)
-        return tma_tile_body<K, KB, NT, INIT, BM, false, TP, R>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
-    return tma_tile_body<K, KB, NT, INIT, BM, true, TP, R>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
+        return tma_tile_body<K, KB, NT, INIT, BM, false, TP, R, SWZ>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
+    return tma_tile_body<K, KB, NT, INIT, BM, true, TP, R, SWZ>(sm, s, j, arrived, t0, sc, acc, pend, refill_t0);
 }
 
 }  // namespace pasc

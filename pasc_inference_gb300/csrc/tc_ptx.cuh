@@ -10,16 +10,7 @@
 
 namespace pasc {
 
-// 2-D tiled TMA load of one box into shared memory, completing on `bar` (complete_tx).
-// x is the innermost coordinate (elements); x * element size must be a multiple of 16 bytes.
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, unsigned long long *bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            smem_addr(dst)),
-        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
-        : "memory");
-}
+// tma_load_2d: sweep_tma.cuh
 
 // ---- tensor memory -------------------------------------------------------------------
 // Allocation by one full warp; the column base is written to *slot (shared memory).
