@@ -130,10 +130,14 @@ __device__ __forceinline__ void block_sum_ff(FF (&v)[NV], float2 *scratch)
 // Block stage of a sweep's four sums (objective, d'd, neighbour differences of d, g'd) into
 // the block's slot of partials (four float-float pairs, 32 bytes); then, in the block that
 // finishes last, the grid stage over the nslot slots slot0 + b * stride (b < nslot) in that
-// order.  Returns true in thread 0 of that block with the four sums in w.
+// order.  Returns true in thread 0 of that block with the four sums in w.  snap_src/snap_dst
+// (nullable): the last block also copies snap_bytes (a multiple of 8) from snap_src (global)
+// to snap_dst (shared), all threads at once, visible to thread 0 on return.
 __device__ __forceinline__ bool sweep_grid_sum4(const KahanF &f, float dd, float dAd, float gd, float2 *partials,
                                                long slot, unsigned int *ticket, unsigned int nslot, long slot0,
-                                               long stride, float2 *scratch, double (&w)[4])
+                                               long stride, float2 *scratch, double (&w)[4],
+                                               const void *snap_src = nullptr, void *snap_dst = nullptr,
+                                               int snap_bytes = 0)
 {
     FF v[4] = {FF{f.s, f.c}, ff_make(dd), ff_make(dAd), ff_make(gd)};
     block_sum_ff<4>(v, scratch);
@@ -148,6 +152,11 @@ __device__ __forceinline__ bool sweep_grid_sum4(const KahanF &f, float dd, float
     __syncthreads();
     if (!am_last4) return false;
     __threadfence();
+    if (snap_dst) {
+        const unsigned long long *src = reinterpret_cast<const unsigned long long *>(snap_src);
+        unsigned long long *dst = reinterpret_cast<unsigned long long *>(snap_dst);
+        for (int q = threadIdx.x; q < snap_bytes / 8; q += blockDim.x) dst[q] = __ldcg(src + q);
+    }
     FF u[4] = {ff_make(0.f), ff_make(0.f), ff_make(0.f), ff_make(0.f)};
     for (long b = threadIdx.x; b < (long)nslot; b += blockDim.x) {
 #pragma unroll

@@ -86,11 +86,16 @@ __device__ __forceinline__ bool batch_segment(TmaSmem<KB, BATCH_NT> &sm, const B
     __syncthreads();
     tma_flush_pending<K, KB, BATCH_NT, false, false, TMA_R>(sm, sc, acc, pend);  // the segment's last tile: its pair terms belong to this signal
 
+    // the block that ends the signal's sweep snapshots its state into the first stage (free:
+    // this item's copies were consumed, the next item's are issued after this) for the step logic
+    static_assert(sizeof(SpgDevState) <= sizeof(sm.x[0]) && sizeof(SpgDevState) % 8 == 0, "state snapshot");
+    SpgDevState *snap = reinterpret_cast<SpgDevState *>(sm.x[0]);
     double w[4];
     if (sweep_grid_sum4(acc.f, acc.dd, acc.dAd, acc.gd, reinterpret_cast<float2 *>(a.partials), seg, &a.ticket[q],
-                        (unsigned int)((I.nseg + m - 1) / m), I.seg0, m, reinterpret_cast<float2 *>(sm.red), w)) {
+                        (unsigned int)((I.nseg + m - 1) / m), I.seg0, m, reinterpret_cast<float2 *>(sm.red), w, st,
+                        snap, (int)sizeof(SpgDevState))) {
         a.ticket[q] = 0;
-        spg_finish_sweep<INIT>(st, cur, w);
+        spg_finish_sweep<INIT>(st, *snap, cur, w);
     }
     return true;
 }

@@ -121,11 +121,16 @@ __global__ void __launch_bounds__(NT, TmaShape<K>::MinBlocks) spg_sweep_tma_kern
     tma_flush_pending<K, K, NT, BM, TP, R>(sm, sc, acc, pend);  // the last tile's pair terms
 
     // block and grid reductions (float-float; the step logic in FP64)
+    // the last block snapshots the state into the first stage (free: every copy was consumed)
+    // for the step logic
+    static_assert(sizeof(SpgDevState) <= sizeof(sm.x[0]) && sizeof(SpgDevState) % 8 == 0, "state snapshot");
+    SpgDevState *snap = reinterpret_cast<SpgDevState *>(sm.x[0]);
     double w[4];
     if (!sweep_grid_sum4(acc.f, acc.dd, acc.dAd, acc.gd, reinterpret_cast<float2 *>(a.partials), blockIdx.x,
-                         &st->counter, gridDim.x, 0, 1, reinterpret_cast<float2 *>(sm.red), w))
+                         &st->counter, gridDim.x, 0, 1, reinterpret_cast<float2 *>(sm.red), w, st, snap,
+                         (int)sizeof(SpgDevState)))
         return;
-    spg_finish_sweep<INIT>(st, cur, w);
+    spg_finish_sweep<INIT>(st, *snap, cur, w);
 }
 
 template <int K, int NT, bool INIT, int MODE, bool SWZ>
