@@ -448,7 +448,7 @@ def main():
     dist_finalize(info)
 
 
-def measure_e2e(sig, theta, eps2, dev, fstar, steps=2):
+def measure_e2e(sig, theta, eps2, dev, fstar, steps=6):
     """The public API end to end with host buffers in page-locked memory from the library's
     allocator (pasc_gb300_host_alloc); the copies are inside the timed region.  Each step:
     set_data, set_gamma, permute, set_theta, update_b, spgqp_solve with the reference's default
