@@ -104,19 +104,47 @@ __device__ __forceinline__ void spg_finish_sweep(SpgDevState *st, const SpgDevSt
             }
         }
         const double fx_max = fs_unkey(k0 > k1 ? k0 : k1);
-        const double xi = (fx_max - fnew) / dAd;
-        const double beta_bar = -gd / dAd;
-        if (cm) {
-            const double einv = eps == 0.0 ? 1.0 : 1.0 / eps;
-            double beta_hat = h.gamma * beta_bar + sqrt(h.gamma * h.gamma * beta_bar * beta_bar + 2 * eps * xi);
-            if (einv * beta_hat < h.sigma1) beta_hat = h.sigma1;
-            nbeta = einv * beta_hat < h.sigma2 ? einv * beta_hat : h.sigma2;
-            nalpha = einv * (dd / dAd);
+        const double dxi = fx_max - fnew;  // >= 0, in FP64 (a difference of close objectives)
+        // The step lengths go to the sweeps as FP32; their rules (xi, beta_bar, the A-condition
+        // root, the BB ratio) run in FP32 on operands scaled by the power of two 2^-e that
+        // brings d'Ad to [1, 2) (exact, and the three ratios do not change), which keeps the
+        // FP32 range out of the way; a d'Ad outside 2^-120..2^120 takes the FP64 path.
+        const long long bits = __double_as_longlong(dAd);
+        const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+        if (e > -120 && e < 120) {
+            const double sc = __longlong_as_double((long long)(1023 - e) << 52);
+            const float a = (float)(dAd * sc), fdx = (float)(dxi * sc), fgd = (float)(-gd * sc), fdd = (float)(dd * sc);
+            const float xi = fdx / a, beta_bar = fgd / a, g = (float)h.gamma;
+            if (cm) {
+                const float epsf = (float)eps, einv = eps == 0.0 ? 1.f : 1.f / epsf;
+                float beta_hat = g * beta_bar + sqrtf(g * g * beta_bar * beta_bar + 2.f * epsf * xi);
+                double bh = (double)(einv * beta_hat);
+                if (bh < h.sigma1) beta_hat = (float)h.sigma1, bh = h.sigma1;
+                bh = (double)(einv * beta_hat);
+                nbeta = bh < h.sigma2 ? bh : h.sigma2;
+                nalpha = (double)(einv * (fdd / a));
+            } else {
+                const float beta_hat = g * beta_bar + sqrtf(g * g * beta_bar * beta_bar + 2.f * xi);
+                double bh = (double)beta_hat;
+                if (bh < h.sigma1) bh = h.sigma1;
+                nbeta = bh < h.sigma2 ? bh : h.sigma2;
+                nalpha = (double)(fdd / a);
+            }
         } else {
-            double beta_hat = h.gamma * beta_bar + sqrt(h.gamma * h.gamma * beta_bar * beta_bar + 2 * xi);
-            if (beta_hat < h.sigma1) beta_hat = h.sigma1;
-            nbeta = beta_hat < h.sigma2 ? beta_hat : h.sigma2;
-            nalpha = dd / dAd;
+            const double xi = dxi / dAd;
+            const double beta_bar = -gd / dAd;
+            if (cm) {
+                const double einv = eps == 0.0 ? 1.0 : 1.0 / eps;
+                double beta_hat = h.gamma * beta_bar + sqrt(h.gamma * h.gamma * beta_bar * beta_bar + 2 * eps * xi);
+                if (einv * beta_hat < h.sigma1) beta_hat = h.sigma1;
+                nbeta = einv * beta_hat < h.sigma2 ? einv * beta_hat : h.sigma2;
+                nalpha = einv * (dd / dAd);
+            } else {
+                double beta_hat = h.gamma * beta_bar + sqrt(h.gamma * h.gamma * beta_bar * beta_bar + 2 * xi);
+                if (beta_hat < h.sigma1) beta_hat = h.sigma1;
+                nbeta = beta_hat < h.sigma2 ? beta_hat : h.sigma2;
+                nalpha = dd / dAd;
+            }
         }
     } else if (gd < 0.0) {
         // d'Ad = 0 with d != 0: the objective is linear along d (A_hat d = 0, e.g. T == 1).
