@@ -26,7 +26,8 @@ namespace pasc {
 
 constexpr int BATCH_NT = 128;
 constexpr int BATCH_W = BATCH_NT * TMA_R - 2 * TMA_HALO;  // owned timesteps per tile
-// tiles per segment (BatchArgs::seg_tiles) are chosen at run time by the batch's tuner
+// tiles per segment (BatchArgs::seg_tiles) and segments per work item are set at run time
+// (batch.cu: batch_layout, batch_merge)
 
 int batch_tile_width() { return BATCH_W; }
 int batch_max_tile() { return BATCH_NT * TMA_R; }
