@@ -207,6 +207,16 @@ public:
         check(pasc_gb300_get_sweep_variant(h_.get(), &v));
         return v;
     }
+    // FP64 Newton rounds on the face the last solve ended on, to the QP optimum (pasc_gb300_polish)
+    pasc_gb300_polish_stats polish(int rounds = 4)
+    {
+        pasc_gb300_polish_opts o;
+        pasc_gb300_polish_default_opts(&o);
+        o.rounds = rounds;
+        pasc_gb300_polish_stats st{};
+        check(pasc_gb300_polish(h_.get(), &o, &st));
+        return st;
+    }
     // 0 automatic (SPGQPSolver), 1 SPGQPSolver, 2 SPGQPSolverC
     void set_gamma_solver_type(int t) { check(pasc_gb300_set_gamma_solver_type(h_.get(), t)); }
     void set_usethetainpenalty(bool on) { check(pasc_gb300_set_usethetainpenalty(h_.get(), on ? 1 : 0)); }
