@@ -132,7 +132,10 @@ __device__ __forceinline__ void block_sum_ff(FF (&v)[NV], float2 *scratch)
 // finishes last, the grid stage over the nslot slots slot0 + b * stride (b < nslot) in that
 // order.  Returns true in thread 0 of that block with the four sums in w.  snap_src/snap_dst
 // (nullable): the last block also copies snap_bytes (a multiple of 8) from snap_src (global)
-// to snap_dst (shared), all threads at once, visible to thread 0 on return.
+// to snap_dst (shared), all threads at once, visible to thread 0 on return.  BATCH: slots whose
+// loads a thread issues before adding them (the additions stay in slot order, so the sums do
+// not depend on it): one L2 latency per BATCH slots, for kernels with registers to spare.
+template <int BATCH = 1>
 __device__ __forceinline__ bool sweep_grid_sum4(const KahanF &f, float dd, float dAd, float gd, float2 *partials,
                                                long slot, unsigned int *ticket, unsigned int nslot, long slot0,
                                                long stride, float2 *scratch, double (&w)[4],
@@ -158,11 +161,30 @@ __device__ __forceinline__ bool sweep_grid_sum4(const KahanF &f, float dd, float
         for (int q = threadIdx.x; q < snap_bytes / 8; q += blockDim.x) dst[q] = __ldcg(src + q);
     }
     FF u[4] = {ff_make(0.f), ff_make(0.f), ff_make(0.f), ff_make(0.f)};
-    for (long b = threadIdx.x; b < (long)nslot; b += blockDim.x) {
+    if constexpr (BATCH == 1) {
+        for (long b = threadIdx.x; b < (long)nslot; b += blockDim.x) {
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const float2 p = __ldcg(partials + (slot0 + b * stride) * 4 + q);
-            u[q] = ff_add(u[q], FF{p.x, p.y});
+            for (int q = 0; q < 4; q++) {
+                const float2 p = __ldcg(partials + (slot0 + b * stride) * 4 + q);
+                u[q] = ff_add(u[q], FF{p.x, p.y});
+            }
+        }
+    } else {
+        for (long b0 = threadIdx.x; b0 < (long)nslot; b0 += BATCH * (long)blockDim.x) {
+            float2 p[BATCH][4];
+#pragma unroll
+            for (int r = 0; r < BATCH; r++) {
+                const long b = b0 + r * (long)blockDim.x;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    p[r][q] = b < (long)nslot ? __ldcg(partials + (slot0 + b * stride) * 4 + q) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int r = 0; r < BATCH; r++) {
+                if (b0 + r * (long)blockDim.x >= (long)nslot) break;
+#pragma unroll
+                for (int q = 0; q < 4; q++) u[q] = ff_add(u[q], FF{p[r][q].x, p[r][q].y});
+            }
         }
     }
     block_sum_ff<4>(u, scratch);

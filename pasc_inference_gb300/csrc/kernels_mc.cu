@@ -770,6 +770,7 @@ int mc_theta_vec_grid(long T) { return (int)((T + MC_THETA_ROWS - 1) / MC_THETA_
 // and one FP64 division per channel; otherwise theta64 as given (S = 1).  Then, in slice 0: the
 // FP32 copy, the three BF16 parts (rows k, K + k, 2K + k of theta_split) and ||theta_k||^2.
 constexpr int MC_PREP_MAX_THREADS = 1024;
+constexpr int MC_PREP_BATCH = 8;
 
 template <int K>
 __global__ void __launch_bounds__(MC_PREP_MAX_THREADS) mc_theta_prepare_kernel(McArgs a, int nparts, int from_partials)
@@ -782,10 +783,23 @@ __global__ void __launch_bounds__(MC_PREP_MAX_THREADS) mc_theta_prepare_kernel(M
     if (from_partials) {
         const float2 *P = reinterpret_cast<const float2 *>(a.partials);
         FF num = ff_make(0.f), den = ff_make(0.f);
-        for (int g = sl; g < nparts; g += S) {
-            const float2 *Pg = P + (long)g * (K * n + K);
-            if (j < n) num = ff_add(num, FF{Pg[k * n + j].x, Pg[k * n + j].y});
-            if (j == 0) den = ff_add(den, FF{Pg[K * n + k].x, Pg[K * n + k].y});
+        // the loads of MC_PREP_BATCH parts are issued before their additions (the additions stay
+        // in part order): one memory latency per batch instead of one per part
+        for (int g0 = sl; g0 < nparts; g0 += MC_PREP_BATCH * S) {
+            float2 pn[MC_PREP_BATCH], pd[MC_PREP_BATCH];
+#pragma unroll
+            for (int u = 0; u < MC_PREP_BATCH; u++) {
+                const int g = g0 + u * S;
+                const float2 *Pg = P + (long)g * (K * n + K);
+                pn[u] = (g < nparts && j < n) ? Pg[k * n + j] : make_float2(0.f, 0.f);
+                pd[u] = (g < nparts && j == 0) ? Pg[K * n + k] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < MC_PREP_BATCH; u++) {
+                if (g0 + u * S >= nparts) break;
+                if (j < n) num = ff_add(num, FF{pn[u].x, pn[u].y});
+                if (j == 0) den = ff_add(den, FF{pd[u].x, pd[u].y});
+            }
         }
         s_part[threadIdx.x] = make_float2(num.hi, num.lo);
         if (j == 0) s_part[MC_PREP_MAX_THREADS + (sl & 7)] = make_float2(den.hi, den.lo);

@@ -126,9 +126,9 @@ __global__ void __launch_bounds__(NT, TmaShape<K>::MinBlocks) spg_sweep_tma_kern
     static_assert(sizeof(SpgDevState) <= sizeof(sm.x[0]) && sizeof(SpgDevState) % 8 == 0, "state snapshot");
     SpgDevState *snap = reinterpret_cast<SpgDevState *>(sm.x[0]);
     double w[4];
-    if (!sweep_grid_sum4(acc.f, acc.dd, acc.dAd, acc.gd, reinterpret_cast<float2 *>(a.partials), blockIdx.x,
-                         &st->counter, gridDim.x, 0, 1, reinterpret_cast<float2 *>(sm.red), w, st, snap,
-                         (int)sizeof(SpgDevState)))
+    if (!sweep_grid_sum4<4>(acc.f, acc.dd, acc.dAd, acc.gd, reinterpret_cast<float2 *>(a.partials), blockIdx.x,
+                            &st->counter, gridDim.x, 0, 1, reinterpret_cast<float2 *>(sm.red), w, st, snap,
+                            (int)sizeof(SpgDevState)))
         return;
     spg_finish_sweep<INIT>(st, *snap, cur, w);
 }
