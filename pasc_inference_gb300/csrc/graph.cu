@@ -100,8 +100,6 @@ cudaError_t launch_graph_matmult_f64(const double *x, double *y, long T, long R,
 // ---------------------------------------------------------------------------------------
 constexpr int GRAPH_NT = 256;
 
-int graph_sweep_threads() { return GRAPH_NT; }
-
 // x^{c+1} of block s: x + beta d, or (INIT) the projected start point
 template <int K, bool INIT>
 __device__ __forceinline__ void next_x(const float *__restrict__ xin, const float *__restrict__ din, long s,

@@ -49,12 +49,9 @@ __device__ __forceinline__ void image_load_row(const ImageSweepArgs &a, const fl
     d = in ? __ldg(a.data + pix) : 0.f;
 }
 
-template <int K>
 struct ImgSmem {
     double red[4 * (IMG_NT / 32)];
 };
-
-size_t image_sweep_smem(int K) { return sizeof(ImgSmem<1>); }
 
 // sum over the in-image neighbours of (v_c - v_n); l, r from the neighbouring lanes, u, d from
 // the rows above and below.  EDGE = false: all four neighbours exist.
@@ -217,7 +214,7 @@ __device__ __forceinline__ void image_strip(const ImageSweepArgs &a, const float
 template <int K, bool INIT>
 __global__ void __launch_bounds__(IMG_NT) image_sweep_kernel(ImageSweepArgs a)
 {
-    __shared__ ImgSmem<K> sm;
+    __shared__ ImgSmem sm;
     SpgDevState *st = a.st;
     if (st->status != PASC_SPG_RUNNING) return;  // uniform across the grid
     const int cur = st->cur;

@@ -181,14 +181,12 @@ cudaError_t launch_fem_prolongate(const TIn *g2, TOut *g1, long T1, long T2, int
 
 // Graph (R > 1) and image mode (graph.cu).
 const char *graph_check(long R, const int *ptr, const int *idx);  // null: valid
-int graph_sweep_threads();
 int graph_sweep_grid(long nblocks);
 cudaError_t launch_graph_sweep(int K, bool init, int grid, const GraphSweepArgs &a, cudaStream_t s);
 cudaError_t launch_graph_matmult_f64(const double *x, double *y, long T, long R, int K, double coeff,
                                      const int *ptr, const int *idx, cudaStream_t s, const double *kc = nullptr);
 
 bool graph_is_grid2d(long R, const int *ptr, const int *idx, int *W, int *H);  // host check
-size_t image_sweep_smem(int K);
 int image_sweep_blocks_per_sm(int K);  // also sets the kernels' shared-memory limit
 int image_sweep_tiles(int W, int H);
 cudaError_t launch_image_sweep(int K, bool init, int grid, const ImageSweepArgs &a, cudaStream_t s);
@@ -203,14 +201,12 @@ cudaError_t launch_theta_batch(int grid, const BatchArgs &a, cudaStream_t s);
 void record_error(const char *msg);
 
 // Launchers (kernels_fused.cu).  Return a cudaError_t.
-int sweep_block_threads();
 int sweep_tile_width();
 int sweep_blocks_per_sm(int K, bool init, bool tp = false);  // tp: the theta-in-penalty form
 cudaError_t launch_sweep(int K, bool init, int grid, const SweepArgs &a, cudaStream_t s);  // a.bmat selects the b source
 // Bulk-copy (TMA) form of the sweep: 4 timesteps per thread, double-buffered tiles.
 bool sweep_tma_supported(int K);
 int sweep_tma_tile_width();
-int sweep_tma_max_tile();
 // bmat: the materialised-b form; tp: the theta-in-penalty form (SweepArgs::kw set)
 int sweep_tma_blocks_per_sm(int K, bool init, bool bmat = false, bool tp = false);
 // tensor map over n floats at base (16-byte aligned, n a multiple of 16) as rows of 16 floats,

@@ -76,7 +76,6 @@ constexpr int SWEEP_HL = 2;    // halo timesteps before the owned range
 constexpr int SWEEP_HR = 3;    // halo timesteps after it
 constexpr int SWEEP_W = SWEEP_NT - SWEEP_HL - SWEEP_HR;  // owned timesteps per tile
 
-int sweep_block_threads() { return SWEEP_NT; }
 int sweep_tile_width() { return SWEEP_W; }
 
 // TP: theta in the penalty, block k of A is coeff * a.kw[k] * A_hat (usethetainpenalty)

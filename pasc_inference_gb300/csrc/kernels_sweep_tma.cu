@@ -242,7 +242,6 @@ cudaError_t sweep_tma_make_rowmap(CUtensorMap *map, const float *base, long n, i
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
-int sweep_tma_max_tile() { return TMA_P; }
 
 bool sweep_tma_supported(int K) { return K >= 1 && K <= 8; }
 
