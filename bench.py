@@ -25,11 +25,13 @@ Besides the headline line it measures, on rank 0:
   roofline   the sweep kernel's algorithmic bytes (8*K*T + 4*T per iteration: gamma read and
              written in FP32, the data read once) over its CUDA-event time, against the
              measured HBM copy bandwidth.
-  cpu_baseline  the FP64 CPU oracle (a port of the reference's CPU path) on all host cores, and
-             on one (`one_thread`), and its time to 1e-6 relative objective; beside them the
-             reference's own SPGQPSolver template compiled from its headers (oracle/_ref, one
-             thread, `reference_one_thread`) on the same QP, with a check that its objective
-             equals the port's bit for bit.
+  cpu_baseline  the reference's own SPGQPSolver template compiled from its headers with a
+             host-array backend (oracle/_ref; OpenMP over the vector operations, its sums in the
+             oracle's chunk order) on all host cores, and its time to 1e-6 relative objective;
+             beside it the FP64 oracle port on all cores (`port_all_cores`) and on one
+             (`one_thread`), and the template on one thread (`reference_one_thread`) with a check
+             that its objective equals the port's bit for bit.  Where oracle/_ref cannot be built
+             the port takes the template's place (kind "port").
   batched    the 256-signal uneven workload (T log-uniform in [1e3, 1e6], K in 2..5, epssqr
              log-uniform in [1, 1000]): every signal's TSSolver (SPG eps 1e-6, m 10; outer loop
              to 1e-6 relative change of L) solved by one batch handle (one CUDA graph launch
@@ -249,8 +251,22 @@ def cpu_cores():
         return os.cpu_count() or 1
 
 
-def oracle_iter_rate(sig, theta, eps2, T, iters, nthreads):
-    """FP64 oracle SPG iterations/s on the first T timesteps (all its iterations run)."""
+def ref_available() -> bool:
+    """Whether the reference's own solver templates are compiled (oracle/_ref: from the reference
+    tree, or from the translation unit its recipe left where the tree is absent)."""
+    from oracle import pasc_oracle as O
+    try:
+        return O.build_ref() is not None
+    except Exception:
+        return False
+
+
+def cpu_iter_rate(kind, sig, theta, eps2, T, iters, nthreads):
+    """SPG iterations/s on the first T timesteps of the signal (every iteration runs) of
+    kind "reference", the reference's own SPGQPSolver template compiled from its headers with
+    the host-array backend (oracle/_ref), or "port", the FP64 oracle; nthreads 0 = all cores.
+    The solve's set-up (first projection and product) is timed apart and taken off.  Returns
+    (iterations/s, seconds, objective after the iterations)."""
     from oracle import pasc_oracle as O
     O.build()
     K = sig.K
@@ -259,78 +275,73 @@ def oracle_iter_rate(sig, theta, eps2, T, iters, nthreads):
                                            sig.gamma0.reshape(K, sig.T)[:, :T].ravel(), T, K)
     b = O.residual_b(data, theta, T, K, nthreads=nthreads)
     coeff = O.A_coeff(eps2, T)
-    o0 = O.spg_opts(maxit=0, m=10)
-    t0 = time.perf_counter()
-    O.spgqp_solve(b, gam, T, K, coeff, o0, nthreads=nthreads)
-    t_init = time.perf_counter() - t0
-    o = O.spg_opts(maxit=iters, m=10, stop_difff=0)
-    t0 = time.perf_counter()
-    _, r, _ = O.spgqp_solve(b, gam, T, K, coeff, o, nthreads=nthreads)
-    t_all = time.perf_counter() - t0
-    dt = max(t_all - t_init, 1e-9)
-    return r.it / dt, dt
 
+    def solve(maxit):
+        if kind == "reference":
+            _, it, _, fx = O.ref_spgqp_solve(b, gam, T, K, coeff, nthreads=nthreads, spgqpsolver_maxit=maxit,
+                                             spgqpsolver_m=10, spgqpsolver_stop_difff=0)
+            return it, fx
+        _, r, _ = O.spgqp_solve(b, gam, T, K, coeff, O.spg_opts(maxit=maxit, m=10, stop_difff=0),
+                                nthreads=nthreads)
+        return r.it, r.fx
 
-def reference_iter_rate(sig, theta, eps2, T, iters):
-    """SPG iterations/s of the reference's own SPGQPSolver template, compiled from its headers
-    with host-array vectors (oracle/_ref; one thread), on the same QP; also whether its
-    objective after `iters` iterations equals the oracle port's bit for bit.  None where the
-    library could not be built."""
-    from oracle import pasc_oracle as O
-    try:
-        if O.build_ref() is None:
-            return None
-    except Exception:
-        return None
-    K = sig.K
-    gam = O.permute_blocked_to_interleaved(sig.gamma0, T, K)
-    b = O.residual_b(sig.data, theta, T, K, nthreads=0)
-    coeff = O.A_coeff(eps2, T)
     t0 = time.perf_counter()
-    O.ref_spgqp_solve(b, gam, T, K, coeff, spgqpsolver_maxit=0, spgqpsolver_m=10, spgqpsolver_stop_difff=0)
+    solve(0)
     t_init = time.perf_counter() - t0
     t0 = time.perf_counter()
-    _, it, _, fx = O.ref_spgqp_solve(b, gam, T, K, coeff, spgqpsolver_maxit=iters, spgqpsolver_m=10,
-                                     spgqpsolver_stop_difff=0)
+    it, fx = solve(iters)
     dt = max(time.perf_counter() - t0 - t_init, 1e-9)
-    # the port on one thread sums in the template's order (its OpenMP sums on more threads do not)
-    _, r, _ = O.spgqp_solve(b, gam, T, K, coeff, O.spg_opts(maxit=iters, m=10, stop_difff=0), nthreads=1)
-    return {"value": it / dt, "unit": UNIT, "cores": 1, "kind": "reference",
-            "sample": f"{it} SPG iterations of the reference's SPGQPSolver template (oracle/_ref, "
+    return it / dt, dt, fx
+
+
+def reference_one_thread(sig, theta, eps2, T, iters):
+    """The reference's own template on one thread (every sum in index order, as a one-rank
+    PETSc host vector sums), with whether its objective equals the port's on one thread bit for
+    bit; None where oracle/_ref could not be built."""
+    if not ref_available():
+        return None
+    rate, dt, fx = cpu_iter_rate("reference", sig, theta, eps2, T, iters, 1)
+    _, _, fx_port = cpu_iter_rate("port", sig, theta, eps2, T, iters, 1)
+    return {"value": rate, "unit": UNIT, "cores": 1, "kind": "reference",
+            "sample": f"{iters} SPG iterations of the reference's SPGQPSolver template (oracle/_ref, "
                       f"host-array vectors) on the full T={T} signal ({dt:.1f} s)",
-            "objective_equals_port": bool(fx == r.fx)}
+            "objective_equals_port": bool(fx == fx_port)}
 
 
 def run_reference(args, info):
-    """The reference path's CPU implementation (the FP64 oracle port), rank 0 only."""
+    """The reference path's CPU implementation on all host cores, rank 0 only: the reference's
+    own SPGQPSolver template (oracle/_ref) where it compiled, else the FP64 oracle port."""
     from pasc_inference_gb300 import datagen
     if info.rank != 0:
         return None
     sig = datagen.signal1d_cfg1(T=args.T)
     theta = np.array([0.0, 1.0, 2.0])
     cores = cpu_cores()
+    kind = "reference" if ref_available() else "port"
+    what = ("the reference's SPGQPSolver template (oracle/_ref, host-array vectors, OpenMP)" if kind == "reference"
+            else "the FP64 oracle port (OpenMP)")
     # size the per-step sample so that warmup + steps stay within ~2 minutes
-    rate_full, _ = oracle_iter_rate(sig, theta, args.eps2, args.T, 1, 0)
+    rate_full, _, _ = cpu_iter_rate(kind, sig, theta, args.eps2, args.T, 1, 0)
     t_full = 1.0 / rate_full
     budget = 120.0 / max(1, args.steps + args.warmup)
     Ts = int(min(args.T, max(100_000, args.T * budget / t_full)))
     steps = args.steps
     if Ts < args.T:
-        rate, dt = oracle_iter_rate(sig, theta, args.eps2, Ts, steps, 0)
+        rate, dt, _ = cpu_iter_rate(kind, sig, theta, args.eps2, Ts, steps, 0)
         value = rate * Ts / args.T
-        sample = f"{steps} SPG iterations on the first {Ts} timesteps, scaled by {Ts}/{args.T}"
+        sample = f"{steps} SPG iterations of {what} on the first {Ts} timesteps, scaled by {Ts}/{args.T}"
     else:
-        rate, dt = oracle_iter_rate(sig, theta, args.eps2, args.T, steps, 0)
+        rate, dt, _ = cpu_iter_rate(kind, sig, theta, args.eps2, args.T, steps, 0)
         value = rate
-        sample = f"{steps} SPG iterations on the full signal"
+        sample = f"{steps} SPG iterations of {what} on the full signal"
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
         "config": bench_config(args.T, 3, args.eps2),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
-        "time_to_1e-6_rel_obj": oracle_tts(sig, theta, args.eps2, args.T),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+        "time_to_1e-6_rel_obj": cpu_tts(kind, sig, theta, args.eps2, args.T),
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     return line
@@ -434,15 +445,20 @@ def main():
     if info.rank == 0 and not args.no_image:
         result["image"] = measure_image(dev, peak)
     if info.rank == 0 and not args.no_cpu:
-        rate, dt = oracle_iter_rate(sig, theta, args.eps2, T, 5, 0)
-        rate1, dt1 = oracle_iter_rate(sig, theta, args.eps2, T, 2, 1)
-        result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
-                                  "sample": f"5 SPG iterations of the FP64 oracle on the full T={T} "
-                                            f"signal ({dt:.1f} s, OpenMP)",
-                                  "one_thread": {"value": rate1, "unit": UNIT, "cores": 1,
+        kind = "reference" if ref_available() else "port"
+        rate, dt, _ = cpu_iter_rate(kind, sig, theta, args.eps2, T, 5, 0)
+        prate, pdt, _ = cpu_iter_rate("port", sig, theta, args.eps2, T, 5, 0)
+        rate1, dt1, _ = cpu_iter_rate("port", sig, theta, args.eps2, T, 2, 1)
+        what = "the reference's SPGQPSolver template (oracle/_ref)" if kind == "reference" else "the FP64 oracle"
+        result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": kind,
+                                  "sample": f"5 SPG iterations of {what} on the full T={T} signal "
+                                            f"({dt:.1f} s, OpenMP)",
+                                  "port_all_cores": {"value": prate, "unit": UNIT, "cores": cpu_cores(),
+                                                     "kind": "port", "sample": f"5 SPG iterations ({pdt:.1f} s)"},
+                                  "one_thread": {"value": rate1, "unit": UNIT, "cores": 1, "kind": "port",
                                                  "sample": f"2 SPG iterations, same signal ({dt1:.1f} s)"},
-                                  "reference_one_thread": reference_iter_rate(sig, theta, args.eps2, T, 2),
-                                  "time_to_1e-6_rel_obj": oracle_tts(sig, theta, args.eps2, T)}
+                                  "reference_one_thread": reference_one_thread(sig, theta, args.eps2, T, 2),
+                                  "time_to_1e-6_rel_obj": cpu_tts(kind, sig, theta, args.eps2, T)}
     if info.rank == 0:
         print(json.dumps(result), flush=True)
     dist_finalize(info)
@@ -592,8 +608,29 @@ def oracle_tts(sig, theta, eps2, T, nthreads=0, maxit=600):
     fend = f[-1]
     hit = int(np.argmax(np.abs(f - fend) <= 1e-6 * abs(fend)))
     return {"seconds": secs * hit / max(r.it, 1), "spg_it": hit, "f_ref": float(fend), "run_it": int(r.it),
-            "run_s": secs, "cores": nthreads if nthreads > 0 else cpu_cores(),
-            "f_ref_rule": "objective of the same run at |f - f_old| < 1e-12"}
+            "run_s": secs, "cores": nthreads if nthreads > 0 else cpu_cores(), "kind": "port",
+            "f_hit": float(f[hit]), "f_ref_rule": "objective of the same run at |f - f_old| < 1e-12"}
+
+
+def cpu_tts(kind, sig, theta, eps2, T):
+    """Time to 1e-6 relative objective on all host cores.  The port's traced run finds the
+    iteration that reaches it; for kind "reference" the reference's own template (whose iterates
+    equal the port's at the same thread count: its sums follow the same chunks) is then timed
+    for exactly that many iterations, and its objective there is checked against the trace."""
+    res = oracle_tts(sig, theta, eps2, T)
+    if kind != "reference" or res["spg_it"] < 1:
+        return res
+    from oracle import pasc_oracle as O
+    K = sig.K
+    b = O.residual_b(sig.data, theta, T, K, nthreads=0)
+    x0 = O.permute_blocked_to_interleaved(sig.gamma0, T, K)
+    t0 = time.perf_counter()
+    _, it, _, fx = O.ref_spgqp_solve(b, x0, T, K, O.A_coeff(eps2, T), nthreads=0, spgqpsolver_maxit=res["spg_it"],
+                                     spgqpsolver_m=10, spgqpsolver_stop_difff=0)
+    secs = time.perf_counter() - t0
+    return {"seconds": secs, "spg_it": int(it), "f_ref": res["f_ref"], "cores": cpu_cores(), "kind": "reference",
+            "objective_equals_port_trace": bool(fx == res["f_hit"]), "port": res,
+            "f_ref_rule": res["f_ref_rule"]}
 
 
 def measure_multichannel(dev, peak):

@@ -13,7 +13,7 @@ if [ ! -f "$REF/include/general/solver/spgqpsolver.h" ]; then
     exit 0
 fi
 mkdir -p "$HERE/_ref"
-${CXX:-g++} -std=c++14 -O2 -fPIC -shared -ffp-contract=off -w \
+${CXX:-g++} -std=c++14 -O2 -fopenmp -fPIC -shared -ffp-contract=off -w \
     -I "$HERE/ref_shim" -I "$REF/include" \
     "$HERE/ref_shim/ref_driver.cpp" \
     "$REF/src/general/solver/spg_fs.cpp" \

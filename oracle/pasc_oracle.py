@@ -69,7 +69,7 @@ def build_ref() -> str | None:
     script = os.path.join(HERE, "build_ref.sh")
     subprocess.check_call(["sh", script])
     if not os.path.exists(REF_LIB_PATH) and os.path.exists(REF_FLAT_PATH):
-        subprocess.check_call([os.environ.get("CXX", "g++"), "-std=c++14", "-O2", "-fPIC", "-shared",
+        subprocess.check_call([os.environ.get("CXX", "g++"), "-std=c++14", "-O2", "-fopenmp", "-fPIC", "-shared",
                                "-ffp-contract=off", "-w", REF_FLAT_PATH, "-o", REF_LIB_PATH])
     return REF_LIB_PATH if os.path.exists(REF_LIB_PATH) else None
 
@@ -472,6 +472,7 @@ def ref():
     if _ref is None:
         R = C.CDLL(REF_LIB_PATH)
         R.ref_set_option.argtypes = [C.c_char_p, C.c_double]
+        R.ref_set_threads.argtypes = [C.c_int]
         R.ref_project.argtypes = [_dp, C.c_int, C.c_int]
         R.ref_fs_sequence.argtypes = [C.c_int, _dp, C.c_int, _dp]
         R.ref_matmult.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_double]
@@ -482,8 +483,12 @@ def ref():
     return _ref
 
 
-def ref_options(**kw):
+def ref_options(nthreads=1, **kw):
+    """Sets the reference's console options for the next call and the threads of its host-array
+    backend (1: sequential sums in index order; n > 1: the oracle's chunked order for n, 0: all
+    cores)."""
     R = ref()
+    R.ref_set_threads(int(nthreads))
     R.ref_clear_options()
     for k, v in kw.items():
         R.ref_set_option(k.encode(), float(v))
@@ -509,8 +514,8 @@ def ref_fs_sequence(m, values):
     return out
 
 
-def ref_spgqp_solve(b, x0, T, K, coeff, **options):
-    ref_options(**options)
+def ref_spgqp_solve(b, x0, T, K, coeff, nthreads=1, **options):
+    ref_options(nthreads, **options)
     x = _f64(x0).copy()
     out = np.zeros(3)
     ref().ref_spgqp_solve(_f64(b), x, T, K, coeff, out)

@@ -4,6 +4,7 @@
  * src/petscvector/algebra/matrix/blockgraphsparse.cpp:51-109 for R = 1 (diagonal 2 at the
  * ends, 4 inside, 0 for T == 1; -2 at t-1 and t+1), multiplied row by row over ascending
  * columns from 0.0 like a CSR MatMult, then scaled by alpha (:152-188, coeffs == NULL).
+ * Rows are independent, so refshim_nthreads threads give the same values as one.
  */
 #ifndef PASC_REFSHIM_BLOCKGRAPHSPARSE_H
 #define PASC_REFSHIM_BLOCKGRAPHSPARSE_H
@@ -31,6 +32,7 @@ template <class VectorBase> class BlockGraphSparseMatrix : public GeneralMatrix<
         const double *xa = x.arr();
         double *ya = y.arr();
         long n = T * (long)K;
+#pragma omp parallel for schedule(static) num_threads(refshim_nthreads) if (refshim_nthreads > 1)
         for (long i = 0; i < n; i++) {
             long t = i / K;
             double sum = 0.0;
@@ -44,6 +46,7 @@ template <class VectorBase> class BlockGraphSparseMatrix : public GeneralMatrix<
             }
             ya[i] = sum;
         }
+#pragma omp parallel for schedule(static) num_threads(refshim_nthreads) if (refshim_nthreads > 1)
         for (long i = 0; i < n; i++) ya[i] = alpha * ya[i];
     }
 };

@@ -7,11 +7,19 @@
  *   d = x - a*g   ->  d_i = x_i - a*g_i        d -= x   ->  d_i = d_i - x_i
  *   x += a*d      ->  x_i = x_i + a*d_i        t = g - b ->  t_i = g_i - b_i
  *   y = A*x       ->  A.matmult(y, x)          dot(a,b) ->  sequential sum of a_i*b_i
+ *
+ * refshim_nthreads (default 1) splits the element-wise loops over OpenMP threads; dot() then
+ * sums static chunks [n*id/cnt, n*(id+1)/cnt) and the chunk sums in thread order -- the scheme
+ * of the oracle's multi-threaded mode, so the two give the same bits at the same thread count.
+ * With 1 thread every loop and sum runs sequentially in index order, as above.
  */
 #ifndef PASC_REFSHIM_GENERALVECTOR_H
 #define PASC_REFSHIM_GENERALVECTOR_H
 
 #include "general/common/common.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace pascinference {
 namespace algebra {
@@ -37,6 +45,8 @@ template <class VectorBase> class GeneralMatrix;
 
 /* Random source for set_random(): the driver installs the vector it wants produced. */
 extern std::vector<double> refshim_random_source;
+/* Threads of the loops below (set by ref_set_threads). */
+extern int refshim_nthreads;
 
 template <> class GeneralVector<HostVec> : public HostVec {
   public:
@@ -57,24 +67,38 @@ template <> class GeneralVector<HostVec> : public HostVec {
         return *this;
     }
     GeneralVector &operator=(const DiffScaled &e) {
-        size_t n = h->v.size();
-        for (size_t i = 0; i < n; i++) h->v[i] = e.x->h->v[i] - e.s.a * e.s.x->h->v[i];
+        const long n = (long)h->v.size();
+        double *y = h->v.data();
+        const double *a = e.x->h->v.data(), *g = e.s.x->h->v.data();
+        const double c = e.s.a;
+#pragma omp parallel for schedule(static) num_threads(refshim_nthreads) if (refshim_nthreads > 1)
+        for (long i = 0; i < n; i++) y[i] = a[i] - c * g[i];
         return *this;
     }
     GeneralVector &operator=(const Diff &e) {
-        size_t n = h->v.size();
-        for (size_t i = 0; i < n; i++) h->v[i] = e.x->h->v[i] - e.y->h->v[i];
+        const long n = (long)h->v.size();
+        double *y = h->v.data();
+        const double *a = e.x->h->v.data(), *b = e.y->h->v.data();
+#pragma omp parallel for schedule(static) num_threads(refshim_nthreads) if (refshim_nthreads > 1)
+        for (long i = 0; i < n; i++) y[i] = a[i] - b[i];
         return *this;
     }
     GeneralVector &operator=(const MatVec &e);
     GeneralVector &operator-=(const GeneralVector &o) {
-        size_t n = h->v.size();
-        for (size_t i = 0; i < n; i++) h->v[i] = h->v[i] - o.h->v[i];
+        const long n = (long)h->v.size();
+        double *y = h->v.data();
+        const double *a = o.h->v.data();
+#pragma omp parallel for schedule(static) num_threads(refshim_nthreads) if (refshim_nthreads > 1)
+        for (long i = 0; i < n; i++) y[i] = y[i] - a[i];
         return *this;
     }
     GeneralVector &operator+=(const Scaled &s) {
-        size_t n = h->v.size();
-        for (size_t i = 0; i < n; i++) h->v[i] = h->v[i] + s.a * s.x->h->v[i];
+        const long n = (long)h->v.size();
+        double *y = h->v.data();
+        const double *a = s.x->h->v.data();
+        const double c = s.a;
+#pragma omp parallel for schedule(static) num_threads(refshim_nthreads) if (refshim_nthreads > 1)
+        for (long i = 0; i < n; i++) y[i] = y[i] + c * a[i];
         return *this;
     }
     void set_random() {
@@ -90,10 +114,32 @@ inline GeneralVector<HostVec>::Diff operator-(const GeneralVector<HostVec> &x,
                                               const GeneralVector<HostVec> &y) { return {&x, &y}; }
 
 inline double dot(const GeneralVector<HostVec> &a, const GeneralVector<HostVec> &b) {
-    double s = 0.0;
-    size_t n = a.h->v.size();
-    for (size_t i = 0; i < n; i++) s += a.h->v[i] * b.h->v[i];
-    return s;
+    const double *x = a.h->v.data(), *y = b.h->v.data();
+    const long n = (long)a.h->v.size();
+    if (refshim_nthreads <= 1) {
+        double s = 0.0;
+        for (long i = 0; i < n; i++) s += x[i] * y[i];
+        return s;
+    }
+    double part[256];
+    const int nt = refshim_nthreads > 256 ? 256 : refshim_nthreads;
+    int used = 1;
+#pragma omp parallel num_threads(nt)
+    {
+        int id = 0, cnt = 1;
+#ifdef _OPENMP
+        id = omp_get_thread_num();
+        cnt = omp_get_num_threads();
+#endif
+        const long lo = n * id / cnt, hi = n * (id + 1) / cnt;
+        double s = 0.0;
+        for (long i = lo; i < hi; i++) s += x[i] * y[i];
+        part[id] = s;
+        if (id == 0) used = cnt;
+    }
+    double tot = 0.0;
+    for (int j = 0; j < used; j++) tot += part[j];
+    return tot;
 }
 inline double norm(const GeneralVector<HostVec> &a) { return std::sqrt(dot(a, a)); }
 inline std::ostream &operator<<(std::ostream &o, const GeneralVector<HostVec> &) { return o; }

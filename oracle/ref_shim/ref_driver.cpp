@@ -37,12 +37,17 @@ GlobalManagerClass GlobalManager;
 }
 namespace algebra {
 std::vector<double> refshim_random_source;
+int refshim_nthreads = 1;
 
+/* project_sub works on block t alone (its sort buffer is allocated per call), so the blocks
+ * are split over the shim's threads with unchanged results. */
 template <>
 void SimplexFeasibleSet_Local<HostVec>::project(GeneralVector<HostVec> &x)
 {
     double *x_arr = x.arr();
-    for (int t = 0; t < T; t++) project_sub(x_arr, t, T, K);
+    const int T_ = T, K_ = K;
+#pragma omp parallel for schedule(static) num_threads(refshim_nthreads) if (refshim_nthreads > 1)
+    for (int t = 0; t < T_; t++) project_sub(x_arr, t, T_, K_);
 }
 } /* namespace algebra */
 
@@ -178,6 +183,15 @@ class RefTSSolver : public TSSolver<HostVec> {
 extern "C" {
 
 void ref_clear_options(void) { consoleArg.overrides.clear(); }
+/* Threads of the host-array backend: 1 (or less than 0) every loop and sum sequential in index
+ * order; 0 all the threads OpenMP offers, as the oracle's nthreads = 0. */
+void ref_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n == 0) n = omp_get_max_threads();
+#endif
+    refshim_nthreads = n > 1 ? n : 1;
+}
 void ref_set_option(const char *name, double value) { consoleArg.overrides[name] = value; }
 
 /* SimplexFeasibleSet_Local<HostVec>::project on T blocks of K doubles, in place. */

@@ -60,3 +60,23 @@ def test_tssolver_given_theta(ref):
     assert r.L == res["L"]
     np.testing.assert_array_equal(go, gr)
     np.testing.assert_array_equal(tho, th0)
+
+
+@pytest.mark.parametrize("nthreads", [2, 3, 5])
+def test_spgqp_threads_follow_the_port(ref, nthreads):
+    """With its vector operations split over threads, the reference's template sums in the
+    oracle's chunk order: the same iterates as the port on as many threads (the timed CPU
+    baseline runs this way on all cores), and one thread differs only by rounding."""
+    rng = np.random.default_rng(nthreads)
+    T, K = 30_000, 3
+    data = np.repeat(rng.integers(0, K, size=30), 1000) + rng.normal(size=T) * 0.5
+    b = ref.residual_b(data, np.arange(K, dtype=np.float64), T, K)
+    x0 = rng.random(T * K)
+    coeff = ref.A_coeff(10.0, T)
+    kw = dict(spgqpsolver_m=10, spgqpsolver_maxit=40, spgqpsolver_stop_difff=0)
+    xr, it, hm, fx = ref.ref_spgqp_solve(b, x0, T, K, coeff, nthreads=nthreads, **kw)
+    xo, r, _ = ref.spgqp_solve(b, x0, T, K, coeff, ref.spg_opts(m=10, maxit=40, stop_difff=0), nthreads=nthreads)
+    assert (r.it, r.hessmult, r.fx) == (it, hm, fx)
+    np.testing.assert_array_equal(xo, xr)
+    _, _, _, f1 = ref.ref_spgqp_solve(b, x0, T, K, coeff, nthreads=1, **kw)
+    assert abs(f1 - fx) <= 1e-12 * abs(fx)
