@@ -245,6 +245,8 @@ class ClockSampler:
 
 
 def cpu_cores():
+    """Host cores this process may run on (its CPU affinity): the thread count of every timed
+    CPU baseline."""
     try:
         return len(os.sched_getaffinity(0))
     except Exception:
@@ -264,7 +266,8 @@ def ref_available() -> bool:
 def cpu_iter_rate(kind, sig, theta, eps2, T, iters, nthreads):
     """SPG iterations/s on the first T timesteps of the signal (every iteration runs) of
     kind "reference", the reference's own SPGQPSolver template compiled from its headers with
-    the host-array backend (oracle/_ref), or "port", the FP64 oracle; nthreads 0 = all cores.
+    the host-array backend (oracle/_ref), or "port", the FP64 oracle, on nthreads OpenMP
+    threads (an explicit count: it overrides OMP_NUM_THREADS, which torchrun sets to 1).
     The solve's set-up (first projection and product) is timed apart and taken off.  Returns
     (iterations/s, seconds, objective after the iterations)."""
     from oracle import pasc_oracle as O
@@ -321,17 +324,17 @@ def run_reference(args, info):
     what = ("the reference's SPGQPSolver template (oracle/_ref, host-array vectors, OpenMP)" if kind == "reference"
             else "the FP64 oracle port (OpenMP)")
     # size the per-step sample so that warmup + steps stay within ~2 minutes
-    rate_full, _, _ = cpu_iter_rate(kind, sig, theta, args.eps2, args.T, 1, 0)
+    rate_full, _, _ = cpu_iter_rate(kind, sig, theta, args.eps2, args.T, 1, cores)
     t_full = 1.0 / rate_full
     budget = 120.0 / max(1, args.steps + args.warmup)
     Ts = int(min(args.T, max(100_000, args.T * budget / t_full)))
     steps = args.steps
     if Ts < args.T:
-        rate, dt, _ = cpu_iter_rate(kind, sig, theta, args.eps2, Ts, steps, 0)
+        rate, dt, _ = cpu_iter_rate(kind, sig, theta, args.eps2, Ts, steps, cores)
         value = rate * Ts / args.T
         sample = f"{steps} SPG iterations of {what} on the first {Ts} timesteps, scaled by {Ts}/{args.T}"
     else:
-        rate, dt, _ = cpu_iter_rate(kind, sig, theta, args.eps2, args.T, steps, 0)
+        rate, dt, _ = cpu_iter_rate(kind, sig, theta, args.eps2, args.T, steps, cores)
         value = rate
         sample = f"{steps} SPG iterations of {what} on the full signal"
     line = {
@@ -446,8 +449,8 @@ def main():
         result["image"] = measure_image(dev, peak)
     if info.rank == 0 and not args.no_cpu:
         kind = "reference" if ref_available() else "port"
-        rate, dt, _ = cpu_iter_rate(kind, sig, theta, args.eps2, T, 5, 0)
-        prate, pdt, _ = cpu_iter_rate("port", sig, theta, args.eps2, T, 5, 0)
+        rate, dt, _ = cpu_iter_rate(kind, sig, theta, args.eps2, T, 5, cpu_cores())
+        prate, pdt, _ = cpu_iter_rate("port", sig, theta, args.eps2, T, 5, cpu_cores())
         rate1, dt1, _ = cpu_iter_rate("port", sig, theta, args.eps2, T, 2, 1)
         what = "the reference's SPGQPSolver template (oracle/_ref)" if kind == "reference" else "the FP64 oracle"
         result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": kind,
@@ -592,11 +595,13 @@ def measure_tts(sig, theta, dev, eps_list=(1.0, 10.0, 100.0, 1000.0)):
     return out
 
 
-def oracle_tts(sig, theta, eps2, T, nthreads=0, maxit=600):
-    """The FP64 oracle on the host cores: time to an objective within 1e-6 (relative) of its
+def oracle_tts(sig, theta, eps2, T, nthreads=None, maxit=600):
+    """The FP64 oracle on the host cores (all of them unless nthreads says otherwise): time to an objective within 1e-6 (relative) of its
     own objective at |f - f_old| < 1e-12 (the reference's SPG loop, traced)."""
     from oracle import pasc_oracle as O
     O.build()
+    if nthreads is None:
+        nthreads = cpu_cores()
     K = sig.K
     b = O.residual_b(sig.data, theta, T, K, nthreads=nthreads)
     x0 = O.permute_blocked_to_interleaved(sig.gamma0, T, K)
@@ -608,7 +613,7 @@ def oracle_tts(sig, theta, eps2, T, nthreads=0, maxit=600):
     fend = f[-1]
     hit = int(np.argmax(np.abs(f - fend) <= 1e-6 * abs(fend)))
     return {"seconds": secs * hit / max(r.it, 1), "spg_it": hit, "f_ref": float(fend), "run_it": int(r.it),
-            "run_s": secs, "cores": nthreads if nthreads > 0 else cpu_cores(), "kind": "port",
+            "run_s": secs, "cores": nthreads, "kind": "port",
             "f_hit": float(f[hit]), "f_ref_rule": "objective of the same run at |f - f_old| < 1e-12"}
 
 
@@ -625,7 +630,7 @@ def cpu_tts(kind, sig, theta, eps2, T):
     b = O.residual_b(sig.data, theta, T, K, nthreads=0)
     x0 = O.permute_blocked_to_interleaved(sig.gamma0, T, K)
     t0 = time.perf_counter()
-    _, it, _, fx = O.ref_spgqp_solve(b, x0, T, K, O.A_coeff(eps2, T), nthreads=0, spgqpsolver_maxit=res["spg_it"],
+    _, it, _, fx = O.ref_spgqp_solve(b, x0, T, K, O.A_coeff(eps2, T), nthreads=cpu_cores(), spgqpsolver_maxit=res["spg_it"],
                                      spgqpsolver_m=10, spgqpsolver_stop_difff=0)
     secs = time.perf_counter() - t0
     return {"seconds": secs, "spg_it": int(it), "f_ref": res["f_ref"], "cores": cpu_cores(), "kind": "reference",

@@ -35,3 +35,19 @@ def test_reference_arm_line():
     assert tts["seconds"] > 0 and tts["spg_it"] >= 1
     if cb["kind"] == "reference":
         assert tts["objective_equals_port_trace"] is True
+
+
+def test_reference_arm_under_two_ranks():
+    """Under torchrun with two ranks rank 0 alone prints the line, both exit 0, and the CPU
+    baseline runs on every core of the process's affinity although torchrun sets
+    OMP_NUM_THREADS=1 for its workers."""
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", "29531", "bench.py", "--impl", "reference",
+                        "--gpus", "2", "--T", "100000", "--steps", "2", "--warmup", "3"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout[-2000:]
+    d = json.loads(lines[0])
+    assert d["n_gpus"] == 2 and d["impl"] == "reference"
+    assert d["cpu_baseline"]["cores"] == len(os.sched_getaffinity(0))
