@@ -55,6 +55,7 @@ Besides the headline line it measures, on rank 0:
 from __future__ import annotations
 
 import argparse
+import functools
 import json
 import os
 import statistics
@@ -253,9 +254,11 @@ def cpu_cores():
         return os.cpu_count() or 1
 
 
+@functools.lru_cache(maxsize=None)
 def ref_available() -> bool:
     """Whether the reference's own solver templates are compiled (oracle/_ref: from the reference
-    tree, or from the translation unit its recipe left where the tree is absent)."""
+    tree, or from the translation unit its recipe left where the tree is absent); built once per
+    process."""
     from oracle import pasc_oracle as O
     try:
         return O.build_ref() is not None
