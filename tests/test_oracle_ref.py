@@ -80,3 +80,18 @@ def test_spgqp_threads_follow_the_port(ref, nthreads):
     np.testing.assert_array_equal(xo, xr)
     _, _, _, f1 = ref.ref_spgqp_solve(b, x0, T, K, coeff, nthreads=1, **kw)
     assert abs(f1 - fx) <= 1e-12 * abs(fx)
+
+
+@pytest.mark.parametrize("T,K,eps2,m", [(1, 3, 10.0, 10), (2, 1, 10.0, 10), (5, 2, 1.0, 1), (3, 4, 1e4, 2)])
+def test_spgqp_edge_sizes(ref, T, K, eps2, m):
+    """One timestep (A = 0), one cluster (every point already feasible), GLL memory 1, a stiff
+    few-timestep case: the oracle follows the reference's template bit for bit."""
+    rng = np.random.default_rng(100 * T + K)
+    data = rng.normal(size=T) + 1.0
+    b = ref.residual_b(data, np.linspace(0, 2, K), T, K)
+    x0 = rng.random(T * K)
+    coeff = ref.A_coeff(eps2, T)
+    xr, it, hm, fx = ref.ref_spgqp_solve(b, x0, T, K, coeff, spgqpsolver_m=m, spgqpsolver_maxit=200)
+    xo, r, _ = ref.spgqp_solve(b, x0, T, K, coeff, ref.spg_opts(m=m, maxit=200))
+    assert (r.it, r.hessmult, r.fx) == (it, hm, fx)
+    np.testing.assert_array_equal(xo, xr)
