@@ -314,6 +314,26 @@ def reference_one_thread(sig, theta, eps2, T, iters):
             "objective_equals_port": bool(fx == fx_port)}
 
 
+def measure_cpu_baseline(sig, theta, eps2, T):
+    """The GPU arm's cpu_baseline object: the reference's template on all host cores (the port
+    where oracle/_ref is not built), the port on all cores and on one, the template on one, and
+    the time to 1e-6 relative objective."""
+    kind = "reference" if ref_available() else "port"
+    cores = cpu_cores()
+    rate, dt, _ = cpu_iter_rate(kind, sig, theta, eps2, T, 5, cores)
+    prate, pdt, _ = cpu_iter_rate("port", sig, theta, eps2, T, 5, cores)
+    rate1, dt1, _ = cpu_iter_rate("port", sig, theta, eps2, T, 2, 1)
+    what = "the reference's SPGQPSolver template (oracle/_ref)" if kind == "reference" else "the FP64 oracle"
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"5 SPG iterations of {what} on the full T={T} signal ({dt:.1f} s, OpenMP)",
+            "port_all_cores": {"value": prate, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"5 SPG iterations ({pdt:.1f} s)"},
+            "one_thread": {"value": rate1, "unit": UNIT, "cores": 1, "kind": "port",
+                           "sample": f"2 SPG iterations, same signal ({dt1:.1f} s)"},
+            "reference_one_thread": reference_one_thread(sig, theta, eps2, T, 2),
+            "time_to_1e-6_rel_obj": cpu_tts(kind, sig, theta, eps2, T)}
+
+
 def run_reference(args, info):
     """The reference path's CPU implementation on all host cores, rank 0 only: the reference's
     own SPGQPSolver template (oracle/_ref) where it compiled, else the FP64 oracle port."""
@@ -451,20 +471,7 @@ def main():
     if info.rank == 0 and not args.no_image:
         result["image"] = measure_image(dev, peak)
     if info.rank == 0 and not args.no_cpu:
-        kind = "reference" if ref_available() else "port"
-        rate, dt, _ = cpu_iter_rate(kind, sig, theta, args.eps2, T, 5, cpu_cores())
-        prate, pdt, _ = cpu_iter_rate("port", sig, theta, args.eps2, T, 5, cpu_cores())
-        rate1, dt1, _ = cpu_iter_rate("port", sig, theta, args.eps2, T, 2, 1)
-        what = "the reference's SPGQPSolver template (oracle/_ref)" if kind == "reference" else "the FP64 oracle"
-        result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cpu_cores(), "kind": kind,
-                                  "sample": f"5 SPG iterations of {what} on the full T={T} signal "
-                                            f"({dt:.1f} s, OpenMP)",
-                                  "port_all_cores": {"value": prate, "unit": UNIT, "cores": cpu_cores(),
-                                                     "kind": "port", "sample": f"5 SPG iterations ({pdt:.1f} s)"},
-                                  "one_thread": {"value": rate1, "unit": UNIT, "cores": 1, "kind": "port",
-                                                 "sample": f"2 SPG iterations, same signal ({dt1:.1f} s)"},
-                                  "reference_one_thread": reference_one_thread(sig, theta, args.eps2, T, 2),
-                                  "time_to_1e-6_rel_obj": cpu_tts(kind, sig, theta, args.eps2, T)}
+        result["cpu_baseline"] = measure_cpu_baseline(sig, theta, args.eps2, T)
     if info.rank == 0:
         print(json.dumps(result), flush=True)
     dist_finalize(info)

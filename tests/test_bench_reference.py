@@ -51,3 +51,22 @@ def test_reference_arm_under_two_ranks():
     d = json.loads(lines[0])
     assert d["n_gpus"] == 2 and d["impl"] == "reference"
     assert d["cpu_baseline"]["cores"] == len(os.sched_getaffinity(0))
+
+
+def test_gpu_arm_cpu_baseline_object():
+    """The cpu_baseline object the GPU arm adds to its line, built on the CPU at a small T."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import pasc_oracle as O
+    from pasc_inference_gb300 import datagen
+    import numpy as np
+    T = 50_000
+    sig = datagen.signal1d_cfg1(T=T)
+    cb = bench.measure_cpu_baseline(sig, np.array([0.0, 1.0, 2.0]), 10.0, T)
+    json.dumps(cb)
+    assert cb["kind"] == ("reference" if O.ref_available() else "port")
+    assert cb["value"] > 0 and cb["cores"] == bench.cpu_cores()
+    assert cb["port_all_cores"]["value"] > 0 and cb["one_thread"]["cores"] == 1
+    if O.ref_available():
+        assert cb["reference_one_thread"]["objective_equals_port"] is True
+        assert cb["time_to_1e-6_rel_obj"]["objective_equals_port_trace"] is True
